@@ -1,0 +1,416 @@
+#!/usr/bin/env python3
+"""Benchmark: semblance evaluations per second (trace x sample x candidate).
+
+Workload (default): CMP linear search at production size -- 2000 CMPs, fold
+60 (half-offsets 0..2950 m), 2000 samples at dt = 2 ms, 401 velocities
+1000..6000 m/s, window 7.  One step = the whole line in one call.
+
+  value : device-resident line and midpoints, the tuned kernel, timed with CUDA
+          events on the engine's stream (the line, 960 MB, exceeds the 129 MB L2
+          so no flush is needed between steps);
+  e2e   : the same step through the public C ABI with host buffers: upload the
+          line from page-locked memory (hpss_upload_gather), search
+          (hpss_linear_search), results copied back to the host;
+  plain : the plain one-(sample, candidate)-per-thread FP32 kernel, same line.
+
+`--impl reference` times the reference algorithm on the host CPU (the oracle's
+C restatement, all cores): the reference's only CPU path is its OpenCL build
+on a host OpenCL device, which this machine does not have.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "semblance evals/s (trace*sample*param), tuned vs plain, 1 GB300, <=1e-4 err"
+UNIT = "evals/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="cmp-production")
+    ap.add_argument("--n-cmp", type=int, default=None, help="smaller line (profiling only)")
+    ap.add_argument("--plain-steps", type=int, default=1)
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+# ----------------------------------------------------------------- helpers
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() in ("active", "1", "0x1"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        return json.loads(p.read_text())
+    return {"hbm_gbs": 6800.0, "sm_max_mhz": 2070.0, "fallback": True}
+
+
+def profile_traffic(kernel_tag: str):
+    """DRAM bytes per launch of the dominant kernel from the committed ncu
+    summary (profiles/<kernel_tag>.md, line 'traffic_bytes_per_launch: N')."""
+    p = ROOT / "profiles" / f"{kernel_tag}.md"
+    if not p.exists():
+        return None, None
+    scale = None
+    val = None
+    for ln in p.read_text().splitlines():
+        if ln.startswith("traffic_bytes_per_launch:"):
+            try:
+                val = float(ln.split(":", 1)[1].split()[0])
+            except ValueError:
+                pass
+        if ln.startswith("traffic_scale_units:"):
+            scale = ln.split(":", 1)[1].strip()
+    return val, scale
+
+
+# ----------------------------------------------------------------- workload
+
+def make_workload(name: str, n_cmp=None):
+    from highperformanceseismicstacking_gb300 import synthetic
+    w = synthetic.WORKLOADS[name]
+    line = w.make_line(n_cmp=n_cmp)
+    lower, upper = synthetic.workload_bounds(w)
+    from highperformanceseismicstacking_gb300.su import tau_index
+    tau = tau_index(w.tau, line.dt)
+    return w, line, lower, upper, tau
+
+
+def evals_per_step(counts, S, P):
+    return float(np.sum(counts)) * S * P
+
+
+# ----------------------------------------------------------------- reference arm
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    from oracle import oracle
+    w, line, lower, upper, tau = make_workload(args.workload, args.n_cmp)
+    params = oracle.build_grid(w.model, lower, upper, w.granularity)
+    m0s = line.cdp_midpoints
+    nthreads = oracle.max_threads()
+    S = line.samples_per_trace
+    rng = np.random.default_rng(0)
+
+    def one_step(m0):
+        sel = np.nonzero(oracle.select(w.model, line.midpoints, line.halfoffsets, m0, w.apm,
+                                       w.h0, S, float(line.dt)))[0].astype(np.uint32)
+        t = time.perf_counter()
+        sem, stk, _ = oracle.ls_eval(w.model, line.samples, line.midpoints, line.halfoffsets,
+                                     sel, m0, float(line.dt), tau, params, w.apm, w.h0,
+                                     nthreads=nthreads)
+        oracle.ls_result(w.model, sem, stk, params)
+        return time.perf_counter() - t, float(sel.size) * S * params.shape[0]
+
+    picks = rng.choice(len(m0s), size=args.warmup + args.steps, replace=True)
+    for i in range(args.warmup):
+        one_step(m0s[picks[i]])
+    tot_t = tot_e = 0.0
+    for i in range(args.steps):
+        dt_, ev = one_step(m0s[picks[args.warmup + i]])
+        tot_t += dt_
+        tot_e += ev
+    v = tot_e / tot_t
+    sample = f"{args.steps} steps of one CMP gather each ({tot_e / args.steps:.3g} evals/step)"
+    out = {"metric": METRIC, "value": v, "unit": UNIT, "impl": "reference",
+           "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": 1e3 * tot_t / args.steps, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": w.name, "cmps": int(len(m0s)), "fold": 60,
+                      "samples": S, "candidates": int(params.shape[0]),
+                      "window": 2 * tau + 1, "parallelism": "host threads"},
+           "cpu_baseline": {"value": v, "unit": UNIT, "cores": nthreads, "kind": "port",
+                            "sample": sample},
+           "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+           "note": "reference CPU path is its OpenCL build on a host OpenCL device (absent); "
+                   "timed here: the oracle's C restatement of the reference kernels"}
+    print(json.dumps(out))
+
+
+# ----------------------------------------------------------------- our arm
+
+def cpu_baseline(w, line, lower, upper, tau, seconds):
+    from oracle import oracle
+    params = oracle.build_grid(w.model, lower, upper, w.granularity)
+    nthreads = oracle.max_threads()
+    S = line.samples_per_trace
+    tot_t = tot_e = 0.0
+    n = 0
+    for m0 in line.cdp_midpoints[::37]:
+        sel = np.nonzero(oracle.select(w.model, line.midpoints, line.halfoffsets, m0, w.apm,
+                                       w.h0, S, float(line.dt)))[0].astype(np.uint32)
+        t = time.perf_counter()
+        oracle.ls_eval(w.model, line.samples, line.midpoints, line.halfoffsets, sel, m0,
+                       float(line.dt), tau, params, w.apm, w.h0, nthreads=nthreads)
+        tot_t += time.perf_counter() - t
+        tot_e += float(sel.size) * S * params.shape[0]
+        n += 1
+        if tot_t >= seconds:
+            break
+    return {"value": tot_e / tot_t, "unit": UNIT, "cores": nthreads, "kind": "port",
+            "sample": f"{n} CMP gathers of the same line ({tot_e:.3g} evals, {tot_t:.1f} s)"}
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+        return
+    import torch
+    from highperformanceseismicstacking_gb300 import capi, sharding
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    w, line, lower, upper, tau = make_workload(args.workload, args.n_cmp)
+    S = line.samples_per_trace
+    all_m0 = line.cdp_midpoints
+    a, b = sharding.shard_midpoints(all_m0, world, rank)
+    m0s = all_m0[a:b]
+    P = int(np.prod(w.granularity))
+
+    eng = capi.Engine(local)
+    eng.upload_gather(line.samples, line.midpoints, line.halfoffsets, float(line.dt))
+    eng.set_traveltime(w.model, lower, upper, w.apm, w.h0)
+    eng.set_window(tau)
+    counts = eng.select_traces(m0s)
+    evals = evals_per_step(counts, S, P)
+
+    dev = torch.device("cuda", local)
+    d_m0 = torch.from_numpy(np.ascontiguousarray(m0s)).to(dev)
+    d_out = torch.empty((len(m0s), 2 + eng.np, S), dtype=torch.float32, device=dev)
+    stream = torch.cuda.ExternalStream(eng.stream, device=dev)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    def run(kernel):
+        eng.linear_search_device(d_m0.data_ptr(), len(m0s), w.granularity, d_out.data_ptr(),
+                                 kernel)
+
+    launches_per_step = 4  # grid, chunk bounds, selection, semblance kernel
+    # ---- tuned, device resident
+    for _ in range(args.warmup):
+        run("tuned")
+    barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    barrier()
+    ev[0].record(stream)
+    for i in range(args.steps):
+        run("tuned")
+        ev[i + 1].record(stream)
+    barrier()
+    clk = clocks.stop()
+    step_ms = [ev[i].elapsed_time(ev[i + 1]) for i in range(args.steps)]
+    total_ms = sum(step_ms)
+    if world > 1:
+        t = torch.tensor([total_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+        e = torch.tensor([evals], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(e)
+        evals_all = float(e.item())
+    else:
+        evals_all = evals
+    value = evals_all * args.steps / (total_ms / 1e3)
+    # kernel-only duration of the semblance launch (stats path, one extra call)
+    st = eng.linear_search_device(d_m0.data_ptr(), len(m0s), w.granularity, d_out.data_ptr(),
+                                  "tuned", stats=True)
+    kernel_ms = st["kernel_ms"]
+    tuned_out = d_out.cpu().numpy()
+
+    # ---- plain kernel, same line
+    run("plain")
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.plain_steps):
+        run("plain")
+    e1.record(stream)
+    torch.cuda.synchronize()
+    plain_ms = e0.elapsed_time(e1) / args.plain_steps
+    plain_value = evals / (plain_ms / 1e3)
+    plain_out = d_out.cpu().numpy()
+    identical = bool(np.array_equal(tuned_out, plain_out))
+
+    # ---- end to end through the C ABI with host buffers
+    pinned = torch.empty(line.samples.shape, dtype=torch.float32, pin_memory=True)
+    pinned.numpy()[:] = line.samples
+    host_samples = pinned.numpy()
+    h2d = host_samples.nbytes + 2 * line.midpoints.nbytes + m0s.nbytes
+    d2h = len(m0s) * (2 + eng.np) * S * 4
+    eng2 = capi.Engine(local)
+    e2e_t = []
+    for i in range(args.e2e_steps + 1):
+        barrier()
+        t0 = time.perf_counter()
+        eng2.upload_gather(host_samples, line.midpoints, line.halfoffsets, float(line.dt))
+        eng2.set_traveltime(w.model, lower, upper, w.apm, w.h0)
+        eng2.set_window(tau)
+        res, _ = eng2.linear_search(m0s, w.granularity, "tuned")
+        t1 = time.perf_counter()
+        if i > 0:
+            e2e_t.append(t1 - t0)
+    e2e_max = max(e2e_t)
+    if world > 1:
+        t = torch.tensor([e2e_max], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_max = float(t.item())
+    e2e_value = evals_all / (sum(e2e_t) / len(e2e_t)) if world == 1 else evals_all / e2e_max
+    e2e_same = bool(np.array_equal(res, tuned_out))
+    eng2.close()
+
+    if rank != 0:
+        eng.close()
+        if world > 1:
+            torch.distributed.barrier()
+            torch.distributed.destroy_process_group()
+        return
+
+    # ---- roofline of the dominant kernel (tuned semblance kernel)
+    peaks = measured_peaks()
+    props = torch.cuda.get_device_properties(dev)
+    sms = props.multi_processor_count
+    fmax = float(peaks.get("sm_max_mhz", 2070.0)) * 1e6
+    wsz = 2 * tau + 1
+    t_model = {"cmp": 2, "zocrs": 5, "oct": 40}[w.model]
+    instr_per_eval = 3 * wsz + t_model
+    instr_per_launch = instr_per_eval * evals
+    peak_instr = sms * 128 * fmax
+    achieved = instr_per_launch / (kernel_ms / 1e3)
+    n_sel = float(np.sum(counts))
+    alg_bytes = n_sel * S * 4 + n_sel * 8 + len(m0s) * (2 + eng.np) * S * 4
+    traffic, traffic_note = profile_traffic(f"ls_tuned_{w.name}")
+    roof = {"bound": "fp32", "achieved": achieved / 1e12, "peak": peak_instr / 1e12,
+            "unit": "Tinstr/s", "frac": achieved / peak_instr,
+            "traffic": traffic,
+            "instr_per_eval": instr_per_eval,
+            "peak_source": "SMs x 128 FP32 lanes x measured max SM clock (MEASURED_PEAKS.json)",
+            "kernel_ms": kernel_ms,
+            "hbm": {"achieved": alg_bytes / (kernel_ms / 1e3) / 1e9,
+                    "peak": float(peaks.get("hbm_gbs", 6800.0)), "unit": "GB/s",
+                    "frac": alg_bytes / (kernel_ms / 1e3) / 1e9 / float(peaks.get("hbm_gbs", 6800.0)),
+                    "bytes_per_launch": alg_bytes}}
+    if traffic_note:
+        roof["traffic_note"] = traffic_note
+
+    cpu = None
+    if not args.no_cpu_baseline and world >= 1:
+        cpu = cpu_baseline(w, line, lower, upper, tau, args.cpu_seconds)
+
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+           "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": w.name, "model": w.model, "algorithm": w.algorithm,
+                      "cmps": int(len(all_m0)), "fold": int(np.max(counts)) if len(counts) else 0,
+                      "samples": S, "candidates": P, "window": wsz,
+                      "evals_per_step": evals_all, "storage": "fp32", "kernel": "tuned",
+                      "l2": "inputs exceed L2 (line %.0f MB > 129 MB); no flush" %
+                            (line.samples.nbytes / 1e6),
+                      "parallelism": f"midpoint shards x{world}"},
+           "plain": {"value": plain_value, "ms_per_step": plain_ms,
+                     "speedup_tuned_vs_plain": value / plain_value,
+                     "identical_results": identical},
+           "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                   "d2h_bytes_per_step": int(d2h), "s_per_step": sum(e2e_t) / len(e2e_t),
+                   "matches_device_result": e2e_same},
+           "gpu_launches": launches_per_step * args.steps,
+           "roofline": roof,
+           "cpu_baseline": cpu,
+           "clocks": clk,
+           "step_ms": step_ms}
+    print(json.dumps(out))
+    eng.close()
+    if world > 1:
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

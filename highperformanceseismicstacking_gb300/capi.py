@@ -1,0 +1,214 @@
+"""ctypes binding of the C ABI in include/hpss.h (libhpss_gb300.so).
+
+There is no fallback: if the CUDA engine is not built, importing this module
+raises, and every call returns the engine's own error.  ``Engine`` is a thin
+numpy-friendly wrapper that owns one ``hpss_handle``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+from typing import Optional, Sequence, Tuple
+
+import numpy as np
+
+_LIB_PATH = Path(__file__).resolve().parent / "lib" / "libhpss_gb300.so"
+
+HPSS_OK = 0
+ERRORS = {
+    -1: "HPSS_ERR_INVALID_ARGUMENT", -2: "HPSS_ERR_LOGIC", -3: "HPSS_ERR_CUDA",
+    -4: "HPSS_ERR_NO_DEVICE", -5: "HPSS_ERR_OUT_OF_MEMORY", -6: "HPSS_ERR_NOT_READY",
+    -7: "HPSS_ERR_TIMEOUT", -8: "HPSS_ERR_DEVICE_CHECK",
+}
+MODELS = {"cmp": 0, "zocrs": 1, "oct": 2}
+STORAGE = {"fp32": 0, "bf16": 1, "fp16": 2}
+KERNELS = {"plain": 0, "tuned": 1}
+N_PARAMS = {"cmp": 1, "zocrs": 3, "oct": 2}
+
+# Every symbol include/hpss.h declares.
+EXPORTED = [
+    "hpss_create", "hpss_destroy", "hpss_last_error", "hpss_version",
+    "hpss_device_count", "hpss_upload_gather", "hpss_set_traveltime",
+    "hpss_set_window", "hpss_linear_search", "hpss_linear_search_device",
+    "hpss_differential_evolution", "hpss_differential_evolution_device",
+    "hpss_stretch_free", "hpss_select_traces", "hpss_stream", "hpss_device_bytes",
+]
+
+
+class Stats(C.Structure):
+    _fields_ = [("evals", C.c_double), ("not_used", C.c_double),
+                ("selected_traces", C.c_double), ("kernel_ms", C.c_double),
+                ("selection_ms", C.c_double), ("device_error", C.c_uint32),
+                ("reserved", C.c_uint32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+
+
+class HpssError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+def load_library(path: Optional[Path] = None) -> C.CDLL:
+    p = Path(path or _LIB_PATH)
+    if not p.exists():
+        raise ImportError(f"CUDA engine not built ({p} missing): run __graft_entry__.build()")
+    lib = C.CDLL(str(p))
+    vp, u32, f32, i32 = C.c_void_p, C.c_uint32, C.c_float, C.c_int
+    fp, up = C.POINTER(C.c_float), C.POINTER(C.c_uint32)
+    sig = {
+        "hpss_create": (i32, [i32, C.POINTER(vp)]),
+        "hpss_destroy": (i32, [vp]),
+        "hpss_last_error": (C.c_char_p, [vp]),
+        "hpss_version": (C.c_char_p, []),
+        "hpss_device_count": (i32, [C.POINTER(C.c_int)]),
+        "hpss_upload_gather": (i32, [vp, fp, fp, fp, u32, u32, f32, i32]),
+        "hpss_set_traveltime": (i32, [vp, i32, u32, fp, fp, f32, f32]),
+        "hpss_set_window": (i32, [vp, i32]),
+        "hpss_linear_search": (i32, [vp, fp, u32, up, i32, fp, C.POINTER(Stats)]),
+        "hpss_linear_search_device": (i32, [vp, vp, u32, up, i32, vp, C.POINTER(Stats)]),
+        "hpss_differential_evolution": (i32, [vp, fp, u32, u32, u32, f32, f32, C.c_uint64, fp,
+                                              C.POINTER(Stats)]),
+        "hpss_differential_evolution_device": (i32, [vp, vp, u32, u32, u32, f32, f32,
+                                                     C.c_uint64, vp, C.POINTER(Stats)]),
+        "hpss_stretch_free": (i32, [vp, fp, u32, fp, i32, fp, C.POINTER(Stats)]),
+        "hpss_select_traces": (i32, [vp, fp, u32, up]),
+        "hpss_stream": (vp, [vp]),
+        "hpss_device_bytes": (C.c_size_t, [vp]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    return lib
+
+
+_lib: Optional[C.CDLL] = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        _lib = load_library()
+    return _lib
+
+
+def _fptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def _uptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_uint32))
+
+
+class Engine:
+    """One device handle: upload a line once, then run searches over midpoints."""
+
+    def __init__(self, device: int = 0):
+        self._lib = lib()
+        h = C.c_void_p()
+        rc = self._lib.hpss_create(device, C.byref(h))
+        if rc != HPSS_OK:
+            raise HpssError(rc, self._lib.hpss_last_error(None).decode())
+        self.h = h
+        self.model = None
+        self.S = 0
+        self.np = 0
+
+    def close(self):
+        if self.h:
+            self._lib.hpss_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, rc: int):
+        if rc != HPSS_OK:
+            raise HpssError(rc, self._lib.hpss_last_error(self.h).decode())
+
+    @property
+    def stream(self) -> int:
+        return int(self._lib.hpss_stream(self.h) or 0)
+
+    def device_bytes(self) -> int:
+        return int(self._lib.hpss_device_bytes(self.h))
+
+    def upload_gather(self, samples: np.ndarray, midpoints: np.ndarray,
+                      halfoffsets: np.ndarray, dt: float, storage: str = "fp32"):
+        samples = np.ascontiguousarray(samples, dtype=np.float32)
+        midpoints = np.ascontiguousarray(midpoints, dtype=np.float32)
+        halfoffsets = np.ascontiguousarray(halfoffsets, dtype=np.float32)
+        n, S = samples.shape
+        self._check(self._lib.hpss_upload_gather(
+            self.h, _fptr(samples), _fptr(midpoints), _fptr(halfoffsets), n, S,
+            C.c_float(dt), STORAGE[storage]))
+        self.S = S
+
+    def set_traveltime(self, model: str, lower: Sequence[float], upper: Sequence[float],
+                       apm: float = 0.0, h0: float = 0.0):
+        lo = np.asarray(lower, np.float32)
+        hi = np.asarray(upper, np.float32)
+        self._check(self._lib.hpss_set_traveltime(self.h, MODELS[model], lo.size, _fptr(lo),
+                                                   _fptr(hi), C.c_float(apm), C.c_float(h0)))
+        self.model = model
+        self.np = N_PARAMS[model]
+
+    def set_window(self, tau_index: int):
+        self._check(self._lib.hpss_set_window(self.h, int(tau_index)))
+
+    def linear_search(self, m0s, granularity: Sequence[int], kernel: str = "tuned"
+                      ) -> Tuple[np.ndarray, dict]:
+        m0s = np.ascontiguousarray(m0s, dtype=np.float32)
+        g = np.asarray(granularity, np.uint32)
+        out = np.zeros((m0s.size, 2 + self.np, self.S), np.float32)
+        st = Stats()
+        self._check(self._lib.hpss_linear_search(self.h, _fptr(m0s), m0s.size, _uptr(g),
+                                                  KERNELS[kernel], _fptr(out), C.byref(st)))
+        return out, st.as_dict()
+
+    def linear_search_device(self, d_m0s: int, n_m0: int, granularity, d_out: int,
+                             kernel: str = "tuned", stats: bool = False):
+        g = np.asarray(granularity, np.uint32)
+        st = Stats()
+        self._check(self._lib.hpss_linear_search_device(
+            self.h, C.c_void_p(d_m0s), n_m0, _uptr(g), KERNELS[kernel], C.c_void_p(d_out),
+            C.byref(st) if stats else None))
+        return st.as_dict() if stats else None
+
+    def differential_evolution(self, m0s, population: int, generations: int, F: float,
+                               CR: float, seed: int) -> Tuple[np.ndarray, dict]:
+        m0s = np.ascontiguousarray(m0s, dtype=np.float32)
+        out = np.zeros((m0s.size, 2 + self.np, self.S), np.float32)
+        st = Stats()
+        self._check(self._lib.hpss_differential_evolution(
+            self.h, _fptr(m0s), m0s.size, population, generations, C.c_float(F),
+            C.c_float(CR), C.c_uint64(seed), _fptr(out), C.byref(st)))
+        return out, st.as_dict()
+
+    def stretch_free(self, m0s, params: np.ndarray, nmax: int = 10
+                     ) -> Tuple[np.ndarray, dict]:
+        m0s = np.ascontiguousarray(m0s, dtype=np.float32)
+        params = np.ascontiguousarray(params, dtype=np.float32)
+        out = np.zeros((m0s.size, 3, self.S), np.float32)
+        st = Stats()
+        self._check(self._lib.hpss_stretch_free(self.h, _fptr(m0s), m0s.size, _fptr(params),
+                                                 nmax, _fptr(out), C.byref(st)))
+        return out, st.as_dict()
+
+    def select_traces(self, m0s) -> np.ndarray:
+        m0s = np.ascontiguousarray(m0s, dtype=np.float32)
+        counts = np.zeros(m0s.size, np.uint32)
+        self._check(self._lib.hpss_select_traces(self.h, _fptr(m0s), m0s.size, _uptr(counts)))
+        return counts

@@ -1,0 +1,587 @@
+// hpss_capi.cu -- the C ABI of libhpss_gb300.so (declared in include/hpss.h).
+//
+// Host-side orchestration only: argument checks with the reference's error
+// semantics, device buffers owned by the handle, and the launch sequence
+// (candidate grid -> trace selection -> semblance kernel) on the handle's
+// stream.  No exception crosses the ABI.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "../../include/hpss.h"
+#include "hpss_internal.h"
+
+namespace hpss {
+cudaError_t launch_select_range(const float *mid, uint32_t n, const float *m0s,
+                                uint32_t nM0, int mode, float apm, float radius,
+                                uint32_t *first, uint32_t *count,
+                                cudaStream_t st);
+cudaError_t launch_exclusive_scan(const uint32_t *count, uint32_t *first,
+                                  uint32_t n, cudaStream_t st);
+cudaError_t launch_ls_tuned_cmp(const LsParams &p, uint32_t grid, uint32_t tiles,
+                                uint32_t nUnits, cudaStream_t st);
+cudaError_t launch_ls_tuned_zocrs(const LsParams &p, uint32_t grid, uint32_t tiles,
+                                  uint32_t nUnits, cudaStream_t st);
+cudaError_t launch_ls_tuned_oct(const LsParams &p, uint32_t grid, uint32_t tiles,
+                                uint32_t nUnits, cudaStream_t st);
+size_t tuned_stage_floats();
+}  // namespace hpss
+
+using namespace hpss;
+
+struct hpss_handle_s : public Handle {
+    // scratch buffers, grown on demand
+    struct Buf {
+        void *p = nullptr;
+        size_t bytes = 0;
+    };
+    Buf params, chunkBounds, selFirst, selCount, selIdx, candFirst, candCount,
+        notUsed, errWord, m0s, out, octCands;
+    std::vector<float> octCandsHost;
+};
+
+namespace {
+
+thread_local std::string g_createError;
+
+const char *kVersion = "hpss-gb300 0.1.0 (sm_103a)";
+
+struct Fail {
+    hpss_status code;
+};
+
+hpss_status set_error(hpss_handle h, hpss_status code, const std::string &msg) {
+    if (h) h->lastError = msg;
+    else g_createError = msg;
+    return code;
+}
+
+#define HPSS_CUDA_TRY(h, expr)                                                 \
+    do {                                                                       \
+        cudaError_t _e = (expr);                                               \
+        if (_e != cudaSuccess) {                                               \
+            return set_error(h, _e == cudaErrorMemoryAllocation                \
+                                    ? HPSS_ERR_OUT_OF_MEMORY                   \
+                                    : HPSS_ERR_CUDA,                           \
+                             std::string("CUDA error at ") + __FILE__ + ":" +  \
+                                 std::to_string(__LINE__) + " (" #expr "): " + \
+                                 cudaGetErrorString(_e));                      \
+        }                                                                      \
+    } while (0)
+
+cudaError_t ensure(hpss_handle h, hpss_handle_s::Buf &b, size_t bytes) {
+    if (bytes == 0) bytes = 16;
+    if (b.bytes >= bytes) return cudaSuccess;
+    if (b.p) {
+        cudaFree(b.p);
+        h->deviceBytes -= b.bytes;
+        b.p = nullptr;
+        b.bytes = 0;
+    }
+    size_t want = std::max(bytes, (size_t)256);
+    cudaError_t e = cudaMalloc(&b.p, want);
+    if (e != cudaSuccess) return e;
+    b.bytes = want;
+    h->deviceBytes += want;
+    return cudaSuccess;
+}
+
+void release(hpss_handle h, hpss_handle_s::Buf &b) {
+    if (b.p) {
+        cudaFree(b.p);
+        h->deviceBytes -= b.bytes;
+    }
+    b.p = nullptr;
+    b.bytes = 0;
+}
+
+void free_gather(hpss_handle h) {
+    auto fr = [&](void *&p, size_t bytes) {
+        if (p) {
+            cudaFree(p);
+            h->deviceBytes -= bytes;
+        }
+        p = nullptr;
+    };
+    size_t n = h->nTraces, st = h->stride;
+    fr(reinterpret_cast<void *&>(h->dSamples), n * st * sizeof(float));
+    fr(reinterpret_cast<void *&>(h->dSamples16), n * st * sizeof(uint16_t));
+    fr(reinterpret_cast<void *&>(h->dScale), n * sizeof(float));
+    fr(reinterpret_cast<void *&>(h->dMid), n * sizeof(float));
+    fr(reinterpret_cast<void *&>(h->dHoff), n * sizeof(float));
+    fr(reinterpret_cast<void *&>(h->dHsq), n * sizeof(float));
+    h->gatherReady = false;
+}
+
+int model_params(int model) {
+    return model == HPSS_MODEL_CMP ? 1 : (model == HPSS_MODEL_ZOCRS ? 3 : 2);
+}
+
+hpss_status check_ready(hpss_handle h) {
+    if (!h) return HPSS_ERR_INVALID_ARGUMENT;
+    if (!h->gatherReady)
+        return set_error(h, HPSS_ERR_NOT_READY, "no gather uploaded (hpss_upload_gather)");
+    if (h->model < 0)
+        return set_error(h, HPSS_ERR_NOT_READY, "no traveltime model set (hpss_set_traveltime)");
+    if (h->tau < 0)
+        return set_error(h, HPSS_ERR_NOT_READY, "no semblance window set (hpss_set_window)");
+    return HPSS_OK;
+}
+
+// The 1024 sampled OCT candidates of the reference's linear-search trace
+// selection (CudaLinearSearchAlgorithm.cu:269-292): a default-constructed
+// std::default_random_engine, one uniform_real_distribution<float> per
+// parameter over [lower, upper); velocity converted to 4/v^2 on the host.
+void build_oct_selection_candidates(hpss_handle h) {
+    const unsigned samplePop = 1024;
+    h->octCandsHost.assign(samplePop * 2, 0.f);
+    std::default_random_engine generator;
+    for (unsigned prm = 0; prm < 2; prm++) {
+        std::uniform_real_distribution<float> dist(h->lower[prm], h->upper[prm]);
+        for (unsigned i = 0; i < samplePop; i++) {
+            float v = dist(generator);
+            if (prm == 0) v = 4.0f / (v * v);
+            h->octCandsHost[i * 2 + prm] = v;
+        }
+    }
+}
+
+// Device-side selection for nM0 midpoints (d_m0s on the device).  Leaves
+// LsParams' selFirst / selCount / selIdx filled.
+hpss_status run_selection(hpss_handle h, const float *d_m0s, uint32_t nM0,
+                          LsParams &lp) {
+    HPSS_CUDA_TRY(h, ensure(h, h->selFirst, nM0 * sizeof(uint32_t)));
+    HPSS_CUDA_TRY(h, ensure(h, h->selCount, nM0 * sizeof(uint32_t)));
+    uint32_t *first = static_cast<uint32_t *>(h->selFirst.p);
+    uint32_t *count = static_cast<uint32_t *>(h->selCount.p);
+    lp.selFirst = first;
+    lp.selCount = count;
+    lp.selIdx = nullptr;
+    if (h->model != HPSS_MODEL_OCT) {
+        HPSS_CUDA_TRY(h, launch_select_range(h->dMid, h->nTraces, d_m0s, nM0,
+                                             h->model == HPSS_MODEL_CMP ? 0 : 1,
+                                             h->apm, 0.f, first, count, h->stream));
+        return HPSS_OK;
+    }
+    // OCT: |mh - m0| <= sqrt(h^2 + h0^2) for any candidate (the displaced
+    // midpoint formula, oct/common.cuh:26-32, divides 2*theta*(h^2-h0^2) by a
+    // root no smaller than 2*|theta|*sqrt(h^2+h0^2)), so only traces with
+    // |m - m0| <= apm + sqrt(hmax^2 + h0^2) can pass; widened for rounding.
+    float hmax = 0.f;
+    for (float v : h->hHoff) hmax = std::max(hmax, std::fabs(v));
+    float radius = (h->apm + std::sqrt(hmax * hmax + h->h0 * h->h0)) * 1.001f + 1.0f;
+    HPSS_CUDA_TRY(h, ensure(h, h->candFirst, nM0 * sizeof(uint32_t)));
+    HPSS_CUDA_TRY(h, ensure(h, h->candCount, nM0 * sizeof(uint32_t)));
+    uint32_t *cf = static_cast<uint32_t *>(h->candFirst.p);
+    uint32_t *cc = static_cast<uint32_t *>(h->candCount.p);
+    HPSS_CUDA_TRY(h, launch_select_range(h->dMid, h->nTraces, d_m0s, nM0, 2,
+                                         h->apm, radius, cf, cc, h->stream));
+    // capacity per midpoint = its candidate count; offsets by prefix sum
+    HPSS_CUDA_TRY(h, launch_exclusive_scan(cc, first, nM0, h->stream));
+    std::vector<uint32_t> ccHost(nM0);
+    HPSS_CUDA_TRY(h, cudaMemcpyAsync(ccHost.data(), cc, nM0 * sizeof(uint32_t),
+                                     cudaMemcpyDeviceToHost, h->stream));
+    HPSS_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    size_t total = 0;
+    for (uint32_t v : ccHost) total += v;
+    HPSS_CUDA_TRY(h, ensure(h, h->selIdx, total * sizeof(uint32_t)));
+    if (h->octCandsHost.empty()) build_oct_selection_candidates(h);
+    HPSS_CUDA_TRY(h, ensure(h, h->octCands, h->octCandsHost.size() * sizeof(float)));
+    HPSS_CUDA_TRY(h, cudaMemcpyAsync(h->octCands.p, h->octCandsHost.data(),
+                                     h->octCandsHost.size() * sizeof(float),
+                                     cudaMemcpyHostToDevice, h->stream));
+    lp.selIdx = static_cast<uint32_t *>(h->selIdx.p);
+    lp.m0s = d_m0s;
+    lp.nM0 = nM0;
+    HPSS_CUDA_TRY(h, launch_select_oct(lp, static_cast<const float *>(h->octCands.p),
+                                       (uint32_t)(h->octCandsHost.size() / 2),
+                                       static_cast<uint32_t *>(h->selIdx.p), count,
+                                       cf, cc, h->stream));
+    return HPSS_OK;
+}
+
+void fill_line_params(hpss_handle h, LsParams &lp) {
+    std::memset(&lp, 0, sizeof(lp));
+    lp.samples = h->dSamples;
+    lp.samples16 = h->dSamples16;
+    lp.scale = h->dScale;
+    lp.stride = h->stride;
+    lp.S = h->S;
+    lp.dt = h->dt;
+    lp.tau = h->tau;
+    lp.w = 2 * h->tau + 1;
+    lp.mid = h->dMid;
+    lp.hoff = h->dHoff;
+    lp.hsq = h->dHsq;
+    lp.np = (int)h->np;
+    lp.apm = h->apm;
+    lp.h0 = h->h0;
+}
+
+int num_sms(hpss_handle h) {
+    int v = 0;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, h->device);
+    return v > 0 ? v : 1;
+}
+
+hpss_status linear_search_impl(hpss_handle h, const float *d_m0s, uint32_t nM0,
+                               const uint32_t *granularity, int kernel,
+                               float *d_out, hpss_stats *stats, bool sync) {
+    hpss_status rc = check_ready(h);
+    if (rc != HPSS_OK) return rc;
+    if (!granularity)
+        return set_error(h, HPSS_ERR_LOGIC, "granularity is required");
+    if (kernel != HPSS_KERNEL_PLAIN && kernel != HPSS_KERNEL_TUNED)
+        return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "unknown kernel family");
+    if (h->storage != HPSS_STORAGE_FP32)
+        return set_error(h, HPSS_ERR_INVALID_ARGUMENT,
+                         "linear search runs on FP32 storage in this build");
+    uint64_t P = 1;
+    uint32_t gran[3] = {1, 1, 1};
+    float inc[3] = {0, 0, 0}, low[3] = {0, 0, 0};
+    for (uint32_t j = 0; j < h->np; j++) {
+        if (granularity[j] == 0)
+            return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "granularity must be > 0");
+        gran[j] = granularity[j];
+        P *= granularity[j];
+        low[j] = h->lower[j];
+        // setupDiscretizationSteps (LinearSearchAlgorithm.cpp:137-139)
+        inc[j] = (h->upper[j] - h->lower[j]) / static_cast<float>(granularity[j]);
+    }
+    if (P > 0x7fffffffull)
+        return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "too many candidates");
+    if (nM0 == 0) return HPSS_OK;
+    cudaSetDevice(h->device);
+
+    LsParams lp;
+    fill_line_params(h, lp);
+    lp.m0s = d_m0s;
+    lp.nM0 = nM0;
+    lp.P = (uint32_t)P;
+    lp.out = d_out;
+
+    HPSS_CUDA_TRY(h, ensure(h, h->params, P * h->np * sizeof(float)));
+    lp.params = static_cast<float *>(h->params.p);
+    HPSS_CUDA_TRY(h, launch_build_grid(h->model, low, inc, gran,
+                                       static_cast<float *>(h->params.p), lp.P, h->stream));
+    lp.chunkSize = kTunedWarps * 4;
+    lp.nChunks = (lp.P + lp.chunkSize - 1) / lp.chunkSize;
+    HPSS_CUDA_TRY(h, ensure(h, h->chunkBounds, (size_t)lp.nChunks * 2 * h->np * sizeof(float)));
+    lp.chunkBounds = static_cast<float *>(h->chunkBounds.p);
+    HPSS_CUDA_TRY(h, launch_chunk_bounds(lp, static_cast<float *>(h->chunkBounds.p), h->stream));
+    HPSS_CUDA_TRY(h, ensure(h, h->notUsed, nM0 * sizeof(unsigned long long)));
+    HPSS_CUDA_TRY(h, ensure(h, h->errWord, sizeof(uint32_t)));
+    lp.notUsed = static_cast<unsigned long long *>(h->notUsed.p);
+    lp.errorWord = static_cast<uint32_t *>(h->errWord.p);
+    HPSS_CUDA_TRY(h, cudaMemsetAsync(lp.notUsed, 0, nM0 * sizeof(unsigned long long), h->stream));
+    HPSS_CUDA_TRY(h, cudaMemsetAsync(lp.errorWord, 0, sizeof(uint32_t), h->stream));
+
+    HPSS_CUDA_TRY(h, cudaEventRecord(h->ev0, h->stream));
+    rc = run_selection(h, d_m0s, nM0, lp);
+    if (rc != HPSS_OK) return rc;
+    HPSS_CUDA_TRY(h, cudaEventRecord(h->ev1, h->stream));
+    if (kernel == HPSS_KERNEL_PLAIN) {
+        HPSS_CUDA_TRY(h, launch_ls_plain(lp, h->stream));
+    } else {
+        if (lp.w > 15 || h->stride + 8 > (uint32_t)tuned_stage_floats()) {
+            HPSS_CUDA_TRY(h, launch_ls_plain(lp, h->stream));
+        } else {
+            uint32_t tiles = (h->S + kTileSamples - 1) / kTileSamples;
+            uint64_t units = (uint64_t)nM0 * tiles;
+            uint32_t grid = (uint32_t)std::min<uint64_t>(units, (uint64_t)num_sms(h) * 2);
+            cudaError_t e;
+            if (h->model == HPSS_MODEL_CMP) e = launch_ls_tuned_cmp(lp, grid, tiles, (uint32_t)units, h->stream);
+            else if (h->model == HPSS_MODEL_ZOCRS) e = launch_ls_tuned_zocrs(lp, grid, tiles, (uint32_t)units, h->stream);
+            else e = launch_ls_tuned_oct(lp, grid, tiles, (uint32_t)units, h->stream);
+            HPSS_CUDA_TRY(h, e);
+        }
+    }
+    HPSS_CUDA_TRY(h, cudaEventRecord(h->ev2, h->stream));
+
+    if (stats || sync) {
+        HPSS_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+        uint32_t err = 0;
+        HPSS_CUDA_TRY(h, cudaMemcpy(&err, lp.errorWord, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+        if (stats) {
+            std::memset(stats, 0, sizeof(*stats));
+            std::vector<uint32_t> cnt(nM0);
+            std::vector<unsigned long long> nu(nM0);
+            HPSS_CUDA_TRY(h, cudaMemcpy(cnt.data(), lp.selCount, nM0 * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+            HPSS_CUDA_TRY(h, cudaMemcpy(nu.data(), lp.notUsed, nM0 * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+            double sel = 0, nus = 0;
+            for (uint32_t i = 0; i < nM0; i++) {
+                sel += cnt[i];
+                nus += (double)nu[i];
+            }
+            stats->selected_traces = sel;
+            stats->evals = sel * (double)h->S * (double)P;
+            stats->not_used = nus;
+            float ms = 0;
+            cudaEventElapsedTime(&ms, h->ev1, h->ev2);
+            stats->kernel_ms = ms;
+            cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+            stats->selection_ms = ms;
+            stats->device_error = err;
+        }
+        if (err)
+            return set_error(h, HPSS_ERR_DEVICE_CHECK,
+                             "device check failed, error word " + std::to_string(err));
+    }
+    return HPSS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *hpss_version(void) { return kVersion; }
+
+hpss_status hpss_device_count(int *count) {
+    if (!count) return HPSS_ERR_INVALID_ARGUMENT;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess) {
+        *count = 0;
+        return set_error(nullptr, HPSS_ERR_NO_DEVICE,
+                         std::string("cudaGetDeviceCount: ") + cudaGetErrorString(e));
+    }
+    *count = n;
+    return HPSS_OK;
+}
+
+hpss_status hpss_create(int device, hpss_handle *out) {
+    if (!out) return set_error(nullptr, HPSS_ERR_INVALID_ARGUMENT, "out is NULL");
+    *out = nullptr;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0)
+        return set_error(nullptr, HPSS_ERR_NO_DEVICE,
+                         "No CUDA devices found on your system.");
+    if (device < 0 || device >= n)
+        return set_error(nullptr, HPSS_ERR_INVALID_ARGUMENT, "device index out of range");
+    hpss_handle h = new (std::nothrow) hpss_handle_s();
+    if (!h) return set_error(nullptr, HPSS_ERR_OUT_OF_MEMORY, "host allocation failed");
+    h->device = device;
+    e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreate(&h->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&h->ev1);
+    if (e == cudaSuccess) e = cudaEventCreate(&h->ev2);
+    if (e != cudaSuccess) {
+        std::string msg = std::string("device init failed: ") + cudaGetErrorString(e);
+        hpss_destroy(h);
+        return set_error(nullptr, HPSS_ERR_CUDA, msg);
+    }
+    *out = h;
+    return HPSS_OK;
+}
+
+hpss_status hpss_destroy(hpss_handle h) {
+    if (!h) return HPSS_OK;
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    free_gather(h);
+    for (auto *b : {&h->params, &h->chunkBounds, &h->selFirst, &h->selCount, &h->selIdx,
+                    &h->candFirst, &h->candCount, &h->notUsed, &h->errWord, &h->m0s,
+                    &h->out, &h->octCands})
+        release(h, *b);
+    if (h->ev0) cudaEventDestroy(h->ev0);
+    if (h->ev1) cudaEventDestroy(h->ev1);
+    if (h->ev2) cudaEventDestroy(h->ev2);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return HPSS_OK;
+}
+
+const char *hpss_last_error(hpss_handle h) {
+    return h ? h->lastError.c_str() : g_createError.c_str();
+}
+
+hpss_status hpss_upload_gather(hpss_handle h, const float *samples,
+                               const float *midpoints, const float *halfoffsets,
+                               uint32_t nTraces, uint32_t samplesPerTrace,
+                               float dtInSeconds, int storage) {
+    if (!h) return HPSS_ERR_INVALID_ARGUMENT;
+    if (nTraces > 0 && (!samples || !midpoints || !halfoffsets))
+        return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "null input array");
+    if (samplesPerTrace == 0 || !(dtInSeconds > 0.f))
+        return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "samplesPerTrace and dt must be > 0");
+    if (storage < HPSS_STORAGE_FP32 || storage > HPSS_STORAGE_FP16)
+        return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "unknown storage");
+    for (uint32_t i = 0; i < nTraces; i++) {
+        float m = midpoints[i], o = halfoffsets[i];
+        if (!(m == m) || !(o == o))
+            return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "NaN midpoint or half-offset");
+        if (i > 0) {
+            float pm = midpoints[i - 1], ph = halfoffsets[i - 1];
+            if (m < pm || (m == pm && o < ph))
+                return set_error(h, HPSS_ERR_INVALID_ARGUMENT,
+                                 "traces must be sorted by (midpoint, half-offset)");
+        }
+    }
+    cudaSetDevice(h->device);
+    cudaStreamSynchronize(h->stream);
+    free_gather(h);
+    h->nTraces = nTraces;
+    h->S = samplesPerTrace;
+    h->stride = (samplesPerTrace + 7u) & ~7u;  // 32-byte rows
+    h->dt = dtInSeconds;
+    h->storage = storage;
+    h->hMid.assign(midpoints, midpoints + nTraces);
+    h->hHoff.assign(halfoffsets, halfoffsets + nTraces);
+    std::vector<float> hsq(nTraces);
+    for (uint32_t i = 0; i < nTraces; i++) hsq[i] = halfoffsets[i] * halfoffsets[i];
+    const size_t n = nTraces, st = h->stride;
+    auto alloc = [&](void **p, size_t bytes) -> cudaError_t {
+        cudaError_t e = cudaMalloc(p, bytes ? bytes : 16);
+        if (e == cudaSuccess) h->deviceBytes += bytes;
+        return e;
+    };
+    HPSS_CUDA_TRY(h, alloc(reinterpret_cast<void **>(&h->dSamples), n * st * sizeof(float)));
+    HPSS_CUDA_TRY(h, alloc(reinterpret_cast<void **>(&h->dMid), n * sizeof(float)));
+    HPSS_CUDA_TRY(h, alloc(reinterpret_cast<void **>(&h->dHoff), n * sizeof(float)));
+    HPSS_CUDA_TRY(h, alloc(reinterpret_cast<void **>(&h->dHsq), n * sizeof(float)));
+    if (n) {
+        if (st != samplesPerTrace)
+            HPSS_CUDA_TRY(h, cudaMemsetAsync(h->dSamples, 0, n * st * sizeof(float), h->stream));
+        HPSS_CUDA_TRY(h, cudaMemcpy2DAsync(h->dSamples, st * sizeof(float), samples,
+                                           samplesPerTrace * sizeof(float),
+                                           samplesPerTrace * sizeof(float), n,
+                                           cudaMemcpyHostToDevice, h->stream));
+        HPSS_CUDA_TRY(h, cudaMemcpyAsync(h->dMid, midpoints, n * sizeof(float),
+                                         cudaMemcpyHostToDevice, h->stream));
+        HPSS_CUDA_TRY(h, cudaMemcpyAsync(h->dHoff, halfoffsets, n * sizeof(float),
+                                         cudaMemcpyHostToDevice, h->stream));
+        HPSS_CUDA_TRY(h, cudaMemcpyAsync(h->dHsq, hsq.data(), n * sizeof(float),
+                                         cudaMemcpyHostToDevice, h->stream));
+    }
+    if (storage != HPSS_STORAGE_FP32) {
+        HPSS_CUDA_TRY(h, alloc(reinterpret_cast<void **>(&h->dSamples16), n * st * sizeof(uint16_t)));
+        HPSS_CUDA_TRY(h, alloc(reinterpret_cast<void **>(&h->dScale), n * sizeof(float)));
+        HPSS_CUDA_TRY(h, launch_convert_storage(h->dSamples, h->dSamples16, h->dScale,
+                                                nTraces, samplesPerTrace, h->stride,
+                                                storage, h->stream));
+    }
+    // the host-side geometry vector `hsq` must outlive the async copy
+    HPSS_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    h->gatherReady = true;
+    return HPSS_OK;
+}
+
+hpss_status hpss_set_traveltime(hpss_handle h, int model, uint32_t nParams,
+                                const float *lower, const float *upper, float apm,
+                                float h0) {
+    if (!h) return HPSS_ERR_INVALID_ARGUMENT;
+    if (model < HPSS_MODEL_CMP || model > HPSS_MODEL_OCT)
+        return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "Invalid traveltime model");
+    if ((int)nParams != model_params(model) || !lower || !upper)
+        return set_error(h, HPSS_ERR_LOGIC,
+                         "model requires exact " + std::to_string(model_params(model)) +
+                             " lower and upper bounds.");
+    h->model = model;
+    h->np = nParams;
+    for (uint32_t j = 0; j < 3; j++) {
+        h->lower[j] = j < nParams ? lower[j] : 0.f;
+        h->upper[j] = j < nParams ? upper[j] : 0.f;
+    }
+    h->apm = apm;
+    h->h0 = model == HPSS_MODEL_OCT ? h0 : 0.f;
+    h->octCandsHost.clear();
+    return HPSS_OK;
+}
+
+hpss_status hpss_set_window(hpss_handle h, int tauIndexDisplacement) {
+    if (!h) return HPSS_ERR_INVALID_ARGUMENT;
+    if (tauIndexDisplacement < 0 || 2 * tauIndexDisplacement + 1 > kMaxWindow)
+        return set_error(h, HPSS_ERR_INVALID_ARGUMENT,
+                         "window 2*tau+1 must be in [1, 31] (MAX_WINDOW_SIZE)");
+    h->tau = tauIndexDisplacement;
+    return HPSS_OK;
+}
+
+hpss_status hpss_linear_search_device(hpss_handle h, const float *d_m0s, uint32_t nM0,
+                                      const uint32_t *granularity, int kernel,
+                                      float *d_out, hpss_stats *stats) {
+    if (!h) return HPSS_ERR_INVALID_ARGUMENT;
+    if (nM0 && (!d_m0s || !d_out))
+        return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "null device pointer");
+    return linear_search_impl(h, d_m0s, nM0, granularity, kernel, d_out, stats, false);
+}
+
+hpss_status hpss_linear_search(hpss_handle h, const float *m0s, uint32_t nM0,
+                               const uint32_t *granularity, int kernel, float *out,
+                               hpss_stats *stats) {
+    if (!h) return HPSS_ERR_INVALID_ARGUMENT;
+    if (nM0 && (!m0s || !out))
+        return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "null host pointer");
+    hpss_status rc = check_ready(h);
+    if (rc != HPSS_OK) return rc;
+    if (nM0 == 0) return HPSS_OK;
+    cudaSetDevice(h->device);
+    const size_t outElems = (size_t)nM0 * (2 + h->np) * h->S;
+    HPSS_CUDA_TRY(h, ensure(h, h->m0s, nM0 * sizeof(float)));
+    HPSS_CUDA_TRY(h, ensure(h, h->out, outElems * sizeof(float)));
+    HPSS_CUDA_TRY(h, cudaMemcpyAsync(h->m0s.p, m0s, nM0 * sizeof(float),
+                                     cudaMemcpyHostToDevice, h->stream));
+    rc = linear_search_impl(h, static_cast<float *>(h->m0s.p), nM0, granularity, kernel,
+                            static_cast<float *>(h->out.p), stats, true);
+    if (rc != HPSS_OK) return rc;
+    HPSS_CUDA_TRY(h, cudaMemcpyAsync(out, h->out.p, outElems * sizeof(float),
+                                     cudaMemcpyDeviceToHost, h->stream));
+    HPSS_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    return HPSS_OK;
+}
+
+hpss_status hpss_select_traces(hpss_handle h, const float *m0s, uint32_t nM0,
+                               uint32_t *counts) {
+    if (!h) return HPSS_ERR_INVALID_ARGUMENT;
+    if (nM0 && (!m0s || !counts))
+        return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "null host pointer");
+    if (!h->gatherReady || h->model < 0)
+        return set_error(h, HPSS_ERR_NOT_READY, "gather and traveltime must be set");
+    if (nM0 == 0) return HPSS_OK;
+    cudaSetDevice(h->device);
+    HPSS_CUDA_TRY(h, ensure(h, h->m0s, nM0 * sizeof(float)));
+    HPSS_CUDA_TRY(h, cudaMemcpyAsync(h->m0s.p, m0s, nM0 * sizeof(float),
+                                     cudaMemcpyHostToDevice, h->stream));
+    LsParams lp;
+    fill_line_params(h, lp);
+    lp.m0s = static_cast<float *>(h->m0s.p);
+    lp.nM0 = nM0;
+    hpss_status rc = run_selection(h, static_cast<float *>(h->m0s.p), nM0, lp);
+    if (rc != HPSS_OK) return rc;
+    HPSS_CUDA_TRY(h, cudaMemcpyAsync(counts, lp.selCount, nM0 * sizeof(uint32_t),
+                                     cudaMemcpyDeviceToHost, h->stream));
+    HPSS_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    return HPSS_OK;
+}
+
+hpss_status hpss_differential_evolution(hpss_handle h, const float *, uint32_t, uint32_t,
+                                        uint32_t, float, float, uint64_t, float *,
+                                        hpss_stats *) {
+    return set_error(h, HPSS_ERR_NOT_READY, "differential evolution not built yet");
+}
+
+hpss_status hpss_differential_evolution_device(hpss_handle h, const float *, uint32_t,
+                                               uint32_t, uint32_t, float, float, uint64_t,
+                                               float *, hpss_stats *) {
+    return set_error(h, HPSS_ERR_NOT_READY, "differential evolution not built yet");
+}
+
+hpss_status hpss_stretch_free(hpss_handle h, const float *, uint32_t, const float *, int,
+                              float *, hpss_stats *) {
+    return set_error(h, HPSS_ERR_NOT_READY, "stretch-free not built yet");
+}
+
+void *hpss_stream(hpss_handle h) { return h ? static_cast<void *>(h->stream) : nullptr; }
+
+size_t hpss_device_bytes(hpss_handle h) { return h ? h->deviceBytes : 0; }
+
+}  // extern "C"

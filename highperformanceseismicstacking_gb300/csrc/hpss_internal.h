@@ -1,0 +1,119 @@
+// hpss_internal.h -- internal declarations shared by the host and device
+// translation units of libhpss_gb300.so.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace hpss {
+
+constexpr int kModelCmp = 0;
+constexpr int kModelZocrs = 1;
+constexpr int kModelOct = 2;
+
+// MAX_WINDOW_SIZE (common/include/gpu/interface.h:10) is 32; odd windows up
+// to 31 are accepted.
+constexpr int kMaxWindow = 31;
+
+// Tuned kernel geometry: a CTA owns 32 consecutive t0 samples (one per lane)
+// of one midpoint, its 8 warps split the candidates.
+constexpr int kTileSamples = 32;
+constexpr int kTunedWarps = 8;
+constexpr int kTunedThreads = kTileSamples * kTunedWarps;
+constexpr int kPlainThreads = 128;
+
+// Device error word bits.
+constexpr uint32_t kErrSmemBounds = 1u << 0;
+constexpr uint32_t kErrSpanOverflow = 1u << 1;
+constexpr uint32_t kErrTimeout = 1u << 2;
+
+// Everything a linear-search (or stretch-free) launch reads and writes.
+struct LsParams {
+    // whole line, resident
+    const float *samples;     // [nTraces][stride] FP32 (when storage = FP32)
+    const uint16_t *samples16;// [nTraces][stride] BF16/FP16
+    const float *scale;       // [nTraces] FP16 per-trace scale
+    uint32_t stride;          // samples per row in memory (>= S, mult. of 8)
+    uint32_t S;
+    float dt;
+    int tau;
+    int w;
+    const float *mid;
+    const float *hoff;
+    const float *hsq;         // h*h in float, as copyOnlySelectedTracesToDevice
+    // per-midpoint selection
+    const float *m0s;
+    uint32_t nM0;
+    const uint32_t *selFirst; // [nM0]
+    const uint32_t *selCount; // [nM0]
+    const uint32_t *selIdx;   // nullptr: trace = first + q; else selIdx[first + q]
+    // candidates (reference parameter array layout, AoS [P][np])
+    const float *params;
+    uint32_t P;
+    int np;
+    // per-chunk parameter bounds for the tuned kernel: [nChunks][2*np]
+    const float *chunkBounds;
+    uint32_t chunkSize;
+    uint32_t nChunks;
+    float apm;
+    float h0;
+    // outputs
+    float *out;               // [nM0][2+np][S]
+    unsigned long long *notUsed; // [nM0] (may be null)
+    uint32_t *errorWord;
+    // stretch-free: prior parameters [nM0][np][S] (raw), n range
+    const float *prior;
+    int nmax;
+};
+
+struct Handle {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
+    std::string lastError;
+    // line
+    uint32_t nTraces = 0, S = 0, stride = 0;
+    float dt = 0;
+    int storage = 0;
+    bool gatherReady = false;
+    float *dSamples = nullptr;
+    uint16_t *dSamples16 = nullptr;
+    float *dScale = nullptr;
+    float *dMid = nullptr, *dHoff = nullptr, *dHsq = nullptr;
+    std::vector<float> hMid, hHoff;
+    // traveltime
+    int model = -1;
+    uint32_t np = 0;
+    float lower[3] = {0, 0, 0}, upper[3] = {0, 0, 0};
+    float apm = 0, h0 = 0;
+    int tau = -1;
+    // scratch (grown on demand, owned by the handle)
+    void *scratch = nullptr;
+    size_t scratchBytes = 0;
+    void *pinned = nullptr;
+    size_t pinnedBytes = 0;
+    size_t deviceBytes = 0;
+};
+
+// Launchers (ls_kernels.cu).
+cudaError_t launch_build_grid(int model, const float *lower, const float *inc,
+                              const uint32_t *gran, float *params, uint32_t P,
+                              cudaStream_t st);
+cudaError_t launch_chunk_bounds(const LsParams &p, float *bounds,
+                                cudaStream_t st);
+cudaError_t launch_ls_plain(const LsParams &p, cudaStream_t st);
+cudaError_t launch_ls_tuned(const LsParams &p, cudaStream_t st);
+cudaError_t launch_select_oct(const LsParams &p, const float *cands,
+                              uint32_t nCand, uint32_t *selIdx,
+                              uint32_t *selCount, const uint32_t *candFirst,
+                              const uint32_t *candCount, cudaStream_t st);
+cudaError_t launch_convert_storage(const float *src, uint16_t *dst,
+                                   float *scale, uint32_t nTraces, uint32_t S,
+                                   uint32_t stride, int storage,
+                                   cudaStream_t st);
+size_t tuned_smem_bytes();
+
+}  // namespace hpss

@@ -1,0 +1,206 @@
+// ls_common.cu -- small kernels around the linear search: candidate grid,
+// per-chunk candidate bounds, OCT trace selection, storage conversion.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include "hpss_device.cuh"
+#include "hpss_internal.h"
+
+namespace hpss {
+
+// Candidate grid, buildParameterArrayFor* (cmp/linear_search.cu:4-17,
+// zocrs/linear_search.cu:4-34, oct/linear_search.cu:4-28): first parameter
+// slowest; velocity v = min + idx*inc stored as 4/v^2 (fast-math division,
+// as the reference computes it on the device).
+__global__ void build_grid_kernel(int model, float l0, float l1, float l2,
+                                  float i0, float i1, float i2, uint32_t g0,
+                                  uint32_t g1, uint32_t g2, float *params,
+                                  uint32_t P) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P) return;
+    if (model == kModelCmp) {
+        float v = l0 + static_cast<float>(i) * i0;
+        params[i] = 4.0f / (v * v);
+    } else if (model == kModelZocrs) {
+        uint32_t iv = (i / (g1 * g2)) % g0;
+        uint32_t ia = (i / g2) % g1;
+        uint32_t ib = i % g2;
+        float v = l0 + static_cast<float>(iv) * i0;
+        float a = l1 + static_cast<float>(ia) * i1;
+        float b = l2 + static_cast<float>(ib) * i2;
+        params[3 * i] = 4.0f / (v * v);
+        params[3 * i + 1] = a;
+        params[3 * i + 2] = b;
+    } else {
+        uint32_t iv = (i / g1) % g0;
+        uint32_t is = i % g1;
+        float v = l0 + static_cast<float>(iv) * i0;
+        float s = l1 + static_cast<float>(is) * i1;
+        params[2 * i] = 4.0f / (v * v);
+        params[2 * i + 1] = s;
+    }
+}
+
+cudaError_t launch_build_grid(int model, const float *lower, const float *inc,
+                              const uint32_t *gran, float *params, uint32_t P,
+                              cudaStream_t st) {
+    uint32_t blocks = (P + 255) / 256;
+    build_grid_kernel<<<blocks, 256, 0, st>>>(
+        model, lower[0], lower[1], lower[2], inc[0], inc[1], inc[2], gran[0],
+        gran[1], gran[2], params, P);
+    return cudaGetLastError();
+}
+
+// Min / max of every parameter over each chunk of `chunkSize` consecutive
+// candidates: bounds[k][2*j] = min, bounds[k][2*j+1] = max.
+__global__ void chunk_bounds_kernel(const float *params, uint32_t P, int np,
+                                    uint32_t chunkSize, uint32_t nChunks,
+                                    float *bounds) {
+    uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nChunks) return;
+    uint32_t p0 = k * chunkSize;
+    uint32_t p1 = min(P, p0 + chunkSize);
+    for (int j = 0; j < np; j++) {
+        float lo = INFINITY, hi = -INFINITY;
+        for (uint32_t p = p0; p < p1; p++) {
+            float v = params[(size_t)p * np + j];
+            lo = fminf(lo, v);
+            hi = fmaxf(hi, v);
+        }
+        bounds[(size_t)k * 2 * np + 2 * j] = lo;
+        bounds[(size_t)k * 2 * np + 2 * j + 1] = hi;
+    }
+}
+
+cudaError_t launch_chunk_bounds(const LsParams &p, float *bounds,
+                                cudaStream_t st) {
+    uint32_t blocks = (p.nChunks + 127) / 128;
+    chunk_bounds_kernel<<<blocks, 128, 0, st>>>(p.params, p.P, p.np,
+                                                p.chunkSize, p.nChunks, bounds);
+    return cudaGetLastError();
+}
+
+// OCT trace selection (oct/linear_search.cu:155-192): a trace is used for m0
+// if some (t0 sample, sampled candidate) gives a valid displaced midpoint
+// within apm of the trace's midpoint.  One warp per candidate trace, lanes
+// over the sampled candidates, early exit on the first hit; then an
+// order-preserving compaction of the selected trace indices per midpoint.
+// candFirst/candCount: per-midpoint range of traces that can pass at all
+// (|m - m0| <= apm + sqrt(h^2 + h0^2), prefiltered on the host).
+__global__ void select_oct_kernel(LsParams a, const float *cands,
+                                  uint32_t nCand, const uint32_t *candFirst,
+                                  const uint32_t *candCount, uint32_t *selIdx,
+                                  uint32_t *selCount) {
+    const uint32_t mi = blockIdx.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nWarps = blockDim.x >> 5;
+    const float m0 = a.m0s[mi];
+    const uint32_t first = candFirst[mi], count = candCount[mi];
+    const uint32_t outBase = a.selFirst[mi];
+    __shared__ uint32_t shCount;
+    __shared__ uint32_t shFlags[256];
+    if (threadIdx.x == 0) shCount = 0;
+    __syncthreads();
+    // process candidate traces in rounds of nWarps, keeping output order
+    for (uint32_t base = 0; base < count; base += nWarps) {
+        uint32_t q = base + warp;
+        bool used = false;
+        if (q < count) {
+            uint32_t ti = first + q;
+            float m = a.mid[ti], h = a.hoff[ti];
+            for (uint32_t s = 0; s < a.S && !used; s++) {
+                float t0 = static_cast<float>(s) * a.dt;
+                for (uint32_t p0 = 0; p0 < nCand && !used; p0 += 32) {
+                    uint32_t p = p0 + lane;
+                    bool hit = false;
+                    if (p < nCand) {
+                        float mh;
+                        int e = oct_displaced_midpoint(h, a.h0, t0, m0,
+                                                       cands[2 * p],
+                                                       cands[2 * p + 1], &mh);
+                        hit = (e == DE_OK && fabsf(m - mh) <= a.apm);
+                    }
+                    used = __any_sync(0xffffffffu, hit);
+                }
+            }
+        }
+        if (lane == 0) shFlags[warp] = used ? 1u : 0u;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (int w = 0; w < nWarps && base + w < count; w++) {
+                if (shFlags[w]) selIdx[outBase + shCount++] = first + base + w;
+            }
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) selCount[mi] = shCount;
+}
+
+cudaError_t launch_select_oct(const LsParams &p, const float *cands,
+                              uint32_t nCand, uint32_t *selIdx,
+                              uint32_t *selCount, const uint32_t *candFirst,
+                              const uint32_t *candCount, cudaStream_t st) {
+    if (p.nM0 == 0) return cudaSuccess;
+    select_oct_kernel<<<p.nM0, 256, 0, st>>>(p, cands, nCand, candFirst,
+                                             candCount, selIdx, selCount);
+    return cudaGetLastError();
+}
+
+// FP32 -> BF16 / FP16 (+ per-trace scale for FP16) storage conversion.
+__global__ void convert_storage_kernel(const float *src, uint16_t *dst,
+                                       float *scale, uint32_t nTraces,
+                                       uint32_t S, uint32_t stride,
+                                       int storage) {
+    uint32_t tr = blockIdx.x;
+    if (tr >= nTraces) return;
+    const float *row = src + (size_t)tr * stride;
+    __shared__ float shMax[32];
+    float mx = 0.f;
+    for (uint32_t i = threadIdx.x; i < S; i += blockDim.x)
+        mx = fmaxf(mx, fabsf(row[i]));
+    for (int o = 16; o; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0) shMax[threadIdx.x >> 5] = mx;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        float v = threadIdx.x < (blockDim.x >> 5) ? shMax[threadIdx.x] : 0.f;
+        for (int o = 16; o; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+        if (threadIdx.x == 0) shMax[0] = v;
+    }
+    __syncthreads();
+    // FP16: scale the trace so its peak maps to 2^14 (inside FP16 range with
+    // headroom); the kernel multiplies back by scale.
+    float sc = 1.f;
+    if (storage == 2) {
+        float peak = shMax[0];
+        sc = peak > 0.f ? peak / 16384.f : 1.f;
+        if (threadIdx.x == 0) scale[tr] = sc;
+    } else if (threadIdx.x == 0 && scale) {
+        scale[tr] = 1.f;
+    }
+    float inv = 1.f / sc;
+    uint16_t *out = dst + (size_t)tr * stride;
+    for (uint32_t i = threadIdx.x; i < stride; i += blockDim.x) {
+        float v = i < S ? row[i] : 0.f;
+        uint16_t bits;
+        if (storage == 1) {
+            __nv_bfloat16 b = __float2bfloat16_rn(v);
+            bits = *reinterpret_cast<uint16_t *>(&b);
+        } else {
+            __half hv = __float2half_rn(v * inv);
+            bits = *reinterpret_cast<uint16_t *>(&hv);
+        }
+        out[i] = bits;
+    }
+}
+
+cudaError_t launch_convert_storage(const float *src, uint16_t *dst,
+                                   float *scale, uint32_t nTraces, uint32_t S,
+                                   uint32_t stride, int storage,
+                                   cudaStream_t st) {
+    if (nTraces == 0) return cudaSuccess;
+    convert_storage_kernel<<<nTraces, 256, 0, st>>>(src, dst, scale, nTraces,
+                                                    S, stride, storage);
+    return cudaGetLastError();
+}
+
+}  // namespace hpss

@@ -1,0 +1,204 @@
+/*
+ * hpss.h -- C ABI of the GB300 semblance engine (libhpss_gb300.so).
+ *
+ * This is the drop-in boundary for the semblance hot path of
+ * HighPerformanceSeismicStacking.  In the reference, the path sits behind the
+ * C++ ComputeAlgorithm family (common/include/semblance/algorithm/
+ * ComputeAlgorithm.hpp:29-100) whose CUDA subclasses launch the kernels
+ * (cuda/src/semblance/algorithm/Cuda*Algorithm.cu).  Each entry point below
+ * names the reference member it replaces.  All signatures use plain C types;
+ * no exception crosses the boundary; every call returns an hpss_status
+ * (0 = OK, < 0 = error, message via hpss_last_error).
+ *
+ * Threading: one handle per host thread (like one ComputeAlgorithm per
+ * device thread in SingleHostRunner.cpp:49-106).  A handle owns all the
+ * device memory it uses and one CUDA stream.
+ *
+ * Data conventions (as the reference):
+ *  - traces are passed sorted by (midpoint, half-offset) ascending, the order
+ *    Gather::readGatherFromFile leaves them in (Gather.cpp:117, Trace.cpp:63);
+ *  - a result block for one midpoint is [(2 + nParams)][S] floats, SoA:
+ *    semblance, stack, then the parameters (velocity, A, B | velocity, slope),
+ *    exactly ComputeAlgorithm::getComputedResults (ComputeAlgorithm.hpp:84);
+ *  - linear-search candidates follow buildParameterArrayFor*: the first
+ *    parameter varies slowest, velocity is searched uniformly in v and stored
+ *    as 4/v^2, the upper bound is excluded (step = (U - L) / G).
+ */
+#ifndef HPSS_H
+#define HPSS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int hpss_status;
+
+/* Status codes.  The reference throws C++ exceptions; the mapping is:
+ * invalid_argument -> HPSS_ERR_INVALID_ARGUMENT, logic_error (wrong number of
+ * bounds / granularities, CudaComputeAlgorithmBuilder.cu:26-31) ->
+ * HPSS_ERR_LOGIC, runtime_error from CUDA_ASSERT (CudaUtils.cu:8-15) ->
+ * HPSS_ERR_CUDA / HPSS_ERR_NO_DEVICE. */
+#define HPSS_OK 0
+#define HPSS_ERR_INVALID_ARGUMENT (-1)
+#define HPSS_ERR_LOGIC (-2)
+#define HPSS_ERR_CUDA (-3)
+#define HPSS_ERR_NO_DEVICE (-4)
+#define HPSS_ERR_OUT_OF_MEMORY (-5)
+#define HPSS_ERR_NOT_READY (-6)
+#define HPSS_ERR_TIMEOUT (-7)
+#define HPSS_ERR_DEVICE_CHECK (-8)
+
+/* traveltime_t (common/include/capability.h:3-7). */
+#define HPSS_MODEL_CMP 0
+#define HPSS_MODEL_ZOCRS 1
+#define HPSS_MODEL_OCT 2
+
+/* Device storage of the trace amplitudes.  FP32 is what the reference
+ * stores; BF16 / FP16 halve the bytes (FP16 with a per-trace FP32 scale).
+ * Interpolation and all sums stay FP32. */
+#define HPSS_STORAGE_FP32 0
+#define HPSS_STORAGE_BF16 1
+#define HPSS_STORAGE_FP16 2
+
+/* Kernel family: PLAIN is the one-(sample, candidate)-per-thread FP32 form of
+ * the reference kernels with the argmax fused (its arithmetic is the
+ * reference's, operation for operation); TUNED stages each gather's trace
+ * windows in shared memory with bulk async copies and shares them across the
+ * candidates of a CTA. */
+#define HPSS_KERNEL_PLAIN 0
+#define HPSS_KERNEL_TUNED 1
+
+typedef struct hpss_handle_s *hpss_handle;
+
+/* Per-call statistics (StatisticResult, common/include/semblance/result/
+ * StatisticResult.hpp:8-15, plus the evaluation count of the metric). */
+typedef struct {
+    double evals;             /* (m0, t0, candidate, selected trace) tuples */
+    double not_used;          /* OCT traces skipped for their displaced midpoint */
+    double selected_traces;   /* sum over midpoints of selected traces */
+    double kernel_ms;         /* device time of the compute launches */
+    double selection_ms;      /* device time of trace selection */
+    uint32_t device_error;    /* device error word (0 = none) */
+    uint32_t reserved;
+} hpss_stats;
+
+/* Device selection and handle creation.
+ * Replaces CudaDeviceContext(devId) + activate()
+ * (cuda/src/semblance/data/CudaDeviceContext.cu:10-17). */
+hpss_status hpss_create(int device, hpss_handle *out);
+hpss_status hpss_destroy(hpss_handle h);
+
+/* Message of the last failed call on this handle (thread-local if h is
+ * NULL: errors of hpss_create). */
+const char *hpss_last_error(hpss_handle h);
+
+/* Library version string. */
+const char *hpss_version(void);
+
+/* Number of visible CUDA devices (CudaSingleHostRunner::getNumOfDevices,
+ * cuda/src/execution/CudaSingleHostRunner.cu:18-29). */
+hpss_status hpss_device_count(int *count);
+
+/* Upload the whole line once: amplitudes [nTraces][S] (row-major, FP32),
+ * midpoints and half-offsets [nTraces].  Replaces
+ * ComputeAlgorithm::copyGatherDataToDevice (ComputeAlgorithm.cpp:31-61) and
+ * the per-midpoint copyOnlySelectedTracesToDevice (ComputeAlgorithm.cpp
+ * :107-153): traces stay resident and are selected on the device.
+ * `storage` is one of HPSS_STORAGE_*.  Host pointers; page-locked memory is
+ * copied asynchronously, pageable memory synchronously. */
+hpss_status hpss_upload_gather(hpss_handle h, const float *samples,
+                               const float *midpoints,
+                               const float *halfoffsets, uint32_t nTraces,
+                               uint32_t samplesPerTrace, float dtInSeconds,
+                               int storage);
+
+/* Traveltime model and its parameter bounds (Traveltime::update*BoundFor
+ * Parameter, common/src/traveltime/Traveltime.cpp:39-53, built by
+ * TraveltimeBuilder, TraveltimeBuilder.cpp:24-106).  nParams must be 1
+ * (CMP), 3 (ZO-CRS: velocity, A, B -- A and B bounds as the builder derived
+ * them) or 2 (OCT: velocity, slope).  apm is Gather::getApm (used by ZO-CRS
+ * and OCT selection, OCT evaluation); h0 is the OCT reference half-offset. */
+hpss_status hpss_set_traveltime(hpss_handle h, int model, uint32_t nParams,
+                                const float *lower, const float *upper,
+                                float apm, float h0);
+
+/* Semblance window: tauIndexDisplacement = (int)(tau / dt), window
+ * w = 2 * tau + 1 (Gather.cpp:75-76).  w must be <= 31
+ * (MAX_WINDOW_SIZE, common/include/gpu/interface.h:10). */
+hpss_status hpss_set_window(hpss_handle h, int tauIndexDisplacement);
+
+/* Linear search over nM0 midpoints in one call.
+ * Replaces LinearSearchAlgorithm::computeSemblanceAndParametersForMidpoint
+ * (LinearSearchAlgorithm.cpp:26-57) with the CUDA steps of
+ * CudaLinearSearchAlgorithm (selectTracesToBeUsedForMidpoint :225-324,
+ * computeSemblanceAtGpuForMidpoint :35-163, initializeParameters :165-223),
+ * batched over midpoints.  granularity[nParams] as the --granularity flag.
+ * out (host): [nM0][2 + nParams][S].  Synchronous. */
+hpss_status hpss_linear_search(hpss_handle h, const float *m0s, uint32_t nM0,
+                               const uint32_t *granularity, int kernel,
+                               float *out, hpss_stats *stats);
+
+/* Same computation with device-resident midpoints and output (d_m0s,
+ * d_out are device pointers).  Enqueued on the handle's stream; returns
+ * without synchronising.  stats may be NULL (its timing fields are then not
+ * filled). */
+hpss_status hpss_linear_search_device(hpss_handle h, const float *d_m0s,
+                                      uint32_t nM0,
+                                      const uint32_t *granularity, int kernel,
+                                      float *d_out, hpss_stats *stats);
+
+/* Differential evolution (DE/rand/1/bin) per (m0, t0) sample.
+ * Replaces DifferentialEvolutionAlgorithm::computeSemblanceAndParametersFor
+ * Midpoint (DifferentialEvolutionAlgorithm.cpp:21-81) and the kernels of
+ * cuda/src/semblance/kernel/common/differential_evolution.cu.  F and CR are
+ * runtime values (the reference compiles F = 0.85, CR = 0.5,
+ * interface.h:5-6); `generations` counts the initial evaluation as the
+ * reference does.  The random stream is a counter-based generator keyed by
+ * `seed` (the reference's curand stream is seeded from time(NULL)).
+ * out (host): [nM0][2 + nParams][S] with RAW parameters (velocity, not 4/v^2),
+ * as selectBestIndividualsFor* write them. */
+hpss_status hpss_differential_evolution(hpss_handle h, const float *m0s,
+                                        uint32_t nM0, uint32_t population,
+                                        uint32_t generations, float F,
+                                        float CR, uint64_t seed, float *out,
+                                        hpss_stats *stats);
+
+/* Device-pointer variant of hpss_differential_evolution (async). */
+hpss_status hpss_differential_evolution_device(
+    hpss_handle h, const float *d_m0s, uint32_t nM0, uint32_t population,
+    uint32_t generations, float F, float CR, uint64_t seed, float *d_out,
+    hpss_stats *stats);
+
+/* Stretch-free stack: for n in [-nmax, nmax] the model parameters chosen at
+ * sample s - n by a previous search (params: host [nM0][nParams][S], RAW
+ * parameters, velocity first -- the layout of the reference's result files
+ * read by StretchFreeAlgorithm::readNonStretchedFreeParameterFromFile,
+ * StretchFreeAlgorithm.cpp:101-125) are applied with a time shift n*dt.
+ * Replaces StretchFreeAlgorithm::computeSemblanceAndParametersForMidpoint
+ * (StretchFreeAlgorithm.cpp:23-50) and CudaStretchFreeAlgorithm
+ * (CudaStretchFreeAlgorithm.cu:28-200).  out: [nM0][3][S] = semblance,
+ * stack, best n. */
+hpss_status hpss_stretch_free(hpss_handle h, const float *m0s, uint32_t nM0,
+                              const float *params, int nmax, float *out,
+                              hpss_stats *stats);
+
+/* Selected-trace count per midpoint, as selectTracesToBeUsedForMidpoint
+ * computes it (filteredTracesCount).  For OCT the selection uses the
+ * linear-search sampling rule (oct/linear_search.cu:155-192). */
+hpss_status hpss_select_traces(hpss_handle h, const float *m0s, uint32_t nM0,
+                               uint32_t *counts);
+
+/* The CUDA stream the handle launches on (cudaStream_t), for callers that
+ * order their own work or record events against it. */
+void *hpss_stream(hpss_handle h);
+
+/* Bytes of device memory currently held by the handle. */
+size_t hpss_device_bytes(hpss_handle h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HPSS_H */

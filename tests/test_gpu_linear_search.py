@@ -1,0 +1,159 @@
+"""Linear-search parity on the GPU, through the C ABI.
+
+* plain kernel vs the oracle (FP32 restatement, IEEE): semblance and stack
+  within tolerance, chosen candidate identical except near-ties (counted);
+* tuned kernel vs plain kernel: identical bits (same per-candidate
+  arithmetic, same trace order);
+* FP64 oracle: chosen parameters agree on >= 99.9% of samples;
+* edge cases the reference has: no selected trace, windows at the trace
+  edges, window sizes 1..15, constant traces (semblance exactly 1, lowest
+  index wins ties), argument errors.
+"""
+import numpy as np
+import pytest
+
+from highperformanceseismicstacking_gb300 import capi, synthetic
+from oracle import oracle
+from parity import Report, compare_block
+
+pytestmark = pytest.mark.gpu
+
+
+def _setup(eng, line, model, lower, upper, tau, apm=0.0, h0=0.0):
+    eng.upload_gather(line.samples, line.midpoints, line.halfoffsets, float(line.dt))
+    eng.set_traveltime(model, lower, upper, apm, h0)
+    eng.set_window(tau)
+
+
+def _check_against_oracle(model, line, m0s, got, lower, upper, gran, tau, apm=0.0, h0=0.0,
+                          cands=None, precision="f32"):
+    """Engine blocks vs the oracle for every midpoint; tolerances in parity.py."""
+    params = oracle.build_grid(model, lower, upper, gran)
+    S = line.samples_per_trace
+    rep = Report()
+    for i, m0 in enumerate(m0s):
+        mask = oracle.select(model, line.midpoints, line.halfoffsets, m0, apm, h0, S,
+                             float(line.dt), cands)
+        sel = np.nonzero(mask)[0].astype(np.uint32)
+        if sel.size == 0:
+            assert np.all(got[i] == 0)
+            continue
+        sem, stk, _ = oracle.ls_eval(model, line.samples, line.midpoints, line.halfoffsets,
+                                     sel, m0, float(line.dt), tau, params, apm, h0,
+                                     precision=precision)
+        rms = float(np.sqrt(np.mean(line.samples[sel] ** 2)))
+        compare_block(rep, got[i], sem, stk, params, rms)
+    rep.check()
+    return rep
+
+
+@pytest.fixture(scope="module")
+def c1_line():
+    return synthetic.WORKLOADS["cmp-small"].make_line()
+
+
+def test_cmp_small_line_plain_vs_oracle_and_tuned(engine, c1_line):
+    w = synthetic.WORKLOADS["cmp-small"]
+    tau = 2
+    _setup(engine, c1_line, "cmp", w.lower, w.upper, tau)
+    m0s = np.concatenate([c1_line.cdp_midpoints, [np.float32(12345.0)]])
+    plain, st_p = engine.linear_search(m0s, w.granularity, "plain")
+    tuned, st_t = engine.linear_search(m0s, w.granularity, "tuned")
+    assert st_t["device_error"] == 0 and st_p["device_error"] == 0
+    assert np.array_equal(plain, tuned)
+    assert np.all(plain[-1] == 0)          # midpoint without traces: zeros
+    assert st_p["evals"] == 50 * 24 * 1000 * 101
+    _check_against_oracle("cmp", c1_line, m0s, plain, w.lower, w.upper, w.granularity, tau)
+
+
+@pytest.mark.parametrize("tau", [0, 1, 3, 5, 7])
+def test_cmp_window_sizes_tuned_equals_plain(engine, c1_line, tau):
+    w = synthetic.WORKLOADS["cmp-small"]
+    _setup(engine, c1_line, "cmp", w.lower, w.upper, tau)
+    m0s = c1_line.cdp_midpoints[:6]
+    plain, _ = engine.linear_search(m0s, w.granularity, "plain")
+    tuned, st = engine.linear_search(m0s, w.granularity, "tuned")
+    assert st["device_error"] == 0
+    assert np.array_equal(plain, tuned)
+
+
+def test_cmp_fp64_oracle_agreement(engine, c1_line):
+    w = synthetic.WORKLOADS["cmp-small"]
+    _setup(engine, c1_line, "cmp", w.lower, w.upper, 2)
+    m0s = c1_line.cdp_midpoints[:5]
+    got, _ = engine.linear_search(m0s, w.granularity, "tuned")
+    rep = _check_against_oracle("cmp", c1_line, m0s, got, w.lower, w.upper, w.granularity, 2,
+                                precision="f64")
+    # chosen parameters agree with the FP64 oracle on >= 99.9% of samples
+    assert rep.mismatches <= 0.001 * rep.samples, rep.summary()
+
+
+def test_constant_traces_known_answer(engine):
+    S, n = 256, 8
+    mid = np.full(n, 2000.0, np.float32)
+    hoff = (np.arange(n) * 100 + 50).astype(np.float32)
+    smp = np.ones((n, S), np.float32)
+    engine.upload_gather(smp, mid, hoff, 0.004)
+    engine.set_traveltime("cmp", [2000.0], [4000.0])
+    engine.set_window(2)
+    for k in ("plain", "tuned"):
+        out, _ = engine.linear_search([2000.0], [16], k)
+        # mid-trace samples: semblance exactly 1, stack 1, lowest index (v = 2000)
+        assert np.all(out[0, 0, 60:150] == 1.0)
+        assert np.all(out[0, 1, 60:150] == 1.0)
+        np.testing.assert_allclose(out[0, 2, 60:150], 2000.0, rtol=1e-6)
+        # t0 = 0: every window starts before sample 0 -> semblance 0, first candidate
+        assert out[0, 0, 0] == 0.0
+
+
+def test_zocrs_small_line(engine):
+    line = synthetic.structured_line(n_cmp=30, fold_range=(8, 14), h_max=1000, ns=300,
+                                     dt_us=4000, n_reflectors=4, f=20.0, snr=5.0, seed=11)
+    a, b = synthetic.zocrs_bounds(1414.2136, 2000.0, 90.0, 0.05)
+    lower, upper, gran = [1414.2136, -a, -b], [6324.5553, a, b], [5, 5, 5]
+    apm, tau = 125.0, 2
+    _setup(engine, line, "zocrs", lower, upper, tau, apm)
+    m0s = line.cdp_midpoints[::3]
+    plain, st_p = engine.linear_search(m0s, gran, "plain")
+    tuned, st_t = engine.linear_search(m0s, gran, "tuned")
+    assert st_t["device_error"] == 0
+    assert np.array_equal(plain, tuned)
+    counts = engine.select_traces(m0s)
+    for i, m0 in enumerate(m0s):
+        assert counts[i] == oracle.select("zocrs", line.midpoints, line.halfoffsets, m0,
+                                          apm).sum()
+    _check_against_oracle("zocrs", line, m0s, plain, lower, upper, gran, tau, apm)
+
+
+@pytest.mark.parametrize("h0", [0.0, 300.0])
+def test_oct_small_line(engine, h0):
+    line = synthetic.structured_line(n_cmp=16, fold_range=(4, 8), h_max=800, ns=200,
+                                     dt_us=4000, n_reflectors=3, f=20.0, snr=8.0, seed=12)
+    lower, upper, gran = [1200.0, -1e-3], [5000.0, 1e-3], [6, 5]
+    apm, tau = 60.0, 2
+    _setup(engine, line, "oct", lower, upper, tau, apm, h0)
+    m0s = line.cdp_midpoints[::4]
+    cands = oracle.oct_selection_candidates(lower, upper)
+    counts = engine.select_traces(m0s)
+    for i, m0 in enumerate(m0s):
+        assert counts[i] == oracle.select("oct", line.midpoints, line.halfoffsets, m0, apm, h0,
+                                          line.samples_per_trace, float(line.dt), cands).sum()
+    plain, st_p = engine.linear_search(m0s, gran, "plain")
+    tuned, st_t = engine.linear_search(m0s, gran, "tuned")
+    assert st_t["device_error"] == 0
+    assert np.array_equal(plain, tuned)
+    assert st_p["not_used"] == st_t["not_used"]
+    _check_against_oracle("oct", line, m0s, plain, lower, upper, gran, tau, apm, h0, cands)
+
+
+def test_argument_errors(engine, c1_line):
+    with pytest.raises(capi.HpssError) as e:
+        engine.set_traveltime("zocrs", [1000.0], [2000.0])
+    assert e.value.code == -2            # logic_error: bound count
+    with pytest.raises(capi.HpssError) as e:
+        engine.set_window(16)            # w = 33 > MAX_WINDOW_SIZE
+    assert e.value.code == -1
+    rev = c1_line.midpoints[::-1].copy()
+    with pytest.raises(capi.HpssError) as e:
+        engine.upload_gather(c1_line.samples, rev, c1_line.halfoffsets, float(c1_line.dt))
+    assert e.value.code == -1
