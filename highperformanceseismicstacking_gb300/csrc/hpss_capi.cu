@@ -9,6 +9,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <random>
@@ -26,11 +27,11 @@ cudaError_t launch_select_range(const float *mid, uint32_t n, const float *m0s,
 cudaError_t launch_exclusive_scan(const uint32_t *count, uint32_t *first,
                                   uint32_t n, cudaStream_t st);
 cudaError_t launch_ls_tuned_cmp(const LsParams &p, uint32_t grid, uint32_t tiles,
-                                uint32_t nUnits, cudaStream_t st);
+                                uint32_t nUnits, cudaStream_t st, int pairs);
 cudaError_t launch_ls_tuned_zocrs(const LsParams &p, uint32_t grid, uint32_t tiles,
-                                  uint32_t nUnits, cudaStream_t st);
+                                  uint32_t nUnits, cudaStream_t st, int pairs);
 cudaError_t launch_ls_tuned_oct(const LsParams &p, uint32_t grid, uint32_t tiles,
-                                uint32_t nUnits, cudaStream_t st);
+                                uint32_t nUnits, cudaStream_t st, int pairs);
 size_t tuned_stage_floats();
 }  // namespace hpss
 
@@ -271,7 +272,15 @@ hpss_status linear_search_impl(hpss_handle h, const float *d_m0s, uint32_t nM0,
     lp.params = static_cast<float *>(h->params.p);
     HPSS_CUDA_TRY(h, launch_build_grid(h->model, low, inc, gran,
                                        static_cast<float *>(h->params.p), lp.P, h->stream));
-    lp.chunkSize = kTunedWarps * 4;
+    // candidates per thread of the tuned kernel: 2 * pairs (CMP / ZO-CRS),
+    // 4 (OCT); HPSS_LS_PAIRS overrides the pair count (1, 2 or 4)
+    int pairs = 2;
+    if (const char *env = std::getenv("HPSS_LS_PAIRS")) {
+        int v = std::atoi(env);
+        if (v == 1 || v == 2 || v == 4) pairs = v;
+    }
+    const int perThread = h->model == HPSS_MODEL_OCT ? 4 : 2 * pairs;
+    lp.chunkSize = kTunedWarps * perThread;
     lp.nChunks = (lp.P + lp.chunkSize - 1) / lp.chunkSize;
     HPSS_CUDA_TRY(h, ensure(h, h->chunkBounds, (size_t)lp.nChunks * 2 * h->np * sizeof(float)));
     lp.chunkBounds = static_cast<float *>(h->chunkBounds.p);
@@ -297,9 +306,9 @@ hpss_status linear_search_impl(hpss_handle h, const float *d_m0s, uint32_t nM0,
             uint64_t units = (uint64_t)nM0 * tiles;
             uint32_t grid = (uint32_t)std::min<uint64_t>(units, (uint64_t)num_sms(h) * 2);
             cudaError_t e;
-            if (h->model == HPSS_MODEL_CMP) e = launch_ls_tuned_cmp(lp, grid, tiles, (uint32_t)units, h->stream);
-            else if (h->model == HPSS_MODEL_ZOCRS) e = launch_ls_tuned_zocrs(lp, grid, tiles, (uint32_t)units, h->stream);
-            else e = launch_ls_tuned_oct(lp, grid, tiles, (uint32_t)units, h->stream);
+            if (h->model == HPSS_MODEL_CMP) e = launch_ls_tuned_cmp(lp, grid, tiles, (uint32_t)units, h->stream, pairs);
+            else if (h->model == HPSS_MODEL_ZOCRS) e = launch_ls_tuned_zocrs(lp, grid, tiles, (uint32_t)units, h->stream, pairs);
+            else e = launch_ls_tuned_oct(lp, grid, tiles, (uint32_t)units, h->stream, pairs);
             HPSS_CUDA_TRY(h, e);
         }
     }

@@ -303,6 +303,282 @@ ls_tuned_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
     }
 }
 
+// ---------------------------------------------------------------------------
+// Branch-free variant for the CMP and ZO-CRS models.
+//
+// Per trace, the window position of every candidate of the thread is computed
+// first (independent chains); a window outside the trace is redirected to a
+// zero pad at the start of shared memory, so it adds exactly 0 to every sum
+// and is not counted in `used` -- the same sums as the reference's skip.
+// The window arithmetic runs on candidate pairs with Blackwell's packed
+// f32x2 FMA / ADD (per lane the same IEEE operation as the scalar form), so a
+// warp instruction advances two candidates.
+// ---------------------------------------------------------------------------
+constexpr int kZeroPad = 32;  // floats of zeros before the staged spans
+
+struct __align__(16) TraceMeta2 {
+    int base;   // shared-memory index of sample 0 of the trace
+    float hsq;  // h * h
+    float dm;   // m - m0 (ZO-CRS)
+    int len;    // staged samples (0: skip the trace)
+};
+
+struct Tuned2Smem {
+    float y[kStageFloats];
+    TraceMeta2 meta[kTunedThreads];
+    int lo[kTunedThreads];
+    int warpSum[kTunedWarps];
+    float bestS[kTunedWarps][kTileSamples];
+    float bestK[kTunedWarps][kTileSamples];
+    uint32_t bestP[kTunedWarps][kTileSamples];
+};
+
+__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
+
+template <int MODEL, int W, int NP>
+__global__ void __launch_bounds__(kTunedThreads, 2)
+ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
+    constexpr int R = 2 * NP;
+    extern __shared__ __align__(16) unsigned char smemRaw[];
+    Tuned2Smem &sm = *reinterpret_cast<Tuned2Smem *>(smemRaw);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int np = a.np;
+    const int S = (int)a.S, tau = a.tau;
+    const float2 kNeg1 = f2(-1.f, -1.f);
+    constexpr int kLastBase = kStageFloats - W - 1;
+
+    if (threadIdx.x < kZeroPad) sm.y[threadIdx.x] = 0.f;
+
+    for (uint32_t unit = blockIdx.x; unit < nUnits; unit += gridDim.x) {
+        const uint32_t mi = unit / tiles;
+        const int s0 = (int)(unit % tiles) * kTileSamples;
+        const int s = s0 + lane;
+        const int sc = min(s, S - 1);
+        const float t0 = static_cast<float>(sc) * a.dt;
+        const float t0a = static_cast<float>(s0) * a.dt;
+        const float t0b = static_cast<float>(min(s0 + kTileSamples - 1, S - 1)) * a.dt;
+        const float m0 = a.m0s[mi];
+        const uint32_t first = a.selFirst[mi], cnt = a.selCount[mi];
+        float *out = a.out + (size_t)mi * (2 + np) * a.S;
+
+        if (cnt == 0) {
+            if (warp < 2 + np && s < S) out[(size_t)warp * a.S + s] = 0.f;
+            continue;
+        }
+
+        float best = -1.f, bestStack = 0.f;
+        uint32_t bestP = 0xffffffffu;
+
+        for (uint32_t chunk = 0; chunk < a.nChunks; chunk++) {
+            float cc[R], c1[R], c2[R];
+            bool valid[R];
+#pragma unroll
+            for (int r = 0; r < R; r++) {
+                uint32_t p = chunk * a.chunkSize + warp * R + r;
+                valid[r] = p < a.P;
+                uint32_t pc = valid[r] ? p : a.P - 1;
+                const float *pr = a.params + (size_t)pc * np;
+                cc[r] = pr[0];
+                c1[r] = MODEL == kModelZocrs ? pr[1] : 0.f;
+                c2[r] = MODEL == kModelZocrs ? pr[2] : 0.f;
+            }
+            const float *cb = a.chunkBounds + (size_t)chunk * 2 * np;
+            float cbl[6];
+#pragma unroll
+            for (int j = 0; j < 6; j++) cbl[j] = j < 2 * np ? cb[j] : 0.f;
+
+            float2 num[NP][W], lin[NP], den[NP];
+            unsigned used[R];
+#pragma unroll
+            for (int q = 0; q < NP; q++) {
+#pragma unroll
+                for (int j = 0; j < W; j++) num[q][j] = f2(0.f, 0.f);
+                lin[q] = den[q] = f2(0.f, 0.f);
+            }
+#pragma unroll
+            for (int r = 0; r < R; r++) used[r] = 0;
+
+            for (uint32_t q0 = 0; q0 < cnt;) {
+                __syncthreads();
+                const uint32_t q = q0 + threadIdx.x;
+                int lo = 0, len = 0;
+                float tm = 0.f, thsq = 0.f;
+                if (q < cnt) {
+                    const uint32_t ti = a.selIdx ? a.selIdx[first + q] : first + q;
+                    tm = a.mid[ti];
+                    thsq = a.hsq[ti];
+                    trace_span<MODEL>(a, cbl, m0, t0a, t0b, tm, thsq, &lo, &len);
+                }
+                int incl = len;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    int v = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= o) incl += v;
+                }
+                if (lane == 31) sm.warpSum[warp] = incl;
+                __syncthreads();
+                int woff = kZeroPad;
+#pragma unroll
+                for (int wv = 0; wv < kTunedWarps; wv++)
+                    woff += wv < warp ? sm.warpSum[wv] : 0;
+                const int off = woff + incl - len;
+                const bool fits = (q < cnt) && (off + len <= kStageFloats);
+                const int nfit = __syncthreads_count(fits);
+                if (fits) {
+                    TraceMeta2 md;
+                    md.base = off - lo;
+                    md.hsq = thsq;
+                    md.dm = tm - m0;
+                    md.len = len;
+                    sm.meta[threadIdx.x] = md;
+                    sm.lo[threadIdx.x] = lo;
+                }
+                if (nfit == 0) {
+                    if (threadIdx.x == 0) atomicOr(a.errorWord, kErrSpanOverflow);
+                    break;
+                }
+                __syncthreads();
+                for (int j = warp; j < nfit; j += kTunedWarps) {
+                    const TraceMeta2 md = sm.meta[j];
+                    if (md.len == 0) continue;
+                    const int lo_j = sm.lo[j];
+                    const uint32_t tj = a.selIdx ? a.selIdx[first + q0 + j] : first + q0 + j;
+                    const float4 *src = reinterpret_cast<const float4 *>(
+                        a.samples + (size_t)tj * a.stride + lo_j);
+                    float4 *dst = reinterpret_cast<float4 *>(sm.y + md.base + lo_j);
+                    for (int v = lane; v < (md.len >> 2); v += 32) dst[v] = __ldg(src + v);
+                }
+                __syncthreads();
+                for (int j = 0; j < nfit; j++) {
+                    const TraceMeta2 md = sm.meta[j];
+                    if (md.len == 0) continue;
+                    int bo[R];
+                    float fr[R];
+#pragma unroll
+                    for (int r = 0; r < R; r++) {
+                        float t;
+                        bool ok = true;
+                        if (MODEL == kModelCmp) {
+                            t = cmp_time(t0, cc[r], md.hsq);
+                        } else {
+                            float tmp = t0 + c1[r] * md.dm;
+                            tmp = tmp * tmp + c2[r] * md.dm * md.dm + cc[r] * md.hsq;
+                            ok = tmp >= 0;
+                            t = sqrtf(fmaxf(tmp, 0.f));
+                        }
+                        WinIdx wi = window_index(t, a.dt);
+                        const bool in = ok && window_in_trace(wi.k, tau, S);
+                        int b = in ? md.base + wi.k - tau : 0;
+#ifdef HPSS_CHECKED
+                        if (in && (b < md.base + sm.lo[j] ||
+                                   b > md.base + sm.lo[j] + md.len - (W + 1)))
+                            atomicOr(a.errorWord, kErrSmemBounds);
+#endif
+                        bo[r] = (int)min((unsigned)b, (unsigned)kLastBase);
+                        fr[r] = in ? wi.frac : 0.f;
+                        used[r] += in ? 1u : 0u;
+                    }
+#pragma unroll
+                    for (int qq = 0; qq < NP; qq++) {
+                        const float *ya = sm.y + bo[2 * qq];
+                        const float *yb = sm.y + bo[2 * qq + 1];
+                        const float2 fq = f2(fr[2 * qq], fr[2 * qq + 1]);
+                        float2 y1 = f2(ya[0], yb[0]);
+#pragma unroll
+                        for (int jj = 0; jj < W; jj++) {
+                            const float2 y0 = y1;
+                            y1 = f2(ya[jj + 1], yb[jj + 1]);
+                            const float2 d = __ffma2_rn(y0, kNeg1, y1);   // y1 - y0
+                            const float2 u = __ffma2_rn(d, fq, y0);       // (y1-y0)*f + y0
+                            num[qq][jj] = __fadd2_rn(num[qq][jj], u);
+                            lin[qq] = __fadd2_rn(lin[qq], u);
+                            den[qq] = __ffma2_rn(u, u, den[qq]);
+                        }
+                    }
+                }
+                q0 += nfit;
+            }
+
+#pragma unroll
+            for (int qq = 0; qq < NP; qq++) {
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    const int r = 2 * qq + h;
+                    float nm[W];
+#pragma unroll
+                    for (int jj = 0; jj < W; jj++) nm[jj] = h ? num[qq][jj].y : num[qq][jj].x;
+                    float sembl, stack;
+                    reduce_semblance(nm, h ? lin[qq].y : lin[qq].x, h ? den[qq].y : den[qq].x,
+                                     W, used[r], &sembl, &stack);
+                    const uint32_t p = chunk * a.chunkSize + warp * R + r;
+                    if (valid[r] && sembl > best) {
+                        best = sembl;
+                        bestStack = stack;
+                        bestP = p;
+                    }
+                }
+            }
+        }
+
+        sm.bestS[warp][lane] = best;
+        sm.bestK[warp][lane] = bestStack;
+        sm.bestP[warp][lane] = bestP;
+        __syncthreads();
+        if (warp == 0) {
+            for (int wv = 1; wv < kTunedWarps; wv++) {
+                float os = sm.bestS[wv][lane];
+                uint32_t op = sm.bestP[wv][lane];
+                if (better(os, op, best, bestP)) {
+                    best = os;
+                    bestStack = sm.bestK[wv][lane];
+                    bestP = op;
+                }
+            }
+            if (s < S) {
+                out[s] = best;
+                out[a.S + s] = bestStack;
+                if (bestP != 0xffffffffu) {
+                    const float *pr = a.params + (size_t)bestP * np;
+                    out[2 * a.S + s] = 2 / sqrtf(pr[0]);
+                    for (int j = 1; j < np; j++) out[(size_t)(2 + j) * a.S + s] = pr[j];
+                } else {
+                    for (int j = 0; j < np; j++) out[(size_t)(2 + j) * a.S + s] = 0.f;
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+template <int MODEL, int NP>
+cudaError_t launch_ls_tuned2_model(const LsParams &p, uint32_t grid,
+                                   uint32_t tiles, uint32_t nUnits,
+                                   cudaStream_t st) {
+    const size_t smem = sizeof(Tuned2Smem);
+#define HPSS_TUNED2_CASE(WV)                                                  \
+    case WV: {                                                                \
+        auto k = ls_tuned2_kernel<MODEL, WV, NP>;                            \
+        cudaError_t e = cudaFuncSetAttribute(                                 \
+            k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);       \
+        if (e != cudaSuccess) return e;                                       \
+        k<<<grid, kTunedThreads, smem, st>>>(p, tiles, nUnits);              \
+        return cudaGetLastError();                                            \
+    }
+    switch (p.w) {
+        HPSS_TUNED2_CASE(1)
+        HPSS_TUNED2_CASE(3)
+        HPSS_TUNED2_CASE(5)
+        HPSS_TUNED2_CASE(7)
+        HPSS_TUNED2_CASE(9)
+        HPSS_TUNED2_CASE(11)
+        HPSS_TUNED2_CASE(13)
+        HPSS_TUNED2_CASE(15)
+        default:
+            return cudaErrorNotSupported;
+    }
+#undef HPSS_TUNED2_CASE
+}
+
 template <int MODEL, int R>
 cudaError_t launch_ls_tuned_model(const LsParams &p, uint32_t grid,
                                   uint32_t tiles, uint32_t nUnits,
@@ -333,10 +609,10 @@ cudaError_t launch_ls_tuned_model(const LsParams &p, uint32_t grid,
 }
 
 cudaError_t launch_ls_tuned_cmp(const LsParams &p, uint32_t grid, uint32_t tiles,
-                                uint32_t nUnits, cudaStream_t st);
+                                uint32_t nUnits, cudaStream_t st, int pairs);
 cudaError_t launch_ls_tuned_zocrs(const LsParams &p, uint32_t grid, uint32_t tiles,
-                                  uint32_t nUnits, cudaStream_t st);
+                                  uint32_t nUnits, cudaStream_t st, int pairs);
 cudaError_t launch_ls_tuned_oct(const LsParams &p, uint32_t grid, uint32_t tiles,
-                                uint32_t nUnits, cudaStream_t st);
+                                uint32_t nUnits, cudaStream_t st, int pairs);
 
 }  // namespace hpss

@@ -1,0 +1,64 @@
+"""Compile the reference's own CUDA kernels, unmodified, from the reference
+source tree into GPU fatbins under oracle/_ref/ (git-ignored).
+
+Test infrastructure only: the fatbins are the reference's kernels, loaded by
+oracle/ref_runner.py through the CUDA driver API to produce golden outputs on
+a GB300.  Flags follow the reference's cuda/Makefile:26 (-O3 --use_fast_math),
+with the target fixed to sm_103a.
+
+Only the .cu files of the hot path are compiled; the reference's host code
+(boost, SPITS) is not.  Run: python oracle/build_ref.py [reference_root]
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+OUT = HERE / "_ref"
+
+KERNELS = [
+    "cuda/src/semblance/kernel/cmp/linear_search.cu",
+    "cuda/src/semblance/kernel/cmp/common.cu",
+    "cuda/src/semblance/kernel/zocrs/linear_search.cu",
+    "cuda/src/semblance/kernel/zocrs/common.cu",
+    "cuda/src/semblance/kernel/oct/linear_search.cu",
+    "cuda/src/semblance/kernel/cmp/stretch_free.cu",
+    "cuda/src/semblance/kernel/zocrs/stretch_free.cu",
+    "cuda/src/semblance/kernel/oct/stretch_free.cu",
+    "cuda/src/semblance/kernel/common/stretch_free.cu",
+    "cuda/src/semblance/kernel/cmp/differential_evolution.cu",
+    "cuda/src/semblance/kernel/zocrs/differential_evolution.cu",
+    "cuda/src/semblance/kernel/oct/differential_evolution.cu",
+    "cuda/src/semblance/kernel/common/differential_evolution.cu",
+]
+
+
+def fatbin_name(rel: str, tag: str = "") -> str:
+    parts = Path(rel).with_suffix("").parts[-2:]
+    return "_".join(parts) + tag + ".fatbin"
+
+
+def build(ref_root: str = "/root/reference") -> list:
+    ref = Path(ref_root)
+    if not ref.exists():
+        return []
+    OUT.mkdir(exist_ok=True)
+    nvcc = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
+    base = [nvcc, "-fatbin", "-O3", "--use_fast_math",
+            "-gencode=arch=compute_103a,code=sm_103a", "-I" + str(ref)]
+    built = []
+    for rel in KERNELS:
+        src = ref / rel
+        out = OUT / fatbin_name(rel)
+        if not out.exists() or out.stat().st_mtime < src.stat().st_mtime:
+            subprocess.run(base + ["-o", str(out), str(src)], check=True)
+        built.append(out)
+    return built
+
+
+if __name__ == "__main__":
+    for p in build(sys.argv[1] if len(sys.argv) > 1 else "/root/reference"):
+        print(p)

@@ -77,7 +77,9 @@ void oracle_build_grid(int model, const float *lower, const float *upper,
             rem /= gran[j];
         }
         for (int j = 0; j < np; j++) {
-            float v = lower[j] + (float)idx[j] * step[j];
+            /* the reference's device code contracts min + idx*inc into one
+             * fused multiply-add (single rounding) */
+            float v = fmaf((float)idx[j], step[j], lower[j]);
             params[(size_t)i * np + j] = j == 0 ? 4.0f / (v * v) : v;
         }
     }

@@ -102,8 +102,10 @@ def test_constant_traces_known_answer(engine):
         assert np.all(out[0, 0, 60:150] == 1.0)
         assert np.all(out[0, 1, 60:150] == 1.0)
         np.testing.assert_allclose(out[0, 2, 60:150], 2000.0, rtol=1e-6)
-        # t0 = 0: every window starts before sample 0 -> semblance 0, first candidate
-        assert out[0, 0, 0] == 0.0
+        # last samples: t >= t0, so every window ends past the trace -> used = 0,
+        # semblance = stack = 0 and the first candidate is reported
+        assert np.all(out[0, 0, -3:] == 0.0) and np.all(out[0, 1, -3:] == 0.0)
+        np.testing.assert_allclose(out[0, 2, -3:], 2000.0, rtol=1e-6)
 
 
 def test_zocrs_small_line(engine):

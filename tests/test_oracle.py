@@ -78,10 +78,11 @@ def test_grid_order_and_steps():
     for i in [0, 7, 23, 59]:
         iv, ia, ib = i // 20, (i // 5) % 4, i % 5
         steps = [f32((f32(hi[j]) - f32(lo[j])) / f32(g[j])) for j in range(3)]
-        v = f32(f32(lo[0]) + f32(iv) * steps[0])
+        v = f32(np.float64(f32(lo[0])) + np.float64(f32(iv)) * np.float64(steps[0]))
         assert p[i, 0] == f32(f32(4.0) / f32(v * v))
-        assert p[i, 1] == f32(f32(lo[1]) + f32(ia) * steps[1])
-        assert p[i, 2] == f32(f32(lo[2]) + f32(ib) * steps[2])
+        # min + idx*inc as one fused multiply-add (the reference's device code)
+        assert p[i, 1] == f32(np.float64(f32(lo[1])) + np.float64(f32(ia)) * np.float64(steps[1]))
+        assert p[i, 2] == f32(np.float64(f32(lo[2])) + np.float64(f32(ib)) * np.float64(steps[2]))
     v_last = f32(f32(lo[0]) + f32(2) * f32((f32(hi[0]) - f32(lo[0])) / f32(3)))
     assert v_last < hi[0]
 
