@@ -302,6 +302,7 @@ def main():
     st = eng.linear_search_device(d_m0.data_ptr(), len(m0s), w.granularity, d_out.data_ptr(),
                                   "tuned", stats=True)
     kernel_ms = st["kernel_ms"]
+    variant = st.get("kernel_variant")
     tuned_out = d_out.cpu().numpy()
 
     # ---- plain kernel, same line
@@ -391,6 +392,7 @@ def main():
                       "cmps": int(len(all_m0)), "fold": int(np.max(counts)) if len(counts) else 0,
                       "samples": S, "candidates": P, "window": wsz,
                       "evals_per_step": evals_all, "storage": "fp32", "kernel": "tuned",
+                      "kernel_variant": variant,
                       "l2": "inputs exceed L2 (line %.0f MB > 129 MB); no flush" %
                             (line.samples.nbytes / 1e6),
                       "parallelism": f"midpoint shards x{world}"},

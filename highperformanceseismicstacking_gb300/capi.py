@@ -39,10 +39,10 @@ class Stats(C.Structure):
     _fields_ = [("evals", C.c_double), ("not_used", C.c_double),
                 ("selected_traces", C.c_double), ("kernel_ms", C.c_double),
                 ("selection_ms", C.c_double), ("device_error", C.c_uint32),
-                ("reserved", C.c_uint32)]
+                ("kernel_variant", C.c_int32)]
 
     def as_dict(self):
-        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class HpssError(RuntimeError):

@@ -1,0 +1,376 @@
+// de.cu -- differential evolution per (midpoint, t0 sample), fused.
+//
+// The reference runs DE/rand/1/bin per sample with one kernel launch and one
+// cudaDeviceSynchronize per operator per generation per midpoint
+// (DifferentialEvolutionAlgorithm.cpp:21-81, kernels in
+// cuda/src/semblance/kernel/common/differential_evolution.cu and the
+// {cmp,zocrs,oct}/differential_evolution.cu evaluators).  Here the whole run
+// -- initialisation, and per generation mutation, crossover, semblance
+// evaluation and selection -- is ONE launch: a warp owns the population of one
+// sample (individual i lives in lane i % 32, slot i / 32), so mutation reads
+// other individuals with warp shuffles and nothing round-trips through global
+// memory between operators.
+//
+// Operator semantics follow the reference:
+//  * init: x_j = min_j + U * (max_j - min_j), U in (0, 1]   (startPopulations)
+//  * mutation: per parameter j three indices r = trunc(U * (pop - 1)) (not
+//    necessarily distinct, may equal i), v_j = x[r1]_j + F (x[r2]_j - x[r3]_j),
+//    clamped with fminf(max) then fmaxf(min)                (mutatePopulations)
+//  * crossover: l = trunc(U * (nParams - 1)); u_j = (U > CR && l != j) ? x_j
+//    : v_j                                                   (crossoverPopulations)
+//  * selection: replace when fu.semblance > fx.semblance (strict) (nextGeneration)
+//  * `generations` counts the initial evaluation (loop gen = 1 .. G-1)
+//  * result: strict '>' scan over individuals from -1 (lowest index wins
+//    ties), raw parameters (velocity, not 4/v^2)        (selectBestIndividualsFor*)
+// The random stream differs: Philox-4x32-10 (Salmon et al., SC'11), keyed by
+// the seed and countered by (midpoint, sample, individual, draw), instead of
+// curand XORWOW seeded from time(NULL).
+#include "hpss_device.cuh"
+#include "hpss_internal.h"
+
+namespace hpss {
+
+// ---- Philox-4x32-10 (counter-based RNG; published constants) -------------
+struct U4 {
+    uint32_t x, y, z, w;
+};
+
+__host__ __device__ __forceinline__ void mulhilo(uint32_t a, uint32_t b, uint32_t &hi,
+                                                 uint32_t &lo) {
+    uint64_t p = (uint64_t)a * b;
+    hi = (uint32_t)(p >> 32);
+    lo = (uint32_t)p;
+}
+
+__host__ __device__ __forceinline__ U4 philox4x32_10(U4 c, uint32_t k0, uint32_t k1) {
+    const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u;
+    const uint32_t W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#pragma unroll
+    for (int r = 0; r < 10; r++) {
+        uint32_t hi0, lo0, hi1, lo1;
+        mulhilo(M0, c.x, hi0, lo0);
+        mulhilo(M1, c.z, hi1, lo1);
+        U4 n;
+        n.x = hi1 ^ c.y ^ k0;
+        n.y = lo1;
+        n.z = hi0 ^ c.w ^ k1;
+        n.w = lo0;
+        c = n;
+        k0 += W0;
+        k1 += W1;
+    }
+    return c;
+}
+
+// uniform in (0, 1] with 24-bit resolution (curand_uniform's range)
+__host__ __device__ __forceinline__ float u01(uint32_t v) {
+    return (float)((v >> 8) + 1u) * (1.0f / 16777216.0f);
+}
+
+// Stream of uniforms for one individual in one generation.
+struct Draws {
+    U4 ctr;
+    uint32_t k0, k1;
+    U4 buf;
+    int left;
+    __device__ __forceinline__ Draws(uint32_t k0_, uint32_t k1_, uint32_t m0i, uint32_t s,
+                                     uint32_t ind, uint32_t gen)
+        : k0(k0_), k1(k1_), left(0) {
+        ctr.x = gen << 8;
+        ctr.y = ind;
+        ctr.z = s;
+        ctr.w = m0i;
+    }
+    __device__ __forceinline__ float next() {
+        if (left == 0) {
+            buf = philox4x32_10(ctr, k0, k1);
+            ctr.x++;
+            left = 4;
+        }
+        uint32_t v = left == 4 ? buf.x : left == 3 ? buf.y : left == 2 ? buf.z : buf.w;
+        left--;
+        return u01(v);
+    }
+};
+
+constexpr int kDeWarps = 8;
+constexpr int kMaxSlots = kDeMaxPopulation / 32;
+
+// Semblance of one candidate (raw parameters) over the selected traces.
+template <int MODEL, int W>
+__device__ __forceinline__ void de_eval(const DeParams &d, float t0, float m0, uint32_t first,
+                                        uint32_t cnt, const float *x, float *sembl,
+                                        float *stack, unsigned *notUsed) {
+    const LsParams &a = d.ls;
+    const float v = x[0];
+    const float c = 4.0f / (v * v);
+    const float p1 = MODEL != kModelCmp ? x[1] : 0.f;
+    const float p2 = MODEL == kModelZocrs ? x[2] : 0.f;
+    float num[W > 0 ? W : kMaxWindow];
+    const int w = W > 0 ? W : a.w;
+#pragma unroll
+    for (int j = 0; j < (W > 0 ? W : kMaxWindow); j++) num[j] = 0.f;
+    float lin = 0.f, den = 0.f;
+    unsigned used = 0, nu = 0;
+    for (uint32_t q = 0; q < cnt; q++) {
+        const uint32_t ti = a.selIdx ? a.selIdx[first + q] : first + q;
+        float t;
+        int ok = model_time<MODEL>(t0, c, p1, p2, a.mid[ti], a.hoff[ti], a.hsq[ti], m0, a.apm,
+                                   a.h0, &t);
+        if (ok < 0) {
+            nu++;
+            continue;
+        }
+        if (ok == 0) continue;
+        WinIdx wi = window_index(t, a.dt);
+        if (window_in_trace(wi.k, a.tau, (int)a.S)) {
+            const float *tr = a.samples + (size_t)ti * a.stride + (wi.k - a.tau);
+            float y1 = __ldg(tr);
+#pragma unroll
+            for (int j = 0; j < (W > 0 ? W : kMaxWindow); j++) {
+                if (W == 0 && j >= w) break;
+                float y0 = y1;
+                y1 = __ldg(tr + j + 1);
+                float u = (y1 - y0) * wi.frac + y0;
+                num[j] += u;
+                lin += u;
+                den += u * u;
+            }
+            used++;
+        }
+    }
+    reduce_semblance(num, lin, den, w, used, sembl, stack);
+    *notUsed += nu;
+}
+
+template <int MODEL, int W>
+__global__ void __launch_bounds__(kDeWarps * 32)
+de_kernel(DeParams d, uint32_t nUnits) {
+    const LsParams &a = d.ls;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    constexpr int NP = MODEL == kModelCmp ? 1 : (MODEL == kModelZocrs ? 3 : 2);
+    const uint32_t pop = d.pop;
+    const int slots = (int)((pop + 31) / 32);
+
+    // unit = (midpoint, sample); one warp per unit
+    for (uint32_t unit = blockIdx.x * kDeWarps + warp; unit < nUnits;
+         unit += gridDim.x * kDeWarps) {
+        const uint32_t mi = unit / a.S;
+        const uint32_t s = unit % a.S;
+        const float m0 = a.m0s[mi];
+        const uint32_t first = a.selFirst[mi], cnt = a.selCount[mi];
+        const float t0 = static_cast<float>(s) * a.dt;
+
+        float x[kMaxSlots][NP], fx[kMaxSlots], fxk[kMaxSlots];
+        unsigned notUsed = 0;
+        // ---- initial population and its fitness (generation 1)
+#pragma unroll
+        for (int sl = 0; sl < kMaxSlots; sl++) {
+            if (sl >= slots) break;
+            const uint32_t ind = sl * 32 + lane;
+            Draws rng(d.seedLo, d.seedHi, mi, s, ind, 0);
+#pragma unroll
+            for (int j = 0; j < NP; j++) {
+                float r = rng.next();
+                x[sl][j] = d.lo[j] + r * (d.hi[j] - d.lo[j]);
+            }
+            fx[sl] = -1.f;
+            fxk[sl] = 0.f;
+            if (ind < pop) de_eval<MODEL, W>(d, t0, m0, first, cnt, x[sl], &fx[sl], &fxk[sl],
+                                             &notUsed);
+        }
+        // ---- generations 2 .. G
+        for (uint32_t gen = 1; gen < d.gens; gen++) {
+            float u[kMaxSlots][NP];
+#pragma unroll
+            for (int sl = 0; sl < kMaxSlots; sl++) {
+                if (sl >= slots) break;
+                const uint32_t ind = sl * 32 + lane;
+                Draws rng(d.seedLo, d.seedHi, mi, s, ind, gen);
+                float v[NP];
+#pragma unroll
+                for (int j = 0; j < NP; j++) {
+                    const float q1 = rng.next(), q2 = rng.next(), q3 = rng.next();
+                    const uint32_t r1 = (uint32_t)(q1 * (float)(pop - 1));
+                    const uint32_t r2 = (uint32_t)(q2 * (float)(pop - 1));
+                    const uint32_t r3 = (uint32_t)(q3 * (float)(pop - 1));
+                    float x1 = 0.f, x2 = 0.f, x3 = 0.f;
+#pragma unroll
+                    for (int ss = 0; ss < kMaxSlots; ss++) {
+                        if (ss >= slots) break;
+                        float o1 = __shfl_sync(0xffffffffu, x[ss][j], r1 & 31);
+                        float o2 = __shfl_sync(0xffffffffu, x[ss][j], r2 & 31);
+                        float o3 = __shfl_sync(0xffffffffu, x[ss][j], r3 & 31);
+                        if ((int)(r1 >> 5) == ss) x1 = o1;
+                        if ((int)(r2 >> 5) == ss) x2 = o2;
+                        if ((int)(r3 >> 5) == ss) x3 = o3;
+                    }
+                    float nv = x1 + d.F * (x2 - x3);
+                    nv = fminf(nv, d.hi[j]);
+                    nv = fmaxf(nv, d.lo[j]);
+                    v[j] = nv;
+                }
+                const uint32_t l = (uint32_t)(rng.next() * (float)(NP - 1));
+#pragma unroll
+                for (int j = 0; j < NP; j++) {
+                    const float r = rng.next();
+                    u[sl][j] = (r > d.CR && l != (uint32_t)j) ? x[sl][j] : v[j];
+                }
+            }
+            // all lanes have read the current population: evaluate and select
+#pragma unroll
+            for (int sl = 0; sl < kMaxSlots; sl++) {
+                if (sl >= slots) break;
+                const uint32_t ind = sl * 32 + lane;
+                if (ind >= pop) continue;
+                float fu, fuk;
+                de_eval<MODEL, W>(d, t0, m0, first, cnt, u[sl], &fu, &fuk, &notUsed);
+                if (fu > fx[sl]) {
+#pragma unroll
+                    for (int j = 0; j < NP; j++) x[sl][j] = u[sl][j];
+                    fx[sl] = fu;
+                    fxk[sl] = fuk;
+                }
+            }
+            __syncwarp();
+        }
+        // ---- best individual: strict '>' from -1 in index order
+        float best = -1.f, bestK = 0.f;
+        uint32_t bestI = 0xffffffffu;
+        float bx[NP];
+#pragma unroll
+        for (int j = 0; j < NP; j++) bx[j] = 0.f;
+#pragma unroll
+        for (int sl = 0; sl < kMaxSlots; sl++) {
+            if (sl >= slots) break;
+            const uint32_t ind = sl * 32 + lane;
+            if (ind < pop && fx[sl] > best) {
+                best = fx[sl];
+                bestK = fxk[sl];
+                bestI = ind;
+#pragma unroll
+                for (int j = 0; j < NP; j++) bx[j] = x[sl][j];
+            }
+        }
+#pragma unroll
+        for (int o = 16; o; o >>= 1) {
+            float os = __shfl_xor_sync(0xffffffffu, best, o);
+            float ok = __shfl_xor_sync(0xffffffffu, bestK, o);
+            uint32_t oi = __shfl_xor_sync(0xffffffffu, bestI, o);
+            float ox[NP];
+#pragma unroll
+            for (int j = 0; j < NP; j++) ox[j] = __shfl_xor_sync(0xffffffffu, bx[j], o);
+            if (better(os, oi, best, bestI)) {
+                best = os;
+                bestK = ok;
+                bestI = oi;
+#pragma unroll
+                for (int j = 0; j < NP; j++) bx[j] = ox[j];
+            }
+        }
+        // not-used count (OCT)
+#pragma unroll
+        for (int o = 16; o; o >>= 1) notUsed += __shfl_xor_sync(0xffffffffu, notUsed, o);
+        if (lane == 0) {
+            float *out = a.out + (size_t)mi * (2 + NP) * a.S;
+            out[s] = best;
+            out[a.S + s] = bestK;
+#pragma unroll
+            for (int j = 0; j < NP; j++) out[(size_t)(2 + j) * a.S + s] = bx[j];
+            if (MODEL == kModelOct && a.notUsed && notUsed) atomicAdd(a.notUsed + mi,
+                                                                       (unsigned long long)notUsed);
+        }
+    }
+}
+
+// OCT trace selection with the initial DE population
+// (selectTracesForOffsetContinuationTrajectoryAndDifferentialEvolution,
+// oct/differential_evolution.cu:130-168): a trace is used if any (sample,
+// initial individual) gives a valid displaced midpoint within apm.  The
+// initial individuals are regenerated from the counter-based stream.
+__global__ void de_select_oct_kernel(DeParams d, const uint32_t *candFirst,
+                                     const uint32_t *candCount, uint32_t *selIdx,
+                                     uint32_t *selCount) {
+    const LsParams &a = d.ls;
+    const uint32_t mi = blockIdx.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nWarps = blockDim.x >> 5;
+    const float m0 = a.m0s[mi];
+    const uint32_t first = candFirst[mi], count = candCount[mi];
+    const uint32_t outBase = a.selFirst[mi];
+    __shared__ uint32_t shCount;
+    __shared__ uint32_t shFlags[32];
+    if (threadIdx.x == 0) shCount = 0;
+    __syncthreads();
+    for (uint32_t base = 0; base < count; base += nWarps) {
+        const uint32_t q = base + warp;
+        bool used = false;
+        if (q < count) {
+            const uint32_t ti = first + q;
+            const float m = a.mid[ti], h = a.hoff[ti];
+            for (uint32_t s = 0; s < a.S && !used; s++) {
+                const float t0 = static_cast<float>(s) * a.dt;
+                for (uint32_t i0 = 0; i0 < d.pop && !used; i0 += 32) {
+                    const uint32_t ind = i0 + lane;
+                    bool hit = false;
+                    if (ind < d.pop) {
+                        Draws rng(d.seedLo, d.seedHi, mi, s, ind, 0);
+                        float v = d.lo[0] + rng.next() * (d.hi[0] - d.lo[0]);
+                        float sl = d.lo[1] + rng.next() * (d.hi[1] - d.lo[1]);
+                        float c = 4.0f / (v * v);
+                        float mh;
+                        int e = oct_displaced_midpoint(h, a.h0, t0, m0, c, sl, &mh);
+                        hit = (e == DE_OK && fabsf(m - mh) <= a.apm);
+                    }
+                    used = __any_sync(0xffffffffu, hit);
+                }
+            }
+        }
+        if (lane == 0) shFlags[warp] = used ? 1u : 0u;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (int w = 0; w < nWarps && base + w < count; w++)
+                if (shFlags[w]) selIdx[outBase + shCount++] = first + base + w;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) selCount[mi] = shCount;
+}
+
+template <int MODEL>
+cudaError_t launch_de_model(const DeParams &d, uint32_t grid, uint32_t nUnits, cudaStream_t st) {
+    switch (d.ls.w) {
+#define HPSS_DE_CASE(WV)                                                       \
+    case WV:                                                                   \
+        de_kernel<MODEL, WV><<<grid, kDeWarps * 32, 0, st>>>(d, nUnits);       \
+        break;
+        HPSS_DE_CASE(1)
+        HPSS_DE_CASE(3)
+        HPSS_DE_CASE(5)
+        HPSS_DE_CASE(7)
+        HPSS_DE_CASE(9)
+        HPSS_DE_CASE(11)
+#undef HPSS_DE_CASE
+        default:
+            de_kernel<MODEL, 0><<<grid, kDeWarps * 32, 0, st>>>(d, nUnits);
+            break;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_de(const DeParams &d, int model, uint32_t grid, uint32_t nUnits,
+                      cudaStream_t st) {
+    if (model == kModelCmp) return launch_de_model<kModelCmp>(d, grid, nUnits, st);
+    if (model == kModelZocrs) return launch_de_model<kModelZocrs>(d, grid, nUnits, st);
+    return launch_de_model<kModelOct>(d, grid, nUnits, st);
+}
+
+cudaError_t launch_de_select_oct(const DeParams &d, const uint32_t *candFirst,
+                                 const uint32_t *candCount, uint32_t *selIdx,
+                                 uint32_t *selCount, cudaStream_t st) {
+    if (d.ls.nM0 == 0) return cudaSuccess;
+    de_select_oct_kernel<<<d.ls.nM0, 256, 0, st>>>(d, candFirst, candCount, selIdx, selCount);
+    return cudaGetLastError();
+}
+
+}  // namespace hpss

@@ -11,6 +11,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <new>
 #include <random>
 #include <string>
@@ -33,6 +34,7 @@ cudaError_t launch_ls_tuned_zocrs(const LsParams &p, uint32_t grid, uint32_t til
 cudaError_t launch_ls_tuned_oct(const LsParams &p, uint32_t grid, uint32_t tiles,
                                 uint32_t nUnits, cudaStream_t st, int pairs);
 size_t tuned_stage_floats();
+size_t tuned_stage_floats_min();
 }  // namespace hpss
 
 using namespace hpss;
@@ -46,6 +48,9 @@ struct hpss_handle_s : public Handle {
     Buf params, chunkBounds, selFirst, selCount, selIdx, candFirst, candCount,
         notUsed, errWord, m0s, out, octCands;
     std::vector<float> octCandsHost;
+    std::map<std::string, int> variantCache;  // autotuner decisions
+    int lastVariant = -1;
+    uint32_t meanFold = 0;                     // traces per distinct midpoint
 };
 
 namespace {
@@ -232,6 +237,62 @@ int num_sms(hpss_handle h) {
     return v > 0 ? v : 1;
 }
 
+// Shapes of the tuned pair kernel: candidate pairs per thread and resident
+// CTAs per SM (more pairs: more independent chains per thread; more CTAs:
+// more warps to hide latency, a smaller shared-memory stage).
+constexpr int kTunedVariants = 3;
+constexpr int kVariantPairs[kTunedVariants] = {2, 1, 2};
+constexpr int kVariantCtasPerSm[kTunedVariants] = {2, 3, 3};
+
+// Autotuner: the first time a (model, window, candidates, samples, fold) key
+// is seen, every variant is timed on a prefix of the work units (results are
+// overwritten by the real launch) and the fastest is cached in the handle.
+// HPSS_LS_VARIANT=<n> forces a variant.
+template <typename SetChunks, typename Launch>
+hpss_status choose_variant(hpss_handle h, const LsParams &lp, uint32_t units,
+                           SetChunks setChunks, Launch launch, int *out) {
+    if (const char *env = std::getenv("HPSS_LS_VARIANT")) {
+        int v = std::atoi(env);
+        if (v >= 0 && v < kTunedVariants) {
+            *out = v;
+            return HPSS_OK;
+        }
+    }
+    const std::string key = std::to_string(h->model) + "/" + std::to_string(lp.w) + "/" +
+                            std::to_string(lp.P) + "/" + std::to_string(lp.S) + "/" +
+                            std::to_string(h->meanFold);
+    auto it = h->variantCache.find(key);
+    if (it != h->variantCache.end()) {
+        *out = it->second;
+        return HPSS_OK;
+    }
+    const uint32_t sub = std::min<uint32_t>(units, (uint32_t)num_sms(h) * 12);
+    cudaEvent_t a, b;
+    HPSS_CUDA_TRY(h, cudaEventCreate(&a));
+    HPSS_CUDA_TRY(h, cudaEventCreate(&b));
+    float best = 3.4e38f;
+    int bestV = 0;
+    for (int v = 0; v < kTunedVariants; v++) {
+        HPSS_CUDA_TRY(h, setChunks(2 * kVariantPairs[v]));
+        HPSS_CUDA_TRY(h, launch(v, std::min<uint32_t>(sub, 64)));  // first-launch costs
+        HPSS_CUDA_TRY(h, cudaEventRecord(a, h->stream));
+        HPSS_CUDA_TRY(h, launch(v, sub));
+        HPSS_CUDA_TRY(h, cudaEventRecord(b, h->stream));
+        HPSS_CUDA_TRY(h, cudaEventSynchronize(b));
+        float ms = 0;
+        HPSS_CUDA_TRY(h, cudaEventElapsedTime(&ms, a, b));
+        if (ms < best) {
+            best = ms;
+            bestV = v;
+        }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    h->variantCache[key] = bestV;
+    *out = bestV;
+    return HPSS_OK;
+}
+
 hpss_status linear_search_impl(hpss_handle h, const float *d_m0s, uint32_t nM0,
                                const uint32_t *granularity, int kernel,
                                float *d_out, hpss_stats *stats, bool sync) {
@@ -274,17 +335,23 @@ hpss_status linear_search_impl(hpss_handle h, const float *d_m0s, uint32_t nM0,
                                        static_cast<float *>(h->params.p), lp.P, h->stream));
     // candidates per thread of the tuned kernel: 2 * pairs (CMP / ZO-CRS),
     // 4 (OCT); HPSS_LS_PAIRS overrides the pair count (1, 2 or 4)
-    int pairs = 2;
-    if (const char *env = std::getenv("HPSS_LS_PAIRS")) {
-        int v = std::atoi(env);
-        if (v == 1 || v == 2 || v == 4) pairs = v;
-    }
-    const int perThread = h->model == HPSS_MODEL_OCT ? 4 : 2 * pairs;
-    lp.chunkSize = kTunedWarps * perThread;
-    lp.nChunks = (lp.P + lp.chunkSize - 1) / lp.chunkSize;
-    HPSS_CUDA_TRY(h, ensure(h, h->chunkBounds, (size_t)lp.nChunks * 2 * h->np * sizeof(float)));
-    lp.chunkBounds = static_cast<float *>(h->chunkBounds.p);
-    HPSS_CUDA_TRY(h, launch_chunk_bounds(lp, static_cast<float *>(h->chunkBounds.p), h->stream));
+    // Tuned kernel: CMP / ZO-CRS run the branch-free pair kernel in one of
+    // kTunedVariants shapes (candidate pairs per thread x CTAs per SM), OCT the
+    // branchy kernel (4 candidates per thread).  The chunk bounds depend on
+    // the chunk size (8 warps x candidates per thread).
+    const bool pairKernel = kernel == HPSS_KERNEL_TUNED && h->model != HPSS_MODEL_OCT &&
+                            lp.w <= 15 && h->stride + 8 <= (uint32_t)tuned_stage_floats_min();
+    const bool branchyKernel = kernel == HPSS_KERNEL_TUNED && h->model == HPSS_MODEL_OCT &&
+                               lp.w <= 15 && h->stride + 8 <= (uint32_t)tuned_stage_floats();
+    auto setChunks = [&](int perThread) -> cudaError_t {
+        lp.chunkSize = kTunedWarps * perThread;
+        lp.nChunks = (lp.P + lp.chunkSize - 1) / lp.chunkSize;
+        cudaError_t e = ensure(h, h->chunkBounds, (size_t)lp.nChunks * 2 * h->np * sizeof(float));
+        if (e != cudaSuccess) return e;
+        lp.chunkBounds = static_cast<float *>(h->chunkBounds.p);
+        return launch_chunk_bounds(lp, static_cast<float *>(h->chunkBounds.p), h->stream);
+    };
+    HPSS_CUDA_TRY(h, setChunks(4));
     HPSS_CUDA_TRY(h, ensure(h, h->notUsed, nM0 * sizeof(unsigned long long)));
     HPSS_CUDA_TRY(h, ensure(h, h->errWord, sizeof(uint32_t)));
     lp.notUsed = static_cast<unsigned long long *>(h->notUsed.p);
@@ -296,22 +363,33 @@ hpss_status linear_search_impl(hpss_handle h, const float *d_m0s, uint32_t nM0,
     rc = run_selection(h, d_m0s, nM0, lp);
     if (rc != HPSS_OK) return rc;
     HPSS_CUDA_TRY(h, cudaEventRecord(h->ev1, h->stream));
-    if (kernel == HPSS_KERNEL_PLAIN) {
-        HPSS_CUDA_TRY(h, launch_ls_plain(lp, h->stream));
-    } else {
-        if (lp.w > 15 || h->stride + 8 > (uint32_t)tuned_stage_floats()) {
-            HPSS_CUDA_TRY(h, launch_ls_plain(lp, h->stream));
-        } else {
-            uint32_t tiles = (h->S + kTileSamples - 1) / kTileSamples;
-            uint64_t units = (uint64_t)nM0 * tiles;
-            uint32_t grid = (uint32_t)std::min<uint64_t>(units, (uint64_t)num_sms(h) * 2);
-            cudaError_t e;
-            if (h->model == HPSS_MODEL_CMP) e = launch_ls_tuned_cmp(lp, grid, tiles, (uint32_t)units, h->stream, pairs);
-            else if (h->model == HPSS_MODEL_ZOCRS) e = launch_ls_tuned_zocrs(lp, grid, tiles, (uint32_t)units, h->stream, pairs);
-            else e = launch_ls_tuned_oct(lp, grid, tiles, (uint32_t)units, h->stream, pairs);
-            HPSS_CUDA_TRY(h, e);
-        }
+    const uint32_t tiles = (h->S + kTileSamples - 1) / kTileSamples;
+    const uint64_t units = (uint64_t)nM0 * tiles;
+    if (units > 0xffffffffull)
+        return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "too many (midpoint, tile) units");
+    auto launchPair = [&](int variant, uint32_t nUnits) -> cudaError_t {
+        const uint32_t grid = (uint32_t)std::min<uint64_t>(
+            nUnits, (uint64_t)num_sms(h) * kVariantCtasPerSm[variant]);
+        return h->model == HPSS_MODEL_CMP
+                   ? launch_ls_tuned_cmp(lp, grid, tiles, nUnits, h->stream, variant)
+                   : launch_ls_tuned_zocrs(lp, grid, tiles, nUnits, h->stream, variant);
+    };
+    int variant = 0;
+    if (pairKernel) {
+        rc = choose_variant(h, lp, (uint32_t)units, setChunks, launchPair, &variant);
+        if (rc != HPSS_OK) return rc;
+        HPSS_CUDA_TRY(h, setChunks(2 * kVariantPairs[variant]));
+        HPSS_CUDA_TRY(h, cudaEventRecord(h->ev1, h->stream));
     }
+    if (pairKernel) {
+        HPSS_CUDA_TRY(h, launchPair(variant, (uint32_t)units));
+    } else if (branchyKernel) {
+        const uint32_t grid = (uint32_t)std::min<uint64_t>(units, (uint64_t)num_sms(h) * 2);
+        HPSS_CUDA_TRY(h, launch_ls_tuned_oct(lp, grid, tiles, (uint32_t)units, h->stream, 0));
+    } else {
+        HPSS_CUDA_TRY(h, launch_ls_plain(lp, h->stream));
+    }
+    h->lastVariant = pairKernel ? variant : -1;
     HPSS_CUDA_TRY(h, cudaEventRecord(h->ev2, h->stream));
 
     if (stats || sync) {
@@ -338,10 +416,119 @@ hpss_status linear_search_impl(hpss_handle h, const float *d_m0s, uint32_t nM0,
             cudaEventElapsedTime(&ms, h->ev0, h->ev1);
             stats->selection_ms = ms;
             stats->device_error = err;
+            stats->kernel_variant = h->lastVariant;
         }
         if (err)
             return set_error(h, HPSS_ERR_DEVICE_CHECK,
                              "device check failed, error word " + std::to_string(err));
+    }
+    return HPSS_OK;
+}
+
+hpss_status de_impl(hpss_handle h, const float *d_m0s, uint32_t nM0, uint32_t pop,
+                    uint32_t gens, float F, float CR, uint64_t seed, float *d_out,
+                    hpss_stats *stats, bool sync) {
+    hpss_status rc = check_ready(h);
+    if (rc != HPSS_OK) return rc;
+    if (pop < 1 || pop > kDeMaxPopulation)
+        return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "population must be in [1, 128]");
+    if (gens < 1) return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "generations must be >= 1");
+    if (nM0 == 0) return HPSS_OK;
+    if (!d_m0s || !d_out) return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "null device pointer");
+    cudaSetDevice(h->device);
+
+    DeParams d;
+    std::memset(&d, 0, sizeof(d));
+    fill_line_params(h, d.ls);
+    d.ls.m0s = d_m0s;
+    d.ls.nM0 = nM0;
+    d.ls.out = d_out;
+    d.pop = pop;
+    d.gens = gens;
+    d.F = F;
+    d.CR = CR;
+    d.seedLo = (uint32_t)seed;
+    d.seedHi = (uint32_t)(seed >> 32);
+    for (int j = 0; j < 3; j++) {
+        d.lo[j] = h->lower[j];
+        d.hi[j] = h->upper[j];
+    }
+    HPSS_CUDA_TRY(h, ensure(h, h->notUsed, nM0 * sizeof(unsigned long long)));
+    HPSS_CUDA_TRY(h, ensure(h, h->errWord, sizeof(uint32_t)));
+    d.ls.notUsed = static_cast<unsigned long long *>(h->notUsed.p);
+    d.ls.errorWord = static_cast<uint32_t *>(h->errWord.p);
+    HPSS_CUDA_TRY(h, cudaMemsetAsync(d.ls.notUsed, 0, nM0 * sizeof(unsigned long long), h->stream));
+    HPSS_CUDA_TRY(h, cudaMemsetAsync(d.ls.errorWord, 0, sizeof(uint32_t), h->stream));
+
+    HPSS_CUDA_TRY(h, cudaEventRecord(h->ev0, h->stream));
+    // selection: CMP / ZO-CRS as linear search; OCT with the initial population
+    HPSS_CUDA_TRY(h, ensure(h, h->selFirst, nM0 * sizeof(uint32_t)));
+    HPSS_CUDA_TRY(h, ensure(h, h->selCount, nM0 * sizeof(uint32_t)));
+    d.ls.selFirst = static_cast<uint32_t *>(h->selFirst.p);
+    d.ls.selCount = static_cast<uint32_t *>(h->selCount.p);
+    d.ls.selIdx = nullptr;
+    if (h->model != HPSS_MODEL_OCT) {
+        HPSS_CUDA_TRY(h, launch_select_range(h->dMid, h->nTraces, d_m0s, nM0,
+                                             h->model == HPSS_MODEL_CMP ? 0 : 1, h->apm, 0.f,
+                                             static_cast<uint32_t *>(h->selFirst.p),
+                                             static_cast<uint32_t *>(h->selCount.p), h->stream));
+    } else {
+        float hmax = 0.f;
+        for (float v : h->hHoff) hmax = std::max(hmax, std::fabs(v));
+        float radius = (h->apm + std::sqrt(hmax * hmax + h->h0 * h->h0)) * 1.001f + 1.0f;
+        HPSS_CUDA_TRY(h, ensure(h, h->candFirst, nM0 * sizeof(uint32_t)));
+        HPSS_CUDA_TRY(h, ensure(h, h->candCount, nM0 * sizeof(uint32_t)));
+        uint32_t *cf = static_cast<uint32_t *>(h->candFirst.p);
+        uint32_t *cc = static_cast<uint32_t *>(h->candCount.p);
+        HPSS_CUDA_TRY(h, launch_select_range(h->dMid, h->nTraces, d_m0s, nM0, 2, h->apm, radius,
+                                             cf, cc, h->stream));
+        HPSS_CUDA_TRY(h, launch_exclusive_scan(cc, static_cast<uint32_t *>(h->selFirst.p), nM0,
+                                               h->stream));
+        std::vector<uint32_t> ccHost(nM0);
+        HPSS_CUDA_TRY(h, cudaMemcpyAsync(ccHost.data(), cc, nM0 * sizeof(uint32_t),
+                                         cudaMemcpyDeviceToHost, h->stream));
+        HPSS_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+        size_t total = 0;
+        for (uint32_t v : ccHost) total += v;
+        HPSS_CUDA_TRY(h, ensure(h, h->selIdx, total * sizeof(uint32_t)));
+        d.ls.selIdx = static_cast<uint32_t *>(h->selIdx.p);
+        HPSS_CUDA_TRY(h, launch_de_select_oct(d, cf, cc, static_cast<uint32_t *>(h->selIdx.p),
+                                              static_cast<uint32_t *>(h->selCount.p),
+                                              h->stream));
+    }
+    HPSS_CUDA_TRY(h, cudaEventRecord(h->ev1, h->stream));
+    const uint64_t units = (uint64_t)nM0 * h->S;
+    if (units > 0xffffffffull)
+        return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "too many (midpoint, sample) units");
+    const uint64_t ctas = (units + 7) / 8;
+    const uint32_t grid = (uint32_t)std::min<uint64_t>(ctas, (uint64_t)num_sms(h) * 8);
+    HPSS_CUDA_TRY(h, launch_de(d, h->model, grid, (uint32_t)units, h->stream));
+    HPSS_CUDA_TRY(h, cudaEventRecord(h->ev2, h->stream));
+    if (stats || sync) {
+        HPSS_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+        if (stats) {
+            std::memset(stats, 0, sizeof(*stats));
+            std::vector<uint32_t> cnt(nM0);
+            std::vector<unsigned long long> nu(nM0);
+            HPSS_CUDA_TRY(h, cudaMemcpy(cnt.data(), d.ls.selCount, nM0 * sizeof(uint32_t),
+                                        cudaMemcpyDeviceToHost));
+            HPSS_CUDA_TRY(h, cudaMemcpy(nu.data(), d.ls.notUsed,
+                                        nM0 * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+            double sel = 0, nus = 0;
+            for (uint32_t i = 0; i < nM0; i++) {
+                sel += cnt[i];
+                nus += (double)nu[i];
+            }
+            stats->selected_traces = sel;
+            stats->evals = sel * (double)h->S * (double)pop * (double)gens;
+            stats->not_used = nus;
+            float ms = 0;
+            cudaEventElapsedTime(&ms, h->ev1, h->ev2);
+            stats->kernel_ms = ms;
+            cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+            stats->selection_ms = ms;
+            stats->kernel_variant = -1;
+        }
     }
     return HPSS_OK;
 }
@@ -445,6 +632,12 @@ hpss_status hpss_upload_gather(hpss_handle h, const float *samples,
     h->storage = storage;
     h->hMid.assign(midpoints, midpoints + nTraces);
     h->hHoff.assign(halfoffsets, halfoffsets + nTraces);
+    {
+        uint32_t distinct = 0;
+        for (uint32_t i = 0; i < nTraces; i++)
+            if (i == 0 || midpoints[i] != midpoints[i - 1]) distinct++;
+        h->meanFold = distinct ? nTraces / distinct : 0;
+    }
     std::vector<float> hsq(nTraces);
     for (uint32_t i = 0; i < nTraces; i++) hsq[i] = halfoffsets[i] * halfoffsets[i];
     const size_t n = nTraces, st = h->stride;
@@ -572,16 +765,37 @@ hpss_status hpss_select_traces(hpss_handle h, const float *m0s, uint32_t nM0,
     return HPSS_OK;
 }
 
-hpss_status hpss_differential_evolution(hpss_handle h, const float *, uint32_t, uint32_t,
-                                        uint32_t, float, float, uint64_t, float *,
-                                        hpss_stats *) {
-    return set_error(h, HPSS_ERR_NOT_READY, "differential evolution not built yet");
+hpss_status hpss_differential_evolution_device(hpss_handle h, const float *d_m0s,
+                                               uint32_t nM0, uint32_t population,
+                                               uint32_t generations, float F, float CR,
+                                               uint64_t seed, float *d_out, hpss_stats *stats) {
+    if (!h) return HPSS_ERR_INVALID_ARGUMENT;
+    return de_impl(h, d_m0s, nM0, population, generations, F, CR, seed, d_out, stats, false);
 }
 
-hpss_status hpss_differential_evolution_device(hpss_handle h, const float *, uint32_t,
-                                               uint32_t, uint32_t, float, float, uint64_t,
-                                               float *, hpss_stats *) {
-    return set_error(h, HPSS_ERR_NOT_READY, "differential evolution not built yet");
+hpss_status hpss_differential_evolution(hpss_handle h, const float *m0s, uint32_t nM0,
+                                        uint32_t population, uint32_t generations, float F,
+                                        float CR, uint64_t seed, float *out,
+                                        hpss_stats *stats) {
+    if (!h) return HPSS_ERR_INVALID_ARGUMENT;
+    if (nM0 && (!m0s || !out))
+        return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "null host pointer");
+    hpss_status rc = check_ready(h);
+    if (rc != HPSS_OK) return rc;
+    if (nM0 == 0) return HPSS_OK;
+    cudaSetDevice(h->device);
+    const size_t outElems = (size_t)nM0 * (2 + h->np) * h->S;
+    HPSS_CUDA_TRY(h, ensure(h, h->m0s, nM0 * sizeof(float)));
+    HPSS_CUDA_TRY(h, ensure(h, h->out, outElems * sizeof(float)));
+    HPSS_CUDA_TRY(h, cudaMemcpyAsync(h->m0s.p, m0s, nM0 * sizeof(float),
+                                     cudaMemcpyHostToDevice, h->stream));
+    rc = de_impl(h, static_cast<float *>(h->m0s.p), nM0, population, generations, F, CR, seed,
+                 static_cast<float *>(h->out.p), stats, true);
+    if (rc != HPSS_OK) return rc;
+    HPSS_CUDA_TRY(h, cudaMemcpyAsync(out, h->out.p, outElems * sizeof(float),
+                                     cudaMemcpyDeviceToHost, h->stream));
+    HPSS_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    return HPSS_OK;
 }
 
 hpss_status hpss_stretch_free(hpss_handle h, const float *, uint32_t, const float *, int,

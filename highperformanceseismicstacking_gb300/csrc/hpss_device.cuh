@@ -20,17 +20,32 @@ namespace hpss {
 // gpu_error_code (common/include/gpu/interface.h:12-18).
 enum DevErr : int { DE_OK = 0, DE_DIV_ZERO = 1, DE_NEG_SQRT = 2 };
 
+// The traveltime expressions are written with explicit round-to-nearest
+// intrinsics (__fmaf_rn / __fmul_rn / __fadd_rn are never re-fused by the
+// compiler), so every kernel of this library computes them with one fixed
+// sequence of roundings.  The sequence is the one the reference's compiled
+// kernels use (nvcc contracts a*b + c*d into one fused multiply-add, keeping
+// the product of loop-invariant factors separate); verified bit for bit
+// against the reference kernels' outputs (tests/golden).
+
 // CMP: t = sqrt(t0^2 + c h^2), c = 4/v^2 (cmp/linear_search.cu:57).
 __device__ __forceinline__ float cmp_time(float t0, float c, float h_sq) {
-    return sqrtf(t0 * t0 + c * h_sq);
+    return sqrtf(__fmaf_rn(c, h_sq, __fmul_rn(t0, t0)));
 }
 
-// ZO-CRS: t^2 = (t0 + A dm)^2 + B dm^2 + C h^2 (zocrs/linear_search.cu:83-87).
-// Returns false when the squared time is negative (window skipped).
+// ZO-CRS squared time (t0 + A dm)^2 + B dm^2 + C h^2
+// (zocrs/linear_search.cu:83-87).
+__device__ __forceinline__ float zocrs_t2(float t0, float c, float a, float b,
+                                          float dm, float h_sq) {
+    const float x = __fmaf_rn(a, dm, t0);
+    const float y = __fmaf_rn(__fmul_rn(b, dm), dm, __fmul_rn(x, x));
+    return __fmaf_rn(c, h_sq, y);
+}
+
+// ZO-CRS time; false when the squared time is negative (window skipped).
 __device__ __forceinline__ bool zocrs_time(float t0, float c, float a, float b,
                                            float dm, float h_sq, float *t) {
-    float tmp = t0 + a * dm;
-    tmp = tmp * tmp + b * dm * dm + c * h_sq;
+    const float tmp = zocrs_t2(t0, c, a, b, dm, h_sq);
     if (tmp >= 0) {
         *t = sqrtf(tmp);
         return true;
@@ -38,23 +53,33 @@ __device__ __forceinline__ bool zocrs_time(float t0, float c, float a, float b,
     return false;
 }
 
+// t0^2 - c h0^2 of the OCT formulas.
+__device__ __forceinline__ float oct_tn0_sq(float t0, float c, float h0) {
+    return __fmaf_rn(t0, t0, -__fmul_rn(__fmul_rn(c, h0), h0));
+}
+
 // OCT displaced midpoint (oct/common.cuh:7-35).
 __device__ __forceinline__ int oct_displaced_midpoint(float h, float h0,
                                                       float t0, float m0,
                                                       float c, float slope,
                                                       float *mh) {
-    float theta = t0 * slope;
-    float gamma = 2 * sqrtf(h * h + h0 * h0);
-    float tn0_sq = t0 * t0 - c * h0 * h0;
-    float theta_sq = theta * theta;
-    float gamma_sq = gamma * gamma;
-    float tn0_quad = tn0_sq * tn0_sq;
-    float arg = tn0_quad * tn0_quad + tn0_quad * theta_sq * gamma_sq +
-                16 * h * h * h0 * h0 * theta_sq * theta_sq;
+    const float h0sq = __fmul_rn(h0, h0);
+    const float theta = __fmul_rn(t0, slope);
+    const float gamma = 2 * sqrtf(__fmaf_rn(h, h, h0sq));
+    const float tn0_sq = oct_tn0_sq(t0, c, h0);
+    const float theta_sq = __fmul_rn(theta, theta);
+    const float gamma_sq = __fmul_rn(gamma, gamma);
+    const float tn0_quad = __fmul_rn(tn0_sq, tn0_sq);
+    const float p16 = __fmul_rn(
+        __fmul_rn(__fmul_rn(__fmul_rn(__fmul_rn(16.f, h), h), h0), h0), theta_sq);
+    float arg = __fmaf_rn(__fmul_rn(tn0_quad, theta_sq), gamma_sq,
+                          __fmul_rn(tn0_quad, tn0_quad));
+    arg = __fmaf_rn(p16, theta_sq, arg);
     if (arg < 0) return DE_NEG_SQRT;
-    arg = theta_sq * gamma_sq + 2 * tn0_quad + 2 * sqrtf(arg);
+    arg = __fadd_rn(__fmaf_rn(theta_sq, gamma_sq, __fmul_rn(2.f, tn0_quad)),
+                    __fmul_rn(2.f, sqrtf(arg)));
     if (arg == 0) return DE_DIV_ZERO;
-    *mh = m0 + 2 * theta * (h * h - h0 * h0) / sqrtf(arg);
+    *mh = __fadd_rn(m0, __fmul_rn(__fmul_rn(2.f, theta), __fmaf_rn(h, h, -h0sq)) / sqrtf(arg));
     return DE_OK;
 }
 
@@ -62,27 +87,32 @@ __device__ __forceinline__ int oct_displaced_midpoint(float h, float h0,
 __device__ __forceinline__ int oct_time(float h, float h0, float t0, float m0,
                                         float m, float mh, float c,
                                         float slope, float *out) {
-    float tn0_sq = t0 * t0 - c * h0 * h0;
-    float w1 = (h + h0) * (h + h0) - (mh - m0) * (mh - m0);
-    float w2 = (h - h0) * (h - h0) - (mh - m0) * (mh - m0);
+    const float tn0_sq = oct_tn0_sq(t0, c, h0);
+    const float b = __fsub_rn(mh, m0);
+    const float bb = __fmul_rn(b, b);
+    const float ap = __fadd_rn(h, h0), am = __fsub_rn(h, h0);
+    const float w1 = __fmaf_rn(ap, ap, -bb);
+    const float w2 = __fmaf_rn(am, am, -bb);
     if (w1 < 0 || w2 < 0) return DE_NEG_SQRT;
-    float u = sqrtf(w1) + sqrtf(w2);
+    const float u = __fadd_rn(sqrtf(w1), sqrtf(w2));
     float th = t0;
     if (fabsf(h) > fabsf(h0)) {
         if (!u) return DE_DIV_ZERO;
-        float arg = c * h * h + 4 * h * h / (u * u) * tn0_sq;
+        const float q = __fmul_rn(__fmul_rn(4.f, h), h) / __fmul_rn(u, u);
+        const float arg = __fmaf_rn(__fmul_rn(c, h), h, __fmul_rn(q, tn0_sq));
         if (arg < 0) return DE_NEG_SQRT;
         th = sqrtf(arg);
     } else if (fabsf(h) < fabsf(h0)) {
         if (!h0) return DE_DIV_ZERO;
-        float arg = c * h * h + u * u / (4 * h0 * h0) * tn0_sq;
+        const float q = __fmul_rn(u, u) / __fmul_rn(__fmul_rn(4.f, h0), h0);
+        const float arg = __fmaf_rn(__fmul_rn(c, h), h, __fmul_rn(q, tn0_sq));
         if (arg < 0) return DE_NEG_SQRT;
         th = sqrtf(arg);
     }
-    float tn_sq = th * th - c * h * h;
+    const float tn_sq = __fmaf_rn(th, th, -__fmul_rn(__fmul_rn(c, h), h));
     if (!th || !tn0_sq) return DE_DIV_ZERO;
-    float ah = (t0 * tn_sq) / (th * tn0_sq) * slope;
-    *out = th + ah * (m - mh);
+    const float ah = __fmul_rn(__fmul_rn(t0, tn_sq) / __fmul_rn(th, tn0_sq), slope);
+    *out = __fmaf_rn(ah, __fsub_rn(m, mh), th);
     return DE_OK;
 }
 

@@ -69,6 +69,17 @@ struct LsParams {
     int nmax;
 };
 
+// Differential evolution launch (de.cu).
+struct DeParams {
+    LsParams ls;          // line, window, selection, outputs
+    uint32_t pop;
+    uint32_t gens;
+    float F, CR;
+    uint32_t seedLo, seedHi;
+    float lo[3], hi[3];
+};
+constexpr uint32_t kDeMaxPopulation = 128;
+
 struct Handle {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -115,5 +126,10 @@ cudaError_t launch_convert_storage(const float *src, uint16_t *dst,
                                    uint32_t stride, int storage,
                                    cudaStream_t st);
 size_t tuned_smem_bytes();
+cudaError_t launch_de(const DeParams &d, int model, uint32_t grid, uint32_t nUnits,
+                      cudaStream_t st);
+cudaError_t launch_de_select_oct(const DeParams &d, const uint32_t *candFirst,
+                                 const uint32_t *candCount, uint32_t *selIdx,
+                                 uint32_t *selCount, cudaStream_t st);
 
 }  // namespace hpss

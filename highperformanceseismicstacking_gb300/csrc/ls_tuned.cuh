@@ -323,8 +323,15 @@ struct __align__(16) TraceMeta2 {
     int len;    // staged samples (0: skip the trace)
 };
 
+// stage size per CTA for MINB resident CTAs per SM
+template <int MINB>
+struct Stage2 {
+    static constexpr int kFloats = MINB >= 3 ? 16384 : 24576;
+};
+
+template <int MINB>
 struct Tuned2Smem {
-    float y[kStageFloats];
+    float y[Stage2<MINB>::kFloats];
     TraceMeta2 meta[kTunedThreads];
     int lo[kTunedThreads];
     int warpSum[kTunedWarps];
@@ -335,17 +342,18 @@ struct Tuned2Smem {
 
 __device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
 
-template <int MODEL, int W, int NP>
-__global__ void __launch_bounds__(kTunedThreads, 2)
+template <int MODEL, int W, int NP, int MINB>
+__global__ void __launch_bounds__(kTunedThreads, MINB)
 ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
+    constexpr int kStage = Stage2<MINB>::kFloats;
     constexpr int R = 2 * NP;
     extern __shared__ __align__(16) unsigned char smemRaw[];
-    Tuned2Smem &sm = *reinterpret_cast<Tuned2Smem *>(smemRaw);
+    Tuned2Smem<MINB> &sm = *reinterpret_cast<Tuned2Smem<MINB> *>(smemRaw);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int np = a.np;
     const int S = (int)a.S, tau = a.tau;
     const float2 kNeg1 = f2(-1.f, -1.f);
-    constexpr int kLastBase = kStageFloats - W - 1;
+    constexpr int kLastBase = kStage - W - 1;
 
     if (threadIdx.x < kZeroPad) sm.y[threadIdx.x] = 0.f;
 
@@ -422,7 +430,7 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
                 for (int wv = 0; wv < kTunedWarps; wv++)
                     woff += wv < warp ? sm.warpSum[wv] : 0;
                 const int off = woff + incl - len;
-                const bool fits = (q < cnt) && (off + len <= kStageFloats);
+                const bool fits = (q < cnt) && (off + len <= kStage);
                 const int nfit = __syncthreads_count(fits);
                 if (fits) {
                     TraceMeta2 md;
@@ -461,8 +469,7 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
                         if (MODEL == kModelCmp) {
                             t = cmp_time(t0, cc[r], md.hsq);
                         } else {
-                            float tmp = t0 + c1[r] * md.dm;
-                            tmp = tmp * tmp + c2[r] * md.dm * md.dm + cc[r] * md.hsq;
+                            const float tmp = zocrs_t2(t0, cc[r], c1[r], c2[r], md.dm, md.hsq);
                             ok = tmp >= 0;
                             t = sqrtf(fmaxf(tmp, 0.f));
                         }
@@ -550,14 +557,14 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
     }
 }
 
-template <int MODEL, int NP>
+template <int MODEL, int NP, int MINB>
 cudaError_t launch_ls_tuned2_model(const LsParams &p, uint32_t grid,
                                    uint32_t tiles, uint32_t nUnits,
                                    cudaStream_t st) {
-    const size_t smem = sizeof(Tuned2Smem);
+    const size_t smem = sizeof(Tuned2Smem<MINB>);
 #define HPSS_TUNED2_CASE(WV)                                                  \
     case WV: {                                                                \
-        auto k = ls_tuned2_kernel<MODEL, WV, NP>;                            \
+        auto k = ls_tuned2_kernel<MODEL, WV, NP, MINB>;                      \
         cudaError_t e = cudaFuncSetAttribute(                                 \
             k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);       \
         if (e != cudaSuccess) return e;                                       \

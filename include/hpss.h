@@ -82,7 +82,8 @@ typedef struct {
     double kernel_ms;         /* device time of the compute launches */
     double selection_ms;      /* device time of trace selection */
     uint32_t device_error;    /* device error word (0 = none) */
-    uint32_t reserved;
+    int32_t kernel_variant;   /* tuned-kernel shape chosen by the autotuner
+                                 (-1: plain / not applicable) */
 } hpss_stats;
 
 /* Device selection and handle creation.

@@ -109,3 +109,72 @@ void oracle_select(int model, const float *mid, const float *hoff,
         }
     }
 }
+
+/* ---- differential evolution helpers (engine's random stream) ----------
+ * Philox-4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11), as the engine keys it:
+ * key = seed (lo, hi words); counter = (gen << 8 | draw block, individual,
+ * sample, midpoint index).  Uniforms in (0, 1]: ((v >> 8) + 1) * 2^-24. */
+static void philox4x32_10(uint32_t c[4], uint32_t k0, uint32_t k1) {
+    for (int r = 0; r < 10; r++) {
+        uint64_t p0 = (uint64_t)0xD2511F53u * c[0];
+        uint64_t p1 = (uint64_t)0xCD9E8D57u * c[2];
+        uint32_t n0 = (uint32_t)(p1 >> 32) ^ c[1] ^ k0;
+        uint32_t n1 = (uint32_t)p1;
+        uint32_t n2 = (uint32_t)(p0 >> 32) ^ c[3] ^ k1;
+        uint32_t n3 = (uint32_t)p0;
+        c[0] = n0; c[1] = n1; c[2] = n2; c[3] = n3;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+}
+
+static float u01(uint32_t v) { return (float)((v >> 8) + 1u) * (1.0f / 16777216.0f); }
+
+/* First n uniforms of the stream of (midpoint index, sample, individual,
+ * generation). */
+void oracle_de_uniforms(uint64_t seed, uint32_t m0i, uint32_t s, uint32_t ind,
+                        uint32_t gen, uint32_t n, float *out) {
+    uint32_t ctr = gen << 8;
+    for (uint32_t i = 0; i < n; i += 4) {
+        uint32_t c[4] = {ctr++, ind, s, m0i};
+        philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+        for (uint32_t j = 0; j < 4 && i + j < n; j++) out[i + j] = u01(c[j]);
+    }
+}
+
+/* Initial population [S][pop][np]: x_j = lo_j + U * (hi_j - lo_j)
+ * (startPopulations, common/differential_evolution.cu:19-41). */
+void oracle_de_initial_population(uint64_t seed, uint32_t m0i, uint32_t S,
+                                  uint32_t pop, int np, const float *lo,
+                                  const float *hi, float *out) {
+    float u[4];
+    for (uint32_t s = 0; s < S; s++)
+        for (uint32_t i = 0; i < pop; i++) {
+            oracle_de_uniforms(seed, m0i, s, i, 0, (uint32_t)np, u);
+            for (int j = 0; j < np; j++)
+                out[((size_t)s * pop + i) * np + j] = lo[j] + u[j] * (hi[j] - lo[j]);
+        }
+}
+
+/* OCT selection with per-sample raw candidates cands [S][n][2] (velocity,
+ * slope), c = 4/v^2 (oct/differential_evolution.cu:130-168). */
+void oracle_select_oct_per_sample(const float *mid, const float *hoff,
+                                  uint32_t ntr, float m0, float apm, float h0,
+                                  uint32_t S, float dt, const float *cands,
+                                  uint32_t n, uint8_t *mask) {
+    for (uint32_t i = 0; i < ntr; i++) {
+        float m = mid[i], h = hoff[i], mh;
+        uint8_t used = 0;
+        for (uint32_t s = 0; !used && s < S; s++) {
+            float t0 = (float)s * dt;
+            for (uint32_t p = 0; !used && p < n; p++) {
+                const float *cd = cands + ((size_t)s * n + p) * 2;
+                float v = cd[0];
+                float c = 4.0f / (v * v);
+                int e = oct_mh_f32(h, h0, t0, m0, c, cd[1], &mh);
+                used = (e == OERR_NONE && fabsf(m - mh) <= apm);
+            }
+        }
+        mask[i] = used;
+    }
+}

@@ -116,6 +116,19 @@ void oracle_eval_raw_f32(int model, const float *samples, uint32_t stride,
 
 int oracle_max_threads(void);
 
+/* Differential evolution: the engine's counter-based random stream
+ * (Philox-4x32-10 keyed by the seed) and the initial population drawn from
+ * it; per-sample OCT selection with raw (velocity, slope) candidates. */
+void oracle_de_uniforms(uint64_t seed, uint32_t m0i, uint32_t s, uint32_t ind,
+                        uint32_t gen, uint32_t n, float *out);
+void oracle_de_initial_population(uint64_t seed, uint32_t m0i, uint32_t S,
+                                  uint32_t pop, int np, const float *lo,
+                                  const float *hi, float *out);
+void oracle_select_oct_per_sample(const float *mid, const float *hoff,
+                                  uint32_t ntr, float m0, float apm, float h0,
+                                  uint32_t S, float dt, const float *cands,
+                                  uint32_t n, uint8_t *mask);
+
 #ifdef __cplusplus
 }
 #endif

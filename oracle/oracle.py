@@ -236,3 +236,46 @@ def linear_search(model: str, samples, mid, hoff, m0s: Sequence[float], dt: floa
         outs.append(o)
         idxs.append(i)
     return np.stack(outs), np.stack(idxs), np.asarray(counts)
+
+
+# ---- differential evolution helpers ------------------------------------
+
+def _de_sigs():
+    L = lib()
+    if getattr(L, "_de_ready", False):
+        return L
+    fp, u32 = C.POINTER(C.c_float), C.c_uint32
+    L.oracle_de_uniforms.argtypes = [C.c_uint64, u32, u32, u32, u32, u32, fp]
+    L.oracle_de_initial_population.argtypes = [C.c_uint64, u32, u32, u32, C.c_int, fp, fp, fp]
+    L.oracle_select_oct_per_sample.argtypes = [fp, fp, u32, C.c_float, C.c_float, C.c_float,
+                                               u32, C.c_float, fp, u32, C.POINTER(C.c_uint8)]
+    L._de_ready = True
+    return L
+
+
+def de_uniforms(seed: int, m0i: int, s: int, ind: int, gen: int, n: int) -> np.ndarray:
+    out = np.zeros(n, np.float32)
+    _de_sigs().oracle_de_uniforms(seed, m0i, s, ind, gen, n, _f(out))
+    return out
+
+
+def de_initial_population(seed: int, m0i: int, S: int, pop: int, lower, upper) -> np.ndarray:
+    """[S][pop][np] raw initial individuals of midpoint index m0i."""
+    lo = np.asarray(lower, np.float32)
+    hi = np.asarray(upper, np.float32)
+    out = np.zeros((S, pop, lo.size), np.float32)
+    _de_sigs().oracle_de_initial_population(seed, m0i, S, pop, lo.size, _f(lo), _f(hi), _f(out))
+    return out
+
+
+def select_oct_per_sample(mid, hoff, m0: float, apm: float, h0: float, S: int, dt: float,
+                          cands: np.ndarray) -> np.ndarray:
+    mid = np.ascontiguousarray(mid, np.float32)
+    hoff = np.ascontiguousarray(hoff, np.float32)
+    c = np.ascontiguousarray(cands, np.float32)
+    mask = np.zeros(mid.size, np.uint8)
+    _de_sigs().oracle_select_oct_per_sample(_f(mid), _f(hoff), mid.size, C.c_float(m0),
+                                            C.c_float(apm), C.c_float(h0), S, C.c_float(dt),
+                                            _f(c), c.shape[1],
+                                            mask.ctypes.data_as(C.POINTER(C.c_uint8)))
+    return mask.astype(bool)

@@ -109,4 +109,8 @@ def test_engine_matches_reference_kernels(engine, name, kernel):
         rms = float(np.sqrt(np.mean(z["samples"][sel] ** 2)))
         compare_block(rep, out[i], sem, stk, params, rms)
     rep.check()
-    assert frac >= 0.99, frac
+    if model in ("cmp", "zocrs"):
+        # traveltime arithmetic pinned to the reference's: bit-identical results
+        assert frac == 1.0, frac
+    else:
+        assert frac >= 0.95, frac

@@ -1,0 +1,134 @@
+"""Differential evolution on the GPU, through the C ABI.
+
+The random stream differs from the reference's (curand seeded from
+time(NULL)), so DE is judged by what it finds: its best semblance against the
+exhaustive-grid optimum of the same line, the reported semblance against the
+oracle's evaluation of the reported parameters, and exact checks of the parts
+that do not depend on the stream's values: the initial population (regenerated
+by the oracle from the same counter-based stream), determinism per seed, the
+bounds, and OCT trace selection from the initial population.
+"""
+import numpy as np
+import pytest
+
+from highperformanceseismicstacking_gb300 import synthetic
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def _cmp_line():
+    return synthetic.cmp_line(n_cmp=3, halfoffsets=list(range(25, 1176, 50)), ns=400,
+                              dt_us=4000, n_reflectors=3, n_multiples=0, f=25.0, snr=10.0,
+                              seed=31)
+
+
+def _setup(eng, line, model, lower, upper, tau=2, apm=0.0, h0=0.0):
+    eng.upload_gather(line.samples, line.midpoints, line.halfoffsets, float(line.dt))
+    eng.set_traveltime(model, lower, upper, apm, h0)
+    eng.set_window(tau)
+
+
+def test_de_cmp_finds_grid_optimum(engine):
+    line = _cmp_line()
+    lower, upper = [1000.0], [5040.0]
+    _setup(engine, line, "cmp", lower, upper)
+    m0s = line.cdp_midpoints
+    de, st = engine.differential_evolution(m0s, 32, 32, 0.85, 0.5, seed=1)
+    assert st["evals"] == 3 * 24 * 400 * 32 * 32
+    ls, _ = engine.linear_search(m0s, [404], "tuned")       # 10 m/s grid
+    assert np.all((de[:, 2] >= 1000.0) & (de[:, 2] <= 5040.0))
+    strong = ls[:, 0] > 0.1
+    ratio = de[:, 0][strong] / ls[:, 0][strong]
+    assert np.median(ratio) >= 0.99, np.median(ratio)
+    assert np.mean(ratio) >= 0.95, np.mean(ratio)
+
+
+def test_de_reported_semblance_is_the_parameters_semblance(engine):
+    line = _cmp_line()
+    _setup(engine, line, "cmp", [1000.0], [5040.0])
+    m0s = line.cdp_midpoints
+    de, _ = engine.differential_evolution(m0s, 16, 8, 0.85, 0.5, seed=5)
+    for i, m0 in enumerate(m0s):
+        sel = np.nonzero(line.midpoints == m0)[0].astype(np.uint32)
+        cands = de[i, 2:].T.reshape(-1, 1, 1)
+        sem, stk = oracle.eval_raw("cmp", line.samples, line.midpoints, line.halfoffsets, sel,
+                                   m0, float(line.dt), 2, cands, precision="f32")
+        rel = np.abs(sem[:, 0] - de[i, 0]) / np.maximum(np.abs(sem[:, 0]), 1e-3)
+        assert np.quantile(rel, 0.999) <= 2e-4
+
+
+def test_de_single_generation_is_best_initial_individual(engine):
+    line = _cmp_line()
+    lower, upper = [1000.0], [5040.0]
+    _setup(engine, line, "cmp", lower, upper)
+    m0s = line.cdp_midpoints[:1]
+    seed, pop = 77, 24
+    de, _ = engine.differential_evolution(m0s, pop, 1, 0.85, 0.5, seed=seed)
+    init = oracle.de_initial_population(seed, 0, line.samples_per_trace, pop, lower, upper)
+    sel = np.nonzero(line.midpoints == m0s[0])[0].astype(np.uint32)
+    sem, _ = oracle.eval_raw("cmp", line.samples, line.midpoints, line.halfoffsets, sel,
+                             m0s[0], float(line.dt), 2, init, precision="f32")
+    # the reported velocity is one of that sample's initial individuals, bit for bit
+    S = line.samples_per_trace
+    member = np.array([np.any(init[s, :, 0] == de[0, 2, s]) for s in range(S)])
+    assert member.all()
+    best = sem.max(axis=1)
+    chosen = np.array([sem[s, np.nonzero(init[s, :, 0] == de[0, 2, s])[0][0]] for s in range(S)])
+    assert np.all(np.abs(chosen - best) <= 1e-4 * np.maximum(best, 1e-3))
+
+
+def test_de_is_deterministic_per_seed(engine):
+    line = _cmp_line()
+    _setup(engine, line, "cmp", [1000.0], [5040.0])
+    m0s = line.cdp_midpoints
+    a, _ = engine.differential_evolution(m0s, 16, 6, 0.5, 0.9, seed=11)
+    b, _ = engine.differential_evolution(m0s, 16, 6, 0.5, 0.9, seed=11)
+    c, _ = engine.differential_evolution(m0s, 16, 6, 0.5, 0.9, seed=12)
+    assert np.array_equal(a, b)
+    assert not np.array_equal(a, c)
+
+
+@pytest.mark.parametrize("pop", [1, 48, 128])
+def test_de_population_sizes(engine, pop):
+    line = _cmp_line()
+    _setup(engine, line, "cmp", [1000.0], [5040.0])
+    de, _ = engine.differential_evolution(line.cdp_midpoints[:1], pop, 4, 0.5, 0.9, seed=3)
+    assert np.all((de[0, 2] >= 1000.0) & (de[0, 2] <= 5040.0))
+    assert np.all(np.isfinite(de))
+
+
+def test_de_zocrs_small_line(engine):
+    line = synthetic.structured_line(n_cmp=20, fold_range=(6, 10), h_max=1000, ns=300,
+                                     dt_us=4000, n_reflectors=4, f=20.0, snr=5.0, seed=41)
+    a, b = synthetic.zocrs_bounds(1414.2136, 2000.0, 90.0, 0.05)
+    lower, upper = [1414.2136, -a, -b], [6324.5553, a, b]
+    _setup(engine, line, "zocrs", lower, upper, apm=125.0)
+    m0s = line.cdp_midpoints[5:8]
+    de, st = engine.differential_evolution(m0s, 32, 40, 0.5, 0.9, seed=2)
+    for j in range(3):
+        assert np.all((de[:, 2 + j] >= lower[j]) & (de[:, 2 + j] <= upper[j]))
+    ls, _ = engine.linear_search(m0s, [21, 11, 11], "tuned")
+    strong = ls[:, 0] > 0.1
+    ratio = de[:, 0][strong] / ls[:, 0][strong]
+    # DE searches the continuous box; the grid is coarse -- DE should match or beat it
+    assert np.median(ratio) >= 0.97, np.median(ratio)
+
+
+def test_de_oct_selection_from_initial_population(engine):
+    line = synthetic.structured_line(n_cmp=10, fold_range=(4, 8), h_max=800, ns=120,
+                                     dt_us=4000, n_reflectors=3, f=20.0, snr=8.0, seed=51)
+    lower, upper = [1200.0, -1e-3], [5000.0, 1e-3]
+    apm, h0, seed, pop = 50.0, 300.0, 9, 8
+    _setup(engine, line, "oct", lower, upper, apm=apm, h0=h0)
+    m0s = line.cdp_midpoints[3:6]
+    de, st = engine.differential_evolution(m0s, pop, 3, 0.5, 0.9, seed=seed)
+    S = line.samples_per_trace
+    want = 0
+    for i, m0 in enumerate(m0s):
+        init = oracle.de_initial_population(seed, i, S, pop, lower, upper)
+        want += int(oracle.select_oct_per_sample(line.midpoints, line.halfoffsets, m0, apm, h0,
+                                                 S, float(line.dt), init).sum())
+    # c = 4/v^2 uses the device's fast division: a boundary trace may flip
+    assert abs(st["selected_traces"] - want) <= 1
+    assert np.all(np.isfinite(de))
