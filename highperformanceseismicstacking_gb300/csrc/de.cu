@@ -172,7 +172,9 @@ de_kernel(DeParams d, uint32_t nUnits) {
 #pragma unroll
             for (int j = 0; j < NP; j++) {
                 float r = rng.next();
-                x[sl][j] = d.lo[j] + r * (d.hi[j] - d.lo[j]);
+                // min + ratio * (max - min) as one fused multiply-add, as the
+                // reference's startPopulations compiles
+                x[sl][j] = __fmaf_rn(r, __fsub_rn(d.hi[j], d.lo[j]), d.lo[j]);
             }
             fx[sl] = -1.f;
             fxk[sl] = 0.f;
@@ -205,7 +207,7 @@ de_kernel(DeParams d, uint32_t nUnits) {
                         if ((int)(r2 >> 5) == ss) x2 = o2;
                         if ((int)(r3 >> 5) == ss) x3 = o3;
                     }
-                    float nv = x1 + d.F * (x2 - x3);
+                    float nv = __fmaf_rn(d.F, __fsub_rn(x2, x3), x1);
                     nv = fminf(nv, d.hi[j]);
                     nv = fmaxf(nv, d.lo[j]);
                     v[j] = nv;
@@ -315,8 +317,8 @@ __global__ void de_select_oct_kernel(DeParams d, const uint32_t *candFirst,
                     bool hit = false;
                     if (ind < d.pop) {
                         Draws rng(d.seedLo, d.seedHi, mi, s, ind, 0);
-                        float v = d.lo[0] + rng.next() * (d.hi[0] - d.lo[0]);
-                        float sl = d.lo[1] + rng.next() * (d.hi[1] - d.lo[1]);
+                        float v = __fmaf_rn(rng.next(), __fsub_rn(d.hi[0], d.lo[0]), d.lo[0]);
+                        float sl = __fmaf_rn(rng.next(), __fsub_rn(d.hi[1], d.lo[1]), d.lo[1]);
                         float c = 4.0f / (v * v);
                         float mh;
                         int e = oct_displaced_midpoint(h, a.h0, t0, m0, c, sl, &mh);

@@ -46,7 +46,7 @@ struct hpss_handle_s : public Handle {
         size_t bytes = 0;
     };
     Buf params, chunkBounds, selFirst, selCount, selIdx, candFirst, candCount,
-        notUsed, errWord, m0s, out, octCands;
+        notUsed, errWord, m0s, out, octCands, prior;
     std::vector<float> octCandsHost;
     std::map<std::string, int> variantCache;  // autotuner decisions
     int lastVariant = -1;
@@ -586,7 +586,7 @@ hpss_status hpss_destroy(hpss_handle h) {
     free_gather(h);
     for (auto *b : {&h->params, &h->chunkBounds, &h->selFirst, &h->selCount, &h->selIdx,
                     &h->candFirst, &h->candCount, &h->notUsed, &h->errWord, &h->m0s,
-                    &h->out, &h->octCands})
+                    &h->out, &h->octCands, &h->prior})
         release(h, *b);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
@@ -798,9 +798,106 @@ hpss_status hpss_differential_evolution(hpss_handle h, const float *m0s, uint32_
     return HPSS_OK;
 }
 
-hpss_status hpss_stretch_free(hpss_handle h, const float *, uint32_t, const float *, int,
-                              float *, hpss_stats *) {
-    return set_error(h, HPSS_ERR_NOT_READY, "stretch-free not built yet");
+hpss_status hpss_stretch_free(hpss_handle h, const float *m0s, uint32_t nM0,
+                              const float *params, int nmax, float *out, hpss_stats *stats) {
+    if (!h) return HPSS_ERR_INVALID_ARGUMENT;
+    hpss_status rc = check_ready(h);
+    if (rc != HPSS_OK) return rc;
+    if (nmax < 0 || nmax > 4096)
+        return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "nmax must be in [0, 4096]");
+    if (nM0 == 0) return HPSS_OK;
+    if (!m0s || !params || !out)
+        return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "null host pointer");
+    cudaSetDevice(h->device);
+    const size_t priorElems = (size_t)nM0 * h->np * h->S;
+    const size_t outElems = (size_t)nM0 * 3 * h->S;
+    HPSS_CUDA_TRY(h, ensure(h, h->m0s, nM0 * sizeof(float)));
+    HPSS_CUDA_TRY(h, ensure(h, h->out, outElems * sizeof(float)));
+    HPSS_CUDA_TRY(h, ensure(h, h->prior, priorElems * sizeof(float)));
+    HPSS_CUDA_TRY(h, cudaMemcpyAsync(h->m0s.p, m0s, nM0 * sizeof(float),
+                                     cudaMemcpyHostToDevice, h->stream));
+    HPSS_CUDA_TRY(h, cudaMemcpyAsync(h->prior.p, params, priorElems * sizeof(float),
+                                     cudaMemcpyHostToDevice, h->stream));
+    LsParams lp;
+    fill_line_params(h, lp);
+    const float *d_m0s = static_cast<float *>(h->m0s.p);
+    lp.m0s = d_m0s;
+    lp.nM0 = nM0;
+    lp.out = static_cast<float *>(h->out.p);
+    lp.prior = static_cast<float *>(h->prior.p);
+    lp.nmax = nmax;
+    HPSS_CUDA_TRY(h, ensure(h, h->notUsed, nM0 * sizeof(unsigned long long)));
+    lp.notUsed = static_cast<unsigned long long *>(h->notUsed.p);
+    HPSS_CUDA_TRY(h, cudaMemsetAsync(lp.notUsed, 0, nM0 * sizeof(unsigned long long), h->stream));
+    HPSS_CUDA_TRY(h, cudaEventRecord(h->ev0, h->stream));
+    HPSS_CUDA_TRY(h, ensure(h, h->selFirst, nM0 * sizeof(uint32_t)));
+    HPSS_CUDA_TRY(h, ensure(h, h->selCount, nM0 * sizeof(uint32_t)));
+    lp.selFirst = static_cast<uint32_t *>(h->selFirst.p);
+    lp.selCount = static_cast<uint32_t *>(h->selCount.p);
+    lp.selIdx = nullptr;
+    if (h->model != HPSS_MODEL_OCT) {
+        HPSS_CUDA_TRY(h, launch_select_range(h->dMid, h->nTraces, d_m0s, nM0,
+                                             h->model == HPSS_MODEL_CMP ? 0 : 1, h->apm, 0.f,
+                                             static_cast<uint32_t *>(h->selFirst.p),
+                                             static_cast<uint32_t *>(h->selCount.p), h->stream));
+    } else {
+        float hmax = 0.f;
+        for (float v : h->hHoff) hmax = std::max(hmax, std::fabs(v));
+        float radius = (h->apm + std::sqrt(hmax * hmax + h->h0 * h->h0)) * 1.001f + 1.0f;
+        HPSS_CUDA_TRY(h, ensure(h, h->candFirst, nM0 * sizeof(uint32_t)));
+        HPSS_CUDA_TRY(h, ensure(h, h->candCount, nM0 * sizeof(uint32_t)));
+        uint32_t *cf = static_cast<uint32_t *>(h->candFirst.p);
+        uint32_t *cc = static_cast<uint32_t *>(h->candCount.p);
+        HPSS_CUDA_TRY(h, launch_select_range(h->dMid, h->nTraces, d_m0s, nM0, 2, h->apm, radius,
+                                             cf, cc, h->stream));
+        HPSS_CUDA_TRY(h, launch_exclusive_scan(cc, static_cast<uint32_t *>(h->selFirst.p), nM0,
+                                               h->stream));
+        std::vector<uint32_t> ccHost(nM0);
+        HPSS_CUDA_TRY(h, cudaMemcpyAsync(ccHost.data(), cc, nM0 * sizeof(uint32_t),
+                                         cudaMemcpyDeviceToHost, h->stream));
+        HPSS_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+        size_t total = 0;
+        for (uint32_t v : ccHost) total += v;
+        HPSS_CUDA_TRY(h, ensure(h, h->selIdx, total * sizeof(uint32_t)));
+        lp.selIdx = static_cast<uint32_t *>(h->selIdx.p);
+        HPSS_CUDA_TRY(h, launch_sf_select_oct(lp, cf, cc, static_cast<uint32_t *>(h->selIdx.p),
+                                              static_cast<uint32_t *>(h->selCount.p),
+                                              h->stream));
+    }
+    HPSS_CUDA_TRY(h, cudaEventRecord(h->ev1, h->stream));
+    const uint64_t units = (uint64_t)nM0 * h->S;
+    if (units > 0xffffffffull)
+        return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "too many (midpoint, sample) units");
+    const uint32_t grid = (uint32_t)std::min<uint64_t>((units + 7) / 8, (uint64_t)num_sms(h) * 8);
+    HPSS_CUDA_TRY(h, launch_sf(lp, h->model, grid, (uint32_t)units, h->stream));
+    HPSS_CUDA_TRY(h, cudaEventRecord(h->ev2, h->stream));
+    HPSS_CUDA_TRY(h, cudaMemcpyAsync(out, lp.out, outElems * sizeof(float),
+                                     cudaMemcpyDeviceToHost, h->stream));
+    HPSS_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    if (stats) {
+        std::memset(stats, 0, sizeof(*stats));
+        std::vector<uint32_t> cnt(nM0);
+        std::vector<unsigned long long> nu(nM0);
+        HPSS_CUDA_TRY(h, cudaMemcpy(cnt.data(), lp.selCount, nM0 * sizeof(uint32_t),
+                                    cudaMemcpyDeviceToHost));
+        HPSS_CUDA_TRY(h, cudaMemcpy(nu.data(), lp.notUsed, nM0 * sizeof(unsigned long long),
+                                    cudaMemcpyDeviceToHost));
+        double sel = 0, nus = 0;
+        for (uint32_t i = 0; i < nM0; i++) {
+            sel += cnt[i];
+            nus += (double)nu[i];
+        }
+        stats->selected_traces = sel;
+        stats->evals = sel * (double)h->S * (double)(2 * nmax + 1);
+        stats->not_used = nus;
+        float ms = 0;
+        cudaEventElapsedTime(&ms, h->ev1, h->ev2);
+        stats->kernel_ms = ms;
+        cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+        stats->selection_ms = ms;
+        stats->kernel_variant = -1;
+    }
+    return HPSS_OK;
 }
 
 void *hpss_stream(hpss_handle h) { return h ? static_cast<void *>(h->stream) : nullptr; }

@@ -128,6 +128,11 @@ cudaError_t launch_convert_storage(const float *src, uint16_t *dst,
 size_t tuned_smem_bytes();
 cudaError_t launch_de(const DeParams &d, int model, uint32_t grid, uint32_t nUnits,
                       cudaStream_t st);
+cudaError_t launch_sf(const LsParams &p, int model, uint32_t grid, uint32_t nUnits,
+                      cudaStream_t st);
+cudaError_t launch_sf_select_oct(const LsParams &p, const uint32_t *candFirst,
+                                 const uint32_t *candCount, uint32_t *selIdx,
+                                 uint32_t *selCount, cudaStream_t st);
 cudaError_t launch_de_select_oct(const DeParams &d, const uint32_t *candFirst,
                                  const uint32_t *candCount, uint32_t *selIdx,
                                  uint32_t *selCount, cudaStream_t st);

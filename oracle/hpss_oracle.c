@@ -152,7 +152,7 @@ void oracle_de_initial_population(uint64_t seed, uint32_t m0i, uint32_t S,
         for (uint32_t i = 0; i < pop; i++) {
             oracle_de_uniforms(seed, m0i, s, i, 0, (uint32_t)np, u);
             for (int j = 0; j < np; j++)
-                out[((size_t)s * pop + i) * np + j] = lo[j] + u[j] * (hi[j] - lo[j]);
+                out[((size_t)s * pop + i) * np + j] = fmaf(u[j], hi[j] - lo[j], lo[j]);
         }
 }
 

@@ -1,0 +1,91 @@
+"""Stretch-free stack on the GPU, through the C ABI.
+
+CMP is checked against the reference's own stretch-free kernels (golden
+fixture: the reference's semblance + best-n kernels fed with the reference's
+linear-search velocities).  ZO-CRS and OCT, which the reference's CUDA path
+does not run (its OCT case falls through into `throw`), are checked against
+the oracle's restatement of the reference kernels.
+"""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from highperformanceseismicstacking_gb300 import synthetic
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+GOLDEN = Path(__file__).resolve().parent / "golden"
+
+
+def _check_sf(out, sem, stk, nmax, near_tie=1e-4):
+    """out: engine block [3][S]; sem/stk: oracle tables [S][2*nmax+1]."""
+    idx = oracle.argmax(sem)
+    S = sem.shape[0]
+    rows = np.arange(S)
+    ref0 = sem[rows, idx]
+    rel = np.abs(out[0] - ref0) / np.maximum(np.abs(ref0), 1e-3)
+    assert np.quantile(rel, 0.999) <= 2e-4
+    n_got = out[2].astype(int)
+    far = 0
+    for s in np.nonzero(n_got != idx - nmax)[0]:
+        alt = sem[s, n_got[s] + nmax]
+        if abs(float(ref0[s]) - float(alt)) > near_tie * max(float(ref0[s]), 1e-3):
+            far += 1
+    assert far <= 0.002 * S, far
+
+
+def test_cmp_stretch_free_matches_reference_kernels(engine):
+    z = np.load(GOLDEN / "ref_cmp.npz")
+    engine.upload_gather(z["samples"], z["midpoints"], z["halfoffsets"], float(z["dt"]))
+    engine.set_traveltime("cmp", z["lower"], z["upper"])
+    engine.set_window(int(z["tau"]))
+    sf = z["sf_results"]
+    m0s = z["m0s"][: sf.shape[0]]
+    prior = z["results"][: sf.shape[0], 2:3]        # reference LS velocities [nM0][1][S]
+    out, st = engine.stretch_free(m0s, prior, 10)
+    assert st["evals"] == float(np.sum(z["counts"][: sf.shape[0]])) * sf.shape[2] * 21
+    exact = float(np.mean(np.all(out == sf, axis=1)))
+    print(f"stretch-free cmp: bit-identical samples {exact:.6f}")
+    assert exact == 1.0
+
+
+@pytest.mark.parametrize("model", ["zocrs", "oct"])
+def test_stretch_free_other_models_vs_oracle(engine, model):
+    line = synthetic.structured_line(n_cmp=12, fold_range=(6, 10), h_max=900, ns=250,
+                                     dt_us=4000, n_reflectors=3, f=20.0, snr=6.0, seed=61)
+    if model == "zocrs":
+        a, b = synthetic.zocrs_bounds(1414.2136, 2000.0, 90.0, 0.05)
+        lower, upper, gran, apm, h0 = [1414.2136, -a, -b], [6324.5553, a, b], [8, 5, 5], 100.0, 0.0
+    else:
+        lower, upper, gran, apm, h0 = [1200.0, -1e-3], [5000.0, 1e-3], [10, 5], 60.0, 200.0
+    engine.upload_gather(line.samples, line.midpoints, line.halfoffsets, float(line.dt))
+    engine.set_traveltime(model, lower, upper, apm, h0)
+    engine.set_window(2)
+    m0s = line.cdp_midpoints[4:7]
+    ls, _ = engine.linear_search(m0s, gran, "plain")
+    prior = np.ascontiguousarray(ls[:, 2:])
+    out, st = engine.stretch_free(m0s, prior, 10)
+    S = line.samples_per_trace
+    cands = oracle.oct_selection_candidates(lower, upper) if model == "oct" else None
+    for i, m0 in enumerate(m0s):
+        if model == "oct":
+            init = np.stack([prior[i, 0], prior[i, 1]], axis=1)[:, None, :]
+            sel = np.nonzero(oracle.select_oct_per_sample(line.midpoints, line.halfoffsets, m0,
+                                                          apm, h0, S, float(line.dt), init))[0]
+        else:
+            sel = np.nonzero(oracle.select(model, line.midpoints, line.halfoffsets, m0, apm))[0]
+        sem, stk, _ = oracle.sf_eval(model, line.samples, line.midpoints, line.halfoffsets,
+                                     sel.astype(np.uint32), m0, float(line.dt), 2, prior[i],
+                                     10, apm, h0)
+        _check_sf(out[i], sem, stk, 10)
+
+
+def test_stretch_free_argument_errors(engine):
+    z = np.load(GOLDEN / "ref_cmp.npz")
+    engine.upload_gather(z["samples"], z["midpoints"], z["halfoffsets"], float(z["dt"]))
+    engine.set_traveltime("cmp", z["lower"], z["upper"])
+    engine.set_window(int(z["tau"]))
+    from highperformanceseismicstacking_gb300 import capi
+    with pytest.raises(capi.HpssError):
+        engine.stretch_free(z["m0s"][:1], z["results"][:1, 2:3], -1)
