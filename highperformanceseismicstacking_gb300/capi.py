@@ -32,6 +32,7 @@ EXPORTED = [
     "hpss_set_window", "hpss_linear_search", "hpss_linear_search_device",
     "hpss_differential_evolution", "hpss_differential_evolution_device",
     "hpss_stretch_free", "hpss_select_traces", "hpss_stream", "hpss_device_bytes",
+    "hpss_linear_search_noalloc",
 ]
 
 
@@ -77,6 +78,8 @@ def load_library(path: Optional[Path] = None) -> C.CDLL:
         "hpss_select_traces": (i32, [vp, fp, u32, up]),
         "hpss_stream": (vp, [vp]),
         "hpss_device_bytes": (C.c_size_t, [vp]),
+        "hpss_linear_search_noalloc": (i32, [i32, vp, u32, vp, vp, u32, u32, f32, i32, fp, fp,
+                                             up, f32, vp, u32, vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

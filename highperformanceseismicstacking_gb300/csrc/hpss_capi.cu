@@ -535,6 +535,11 @@ hpss_status de_impl(hpss_handle h, const float *d_m0s, uint32_t nM0, uint32_t po
 
 }  // namespace
 
+namespace hpss {
+// error message of a handle-less call, read back with hpss_last_error(NULL)
+void set_thread_error(const std::string &msg) { g_createError = msg; }
+}  // namespace hpss
+
 extern "C" {
 
 const char *hpss_version(void) { return kVersion; }

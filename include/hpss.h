@@ -199,6 +199,27 @@ void *hpss_stream(hpss_handle h);
 /* Bytes of device memory currently held by the handle. */
 size_t hpss_device_bytes(hpss_handle h);
 
+/* Linear search that allocates nothing -- no counterpart in the reference.
+ * For callers that may not call cudaMalloc (a plug-in inside another
+ * framework's memory pool, a process with a fixed device-memory budget): the
+ * caller passes device buffers for the line (samples [nTraces][stride] FP32,
+ * stride >= S and a multiple of 4, 16-byte aligned; midpoints, half-offsets),
+ * the midpoints d_m0s and the output d_out [nM0][2+nParams][S]; the scratch
+ * lives in a fixed __device__ array of the library (about 5.3 MB, held on
+ * every device that loads the library).  CMP and ZO-CRS only; limits:
+ * candidates <= 65536, midpoints <= 16384, traces <= 1048576 (larger sizes are
+ * rejected with HPSS_ERR_INVALID_ARGUMENT).  The first call on a device looks
+ * the scratch up (make it before any stream capture).  Calls share the
+ * scratch: calls that overlap on the GPU race.  Enqueued on `stream`
+ * (cudaStream_t; NULL = default stream); errors via hpss_last_error(NULL).
+ * Same results as hpss_linear_search with the tuned kernel. */
+hpss_status hpss_linear_search_noalloc(
+    int model, const float *d_samples, uint32_t stride, const float *d_midpoints,
+    const float *d_halfoffsets, uint32_t nTraces, uint32_t samplesPerTrace,
+    float dtInSeconds, int tauIndexDisplacement, const float *lower,
+    const float *upper, const uint32_t *granularity, float apm,
+    const float *d_m0s, uint32_t nM0, float *d_out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
