@@ -354,6 +354,8 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
     const int S = (int)a.S, tau = a.tau;
     const float2 kNeg1 = f2(-1.f, -1.f);
     constexpr int kLastBase = kStage - W - 1;
+    // window starts k - tau that keep the whole window inside the trace
+    const unsigned winSpan = S > 2 * tau + 1 ? (unsigned)(S - 2 * tau - 1) : 0u;
 
     if (threadIdx.x < kZeroPad) sm.y[threadIdx.x] = 0.f;
 
@@ -474,7 +476,8 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
                             t = sqrtf(fmaxf(tmp, 0.f));
                         }
                         WinIdx wi = window_index(t, a.dt);
-                        const bool in = ok && window_in_trace(wi.k, tau, S);
+                        // k - tau >= 0 && k + tau + 1 < S as one unsigned compare
+                        const bool in = ok && (unsigned)(wi.k - tau) < winSpan;
                         int b = in ? md.base + wi.k - tau : 0;
 #ifdef HPSS_CHECKED
                         if (in && (b < md.base + sm.lo[j] ||
@@ -482,7 +485,9 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
                             atomicOr(a.errorWord, kErrSmemBounds);
 #endif
                         bo[r] = (int)min((unsigned)b, (unsigned)kLastBase);
-                        fr[r] = in ? wi.frac : 0.f;
+                        // out-of-trace windows read the zero pad: u = 0 for any
+                        // finite fraction, so the fraction needs no select
+                        fr[r] = wi.frac;
                         used[r] += in ? 1u : 0u;
                     }
 #pragma unroll
