@@ -334,7 +334,9 @@ struct Tuned2Smem {
     float y[Stage2<MINB>::kFloats];
     TraceMeta2 meta[kTunedThreads];
     int lo[kTunedThreads];
+    int ti[kTunedThreads];
     int warpSum[kTunedWarps];
+    int warpKeep[kTunedWarps];
     float bestS[kTunedWarps][kTileSamples];
     float bestK[kTunedWarps][kTileSamples];
     uint32_t bestP[kTunedWarps][kTileSamples];
@@ -356,6 +358,7 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
     constexpr int kLastBase = kStage - W - 1;
     // window starts k - tau that keep the whole window inside the trace
     const unsigned winSpan = S > 2 * tau + 1 ? (unsigned)(S - 2 * tau - 1) : 0u;
+    const float rdt = 1.0f / a.dt;
 
     if (threadIdx.x < kZeroPad) sm.y[threadIdx.x] = 0.f;
 
@@ -433,35 +436,45 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
                     woff += wv < warp ? sm.warpSum[wv] : 0;
                 const int off = woff + incl - len;
                 const bool fits = (q < cnt) && (off + len <= kStage);
+                // traces whose span is empty contribute nothing: compact the
+                // others so the evaluation loop has no per-trace branch
+                const bool keep = fits && len > 0;
+                const unsigned keepMask = __ballot_sync(0xffffffffu, keep);
+                if (lane == 0) sm.warpKeep[warp] = __popc(keepMask);
                 const int nfit = __syncthreads_count(fits);
-                if (fits) {
+                int slot = __popc(keepMask & ((1u << lane) - 1u));
+#pragma unroll
+                for (int wv = 0; wv < kTunedWarps; wv++) slot += wv < warp ? sm.warpKeep[wv] : 0;
+                int nkeep = 0;
+#pragma unroll
+                for (int wv = 0; wv < kTunedWarps; wv++) nkeep += sm.warpKeep[wv];
+                if (keep) {
                     TraceMeta2 md;
                     md.base = off - lo;
                     md.hsq = thsq;
                     md.dm = tm - m0;
                     md.len = len;
-                    sm.meta[threadIdx.x] = md;
-                    sm.lo[threadIdx.x] = lo;
+                    sm.meta[slot] = md;
+                    sm.lo[slot] = lo;
+                    sm.ti[slot] = (int)(a.selIdx ? a.selIdx[first + q] : first + q);
                 }
                 if (nfit == 0) {
                     if (threadIdx.x == 0) atomicOr(a.errorWord, kErrSpanOverflow);
                     break;
                 }
                 __syncthreads();
-                for (int j = warp; j < nfit; j += kTunedWarps) {
+                for (int j = warp; j < nkeep; j += kTunedWarps) {
                     const TraceMeta2 md = sm.meta[j];
-                    if (md.len == 0) continue;
                     const int lo_j = sm.lo[j];
-                    const uint32_t tj = a.selIdx ? a.selIdx[first + q0 + j] : first + q0 + j;
                     const float4 *src = reinterpret_cast<const float4 *>(
-                        a.samples + (size_t)tj * a.stride + lo_j);
+                        a.samples + (size_t)sm.ti[j] * a.stride + lo_j);
                     float4 *dst = reinterpret_cast<float4 *>(sm.y + md.base + lo_j);
                     for (int v = lane; v < (md.len >> 2); v += 32) dst[v] = __ldg(src + v);
                 }
                 __syncthreads();
-                for (int j = 0; j < nfit; j++) {
+#pragma unroll 2
+                for (int j = 0; j < nkeep; j++) {
                     const TraceMeta2 md = sm.meta[j];
-                    if (md.len == 0) continue;
                     int bo[R];
                     float fr[R];
 #pragma unroll
@@ -475,7 +488,14 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
                             ok = tmp >= 0;
                             t = sqrtf(fmaxf(tmp, 0.f));
                         }
-                        WinIdx wi = window_index(t, a.dt);
+                        // t / dt: the fast-math quotient equals t * (1/dt)
+                        // bit for bit, so the reciprocal is taken once
+                        WinIdx wi;
+                        {
+                            const float ti = __fmul_rn(t, rdt);
+                            wi.k = (int)ti;
+                            wi.frac = ti - (float)wi.k;
+                        }
                         // k - tau >= 0 && k + tau + 1 < S as one unsigned compare
                         const bool in = ok && (unsigned)(wi.k - tau) < winSpan;
                         int b = in ? md.base + wi.k - tau : 0;
