@@ -50,6 +50,9 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--zocrs-cmps", type=int, default=8,
+                    help="midpoints of the ZO-CRS line measured beside the main workload "
+                         "(0 = skip)")
     return ap.parse_args()
 
 
@@ -155,6 +158,49 @@ def make_workload(name: str, n_cmp=None):
 
 def evals_per_step(counts, S, P):
     return float(np.sum(counts)) * S * P
+
+
+def zocrs_side_measure(n_cmp, local):
+    """ZO-CRS linear search on midpoints of the 1000-CMP ZO-CRS line (full
+    +-15-CMP apertures, 21 x 21 x 41 grid): tuned vs plain, device-resident,
+    CUDA events on the engine's stream."""
+    import torch
+    from highperformanceseismicstacking_gb300 import capi
+    w, line, lower, upper, tau = make_workload("zocrs-ls")
+    P = int(np.prod(w.granularity))
+    mid = len(line.cdp_midpoints) // 2
+    m0s = np.ascontiguousarray(line.cdp_midpoints[mid:mid + n_cmp])
+    eng = capi.Engine(local)
+    eng.upload_gather(line.samples, line.midpoints, line.halfoffsets, float(line.dt))
+    eng.set_traveltime(w.model, lower, upper, w.apm, w.h0)
+    eng.set_window(tau)
+    evals = evals_per_step(eng.select_traces(m0s), line.samples_per_trace, P)
+    dev = torch.device("cuda", local)
+    d_m0 = torch.from_numpy(m0s).to(dev)
+    outs = {}
+    res = {}
+    stream = torch.cuda.ExternalStream(eng.stream, device=dev)
+    for kernel in ("tuned", "plain"):
+        d_out = torch.empty((len(m0s), 2 + eng.np, line.samples_per_trace), dtype=torch.float32,
+                            device=dev)
+        eng.linear_search_device(d_m0.data_ptr(), len(m0s), w.granularity, d_out.data_ptr(),
+                                 kernel)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        eng.linear_search_device(d_m0.data_ptr(), len(m0s), w.granularity, d_out.data_ptr(),
+                                 kernel)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        res[kernel] = {"value": evals / (ms / 1e3), "ms": ms}
+        outs[kernel] = d_out.cpu().numpy()
+    eng.close()
+    return {"workload": "zocrs-ls", "cmps": int(len(m0s)), "evals": evals,
+            "candidates": P, "mean_traces_per_midpoint": evals / P / line.samples_per_trace / len(m0s),
+            "tuned": res["tuned"], "plain": res["plain"],
+            "speedup_tuned_vs_plain": res["tuned"]["value"] / res["plain"]["value"],
+            "identical_results": bool(np.array_equal(outs["tuned"], outs["plain"]))}
 
 
 # ----------------------------------------------------------------- reference arm
@@ -383,6 +429,10 @@ def main():
     cpu = None
     if not args.no_cpu_baseline and world >= 1:
         cpu = cpu_baseline(w, line, lower, upper, tau, args.cpu_seconds)
+    zocrs = None
+    if args.zocrs_cmps > 0 and args.workload != "zocrs-ls":
+        del pinned, host_samples
+        zocrs = zocrs_side_measure(args.zocrs_cmps, local)
 
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
            "steps": args.steps, "warmup": args.warmup,
@@ -405,6 +455,7 @@ def main():
            "gpu_launches": launches_per_step * args.steps,
            "roofline": roof,
            "cpu_baseline": cpu,
+           "zocrs_linear_search": zocrs,
            "clocks": clk,
            "step_ms": step_ms}
     print(json.dumps(out))

@@ -216,8 +216,11 @@ hpss_status run_selection(hpss_handle h, const float *d_m0s, uint32_t nM0,
 void fill_line_params(hpss_handle h, LsParams &lp) {
     std::memset(&lp, 0, sizeof(lp));
     lp.samples = h->dSamples;
+    // 16-bit copies are read only by the tuned pair kernel's staging; every
+    // other kernel reads the FP32 line
     lp.samples16 = h->dSamples16;
     lp.scale = h->dScale;
+    lp.storage = h->storage;
     lp.stride = h->stride;
     lp.S = h->S;
     lp.dt = h->dt;
@@ -302,9 +305,6 @@ hpss_status linear_search_impl(hpss_handle h, const float *d_m0s, uint32_t nM0,
         return set_error(h, HPSS_ERR_LOGIC, "granularity is required");
     if (kernel != HPSS_KERNEL_PLAIN && kernel != HPSS_KERNEL_TUNED)
         return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "unknown kernel family");
-    if (h->storage != HPSS_STORAGE_FP32)
-        return set_error(h, HPSS_ERR_INVALID_ARGUMENT,
-                         "linear search runs on FP32 storage in this build");
     uint64_t P = 1;
     uint32_t gran[3] = {1, 1, 1};
     float inc[3] = {0, 0, 0}, low[3] = {0, 0, 0};

@@ -36,6 +36,7 @@ struct LsParams {
     const float *samples;     // [nTraces][stride] FP32 (when storage = FP32)
     const uint16_t *samples16;// [nTraces][stride] BF16/FP16
     const float *scale;       // [nTraces] FP16 per-trace scale
+    int storage;              // HPSS_STORAGE_* of samples16 (tuned kernel staging)
     uint32_t stride;          // samples per row in memory (>= S, mult. of 8)
     uint32_t S;
     float dt;

@@ -17,6 +17,8 @@
 // ties).  CTAs are persistent over the work units.
 #pragma once
 
+#include <cuda_fp16.h>
+
 #include "hpss_device.cuh"
 #include "hpss_internal.h"
 
@@ -344,6 +346,10 @@ struct Tuned2Smem {
 
 __device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
 
+__device__ __forceinline__ float half_bits_to_float(unsigned bits) {
+    return __half2float(__ushort_as_half((unsigned short)bits));
+}
+
 template <int MODEL, int W, int NP, int MINB>
 __global__ void __launch_bounds__(kTunedThreads, MINB)
 ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
@@ -466,10 +472,29 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
                 for (int j = warp; j < nkeep; j += kTunedWarps) {
                     const TraceMeta2 md = sm.meta[j];
                     const int lo_j = sm.lo[j];
-                    const float4 *src = reinterpret_cast<const float4 *>(
-                        a.samples + (size_t)sm.ti[j] * a.stride + lo_j);
                     float4 *dst = reinterpret_cast<float4 *>(sm.y + md.base + lo_j);
-                    for (int v = lane; v < (md.len >> 2); v += 32) dst[v] = __ldg(src + v);
+                    if (a.samples16 == nullptr) {
+                        const float4 *src = reinterpret_cast<const float4 *>(
+                            a.samples + (size_t)sm.ti[j] * a.stride + lo_j);
+                        for (int v = lane; v < (md.len >> 2); v += 32) dst[v] = __ldg(src + v);
+                    } else {
+                        // 16-bit storage: 4 samples per 8-byte load, widened to FP32
+                        const uint2 *src = reinterpret_cast<const uint2 *>(
+                            a.samples16 + (size_t)sm.ti[j] * a.stride + lo_j);
+                        const float sc = a.storage == 2 ? a.scale[sm.ti[j]] : 1.f;
+                        for (int v = lane; v < (md.len >> 2); v += 32) {
+                            const uint2 q = __ldg(src + v);
+                            dst[v] = a.storage == 2
+                                         ? make_float4(half_bits_to_float(q.x & 0xffffu) * sc,
+                                                       half_bits_to_float(q.x >> 16) * sc,
+                                                       half_bits_to_float(q.y & 0xffffu) * sc,
+                                                       half_bits_to_float(q.y >> 16) * sc)
+                                         : make_float4(__uint_as_float(q.x << 16),
+                                                       __uint_as_float(q.x & 0xffff0000u),
+                                                       __uint_as_float(q.y << 16),
+                                                       __uint_as_float(q.y & 0xffff0000u));
+                        }
+                    }
                 }
                 __syncthreads();
 #pragma unroll 2

@@ -1,0 +1,47 @@
+"""16-bit amplitude storage (BF16; FP16 with a per-trace FP32 scale).
+
+The tuned kernel stages the trace windows from the 16-bit copy (half the
+bytes) and widens them to FP32 in shared memory; interpolation and all sums
+stay FP32.  Rounding the amplitudes is a precision loss, so these modes are
+judged against the FP64 oracle: the fraction of samples whose chosen
+candidate differs (printed; bounded here) and the error of the chosen
+semblance.
+"""
+import numpy as np
+import pytest
+
+from highperformanceseismicstacking_gb300 import synthetic
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+# storage -> (max fraction of changed chosen candidates, p99.9 rel. semblance error)
+BOUNDS = {"fp32": (0.001, 2e-4), "fp16": (0.01, 2e-3), "bf16": (0.05, 2e-2)}
+
+
+@pytest.mark.parametrize("storage", ["fp32", "fp16", "bf16"])
+def test_storage_modes_against_fp64(engine, storage):
+    w = synthetic.WORKLOADS["cmp-small"]
+    line = w.make_line()
+    m0s = line.cdp_midpoints[:6]
+    engine.upload_gather(line.samples, line.midpoints, line.halfoffsets, float(line.dt),
+                         storage=storage)
+    engine.set_traveltime("cmp", w.lower, w.upper)
+    engine.set_window(2)
+    got, st = engine.linear_search(m0s, w.granularity, "tuned")
+    assert st["device_error"] == 0
+    ref, idx, _ = oracle.linear_search("cmp", line.samples, line.midpoints, line.halfoffsets, m0s,
+                                       float(line.dt), 2, w.lower, w.upper, w.granularity,
+                                       precision="f64")
+    changed = float(np.mean(~np.isclose(got[:, 2], ref[:, 2], rtol=1e-5)))
+    rel = np.abs(got[:, 0] - ref[:, 0]) / np.maximum(np.abs(ref[:, 0]), 1e-3)
+    p999 = float(np.quantile(rel, 0.999))
+    print(f"storage {storage}: changed chosen candidates {changed:.5f}, "
+          f"semblance rel. error p99.9 {p999:.2e}")
+    max_changed, max_err = BOUNDS[storage]
+    assert changed <= max_changed
+    assert p999 <= max_err
+    # plain kernel always reads FP32: unaffected by the storage mode
+    plain, _ = engine.linear_search(m0s, w.granularity, "plain")
+    if storage == "fp32":
+        assert np.array_equal(plain, got)
