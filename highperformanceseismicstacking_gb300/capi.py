@@ -22,7 +22,7 @@ ERRORS = {
 }
 MODELS = {"cmp": 0, "zocrs": 1, "oct": 2}
 STORAGE = {"fp32": 0, "bf16": 1, "fp16": 2}
-KERNELS = {"plain": 0, "tuned": 1}
+KERNELS = {"plain": 0, "tuned": 1, "tuned_exact": 2}
 N_PARAMS = {"cmp": 1, "zocrs": 3, "oct": 2}
 
 # Every symbol include/hpss.h declares.

@@ -27,12 +27,6 @@ cudaError_t launch_select_range(const float *mid, uint32_t n, const float *m0s,
                                 cudaStream_t st);
 cudaError_t launch_exclusive_scan(const uint32_t *count, uint32_t *first,
                                   uint32_t n, cudaStream_t st);
-cudaError_t launch_ls_tuned_cmp(const LsParams &p, uint32_t grid, uint32_t tiles,
-                                uint32_t nUnits, cudaStream_t st, int pairs);
-cudaError_t launch_ls_tuned_zocrs(const LsParams &p, uint32_t grid, uint32_t tiles,
-                                  uint32_t nUnits, cudaStream_t st, int pairs);
-cudaError_t launch_ls_tuned_oct(const LsParams &p, uint32_t grid, uint32_t tiles,
-                                uint32_t nUnits, cudaStream_t st, int pairs);
 size_t tuned_stage_floats();
 size_t tuned_stage_floats_min();
 }  // namespace hpss
@@ -252,7 +246,7 @@ constexpr int kVariantCtasPerSm[kTunedVariants] = {2, 3, 3};
 // overwritten by the real launch) and the fastest is cached in the handle.
 // HPSS_LS_VARIANT=<n> forces a variant.
 template <typename SetChunks, typename Launch>
-hpss_status choose_variant(hpss_handle h, const LsParams &lp, uint32_t units,
+hpss_status choose_variant(hpss_handle h, const LsParams &lp, uint32_t units, bool exactStack,
                            SetChunks setChunks, Launch launch, int *out) {
     if (const char *env = std::getenv("HPSS_LS_VARIANT")) {
         int v = std::atoi(env);
@@ -261,7 +255,8 @@ hpss_status choose_variant(hpss_handle h, const LsParams &lp, uint32_t units,
             return HPSS_OK;
         }
     }
-    const std::string key = std::to_string(h->model) + "/" + std::to_string(lp.w) + "/" +
+    const std::string key = std::to_string(h->model) + "/" + std::to_string(exactStack) + "/" +
+                            std::to_string(lp.w) + "/" +
                             std::to_string(lp.P) + "/" + std::to_string(lp.S) + "/" +
                             std::to_string(h->meanFold);
     auto it = h->variantCache.find(key);
@@ -303,8 +298,11 @@ hpss_status linear_search_impl(hpss_handle h, const float *d_m0s, uint32_t nM0,
     if (rc != HPSS_OK) return rc;
     if (!granularity)
         return set_error(h, HPSS_ERR_LOGIC, "granularity is required");
-    if (kernel != HPSS_KERNEL_PLAIN && kernel != HPSS_KERNEL_TUNED)
+    if (kernel != HPSS_KERNEL_PLAIN && kernel != HPSS_KERNEL_TUNED &&
+        kernel != HPSS_KERNEL_TUNED_EXACT)
         return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "unknown kernel family");
+    const bool tuned = kernel != HPSS_KERNEL_PLAIN;
+    const bool exactStack = kernel == HPSS_KERNEL_TUNED_EXACT;
     uint64_t P = 1;
     uint32_t gran[3] = {1, 1, 1};
     float inc[3] = {0, 0, 0}, low[3] = {0, 0, 0};
@@ -339,9 +337,9 @@ hpss_status linear_search_impl(hpss_handle h, const float *d_m0s, uint32_t nM0,
     // kTunedVariants shapes (candidate pairs per thread x CTAs per SM), OCT the
     // branchy kernel (4 candidates per thread).  The chunk bounds depend on
     // the chunk size (8 warps x candidates per thread).
-    const bool pairKernel = kernel == HPSS_KERNEL_TUNED && h->model != HPSS_MODEL_OCT &&
+    const bool pairKernel = tuned && h->model != HPSS_MODEL_OCT &&
                             lp.w <= 15 && h->stride + 8 <= (uint32_t)tuned_stage_floats_min();
-    const bool branchyKernel = kernel == HPSS_KERNEL_TUNED && h->model == HPSS_MODEL_OCT &&
+    const bool branchyKernel = tuned && h->model == HPSS_MODEL_OCT &&
                                lp.w <= 15 && h->stride + 8 <= (uint32_t)tuned_stage_floats();
     auto setChunks = [&](int perThread) -> cudaError_t {
         lp.chunkSize = kTunedWarps * perThread;
@@ -371,12 +369,13 @@ hpss_status linear_search_impl(hpss_handle h, const float *d_m0s, uint32_t nM0,
         const uint32_t grid = (uint32_t)std::min<uint64_t>(
             nUnits, (uint64_t)num_sms(h) * kVariantCtasPerSm[variant]);
         return h->model == HPSS_MODEL_CMP
-                   ? launch_ls_tuned_cmp(lp, grid, tiles, nUnits, h->stream, variant)
-                   : launch_ls_tuned_zocrs(lp, grid, tiles, nUnits, h->stream, variant);
+                   ? launch_ls_tuned_cmp(lp, grid, tiles, nUnits, h->stream, variant, exactStack)
+                   : launch_ls_tuned_zocrs(lp, grid, tiles, nUnits, h->stream, variant,
+                                           exactStack);
     };
     int variant = 0;
     if (pairKernel) {
-        rc = choose_variant(h, lp, (uint32_t)units, setChunks, launchPair, &variant);
+        rc = choose_variant(h, lp, (uint32_t)units, exactStack, setChunks, launchPair, &variant);
         if (rc != HPSS_OK) return rc;
         HPSS_CUDA_TRY(h, setChunks(2 * kVariantPairs[variant]));
         HPSS_CUDA_TRY(h, cudaEventRecord(h->ev1, h->stream));

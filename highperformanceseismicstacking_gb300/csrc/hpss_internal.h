@@ -117,7 +117,24 @@ cudaError_t launch_build_grid(int model, const float *lower, const float *inc,
 cudaError_t launch_chunk_bounds(const LsParams &p, float *bounds,
                                 cudaStream_t st);
 cudaError_t launch_ls_plain(const LsParams &p, cudaStream_t st);
-cudaError_t launch_ls_tuned(const LsParams &p, cudaStream_t st);
+// Tuned pair kernel (CMP / ZO-CRS) shapes, `variant`: 0 = 2 candidate pairs
+// per thread, 2 CTAs/SM; 1 = 1 pair, 3 CTAs/SM; 2 = 2 pairs, 3 CTAs/SM
+// (chunk = 8 warps x 2*pairs candidates).  exactStack selects the
+// instantiations that accumulate the stack's linear sum in the reference's
+// order.
+cudaError_t launch_ls_tuned_cmp(const LsParams &p, uint32_t grid, uint32_t tiles,
+                                uint32_t nUnits, cudaStream_t st, int variant,
+                                bool exactStack);
+cudaError_t launch_ls_tuned_zocrs(const LsParams &p, uint32_t grid, uint32_t tiles,
+                                  uint32_t nUnits, cudaStream_t st, int variant,
+                                  bool exactStack);
+cudaError_t launch_ls_tuned_cmp_exact(const LsParams &p, uint32_t grid, uint32_t tiles,
+                                      uint32_t nUnits, cudaStream_t st, int variant);
+cudaError_t launch_ls_tuned_zocrs_exact(const LsParams &p, uint32_t grid, uint32_t tiles,
+                                        uint32_t nUnits, cudaStream_t st, int variant);
+// Tuned kernel for OCT (4 candidates per thread, branchy window loop).
+cudaError_t launch_ls_tuned_oct(const LsParams &p, uint32_t grid, uint32_t tiles,
+                                uint32_t nUnits, cudaStream_t st, int unused);
 cudaError_t launch_select_oct(const LsParams &p, const float *cands,
                               uint32_t nCand, uint32_t *selIdx,
                               uint32_t *selCount, const uint32_t *candFirst,

@@ -12,7 +12,9 @@
 // against them.  Lanes of a warp read nearly consecutive shared-memory words
 // (one sample apart), so the window loads are free of bank conflicts.  The
 // per-candidate arithmetic is the reference's (interface.h:26-55), so the
-// results equal the plain kernel's bit for bit.  The argmax over candidates
+// semblances and chosen candidates equal the plain kernel's bit for bit (the
+// stack too, except where the pair kernel derives the linear sum from the
+// per-tap sums, see EXACT_STACK below).  The argmax over candidates
 // is kept in registers and reduced across warps at the end (lowest index wins
 // ties).  CTAs are persistent over the work units.
 #pragma once
@@ -350,7 +352,12 @@ __device__ __forceinline__ float half_bits_to_float(unsigned bits) {
     return __half2float(__ushort_as_half((unsigned short)bits));
 }
 
-template <int MODEL, int W, int NP, int MINB>
+// EXACT_STACK: accumulate the linear sum tap by tap in the reference's order
+// (stack bit-identical to the reference); otherwise the linear sum is taken
+// as the sum of the W per-tap numerator sums at the end (the same quantity
+// summed in another order: one FADD2 per tap less, the stack within a few
+// ulp).  Semblance and the chosen candidate are identical either way.
+template <int MODEL, int W, int NP, int MINB, bool EXACT_STACK>
 __global__ void __launch_bounds__(kTunedThreads, MINB)
 ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
     constexpr int kStage = Stage2<MINB>::kFloats;
@@ -548,7 +555,7 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
                             const float2 d = __ffma2_rn(y0, kNeg1, y1);   // y1 - y0
                             const float2 u = __ffma2_rn(d, fq, y0);       // (y1-y0)*f + y0
                             num[qq][jj] = __fadd2_rn(num[qq][jj], u);
-                            lin[qq] = __fadd2_rn(lin[qq], u);
+                            if (EXACT_STACK) lin[qq] = __fadd2_rn(lin[qq], u);
                             den[qq] = __ffma2_rn(u, u, den[qq]);
                         }
                     }
@@ -564,9 +571,15 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
                     float nm[W];
 #pragma unroll
                     for (int jj = 0; jj < W; jj++) nm[jj] = h ? num[qq][jj].y : num[qq][jj].x;
+                    float ls = h ? lin[qq].y : lin[qq].x;
+                    if (!EXACT_STACK) {
+                        ls = 0.f;
+#pragma unroll
+                        for (int jj = 0; jj < W; jj++) ls += nm[jj];
+                    }
                     float sembl, stack;
-                    reduce_semblance(nm, h ? lin[qq].y : lin[qq].x, h ? den[qq].y : den[qq].x,
-                                     W, used[r], &sembl, &stack);
+                    reduce_semblance(nm, ls, h ? den[qq].y : den[qq].x, W, used[r], &sembl,
+                                     &stack);
                     const uint32_t p = chunk * a.chunkSize + warp * R + r;
                     if (valid[r] && sembl > best) {
                         best = sembl;
@@ -607,14 +620,14 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
     }
 }
 
-template <int MODEL, int NP, int MINB>
+template <int MODEL, int NP, int MINB, bool EXACT_STACK>
 cudaError_t launch_ls_tuned2_model(const LsParams &p, uint32_t grid,
                                    uint32_t tiles, uint32_t nUnits,
                                    cudaStream_t st) {
     const size_t smem = sizeof(Tuned2Smem<MINB>);
 #define HPSS_TUNED2_CASE(WV)                                                  \
     case WV: {                                                                \
-        auto k = ls_tuned2_kernel<MODEL, WV, NP, MINB>;                      \
+        auto k = ls_tuned2_kernel<MODEL, WV, NP, MINB, EXACT_STACK>;         \
         cudaError_t e = cudaFuncSetAttribute(                                 \
             k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);       \
         if (e != cudaSuccess) return e;                                       \
@@ -664,12 +677,5 @@ cudaError_t launch_ls_tuned_model(const LsParams &p, uint32_t grid,
     }
 #undef HPSS_TUNED_CASE
 }
-
-cudaError_t launch_ls_tuned_cmp(const LsParams &p, uint32_t grid, uint32_t tiles,
-                                uint32_t nUnits, cudaStream_t st, int pairs);
-cudaError_t launch_ls_tuned_zocrs(const LsParams &p, uint32_t grid, uint32_t tiles,
-                                  uint32_t nUnits, cudaStream_t st, int pairs);
-cudaError_t launch_ls_tuned_oct(const LsParams &p, uint32_t grid, uint32_t tiles,
-                                uint32_t nUnits, cudaStream_t st, int pairs);
 
 }  // namespace hpss

@@ -31,10 +31,6 @@ namespace hpss {
 cudaError_t launch_select_range(const float *mid, uint32_t n, const float *m0s,
                                 uint32_t nM0, int mode, float apm, float radius,
                                 uint32_t *first, uint32_t *count, cudaStream_t st);
-cudaError_t launch_ls_tuned_cmp(const LsParams &p, uint32_t grid, uint32_t tiles,
-                                uint32_t nUnits, cudaStream_t st, int variant);
-cudaError_t launch_ls_tuned_zocrs(const LsParams &p, uint32_t grid, uint32_t tiles,
-                                  uint32_t nUnits, cudaStream_t st, int variant);
 size_t tuned_stage_floats();
 void set_thread_error(const std::string &msg);
 }  // namespace hpss
@@ -184,8 +180,8 @@ extern "C" hpss_status hpss_linear_search_noalloc(
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         const uint32_t grid = (uint32_t)std::min<uint64_t>(units, (uint64_t)sms * 2);
         e = model == HPSS_MODEL_CMP
-                ? launch_ls_tuned_cmp(lp, grid, tiles, (uint32_t)units, st, 0)
-                : launch_ls_tuned_zocrs(lp, grid, tiles, (uint32_t)units, st, 0);
+                ? launch_ls_tuned_cmp(lp, grid, tiles, (uint32_t)units, st, 0, false)
+                : launch_ls_tuned_zocrs(lp, grid, tiles, (uint32_t)units, st, 0, false);
     } else {
         e = launch_ls_plain(lp, st);
     }

@@ -712,7 +712,8 @@ EngineOptions Parser::engineOptions() const {
         std::string k = str("kernel");
         if (k == "plain") o.kernel = HPSS_KERNEL_PLAIN;
         else if (k == "tuned") o.kernel = HPSS_KERNEL_TUNED;
-        else throw std::invalid_argument("--kernel must be tuned or plain");
+        else if (k == "tuned-exact") o.kernel = HPSS_KERNEL_TUNED_EXACT;
+        else throw std::invalid_argument("--kernel must be tuned, tuned-exact or plain");
     }
     if (has("seed")) {
         o.seed = std::stoull(str("seed"));

@@ -66,10 +66,15 @@ typedef int hpss_status;
 /* Kernel family: PLAIN is the one-(sample, candidate)-per-thread FP32 form of
  * the reference kernels with the argmax fused (its arithmetic is the
  * reference's, operation for operation); TUNED stages each gather's trace
- * windows in shared memory with bulk async copies and shares them across the
- * candidates of a CTA. */
+ * windows in shared memory and shares them across the candidates of a CTA.
+ * For CMP and ZO-CRS, TUNED takes the stack's linear sum as the sum of the
+ * per-tap window sums (semblance and chosen parameters identical to PLAIN,
+ * the stack within a few ulp); TUNED_EXACT accumulates it in the reference's
+ * order (every output identical to PLAIN) at one more add per tap.  For OCT
+ * both run the same kernel. */
 #define HPSS_KERNEL_PLAIN 0
 #define HPSS_KERNEL_TUNED 1
+#define HPSS_KERNEL_TUNED_EXACT 2
 
 typedef struct hpss_handle_s *hpss_handle;
 

@@ -95,3 +95,32 @@ def compare_block(rep: Report, got: np.ndarray, sem: np.ndarray, stk: np.ndarray
     if same.any():
         rep.stack_err.append(np.abs(got[1][same] - stk[rows[same], idx[same]]) / max(rms, 1e-12))
     return rep
+
+
+# Stack of the tuned kernel against the plain kernel (or the reference's
+# kernels): the tuned kernel sums the same window values in another order
+# (the per-tap sums first), so the stack agrees to a few ulp of the summands:
+# |a - b| <= STACK_REL * (|b| + max |b| over the midpoint).
+STACK_REL = 1e-5
+
+
+def assert_same_but_stack(a: np.ndarray, b: np.ndarray, n_params: int):
+    """a, b: result tables [nM0][2+np][S] (or [S][2+np] rows).  Semblance and
+    parameter rows identical; stack within STACK_REL."""
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    assert a.shape == b.shape
+    if a.ndim == 3:
+        assert np.array_equal(a[:, 0], b[:, 0]), "semblance differs"
+        assert np.array_equal(a[:, 2:], b[:, 2:]), "chosen parameters differ"
+        sa, sb = a[:, 1], b[:, 1]
+        scale = np.max(np.abs(sb), axis=1, keepdims=True)
+    else:
+        keep = [0] + list(range(2, 2 + n_params))
+        assert np.array_equal(a[..., keep], b[..., keep]), "semblance or parameters differ"
+        sa, sb = a[..., 1], b[..., 1]
+        scale = np.max(np.abs(sb))
+    err = np.abs(sa - sb)
+    tol = STACK_REL * (np.abs(sb) + scale)
+    assert np.all(err <= tol), float(np.max(err / np.maximum(tol, 1e-30)))
+    return float(np.max(err / np.maximum(np.abs(sb) + scale, 1e-30)))

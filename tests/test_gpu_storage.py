@@ -12,6 +12,7 @@ import pytest
 
 from highperformanceseismicstacking_gb300 import synthetic
 from oracle import oracle
+from parity import assert_same_but_stack
 
 pytestmark = pytest.mark.gpu
 
@@ -44,4 +45,4 @@ def test_storage_modes_against_fp64(engine, storage):
     # plain kernel always reads FP32: unaffected by the storage mode
     plain, _ = engine.linear_search(m0s, w.granularity, "plain")
     if storage == "fp32":
-        assert np.array_equal(plain, got)
+        assert_same_but_stack(got, plain, 1)
