@@ -362,6 +362,7 @@ def main():
                                   "tuned", stats=True)
     kernel_ms = st["kernel_ms"]
     variant = st.get("kernel_variant")
+    near_ties = st.get("near_ties", 0.0)
     tuned_out = d_out.cpu().numpy()
 
     # ---- plain kernel, same line
@@ -473,6 +474,8 @@ def main():
            "plain": {"value": plain_value, "ms_per_step": plain_ms,
                      "speedup_tuned_vs_plain": value / plain_value,
                      "tuned_vs_plain": agreement},
+           "near_ties": {"samples": near_ties, "of": int(len(m0s)) * S,
+                         "rel_tolerance": 1e-4},
            "tuned_exact": {"value": evals / (exact_ms / 1e3), "ms_per_step": exact_ms,
                            "identical_to_plain": exact_same},
            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),

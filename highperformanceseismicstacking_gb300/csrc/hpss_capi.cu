@@ -208,7 +208,7 @@ hpss_status run_selection(hpss_handle h, const float *d_m0s, uint32_t nM0,
 }
 
 void fill_line_params(hpss_handle h, LsParams &lp) {
-    std::memset(&lp, 0, sizeof(lp));
+    lp = LsParams{};
     lp.samples = h->dSamples;
     // 16-bit copies are read only by the tuned pair kernel's staging; every
     // other kernel reads the FP32 line
@@ -351,11 +351,13 @@ hpss_status linear_search_impl(hpss_handle h, const float *d_m0s, uint32_t nM0,
     };
     HPSS_CUDA_TRY(h, setChunks(4));
     HPSS_CUDA_TRY(h, ensure(h, h->notUsed, nM0 * sizeof(unsigned long long)));
-    HPSS_CUDA_TRY(h, ensure(h, h->errWord, sizeof(uint32_t)));
+    // error word at byte 0, near-tie counter at byte 8
+    HPSS_CUDA_TRY(h, ensure(h, h->errWord, 16));
     lp.notUsed = static_cast<unsigned long long *>(h->notUsed.p);
     lp.errorWord = static_cast<uint32_t *>(h->errWord.p);
+    lp.nearTies = reinterpret_cast<unsigned long long *>(static_cast<char *>(h->errWord.p) + 8);
     HPSS_CUDA_TRY(h, cudaMemsetAsync(lp.notUsed, 0, nM0 * sizeof(unsigned long long), h->stream));
-    HPSS_CUDA_TRY(h, cudaMemsetAsync(lp.errorWord, 0, sizeof(uint32_t), h->stream));
+    HPSS_CUDA_TRY(h, cudaMemsetAsync(lp.errorWord, 0, 16, h->stream));
 
     HPSS_CUDA_TRY(h, cudaEventRecord(h->ev0, h->stream));
     rc = run_selection(h, d_m0s, nM0, lp);
@@ -378,6 +380,8 @@ hpss_status linear_search_impl(hpss_handle h, const float *d_m0s, uint32_t nM0,
         rc = choose_variant(h, lp, (uint32_t)units, exactStack, setChunks, launchPair, &variant);
         if (rc != HPSS_OK) return rc;
         HPSS_CUDA_TRY(h, setChunks(2 * kVariantPairs[variant]));
+        // the timing launches counted near-ties of a prefix
+        HPSS_CUDA_TRY(h, cudaMemsetAsync(lp.nearTies, 0, sizeof(unsigned long long), h->stream));
         HPSS_CUDA_TRY(h, cudaEventRecord(h->ev1, h->stream));
     }
     if (pairKernel) {
@@ -394,9 +398,12 @@ hpss_status linear_search_impl(hpss_handle h, const float *d_m0s, uint32_t nM0,
     if (stats || sync) {
         HPSS_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
         uint32_t err = 0;
+        unsigned long long ties = 0;
         HPSS_CUDA_TRY(h, cudaMemcpy(&err, lp.errorWord, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+        HPSS_CUDA_TRY(h, cudaMemcpy(&ties, lp.nearTies, sizeof(ties), cudaMemcpyDeviceToHost));
         if (stats) {
             std::memset(stats, 0, sizeof(*stats));
+            stats->near_ties = (double)ties;
             std::vector<uint32_t> cnt(nM0);
             std::vector<unsigned long long> nu(nM0);
             HPSS_CUDA_TRY(h, cudaMemcpy(cnt.data(), lp.selCount, nM0 * sizeof(uint32_t), cudaMemcpyDeviceToHost));
@@ -436,8 +443,7 @@ hpss_status de_impl(hpss_handle h, const float *d_m0s, uint32_t nM0, uint32_t po
     if (!d_m0s || !d_out) return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "null device pointer");
     cudaSetDevice(h->device);
 
-    DeParams d;
-    std::memset(&d, 0, sizeof(d));
+    DeParams d{};
     fill_line_params(h, d.ls);
     d.ls.m0s = d_m0s;
     d.ls.nM0 = nM0;
@@ -613,12 +619,15 @@ hpss_status hpss_upload_gather(hpss_handle h, const float *samples,
         return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "null input array");
     if (samplesPerTrace == 0 || !(dtInSeconds > 0.f))
         return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "samplesPerTrace and dt must be > 0");
+    // the tuned kernels take floor(t/dt) through a 2^23 offset add
+    if (samplesPerTrace > (1u << 22))
+        return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "samplesPerTrace must be <= 2^22");
     if (storage < HPSS_STORAGE_FP32 || storage > HPSS_STORAGE_FP16)
         return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "unknown storage");
     for (uint32_t i = 0; i < nTraces; i++) {
         float m = midpoints[i], o = halfoffsets[i];
-        if (!(m == m) || !(o == o))
-            return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "NaN midpoint or half-offset");
+        if (!std::isfinite(m) || !std::isfinite(o))
+            return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "non-finite midpoint or half-offset");
         if (i > 0) {
             float pm = midpoints[i - 1], ph = halfoffsets[i - 1];
             if (m < pm || (m == pm && o < ph))
@@ -691,6 +700,13 @@ hpss_status hpss_set_traveltime(hpss_handle h, int model, uint32_t nParams,
         return set_error(h, HPSS_ERR_LOGIC,
                          "model requires exact " + std::to_string(model_params(model)) +
                              " lower and upper bounds.");
+    for (uint32_t j = 0; j < nParams; j++)
+        if (!std::isfinite(lower[j]) || !std::isfinite(upper[j]))
+            return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "bounds must be finite");
+    // the first parameter is a velocity, stored as 4/v^2
+    if (!(lower[0] > 0.f) || !(upper[0] > 0.f) || !std::isfinite(4.f / (lower[0] * lower[0])) ||
+        !std::isfinite(4.f / (upper[0] * upper[0])))
+        return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "velocity bounds must be > 0");
     h->model = model;
     h->np = nParams;
     for (uint32_t j = 0; j < 3; j++) {

@@ -188,4 +188,28 @@ __device__ __forceinline__ bool better(float s1, uint32_t p1, float s0,
     return s1 > s0 || (s1 == s0 && p1 < p0);
 }
 
+// Runner-up tracking for the near-tie count: `second` is the largest
+// semblance of the candidates other than the chosen one (-1: none).  A sample
+// is a near-tie when its best semblance is positive and the runner-up lies
+// within kNearTieRel * max(best, 1e-3) of it -- where another rounding order
+// could choose another candidate.  NaN semblances never enter.
+__device__ __forceinline__ void top2_offer(float s, float best, float &second) {
+    // called before `best` is updated with s
+    if (s > best) second = best;
+    else if (s > second) second = s;
+}
+__device__ __forceinline__ void top2_merge(float b2, uint32_t p2, float s2, float &b1,
+                                           uint32_t &p1, float &s1) {
+    if (better(b2, p2, b1, p1)) {
+        s1 = fmaxf(b1, s2);
+        b1 = b2;
+        p1 = p2;
+    } else {
+        s1 = fmaxf(s1, b2);
+    }
+}
+__device__ __forceinline__ bool near_tie(float best, float second) {
+    return best > 0.f && second >= 0.f && best - second <= kNearTieRel * fmaxf(best, 1e-3f);
+}
+
 }  // namespace hpss

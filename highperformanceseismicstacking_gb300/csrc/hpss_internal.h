@@ -25,6 +25,9 @@ constexpr int kTunedWarps = 8;
 constexpr int kTunedThreads = kTileSamples * kTunedWarps;
 constexpr int kPlainThreads = 128;
 
+// Near-tie tolerance (HPSS_NEAR_TIE_REL of hpss.h).
+constexpr float kNearTieRel = 1e-4f;
+
 // Device error word bits.
 constexpr uint32_t kErrSmemBounds = 1u << 0;
 constexpr uint32_t kErrSpanOverflow = 1u << 1;
@@ -64,6 +67,7 @@ struct LsParams {
     // outputs
     float *out;               // [nM0][2+np][S]
     unsigned long long *notUsed; // [nM0] (may be null)
+    unsigned long long *nearTies = nullptr; // one counter (may be null)
     uint32_t *errorWord;
     // stretch-free: prior parameters [nM0][np][S] (raw), n range
     const float *prior;

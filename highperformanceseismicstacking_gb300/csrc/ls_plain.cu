@@ -34,7 +34,7 @@ ls_plain_kernel(LsParams a) {
     }
 
     const float t0 = static_cast<float>(s) * a.dt;
-    float best = -1.f, bestStack = 0.f;
+    float best = -1.f, bestStack = 0.f, second = -1.f;
     uint32_t bestP = 0xffffffffu;
     unsigned long long notUsed = 0;
 
@@ -75,6 +75,7 @@ ls_plain_kernel(LsParams a) {
         }
         float sembl, stack;
         reduce_semblance(num, lin, den, a.w, used, &sembl, &stack);
+        top2_offer(sembl, best, second);
         if (sembl > best) {
             best = sembl;
             bestStack = stack;
@@ -84,19 +85,18 @@ ls_plain_kernel(LsParams a) {
     }
 
     // CTA argmax (lowest candidate index wins ties).
-    __shared__ float shS[kPlainThreads / 32], shK[kPlainThreads / 32];
+    __shared__ float shS[kPlainThreads / 32], shK[kPlainThreads / 32], sh2[kPlainThreads / 32];
     __shared__ uint32_t shP[kPlainThreads / 32];
     __shared__ unsigned long long shNu[kPlainThreads / 32];
     for (int o = 16; o; o >>= 1) {
         float os = __shfl_down_sync(0xffffffffu, best, o);
         float ok = __shfl_down_sync(0xffffffffu, bestStack, o);
         uint32_t op = __shfl_down_sync(0xffffffffu, bestP, o);
+        float o2 = __shfl_down_sync(0xffffffffu, second, o);
         unsigned long long on = __shfl_down_sync(0xffffffffu, notUsed, o);
-        if (better(os, op, best, bestP)) {
-            best = os;
-            bestStack = ok;
-            bestP = op;
-        }
+        const bool take = better(os, op, best, bestP);
+        top2_merge(os, op, o2, best, bestP, second);
+        if (take) bestStack = ok;
         notUsed += on;
     }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -104,18 +104,17 @@ ls_plain_kernel(LsParams a) {
         shS[warp] = best;
         shK[warp] = bestStack;
         shP[warp] = bestP;
+        sh2[warp] = second;
         shNu[warp] = notUsed;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
         for (int wv = 1; wv < kPlainThreads / 32; wv++) {
-            if (better(shS[wv], shP[wv], best, bestP)) {
-                best = shS[wv];
-                bestStack = shK[wv];
-                bestP = shP[wv];
-            }
+            if (better(shS[wv], shP[wv], best, bestP)) bestStack = shK[wv];
+            top2_merge(shS[wv], shP[wv], sh2[wv], best, bestP, second);
             notUsed += shNu[wv];
         }
+        if (a.nearTies && near_tie(best, second)) atomicAdd(a.nearTies, 1ull);
         out[s] = best;
         out[a.S + s] = bestStack;
         if (bestP != 0xffffffffu) {

@@ -45,6 +45,7 @@ struct TunedSmem {
     float bestS[kTunedWarps][kTileSamples];
     float bestK[kTunedWarps][kTileSamples];
     uint32_t bestP[kTunedWarps][kTileSamples];
+    float bestSec[kTunedWarps][kTileSamples];
 };
 
 // Sample span [lo, lo+len) of trace (m, h, hsq) touched by any in-trace
@@ -131,6 +132,7 @@ ls_tuned_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
 
         float best = -1.f, bestStack = 0.f;
         uint32_t bestP = 0xffffffffu;
+        float second = -1.f;  // runner-up semblance (near-tie count)
         unsigned long long notUsed = 0;
 
         for (uint32_t chunk = 0; chunk < a.nChunks; chunk++) {
@@ -262,6 +264,7 @@ ls_tuned_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
                 float sembl, stack;
                 reduce_semblance(num[r], lin[r], den[r], W, used[r], &sembl, &stack);
                 const uint32_t p = chunk * a.chunkSize + warp * R + r;
+                if (valid[r]) top2_offer(sembl, best, second);
                 if (valid[r] && sembl > best) {
                     best = sembl;
                     bestStack = stack;
@@ -275,6 +278,7 @@ ls_tuned_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
         sm.bestS[warp][lane] = best;
         sm.bestK[warp][lane] = bestStack;
         sm.bestP[warp][lane] = bestP;
+        sm.bestSec[warp][lane] = second;
         if (MODEL == kModelOct) {
 #pragma unroll
             for (int o = 16; o; o >>= 1) notUsed += __shfl_xor_sync(0xffffffffu, notUsed, o);
@@ -285,11 +289,12 @@ ls_tuned_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
             for (int wv = 1; wv < kTunedWarps; wv++) {
                 float os = sm.bestS[wv][lane];
                 uint32_t op = sm.bestP[wv][lane];
-                if (better(os, op, best, bestP)) {
-                    best = os;
-                    bestStack = sm.bestK[wv][lane];
-                    bestP = op;
-                }
+                if (better(os, op, best, bestP)) bestStack = sm.bestK[wv][lane];
+                top2_merge(os, op, sm.bestSec[wv][lane], best, bestP, second);
+            }
+            if (a.nearTies) {
+                const unsigned tie = __ballot_sync(0xffffffffu, s < S && near_tie(best, second));
+                if (lane == 0 && tie) atomicAdd(a.nearTies, (unsigned long long)__popc(tie));
             }
             if (s < S) {
                 out[s] = best;
@@ -344,6 +349,7 @@ struct Tuned2Smem {
     float bestS[kTunedWarps][kTileSamples];
     float bestK[kTunedWarps][kTileSamples];
     uint32_t bestP[kTunedWarps][kTileSamples];
+    float bestSec[kTunedWarps][kTileSamples];
 };
 
 __device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
@@ -372,6 +378,10 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
     // window starts k - tau that keep the whole window inside the trace
     const unsigned winSpan = S > 2 * tau + 1 ? (unsigned)(S - 2 * tau - 1) : 0u;
     const float rdt = 1.0f / a.dt;
+    const float2 rdt2 = f2(rdt, rdt);
+    const float2 kMagic2 = f2(8388608.f, 8388608.f);      // 2^23
+    const float2 kNegMagic2 = f2(-8388608.f, -8388608.f);
+    const int magicTau = 0x4B000000 + tau;                  // bits of 2^23, plus tau
 
     if (threadIdx.x < kZeroPad) sm.y[threadIdx.x] = 0.f;
 
@@ -381,6 +391,8 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
         const int s = s0 + lane;
         const int sc = min(s, S - 1);
         const float t0 = static_cast<float>(sc) * a.dt;
+        const float t0sq = __fmul_rn(t0, t0);
+        const float2 t0sq2 = f2(t0sq, t0sq), t0p2 = f2(t0, t0);
         const float t0a = static_cast<float>(s0) * a.dt;
         const float t0b = static_cast<float>(min(s0 + kTileSamples - 1, S - 1)) * a.dt;
         const float m0 = a.m0s[mi];
@@ -394,6 +406,7 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
 
         float best = -1.f, bestStack = 0.f;
         uint32_t bestP = 0xffffffffu;
+        float second = -1.f;  // runner-up semblance (near-tie count)
 
         for (uint32_t chunk = 0; chunk < a.nChunks; chunk++) {
             float cc[R], c1[R], c2[R];
@@ -510,37 +523,56 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
                     int bo[R];
                     float fr[R];
 #pragma unroll
-                    for (int r = 0; r < R; r++) {
-                        float t;
-                        bool ok = true;
+                    for (int qq = 0; qq < NP; qq++) {
+                        // traveltime of both candidates of the pair, the
+                        // roundings of cmp_time / zocrs_t2 lane by lane
+                        const float2 cq = f2(cc[2 * qq], cc[2 * qq + 1]);
+                        const float2 hsq2 = f2(md.hsq, md.hsq);
+                        float2 t2;
                         if (MODEL == kModelCmp) {
-                            t = cmp_time(t0, cc[r], md.hsq);
+                            t2 = __ffma2_rn(cq, hsq2, t0sq2);
                         } else {
-                            const float tmp = zocrs_t2(t0, cc[r], c1[r], c2[r], md.dm, md.hsq);
-                            ok = tmp >= 0;
-                            t = sqrtf(fmaxf(tmp, 0.f));
+                            const float2 dm2 = f2(md.dm, md.dm);
+                            const float2 x = __ffma2_rn(f2(c1[2 * qq], c1[2 * qq + 1]), dm2, t0p2);
+                            const float2 bd = __fmul2_rn(f2(c2[2 * qq], c2[2 * qq + 1]), dm2);
+                            t2 = __ffma2_rn(cq, hsq2, __ffma2_rn(bd, dm2, __fmul2_rn(x, x)));
+                        }
+                        float2 t;
+                        if (MODEL == kModelCmp) {
+                            t = f2(sqrtf(t2.x), sqrtf(t2.y));
+                        } else {
+                            t = f2(sqrtf(fmaxf(t2.x, 0.f)), sqrtf(fmaxf(t2.y, 0.f)));
                         }
                         // t / dt: the fast-math quotient equals t * (1/dt)
                         // bit for bit, so the reciprocal is taken once
-                        WinIdx wi;
-                        {
-                            const float ti = __fmul_rn(t, rdt);
-                            wi.k = (int)ti;
-                            wi.frac = ti - (float)wi.k;
-                        }
-                        // k - tau >= 0 && k + tau + 1 < S as one unsigned compare
-                        const bool in = ok && (unsigned)(wi.k - tau) < winSpan;
-                        int b = in ? md.base + wi.k - tau : 0;
+                        const float2 ti = __fmul2_rn(t, rdt2);
+                        // k = (int)ti and frac = ti - k without conversions:
+                        // for 0 <= ti < 2^23, ti + 2^23 rounded toward zero is
+                        // 2^23 + floor(ti) exactly; its bits carry k, and
+                        // subtracting 2^23 (exact) gives k as a float
+                        const float2 rk = __fadd2_rz(ti, kMagic2);
+                        const float2 kf = __fadd2_rn(rk, kNegMagic2);
+                        const float2 fq = __ffma2_rn(kf, kNeg1, ti);  // ti - k, exact
+#pragma unroll
+                        for (int h = 0; h < 2; h++) {
+                            const int r = 2 * qq + h;
+                            // k - tau (ti >= 2^23, inf: far out of range)
+                            const int km = __float_as_int(h ? rk.y : rk.x) - magicTau;
+                            // k - tau >= 0 && k + tau + 1 < S as one unsigned compare
+                            bool in = (unsigned)km < winSpan;
+                            if (MODEL != kModelCmp) in = in && (h ? t2.y : t2.x) >= 0;
+                            int b = in ? md.base + km : 0;
 #ifdef HPSS_CHECKED
-                        if (in && (b < md.base + sm.lo[j] ||
-                                   b > md.base + sm.lo[j] + md.len - (W + 1)))
-                            atomicOr(a.errorWord, kErrSmemBounds);
+                            if (in && (b < md.base + sm.lo[j] ||
+                                       b > md.base + sm.lo[j] + md.len - (W + 1)))
+                                atomicOr(a.errorWord, kErrSmemBounds);
 #endif
-                        bo[r] = (int)min((unsigned)b, (unsigned)kLastBase);
-                        // out-of-trace windows read the zero pad: u = 0 for any
-                        // finite fraction, so the fraction needs no select
-                        fr[r] = wi.frac;
-                        used[r] += in ? 1u : 0u;
+                            bo[r] = (int)min((unsigned)b, (unsigned)kLastBase);
+                            // out-of-trace windows read the zero pad: u = 0 for
+                            // any finite fraction, so the fraction needs no select
+                            fr[r] = h ? fq.y : fq.x;
+                            used[r] += in ? 1u : 0u;
+                        }
                     }
 #pragma unroll
                     for (int qq = 0; qq < NP; qq++) {
@@ -581,6 +613,7 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
                     reduce_semblance(nm, ls, h ? den[qq].y : den[qq].x, W, used[r], &sembl,
                                      &stack);
                     const uint32_t p = chunk * a.chunkSize + warp * R + r;
+                    if (valid[r]) top2_offer(sembl, best, second);
                     if (valid[r] && sembl > best) {
                         best = sembl;
                         bestStack = stack;
@@ -593,16 +626,18 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
         sm.bestS[warp][lane] = best;
         sm.bestK[warp][lane] = bestStack;
         sm.bestP[warp][lane] = bestP;
+        sm.bestSec[warp][lane] = second;
         __syncthreads();
         if (warp == 0) {
             for (int wv = 1; wv < kTunedWarps; wv++) {
                 float os = sm.bestS[wv][lane];
                 uint32_t op = sm.bestP[wv][lane];
-                if (better(os, op, best, bestP)) {
-                    best = os;
-                    bestStack = sm.bestK[wv][lane];
-                    bestP = op;
-                }
+                if (better(os, op, best, bestP)) bestStack = sm.bestK[wv][lane];
+                top2_merge(os, op, sm.bestSec[wv][lane], best, bestP, second);
+            }
+            if (a.nearTies) {
+                const unsigned tie = __ballot_sync(0xffffffffu, s < S && near_tie(best, second));
+                if (lane == 0 && tie) atomicAdd(a.nearTies, (unsigned long long)__popc(tie));
             }
             if (s < S) {
                 out[s] = best;

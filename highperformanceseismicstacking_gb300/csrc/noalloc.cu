@@ -129,8 +129,7 @@ extern "C" hpss_status hpss_linear_search_noalloc(
     uint32_t *w = static_cast<uint32_t *>(base);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
 
-    LsParams lp;
-    std::memset(&lp, 0, sizeof(lp));
+    LsParams lp{};
     lp.samples = d_samples;
     lp.stride = stride;
     lp.S = samplesPerTrace;

@@ -89,7 +89,15 @@ typedef struct {
     uint32_t device_error;    /* device error word (0 = none) */
     int32_t kernel_variant;   /* tuned-kernel shape chosen by the autotuner
                                  (-1: plain / not applicable) */
+    double near_ties;         /* linear search: (m0, t0) samples whose best
+                                 semblance is > 0 and whose runner-up lies
+                                 within HPSS_NEAR_TIE_REL * max(best, 1e-3)
+                                 of it (the chosen index may differ from
+                                 another FP32 evaluation's there); 0 for
+                                 differential evolution and stretch-free */
 } hpss_stats;
+
+#define HPSS_NEAR_TIE_REL 1e-4f
 
 /* Device selection and handle creation.
  * Replaces CudaDeviceContext(devId) + activate()

@@ -124,3 +124,17 @@ def assert_same_but_stack(a: np.ndarray, b: np.ndarray, n_params: int):
     tol = STACK_REL * (np.abs(sb) + scale)
     assert np.all(err <= tol), float(np.max(err / np.maximum(tol, 1e-30)))
     return float(np.max(err / np.maximum(np.abs(sb) + scale, 1e-30)))
+
+
+def count_near_ties(sem: np.ndarray, rel: float = 1e-4) -> int:
+    """Samples of an oracle semblance table [S][P] counted as near-ties by the
+    engine (hpss_stats.near_ties): best > 0 and the runner-up within
+    rel * max(best, 1e-3) of it."""
+    sem = np.where(np.isnan(sem), -np.inf, sem.astype(np.float32))
+    if sem.shape[1] < 2:
+        return 0
+    top = np.sort(sem, axis=1)[:, -2:]
+    best, second = top[:, 1], top[:, 0]
+    tie = (best > 0) & (second >= 0) & \
+        (best - second <= np.float32(rel) * np.maximum(best, np.float32(1e-3)))
+    return int(np.sum(tie))

@@ -16,7 +16,7 @@ import pytest
 
 from highperformanceseismicstacking_gb300 import capi, synthetic
 from oracle import oracle
-from parity import Report, assert_same_but_stack, compare_block
+from parity import Report, assert_same_but_stack, compare_block, count_near_ties
 
 pytestmark = pytest.mark.gpu
 
@@ -65,6 +65,9 @@ def test_cmp_small_line_plain_vs_oracle_and_tuned(engine, c1_line):
     assert st_t["device_error"] == 0 and st_p["device_error"] == 0 and st_e["device_error"] == 0
     assert np.array_equal(plain, exact)
     assert_same_but_stack(tuned, plain, 1)
+    # identical semblances: identical near-tie counts
+    assert st_p["near_ties"] == st_t["near_ties"] == st_e["near_ties"]
+    print(f"cmp-small near-ties: {st_p['near_ties']:.0f} of {plain.shape[0] * plain.shape[2]}")
     assert np.all(plain[-1] == 0)          # midpoint without traces: zeros
     assert st_p["evals"] == 50 * 24 * 1000 * 101
     _check_against_oracle("cmp", c1_line, m0s, plain, w.lower, w.upper, w.granularity, tau)
@@ -102,8 +105,14 @@ def test_constant_traces_known_answer(engine):
     engine.upload_gather(smp, mid, hoff, 0.004)
     engine.set_traveltime("cmp", [2000.0], [4000.0])
     engine.set_window(2)
+    sem, _, _ = oracle.ls_eval("cmp", smp, mid, hoff, np.arange(n, dtype=np.uint32), 2000.0,
+                               0.004, 2, oracle.build_grid("cmp", [2000.0], [4000.0], [16]))
+    ties = count_near_ties(sem)
+    assert ties > 0
     for k in ("plain", "tuned", "tuned_exact"):
-        out, _ = engine.linear_search([2000.0], [16], k)
+        out, st = engine.linear_search([2000.0], [16], k)
+        # every candidate whose windows fit gives semblance exactly 1: near-ties
+        assert st["near_ties"] == ties, (k, st["near_ties"], ties)
         # mid-trace samples: semblance exactly 1, stack 1, lowest index (v = 2000)
         assert np.all(out[0, 0, 60:150] == 1.0)
         assert np.all(out[0, 1, 60:150] == 1.0)
@@ -167,3 +176,23 @@ def test_argument_errors(engine, c1_line):
     with pytest.raises(capi.HpssError) as e:
         engine.upload_gather(c1_line.samples, rev, c1_line.halfoffsets, float(c1_line.dt))
     assert e.value.code == -1
+    # velocity bounds must give a finite 4/v^2; geometry must be finite;
+    # traces longer than 2^22 samples are refused
+    for lo, hi in (([0.0], [2000.0]), ([-1000.0], [2000.0]), ([1e-30], [2000.0]),
+                   ([1000.0], [float("inf")])):
+        with pytest.raises(capi.HpssError) as e:
+            engine.set_traveltime("cmp", lo, hi)
+        assert e.value.code == -1
+    bad = c1_line.halfoffsets.copy()
+    bad[-1] = np.inf
+    with pytest.raises(capi.HpssError) as e:
+        engine.upload_gather(c1_line.samples, c1_line.midpoints, bad, float(c1_line.dt))
+    assert e.value.code == -1
+    import ctypes as C
+    lib = engine._lib
+    z = np.zeros(1, np.float32)
+    rc = lib.hpss_upload_gather(engine.h, z.ctypes.data_as(C.POINTER(C.c_float)),
+                                z.ctypes.data_as(C.POINTER(C.c_float)),
+                                z.ctypes.data_as(C.POINTER(C.c_float)), 0, (1 << 22) + 1,
+                                C.c_float(0.004), 0)
+    assert rc == -1
