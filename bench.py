@@ -50,6 +50,10 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--de-cmps", type=int, default=2,
+                    help="midpoints of the DE side measurement (0: skip)")
+    ap.add_argument("--no-storage-side", action="store_true",
+                    help="skip the BF16 / FP16 storage side measurement")
     ap.add_argument("--zocrs-cmps", type=int, default=8,
                     help="midpoints of the ZO-CRS line measured beside the main workload "
                          "(0 = skip)")
@@ -196,24 +200,80 @@ def zocrs_side_measure(n_cmp, local):
     for kernel in ("tuned", "plain"):
         d_out = torch.empty((len(m0s), 2 + eng.np, line.samples_per_trace), dtype=torch.float32,
                             device=dev)
-        eng.linear_search_device(d_m0.data_ptr(), len(m0s), w.granularity, d_out.data_ptr(),
-                                 kernel)
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        eng.linear_search_device(d_m0.data_ptr(), len(m0s), w.granularity, d_out.data_ptr(),
-                                 kernel)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        ms = e0.elapsed_time(e1)
+        ms = time_call(eng, stream, d_m0, len(m0s), w.granularity, d_out, kernel)
         res[kernel] = {"value": evals / (ms / 1e3), "ms": ms}
         outs[kernel] = d_out.cpu().numpy()
+    storage = storage_side(eng, line, stream, d_m0, len(m0s), w.granularity, evals,
+                           outs["tuned"])
     eng.close()
     return {"workload": "zocrs-ls", "cmps": int(len(m0s)), "evals": evals,
             "candidates": P, "mean_traces_per_midpoint": evals / P / line.samples_per_trace / len(m0s),
             "tuned": res["tuned"], "plain": res["plain"],
             "speedup_tuned_vs_plain": res["tuned"]["value"] / res["plain"]["value"],
-            "tuned_vs_plain": compare_outputs(outs["tuned"], outs["plain"])}
+            "tuned_vs_plain": compare_outputs(outs["tuned"], outs["plain"]),
+            "storage": storage}
+
+
+def de_side_measure(n_cmp, local):
+    """Fused differential evolution on midpoints of the DE workloads: ZO-CRS
+    (500-CMP line, 1500 samples, population 32, 60 generations, F 0.5, CR 0.9)
+    and OCT (800-CMP line, 3000 samples, population 48, 80 generations,
+    h0 = 0).  Device time of the DE launch from the engine's own events."""
+    from highperformanceseismicstacking_gb300 import capi
+    out = {}
+    for name in ("zocrs-de", "oct-de"):
+        w, line, lower, upper, tau = make_workload(name)
+        mid = len(line.cdp_midpoints) // 2
+        m0s = np.ascontiguousarray(line.cdp_midpoints[mid:mid + n_cmp])
+        with capi.Engine(local) as eng:
+            eng.upload_gather(line.samples, line.midpoints, line.halfoffsets, float(line.dt))
+            eng.set_traveltime(w.model, lower, upper, w.apm, w.h0)
+            eng.set_window(tau)
+            eng.differential_evolution(m0s, w.population, 2, w.de_f, w.de_cr, seed=1)
+            res, st = eng.differential_evolution(m0s, w.population, w.generations, w.de_f,
+                                                 w.de_cr, seed=7)
+        out[name] = {"cmps": int(len(m0s)), "samples": line.samples_per_trace,
+                     "population": w.population, "generations": w.generations,
+                     "evals": st["evals"], "not_used": st["not_used"],
+                     "kernel_ms": st["kernel_ms"],
+                     "value": st["evals"] / (st["kernel_ms"] / 1e3),
+                     "mean_best_semblance": float(np.mean(res[:, 0]))}
+    return out
+
+
+def time_call(eng, stream, d_m0, n_m0, gran, d_out, kernel, reps=1):
+    """One untimed call (autotuning, first-launch costs), then `reps` calls
+    timed with CUDA events on the engine's stream; ms per call."""
+    import torch
+    eng.linear_search_device(d_m0.data_ptr(), n_m0, gran, d_out.data_ptr(), kernel)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        eng.linear_search_device(d_m0.data_ptr(), n_m0, gran, d_out.data_ptr(), kernel)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def storage_side(eng, line, stream, d_m0, n_m0, gran, evals, fp32_out, reps=1):
+    """Tuned kernel with the amplitudes stored as BF16 / FP16 (re-uploaded on
+    the same engine): throughput and the fraction of samples whose chosen
+    parameters differ from the FP32-storage run.  Leaves the engine with FP32
+    storage."""
+    import torch
+    out = {}
+    d_out = torch.empty(fp32_out.shape, dtype=torch.float32, device=d_m0.device)
+    for st in ("bf16", "fp16"):
+        eng.upload_gather(line.samples, line.midpoints, line.halfoffsets, float(line.dt),
+                          storage=st)
+        ms = time_call(eng, stream, d_m0, n_m0, gran, d_out, "tuned", reps)
+        got = d_out.cpu().numpy()
+        changed = float(np.mean(np.any(got[:, 2:] != fp32_out[:, 2:], axis=1)))
+        out[st] = {"value": evals / (ms / 1e3), "ms": ms,
+                   "chosen_parameters_changed_vs_fp32": changed}
+    eng.upload_gather(line.samples, line.midpoints, line.halfoffsets, float(line.dt))
+    return out
 
 
 # ----------------------------------------------------------------- reference arm
@@ -390,6 +450,12 @@ def main():
     exact_ms = e0.elapsed_time(e1) / args.plain_steps
     exact_same = bool(np.array_equal(d_out.cpu().numpy(), plain_out))
 
+    # ---- 16-bit amplitude storage (tuned kernel), same line
+    storage = None
+    if not args.no_storage_side:
+        storage = storage_side(eng, line, stream, d_m0, len(m0s), w.granularity, evals,
+                               tuned_out, reps=args.plain_steps)
+
     # ---- end to end through the C ABI with host buffers
     pinned = torch.empty(line.samples.shape, dtype=torch.float32, pin_memory=True)
     pinned.numpy()[:] = line.samples
@@ -458,6 +524,9 @@ def main():
     if args.zocrs_cmps > 0 and args.workload != "zocrs-ls":
         del pinned, host_samples
         zocrs = zocrs_side_measure(args.zocrs_cmps, local)
+    de = None
+    if args.de_cmps > 0:
+        de = de_side_measure(args.de_cmps, local)
 
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
            "steps": args.steps, "warmup": args.warmup,
@@ -474,6 +543,7 @@ def main():
            "plain": {"value": plain_value, "ms_per_step": plain_ms,
                      "speedup_tuned_vs_plain": value / plain_value,
                      "tuned_vs_plain": agreement},
+           "storage_modes": storage,
            "near_ties": {"samples": near_ties, "of": int(len(m0s)) * S,
                          "rel_tolerance": 1e-4},
            "tuned_exact": {"value": evals / (exact_ms / 1e3), "ms_per_step": exact_ms,
@@ -485,6 +555,7 @@ def main():
            "roofline": roof,
            "cpu_baseline": cpu,
            "zocrs_linear_search": zocrs,
+           "differential_evolution": de,
            "clocks": clk,
            "step_ms": step_ms}
     print(json.dumps(out))

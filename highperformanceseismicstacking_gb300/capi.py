@@ -23,13 +23,14 @@ ERRORS = {
 MODELS = {"cmp": 0, "zocrs": 1, "oct": 2}
 STORAGE = {"fp32": 0, "bf16": 1, "fp16": 2}
 KERNELS = {"plain": 0, "tuned": 1, "tuned_exact": 2}
+GRID_MODES = {"reference": 0, "inclusive": 1}
 N_PARAMS = {"cmp": 1, "zocrs": 3, "oct": 2}
 
 # Every symbol include/hpss.h declares.
 EXPORTED = [
     "hpss_create", "hpss_destroy", "hpss_last_error", "hpss_version",
     "hpss_device_count", "hpss_upload_gather", "hpss_set_traveltime",
-    "hpss_set_window", "hpss_linear_search", "hpss_linear_search_device",
+    "hpss_set_window", "hpss_set_grid_mode", "hpss_linear_search", "hpss_linear_search_device",
     "hpss_differential_evolution", "hpss_differential_evolution_device",
     "hpss_stretch_free", "hpss_select_traces", "hpss_stream", "hpss_device_bytes",
     "hpss_linear_search_noalloc",
@@ -68,6 +69,7 @@ def load_library(path: Optional[Path] = None) -> C.CDLL:
         "hpss_upload_gather": (i32, [vp, fp, fp, fp, u32, u32, f32, i32]),
         "hpss_set_traveltime": (i32, [vp, i32, u32, fp, fp, f32, f32]),
         "hpss_set_window": (i32, [vp, i32]),
+        "hpss_set_grid_mode": (i32, [vp, i32]),
         "hpss_linear_search": (i32, [vp, fp, u32, up, i32, fp, C.POINTER(Stats)]),
         "hpss_linear_search_device": (i32, [vp, vp, u32, up, i32, vp, C.POINTER(Stats)]),
         "hpss_differential_evolution": (i32, [vp, fp, u32, u32, u32, f32, f32, C.c_uint64, fp,
@@ -170,6 +172,11 @@ class Engine:
 
     def set_window(self, tau_index: int):
         self._check(self._lib.hpss_set_window(self.h, int(tau_index)))
+
+    def set_grid_mode(self, mode: str):
+        """'reference' (uniform in v, upper bound excluded) or 'inclusive'
+        (both bounds included, velocity uniform in 4/v^2)."""
+        self._check(self._lib.hpss_set_grid_mode(self.h, GRID_MODES[mode]))
 
     def linear_search(self, m0s, granularity: Sequence[int], kernel: str = "tuned"
                       ) -> Tuple[np.ndarray, dict]:

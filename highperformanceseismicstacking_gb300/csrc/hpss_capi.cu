@@ -305,15 +305,27 @@ hpss_status linear_search_impl(hpss_handle h, const float *d_m0s, uint32_t nM0,
     const bool exactStack = kernel == HPSS_KERNEL_TUNED_EXACT;
     uint64_t P = 1;
     uint32_t gran[3] = {1, 1, 1};
-    float inc[3] = {0, 0, 0}, low[3] = {0, 0, 0};
+    float inc[3] = {0, 0, 0}, low[3] = {0, 0, 0}, last[3] = {0, 0, 0};
     for (uint32_t j = 0; j < h->np; j++) {
         if (granularity[j] == 0)
             return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "granularity must be > 0");
         gran[j] = granularity[j];
         P *= granularity[j];
-        low[j] = h->lower[j];
-        // setupDiscretizationSteps (LinearSearchAlgorithm.cpp:137-139)
-        inc[j] = (h->upper[j] - h->lower[j]) / static_cast<float>(granularity[j]);
+        if (h->gridMode == kGridReference) {
+            low[j] = h->lower[j];
+            // setupDiscretizationSteps (LinearSearchAlgorithm.cpp:137-139)
+            inc[j] = (h->upper[j] - h->lower[j]) / static_cast<float>(granularity[j]);
+        } else {
+            // inclusive: velocity uniform in c = 4/v^2 from c(lower) to c(upper)
+            float a = h->lower[j], b = h->upper[j];
+            if (j == 0) {
+                a = 4.0f / (h->lower[0] * h->lower[0]);
+                b = 4.0f / (h->upper[0] * h->upper[0]);
+            }
+            low[j] = a;
+            last[j] = b;
+            inc[j] = granularity[j] > 1 ? (b - a) / static_cast<float>(granularity[j] - 1) : 0.f;
+        }
     }
     if (P > 0x7fffffffull)
         return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "too many candidates");
@@ -329,7 +341,7 @@ hpss_status linear_search_impl(hpss_handle h, const float *d_m0s, uint32_t nM0,
 
     HPSS_CUDA_TRY(h, ensure(h, h->params, P * h->np * sizeof(float)));
     lp.params = static_cast<float *>(h->params.p);
-    HPSS_CUDA_TRY(h, launch_build_grid(h->model, low, inc, gran,
+    HPSS_CUDA_TRY(h, launch_build_grid(h->model, h->gridMode, low, inc, last, gran,
                                        static_cast<float *>(h->params.p), lp.P, h->stream));
     // candidates per thread of the tuned kernel: 2 * pairs (CMP / ZO-CRS),
     // 4 (OCT); HPSS_LS_PAIRS overrides the pair count (1, 2 or 4)
@@ -716,6 +728,14 @@ hpss_status hpss_set_traveltime(hpss_handle h, int model, uint32_t nParams,
     h->apm = apm;
     h->h0 = model == HPSS_MODEL_OCT ? h0 : 0.f;
     h->octCandsHost.clear();
+    return HPSS_OK;
+}
+
+hpss_status hpss_set_grid_mode(hpss_handle h, int mode) {
+    if (!h) return HPSS_ERR_INVALID_ARGUMENT;
+    if (mode != HPSS_GRID_REFERENCE && mode != HPSS_GRID_INCLUSIVE)
+        return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "unknown grid mode");
+    h->gridMode = mode;
     return HPSS_OK;
 }
 

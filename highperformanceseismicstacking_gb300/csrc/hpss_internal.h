@@ -25,6 +25,10 @@ constexpr int kTunedWarps = 8;
 constexpr int kTunedThreads = kTileSamples * kTunedWarps;
 constexpr int kPlainThreads = 128;
 
+// Candidate grid modes (HPSS_GRID_* of hpss.h).
+constexpr int kGridReference = 0;
+constexpr int kGridInclusive = 1;
+
 // Near-tie tolerance (HPSS_NEAR_TIE_REL of hpss.h).
 constexpr float kNearTieRel = 1e-4f;
 
@@ -106,6 +110,7 @@ struct Handle {
     float lower[3] = {0, 0, 0}, upper[3] = {0, 0, 0};
     float apm = 0, h0 = 0;
     int tau = -1;
+    int gridMode = kGridReference;
     // scratch (grown on demand, owned by the handle)
     void *scratch = nullptr;
     size_t scratchBytes = 0;
@@ -115,9 +120,9 @@ struct Handle {
 };
 
 // Launchers (ls_kernels.cu).
-cudaError_t launch_build_grid(int model, const float *lower, const float *inc,
-                              const uint32_t *gran, float *params, uint32_t P,
-                              cudaStream_t st);
+cudaError_t launch_build_grid(int model, int mode, const float *lower, const float *inc,
+                              const float *last, const uint32_t *gran, float *params,
+                              uint32_t P, cudaStream_t st);
 cudaError_t launch_chunk_bounds(const LsParams &p, float *bounds,
                                 cudaStream_t st);
 cudaError_t launch_ls_plain(const LsParams &p, cudaStream_t st);

@@ -8,46 +8,65 @@
 
 namespace hpss {
 
-// Candidate grid, buildParameterArrayFor* (cmp/linear_search.cu:4-17,
-// zocrs/linear_search.cu:4-34, oct/linear_search.cu:4-28): first parameter
-// slowest; velocity v = min + idx*inc stored as 4/v^2 (fast-math division,
-// as the reference computes it on the device).
-__global__ void build_grid_kernel(int model, float l0, float l1, float l2,
-                                  float i0, float i1, float i2, uint32_t g0,
-                                  uint32_t g1, uint32_t g2, float *params,
-                                  uint32_t P) {
+// Candidate grid, first parameter slowest (buildParameterArrayFor*,
+// cmp/linear_search.cu:4-17, zocrs/linear_search.cu:4-34,
+// oct/linear_search.cu:4-28).
+//  mode 0 (reference): value = lo + idx * inc (one fused multiply-add, as the
+//    reference's compiled kernels round it); the velocity is stored as 4/v^2
+//    (fast-math division, as the reference computes it on the device).
+//  mode 1 (inclusive): both bounds included; the velocity parameter is
+//    uniform in c = 4/v^2 from c(lower v) down to c(upper v), the others
+//    uniform in value; lo/inc/last arrive as c or value, the last index takes
+//    `last` exactly.
+struct GridArgs {
+    int model, mode;
+    float lo[3], inc[3], last[3];
+    uint32_t g[3];
+};
+
+__device__ __forceinline__ float grid_value(const GridArgs &a, int j, uint32_t idx) {
+    if (a.mode == kGridInclusive) {
+        if (a.g[j] > 1 && idx == a.g[j] - 1) return a.last[j];
+        return __fmaf_rn(static_cast<float>(idx), a.inc[j], a.lo[j]);
+    }
+    const float v = a.lo[j] + static_cast<float>(idx) * a.inc[j];
+    return j == 0 ? 4.0f / (v * v) : v;
+}
+
+__global__ void build_grid_kernel(GridArgs a, float *params, uint32_t P) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P) return;
-    if (model == kModelCmp) {
-        float v = l0 + static_cast<float>(i) * i0;
-        params[i] = 4.0f / (v * v);
-    } else if (model == kModelZocrs) {
-        uint32_t iv = (i / (g1 * g2)) % g0;
-        uint32_t ia = (i / g2) % g1;
-        uint32_t ib = i % g2;
-        float v = l0 + static_cast<float>(iv) * i0;
-        float a = l1 + static_cast<float>(ia) * i1;
-        float b = l2 + static_cast<float>(ib) * i2;
-        params[3 * i] = 4.0f / (v * v);
-        params[3 * i + 1] = a;
-        params[3 * i + 2] = b;
+    if (a.model == kModelCmp) {
+        params[i] = grid_value(a, 0, i);
+    } else if (a.model == kModelZocrs) {
+        const uint32_t iv = (i / (a.g[1] * a.g[2])) % a.g[0];
+        const uint32_t ia = (i / a.g[2]) % a.g[1];
+        const uint32_t ib = i % a.g[2];
+        params[3 * i] = grid_value(a, 0, iv);
+        params[3 * i + 1] = grid_value(a, 1, ia);
+        params[3 * i + 2] = grid_value(a, 2, ib);
     } else {
-        uint32_t iv = (i / g1) % g0;
-        uint32_t is = i % g1;
-        float v = l0 + static_cast<float>(iv) * i0;
-        float s = l1 + static_cast<float>(is) * i1;
-        params[2 * i] = 4.0f / (v * v);
-        params[2 * i + 1] = s;
+        const uint32_t iv = (i / a.g[1]) % a.g[0];
+        const uint32_t is = i % a.g[1];
+        params[2 * i] = grid_value(a, 0, iv);
+        params[2 * i + 1] = grid_value(a, 1, is);
     }
 }
 
-cudaError_t launch_build_grid(int model, const float *lower, const float *inc,
-                              const uint32_t *gran, float *params, uint32_t P,
-                              cudaStream_t st) {
+cudaError_t launch_build_grid(int model, int mode, const float *lower, const float *inc,
+                              const float *last, const uint32_t *gran, float *params,
+                              uint32_t P, cudaStream_t st) {
+    GridArgs a;
+    a.model = model;
+    a.mode = mode;
+    for (int j = 0; j < 3; j++) {
+        a.lo[j] = lower[j];
+        a.inc[j] = inc[j];
+        a.last[j] = last ? last[j] : 0.f;
+        a.g[j] = gran[j];
+    }
     uint32_t blocks = (P + 255) / 256;
-    build_grid_kernel<<<blocks, 256, 0, st>>>(
-        model, lower[0], lower[1], lower[2], inc[0], inc[1], inc[2], gran[0],
-        gran[1], gran[2], params, P);
+    build_grid_kernel<<<blocks, 256, 0, st>>>(a, params, P);
     return cudaGetLastError();
 }
 

@@ -316,7 +316,8 @@ void ComputeAlgorithm::setUp() {
     check(h, hpss_upload_gather(h, smp.data(), m.data(), hoff.data(), n, S ? S : 1,
                                 g->getSamplePeriodInSeconds() > 0 ? g->getSamplePeriodInSeconds()
                                                                   : 1e-3f,
-                                HPSS_STORAGE_FP32));
+                                storage));
+    check(h, hpss_set_grid_mode(h, gridMode));
     const unsigned np = traveltime->getNumberOfParameters();
     std::vector<float> lo(np), hi(np);
     for (unsigned j = 0; j < np; j++) {
@@ -497,15 +498,20 @@ LinearSearchAlgorithm *Gb300ComputeAlgorithmBuilder::buildLinearSearchAlgorithm(
           << " discretization granularities.";
         throw std::logic_error(e.str());
     }
-    return new LinearSearchAlgorithm(tt, ctx, threadCount, g, opts.kernel);
+    auto *alg = new LinearSearchAlgorithm(tt, ctx, threadCount, g, opts.kernel);
+    alg->setEngineStorage(opts.storage);
+    alg->setEngineGridMode(opts.gridMode);
+    return alg;
 }
 
 DifferentialEvolutionAlgorithm *Gb300ComputeAlgorithmBuilder::buildDifferentialEvolutionAlgorithm(
     std::shared_ptr<Traveltime> tt, std::shared_ptr<DeviceContext> ctx, unsigned threadCount,
     unsigned generations, unsigned population) {
     uint64_t seed = opts.seedGiven ? opts.seed : (uint64_t)time(nullptr);
-    return new DifferentialEvolutionAlgorithm(tt, ctx, threadCount, generations, population,
-                                              opts.deF, opts.deCR, seed);
+    auto *alg = new DifferentialEvolutionAlgorithm(tt, ctx, threadCount, generations, population,
+                                                   opts.deF, opts.deCR, seed);
+    alg->setEngineStorage(opts.storage);
+    return alg;
 }
 
 StretchFreeAlgorithm *Gb300ComputeAlgorithmBuilder::buildStretchFreeAlgorithm(
@@ -603,7 +609,12 @@ Parser::Parser() {
     add("v0", "Velocity used to compute ZO-CRS A parameter.");
     add("verbose", "Verbosity level. Must be in the [0..4] integer range.");
     // engine options (no reference counterpart)
-    add("kernel", "Engine kernel: tuned (default) or plain.", false, false, "tuned");
+    add("kernel", "Engine kernel: tuned (default), tuned-exact or plain.", false, false, "tuned");
+    add("precision", "Amplitude storage on the device: fp32 (default), bf16 or fp16.", false,
+        false, "fp32");
+    add("grid-mode", "Linear-search grid: reference (default; uniform in v, upper bound "
+        "excluded) or inclusive (both bounds, velocity uniform in 4/v^2).", false, false,
+        "reference");
 }
 
 void Parser::add(const std::string &name, const std::string &help, bool required, bool multi,
@@ -721,6 +732,19 @@ EngineOptions Parser::engineOptions() const {
     }
     if (has("de-f")) o.deF = f("de-f");
     if (has("de-cr")) o.deCR = f("de-cr");
+    if (has("precision")) {
+        std::string p = str("precision");
+        if (p == "fp32") o.storage = HPSS_STORAGE_FP32;
+        else if (p == "bf16") o.storage = HPSS_STORAGE_BF16;
+        else if (p == "fp16") o.storage = HPSS_STORAGE_FP16;
+        else throw std::invalid_argument("--precision must be fp32, bf16 or fp16");
+    }
+    if (has("grid-mode")) {
+        std::string gm = str("grid-mode");
+        if (gm == "reference") o.gridMode = HPSS_GRID_REFERENCE;
+        else if (gm == "inclusive") o.gridMode = HPSS_GRID_INCLUSIVE;
+        else throw std::invalid_argument("--grid-mode must be reference or inclusive");
+    }
     return o;
 }
 

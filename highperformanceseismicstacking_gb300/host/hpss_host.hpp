@@ -365,6 +365,10 @@ class ComputeAlgorithm {
                                                            std::vector<std::map<StatisticResult, float>> &stats) = 0;
     virtual std::string toString() const = 0;
     unsigned resultRows() const { return traveltime->getNumberOfResults(); }
+    // engine options (no reference counterpart): amplitude storage
+    // (HPSS_STORAGE_*) and linear-search grid (HPSS_GRID_*), applied by setUp
+    void setEngineStorage(int s) { storage = s; }
+    void setEngineGridMode(int m) { gridMode = m; }
 
   protected:
     void fillStats(const std::vector<float> &m0s, const hpss_stats &st, double perCandidateFactor,
@@ -376,6 +380,8 @@ class ComputeAlgorithm {
     unsigned threadCount;
     std::vector<float> computedResults;
     std::unordered_map<int, float> computedStatisticalResults;
+    int storage = HPSS_STORAGE_FP32;
+    int gridMode = HPSS_GRID_REFERENCE;
 };
 
 class LinearSearchAlgorithm : public ComputeAlgorithm {
@@ -444,6 +450,8 @@ class ComputeAlgorithmBuilder {
 // Options beyond the reference's flags: --kernel, --seed, --de-f, --de-cr.
 struct EngineOptions {
     int kernel = HPSS_KERNEL_TUNED;
+    int storage = HPSS_STORAGE_FP32;
+    int gridMode = HPSS_GRID_REFERENCE;
     uint64_t seed = 0;
     bool seedGiven = false;
     float deF = 0.85f, deCR = 0.5f;

@@ -139,6 +139,18 @@ hpss_status hpss_set_traveltime(hpss_handle h, int model, uint32_t nParams,
                                 const float *lower, const float *upper,
                                 float apm, float h0);
 
+/* Candidate grid of the linear search.  REFERENCE is
+ * buildParameterArrayFor* with setupDiscretizationSteps
+ * (LinearSearchAlgorithm.cpp:129-141): uniform in velocity, step (U - L) / G,
+ * U never reached.  INCLUSIVE includes both bounds: the velocity parameter is
+ * uniform in c = 4/v^2 from 4/L^2 (index 0, lowest velocity) to 4/U^2, the
+ * others uniform from L to U, G values each.  No reference counterpart for
+ * INCLUSIVE (the grids of the ZO-CRS workloads are stated inclusive in C).
+ * Default REFERENCE; applies to hpss_linear_search*. */
+#define HPSS_GRID_REFERENCE 0
+#define HPSS_GRID_INCLUSIVE 1
+hpss_status hpss_set_grid_mode(hpss_handle h, int mode);
+
 /* Semblance window: tauIndexDisplacement = (int)(tau / dt), window
  * w = 2 * tau + 1 (Gather.cpp:75-76).  w must be <= 31
  * (MAX_WINDOW_SIZE, common/include/gpu/interface.h:10). */

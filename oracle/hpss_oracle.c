@@ -85,6 +85,37 @@ void oracle_build_grid(int model, const float *lower, const float *upper,
     }
 }
 
+/* Inclusive grid (the engine's HPSS_GRID_INCLUSIVE): both bounds included,
+ * velocity uniform in c = 4/v^2 from 4/L^2 down to 4/U^2, the others uniform
+ * from L to U; value = fmaf(idx, step, first), the last index takes the end
+ * value exactly.  Same order as oracle_build_grid. */
+void oracle_build_grid_inclusive(int model, const float *lower, const float *upper,
+                                 const uint32_t *gran, float *params) {
+    int np = model == ORACLE_CMP ? 1 : (model == ORACLE_ZOCRS ? 3 : 2);
+    float first[3], last[3], step[3];
+    uint32_t total = 1;
+    for (int j = 0; j < np; j++) {
+        first[j] = j == 0 ? 4.0f / (lower[0] * lower[0]) : lower[j];
+        last[j] = j == 0 ? 4.0f / (upper[0] * upper[0]) : upper[j];
+        step[j] = gran[j] > 1 ? (last[j] - first[j]) / (float)(gran[j] - 1) : 0.0f;
+        total *= gran[j];
+    }
+    for (uint32_t i = 0; i < total; i++) {
+        uint32_t rem = i;
+        uint32_t idx[3] = {0, 0, 0};
+        for (int j = np - 1; j >= 0; j--) {
+            idx[j] = rem % gran[j];
+            rem /= gran[j];
+        }
+        for (int j = 0; j < np; j++) {
+            float v = (gran[j] > 1 && idx[j] == gran[j] - 1)
+                          ? last[j]
+                          : fmaf((float)idx[j], step[j], first[j]);
+            params[(size_t)i * np + j] = v;
+        }
+    }
+}
+
 void oracle_select(int model, const float *mid, const float *hoff,
                    uint32_t ntr, float m0, float apm, float h0, uint32_t S,
                    float dt, const float *cands, uint32_t ncand,

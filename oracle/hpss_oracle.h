@@ -68,6 +68,11 @@ void oracle_argmax_f64(const double *sembl, uint32_t S, uint32_t P,
 void oracle_build_grid(int model, const float *lower, const float *upper,
                        const uint32_t *gran, float *params);
 
+/* Inclusive grid: both bounds included, velocity uniform in 4/v^2 (the
+ * engine's HPSS_GRID_INCLUSIVE; no reference counterpart). */
+void oracle_build_grid_inclusive(int model, const float *lower, const float *upper,
+                                 const uint32_t *gran, float *params);
+
 /* Trace selection masks (mask[i] for every trace of the line).
  * CMP:   m == m0 (cmp/common.cu:3-15)
  * ZOCRS: |m0 - m| <= apm (zocrs/common.cu:3-16)

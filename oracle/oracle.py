@@ -43,6 +43,7 @@ def lib():
         _lib.oracle_argmax_f32.argtypes = [fp, u32, u32, C.POINTER(C.c_int32)]
         _lib.oracle_argmax_f64.argtypes = [dp, u32, u32, C.POINTER(C.c_int32)]
         _lib.oracle_build_grid.argtypes = [i32, fp, fp, up, fp]
+        _lib.oracle_build_grid_inclusive.argtypes = [i32, fp, fp, up, fp]
         _lib.oracle_select.argtypes = [i32, fp, fp, u32, f32, f32, f32, u32, f32, fp, u32,
                                        C.POINTER(C.c_uint8)]
         _lib.oracle_max_threads.restype = i32
@@ -65,13 +66,14 @@ def max_threads() -> int:
     return int(lib().oracle_max_threads())
 
 
-def build_grid(model: str, lower, upper, gran) -> np.ndarray:
+def build_grid(model: str, lower, upper, gran, mode: str = "reference") -> np.ndarray:
     lo = np.asarray(lower, np.float32)
     hi = np.asarray(upper, np.float32)
     g = np.asarray(gran, np.uint32)
     P = int(np.prod(g))
     out = np.zeros(P * N_PARAMS[model], np.float32)
-    lib().oracle_build_grid(MODELS[model], _f(lo), _f(hi), _u(g), _f(out))
+    fn = lib().oracle_build_grid if mode == "reference" else lib().oracle_build_grid_inclusive
+    fn(MODELS[model], _f(lo), _f(hi), _u(g), _f(out))
     return out.reshape(P, N_PARAMS[model])
 
 
@@ -214,11 +216,11 @@ def eval_raw(model: str, samples, mid, hoff, sel, m0: float, dt: float, tau: int
 def linear_search(model: str, samples, mid, hoff, m0s: Sequence[float], dt: float, tau: int,
                   lower, upper, gran, apm: float = 0.0, h0: float = 0.0,
                   precision: str = "f32", oct_cands: Optional[np.ndarray] = None,
-                  nthreads: int = 0):
+                  nthreads: int = 0, grid_mode: str = "reference"):
     """Whole reference linear-search flow for a list of midpoints: selection,
     grid, evaluation, argmax.  Returns out [nM0][2+np][S], idx [nM0][S],
     counts [nM0]."""
-    params = build_grid(model, lower, upper, gran)
+    params = build_grid(model, lower, upper, gran, grid_mode)
     S = samples.shape[1]
     outs, idxs, counts = [], [], []
     for m0 in m0s:

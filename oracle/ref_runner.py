@@ -241,3 +241,115 @@ class ReferenceKernels:
         self.d.launch(best, _grid(S), THREADS, [self._ptr(sem), self._ptr(stk), self._ptr(narr),
                                                 C.c_uint(nn), C.c_uint(S), self._ptr(res)])
         return res.cpu().numpy().reshape(3, S)
+
+    def differential_evolution_midpoint(self, model: str, samples, mid, hoff, m0: float,
+                                        dt: float, tau: int, lower, upper, pop: int, gens: int,
+                                        seed: int, apm: float = 0.0, h0: float = 0.0,
+                                        sel=None, operators: str = "common_differential_evolution"):
+        """DifferentialEvolutionAlgorithm::computeSemblanceAndParametersForMidpoint
+        (DifferentialEvolutionAlgorithm.cpp:21-81) with the kernels of
+        CudaDifferentialEvolutionAlgorithm (CudaDifferentialEvolutionAlgorithm.cu
+        :35-353): setupRandomSeed, startPopulations, selection, evaluation of
+        the initial population, then per generation mutate, crossover, evaluate
+        u, nextGeneration; selectBestIndividuals.  `seed` replaces the
+        reference's srand(time(NULL)); rand().  `operators` names the fatbin of
+        the DE operators (F and CR are compile-time constants there).  `sel`
+        (CMP / ZO-CRS): selected trace indices (the linear-search rule); OCT
+        runs the reference's DE selection on the initial population.
+        Returns (result [(2+np)][S], device ms from the first evaluation to
+        the selection of the best individuals, selected trace count)."""
+        torch = self.torch
+        S = samples.shape[1]
+        npar = {"cmp": 1, "zocrs": 3, "oct": 2}[model]
+        n_ind = S * pop
+        w = 2 * tau + 1
+        ncr = 2
+        f32 = torch.float32
+        x = torch.zeros(n_ind * npar, dtype=f32, device="cuda")
+        u = torch.zeros_like(x)
+        v = torch.zeros_like(x)
+        fx = torch.zeros(n_ind * ncr, dtype=f32, device="cuda")
+        fu = torch.zeros_like(fx)
+        nu = torch.zeros(n_ind, dtype=f32, device="cuda")
+        res = torch.zeros((2 + npar) * S, dtype=f32, device="cuda")
+        dmin = self._dev(np.asarray(lower, np.float32))
+        dmax = self._dev(np.asarray(upper, np.float32))
+        # curandStateXORWOW is 48 bytes; 64 per state leaves room
+        st = torch.zeros(n_ind * 64, dtype=torch.uint8, device="cuda")
+        ops = self.d.module(operators)
+        ev = self.d.module(f"{model}_differential_evolution")
+        g = _grid(n_ind)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        self.d.launch(ops["setupRandomSeed"], g, THREADS,
+                      [self._ptr(st), C.c_uint(seed & 0xffffffff), C.c_uint(pop), C.c_uint(S)])
+        self.d.launch(ops["startPopulations"], g, THREADS,
+                      [self._ptr(x), self._ptr(dmin), self._ptr(dmax), self._ptr(st),
+                       C.c_uint(pop), C.c_uint(S), C.c_uint(npar)])
+        mid = np.asarray(mid, np.float32)
+        hoff = np.asarray(hoff, np.float32)
+        if model == "oct":
+            n_all = len(mid)
+            mask = torch.zeros(n_all, dtype=torch.uint8, device="cuda")
+            # device copies held in locals: a temporary could be recycled by
+            # the allocator for the next one before the launch
+            dmid_all, dhoff_all = self._dev(mid), self._dev(hoff)
+            self.d.launch(ev["selectTracesForOffsetContinuationTrajectoryAndDifferentialEvolution"],
+                          _grid(n_all), THREADS,
+                          [self._ptr(dmid_all), self._ptr(dhoff_all), self._ptr(x),
+                           C.c_uint(n_all), C.c_uint(S), C.c_uint(pop), C.c_float(dt),
+                           C.c_float(apm), C.c_float(m0), C.c_float(h0), self._ptr(mask)])
+            sel = np.nonzero(mask.cpu().numpy())[0]
+        sel = np.asarray(sel)
+        n = int(sel.size)
+        smp = self._dev(np.ascontiguousarray(samples[sel], np.float32).ravel() if n
+                        else np.zeros(1, np.float32))
+        dm = self._dev(mid[sel] if n else np.zeros(1, np.float32))
+        dh = self._dev(hoff[sel] if n else np.zeros(1, np.float32))
+        dh2 = self._dev((hoff[sel] * hoff[sel]).astype(np.float32) if n
+                        else np.zeros(1, np.float32))
+
+        def evaluate(pp, ff):
+            if model == "cmp":
+                self.d.launch(ev["computeSemblancesForCommonMidPoint"], g, THREADS,
+                              [self._ptr(smp), self._ptr(dh2), C.c_uint(n), C.c_uint(S),
+                               C.c_uint(pop), C.c_float(dt), C.c_int(tau), C.c_int(w),
+                               C.c_uint(ncr), self._ptr(pp), self._ptr(ff)])
+            elif model == "zocrs":
+                self.d.launch(ev["computeSemblancesForZeroOffsetCommonReflectionSurface"], g,
+                              THREADS,
+                              [self._ptr(smp), self._ptr(dm), self._ptr(dh2), C.c_uint(n),
+                               C.c_uint(S), C.c_uint(pop), C.c_float(m0), C.c_float(dt),
+                               C.c_int(tau), C.c_int(w), C.c_uint(ncr), self._ptr(pp),
+                               self._ptr(ff)])
+            else:
+                self.d.launch(ev["computeSemblancesForOffsetContinuationTrajectory"], g, THREADS,
+                              [self._ptr(smp), self._ptr(dm), self._ptr(dh), C.c_uint(n),
+                               C.c_uint(S), C.c_uint(pop), C.c_float(apm), C.c_float(m0),
+                               C.c_float(h0), C.c_float(dt), C.c_int(tau), C.c_int(w),
+                               C.c_uint(ncr), self._ptr(nu), self._ptr(pp), self._ptr(ff)])
+
+        # timed from the first evaluation to the best-individual selection
+        # (selection and packing excluded, as the engine's kernel_ms)
+        e0.record()
+        evaluate(x, fx)
+        for _ in range(1, gens):
+            self.d.launch(ops["mutatePopulations"], g, THREADS,
+                          [self._ptr(v), self._ptr(x), self._ptr(dmin), self._ptr(dmax),
+                           self._ptr(st), C.c_uint(pop), C.c_uint(S), C.c_uint(npar)])
+            self.d.launch(ops["crossoverPopulations"], g, THREADS,
+                          [self._ptr(u), self._ptr(x), self._ptr(v), self._ptr(st),
+                           C.c_uint(pop), C.c_uint(S), C.c_uint(npar)])
+            evaluate(u, fu)
+            self.d.launch(ops["nextGeneration"], g, THREADS,
+                          [self._ptr(x), self._ptr(fx), self._ptr(u), self._ptr(fu),
+                           C.c_uint(pop), C.c_uint(S), C.c_uint(npar), C.c_uint(ncr)])
+        best = {"cmp": "selectBestIndividualsForCommonMidPoint",
+                "zocrs": "selectBestIndividualsForZeroOffsetCommonReflectionSurface",
+                "oct": "selectBestIndividualsForOffsetContinuationTrajectory"}[model]
+        self.d.launch(ev[best], _grid(S), THREADS,
+                      [self._ptr(x), self._ptr(fx), self._ptr(res), C.c_uint(pop), C.c_uint(S),
+                       C.c_uint(ncr)])
+        e1.record()
+        torch.cuda.synchronize()
+        return res.cpu().numpy().reshape(2 + npar, S), e0.elapsed_time(e1), n

@@ -1,13 +1,21 @@
 #!/usr/bin/env python3
 """Time the reference's own CUDA kernels (fatbins built from the reference
-sources by oracle/build_ref.py) on the bench line: CMP production line, 401
-velocities, window 7.  Per midpoint the reference's launch sequence
-(computeSemblancesForCommonMidPoint + selectBestSemblancesForCommonMidPoint,
-CudaLinearSearchAlgorithm.cu:35-163) is timed with CUDA events; trace
-selection and packing are excluded, as in the reference's own
-total_kernel_exec_time.  Prints one JSON line.
+sources by oracle/build_ref.py) on the workloads of the engine's bench, next
+to the engine on the same midpoints.  Prints one JSON line per workload.
 
-    python tests/golden/time_reference_kernels.py [n_midpoints]
+  ls [n]  CMP production line, 401 velocities, window 7: per midpoint the
+          reference's launch sequence (computeSemblancesForCommonMidPoint +
+          selectBestSemblancesForCommonMidPoint, CudaLinearSearchAlgorithm.cu
+          :35-163) timed with CUDA events; trace selection and packing are
+          excluded, as in the reference's own total_kernel_exec_time.
+  de [n]  ZO-CRS and OCT differential evolution workloads (population 32 / 48,
+          60 / 80 generations, F 0.5, CR 0.9): the reference's whole DE
+          sequence per midpoint (CudaDifferentialEvolutionAlgorithm.cu:35-353,
+          one synchronised launch per operator and generation, as the
+          reference runs it) against the engine's fused DE launch.
+
+    python tests/golden/time_reference_kernels.py ls 40
+    python tests/golden/time_reference_kernels.py de 2
 """
 from __future__ import annotations
 
@@ -21,12 +29,12 @@ import numpy as np
 ROOT = Path(__file__).resolve().parents[2]
 sys.path.insert(0, str(ROOT))
 
-from highperformanceseismicstacking_gb300 import synthetic  # noqa: E402
+from highperformanceseismicstacking_gb300 import capi, synthetic  # noqa: E402
 from highperformanceseismicstacking_gb300.su import tau_index  # noqa: E402
 from oracle import ref_runner  # noqa: E402
 
 
-def main(n_mid: int = 20):
+def time_ls(n_mid: int = 20):
     import torch
     w = synthetic.WORKLOADS["cmp-production"]
     line = w.make_line(n_cmp=n_mid)
@@ -69,10 +77,61 @@ def main(n_mid: int = 20):
         total_ms += e0.elapsed_time(e1)
         evals += float(sel.size) * S * P
     print(json.dumps({"impl": "reference CUDA kernels (sm_103a build of the reference sources)",
-                      "workload": "cmp-production", "midpoints": n_mid, "evals": evals,
-                      "kernel_ms": total_ms, "value": evals / (total_ms / 1e3),
-                      "unit": "evals/s"}))
+                      "workload": "cmp-production", "algorithm": "linear-search",
+                      "midpoints": n_mid, "evals": evals, "kernel_ms": total_ms,
+                      "value": evals / (total_ms / 1e3), "unit": "evals/s"}))
+
+
+def time_de(n_mid: int = 2):
+    rk = ref_runner.ReferenceKernels()
+    ops = "common_differential_evolution_f05cr09"
+    for name in ("zocrs-de", "oct-de"):
+        w = synthetic.WORKLOADS[name]
+        line = w.make_line()
+        lower, upper = synthetic.workload_bounds(w)
+        tau = tau_index(w.tau, line.dt)
+        S = line.samples_per_trace
+        mid = len(line.cdp_midpoints) // 2
+        m0s = np.ascontiguousarray(line.cdp_midpoints[mid:mid + n_mid])
+        ref_ms, ref_evals, ref_best = 0.0, 0.0, []
+        for i, m0 in enumerate(m0s):
+            sel = None
+            if w.model == "zocrs":
+                sel = np.nonzero(np.abs(np.float32(m0) - line.midpoints) <= np.float32(w.apm))[0]
+            res, ms, n_sel = rk.differential_evolution_midpoint(
+                w.model, line.samples, line.midpoints, line.halfoffsets, float(m0),
+                float(line.dt), tau, lower, upper, w.population, w.generations, seed=11 + i,
+                apm=w.apm, h0=w.h0, sel=sel, operators=ops)
+            ref_ms += ms
+            ref_best.append(res[0])
+            ref_evals += float(n_sel) * S * w.population * w.generations
+        with capi.Engine(0) as eng:
+            eng.upload_gather(line.samples, line.midpoints, line.halfoffsets, float(line.dt))
+            eng.set_traveltime(w.model, lower, upper, w.apm, w.h0)
+            eng.set_window(tau)
+            eng.differential_evolution(m0s, w.population, 2, w.de_f, w.de_cr, seed=1)
+            got, st = eng.differential_evolution(m0s, w.population, w.generations, w.de_f,
+                                                 w.de_cr, seed=7)
+        line_out = {"workload": name, "algorithm": "differential-evolution",
+                    "midpoints": int(len(m0s)), "samples": S, "population": w.population,
+                    "generations": w.generations,
+                    "reference": {"ms": ref_ms,
+                                  "mean_best_semblance": float(np.mean(ref_best))},
+                    "engine": {"ms": st["kernel_ms"], "evals": st["evals"],
+                               "value": st["evals"] / (st["kernel_ms"] / 1e3),
+                               "mean_best_semblance": float(np.mean(got[:, 0]))},
+                    "speedup_engine_vs_reference": ref_ms / st["kernel_ms"]}
+        line_out["reference"]["evals"] = ref_evals
+        line_out["reference"]["value"] = ref_evals / (ref_ms / 1e3)
+        print(json.dumps(line_out))
 
 
 if __name__ == "__main__":
-    main(int(sys.argv[1]) if len(sys.argv) > 1 else 20)
+    mode = sys.argv[1] if len(sys.argv) > 1 else "ls"
+    n = int(sys.argv[2]) if len(sys.argv) > 2 else (20 if mode == "ls" else 2)
+    if mode == "ls":
+        time_ls(n)
+    elif mode == "de":
+        time_de(n)
+    else:
+        raise SystemExit(f"unknown mode {mode}")

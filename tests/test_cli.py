@@ -134,3 +134,40 @@ def test_de_cli_runs_with_seed(tmp_path):
         outs.append(v)
     assert np.array_equal(outs[0], outs[1])
     assert np.all((outs[0][1:] >= 1000) & (outs[0][1:] <= 5000))
+
+
+@pytest.mark.gpu
+def test_linear_search_cli_engine_options(tmp_path):
+    """--grid-mode inclusive, --precision fp16 and --kernel tuned-exact reach
+    the engine: results equal an engine configured the same way."""
+    line = synthetic.cmp_line(n_cmp=3, halfoffsets=list(range(25, 1176, 50)), ns=300,
+                              dt_us=4000, n_reflectors=3, n_multiples=0, f=25.0, snr=10.0,
+                              seed=83)
+    inp = tmp_path / "line.su"
+    su.write_su(str(inp), line.headers, line.samples)
+    out = tmp_path / "ls"
+    out.mkdir()
+    rc, log = _run("single_host_linear_search", "--aph", 2000, "--apm", 0, "--azimuth", 0,
+                   "--tau", 0.010, "--input", inp, "--output", out, "--lower-bounds", 1000,
+                   "--upper-bounds", 5000, "--granularity", 41, "--traveltime", "cmp",
+                   "--grid-mode", "inclusive", "--precision", "fp16", "--kernel", "tuned-exact")
+    assert rc == 0, log
+    res = _results(out)
+    _, coh = su.read_su(str(res / "coherence.su"))
+    _, stk = su.read_su(str(res / "stack.su"))
+    _, vel = su.read_su(str(res / "velocity.su"))
+    g = su.read_gather(str(inp), aph=2000, apm=0, tau=0.010)
+    with capi.Engine(0) as eng:
+        eng.upload_gather(g.samples, g.midpoints, g.halfoffsets, float(g.dt), storage="fp16")
+        eng.set_traveltime("cmp", [1000.0], [5000.0])
+        eng.set_window(g.tau_index)
+        eng.set_grid_mode("inclusive")
+        want, _ = eng.linear_search(line.cdp_midpoints, [41], "tuned_exact")
+    assert np.array_equal(coh[1:], want[:, 0])
+    assert np.array_equal(stk[1:], want[:, 1])
+    assert np.array_equal(vel[1:], want[:, 2])
+    rc, log = _run("single_host_linear_search", "--aph", 2000, "--apm", 0, "--azimuth", 0,
+                   "--tau", 0.010, "--input", inp, "--output", out, "--lower-bounds", 1000,
+                   "--upper-bounds", 5000, "--granularity", 41, "--traveltime", "cmp",
+                   "--grid-mode", "sideways")
+    assert "--grid-mode must be reference or inclusive" in log

@@ -28,9 +28,9 @@ def _setup(eng, line, model, lower, upper, tau, apm=0.0, h0=0.0):
 
 
 def _check_against_oracle(model, line, m0s, got, lower, upper, gran, tau, apm=0.0, h0=0.0,
-                          cands=None, precision="f32"):
+                          cands=None, precision="f32", grid_mode="reference"):
     """Engine blocks vs the oracle for every midpoint; tolerances in parity.py."""
-    params = oracle.build_grid(model, lower, upper, gran)
+    params = oracle.build_grid(model, lower, upper, gran, grid_mode)
     S = line.samples_per_trace
     rep = Report()
     for i, m0 in enumerate(m0s):
@@ -196,3 +196,32 @@ def test_argument_errors(engine, c1_line):
                                 z.ctypes.data_as(C.POINTER(C.c_float)), 0, (1 << 22) + 1,
                                 C.c_float(0.004), 0)
     assert rc == -1
+
+
+def test_inclusive_grid_zocrs(engine):
+    """HPSS_GRID_INCLUSIVE: both bounds included, velocity uniform in 4/v^2;
+    the engine's grid equals the oracle's bit for bit (chosen parameters are
+    reported from it) and the search passes the parity bar against the
+    oracle on that grid."""
+    line = synthetic.structured_line(n_cmp=30, fold_range=(8, 14), h_max=1000, ns=300,
+                                     dt_us=4000, n_reflectors=4, f=20.0, snr=5.0, seed=11)
+    a, b = synthetic.zocrs_bounds(1414.2136, 2000.0, 90.0, 0.05)
+    lower, upper, gran = [1414.2136, -a, -b], [6324.5553, a, b], [6, 5, 5]
+    apm, tau = 125.0, 2
+    _setup(engine, line, "zocrs", lower, upper, tau, apm)
+    m0s = line.cdp_midpoints[::5]
+    try:
+        engine.set_grid_mode("inclusive")
+        plain, _ = engine.linear_search(m0s, gran, "plain")
+        tuned, st = engine.linear_search(m0s, gran, "tuned")
+    finally:
+        engine.set_grid_mode("reference")
+    assert st["device_error"] == 0
+    assert_same_but_stack(tuned, plain, 3)
+    grid = oracle.build_grid("zocrs", lower, upper, gran, "inclusive")
+    # reported A and B lie on the inclusive grid, whose ends are the bounds
+    assert set(np.unique(plain[:, 3])) <= set(np.unique(grid[:, 1]))
+    assert np.float32(-a) in grid[:, 1] and np.float32(a) in grid[:, 1]
+    _check_against_oracle("zocrs", line, m0s, plain, lower, upper, gran, tau, apm,
+                          grid_mode="inclusive")
+    assert engine._lib.hpss_set_grid_mode(engine.h, 7) == -1     # unknown mode

@@ -139,3 +139,22 @@ def test_oct_candidates_match_libstdcxx_restatement():
     assert np.float32(c[1023, 0]) == np.float32(1.48173527e-07)
     assert np.float32(c[0, 1]) == np.float32(-0.000258325541)
     assert np.float32(c[1023, 1]) == np.float32(-0.000674933894)
+
+
+def test_inclusive_grid():
+    """Inclusive grid: G values per parameter, both bounds included, the
+    velocity uniform in c = 4/v^2 from 4/L^2 (index 0) to 4/U^2."""
+    lo, hi, g = [1500.0, -1e-3, -1e-7], [6000.0, 1e-3, 1e-7], [41, 21, 21]
+    p = oracle.build_grid("zocrs", lo, hi, g, "inclusive")
+    assert p.shape == (41 * 21 * 21, 3)
+    c = p[:: 21 * 21, 0]
+    assert c[0] == np.float32(4.0) / np.float32(np.float32(1500.0) * np.float32(1500.0))
+    assert c[-1] == np.float32(4.0) / np.float32(np.float32(6000.0) * np.float32(6000.0))
+    np.testing.assert_allclose(np.diff(c), (c[-1] - c[0]) / 40, rtol=1e-4)
+    a = p[:21 * 21:21, 1]
+    assert a[0] == np.float32(-1e-3) and a[-1] == np.float32(1e-3)
+    bb = p[:21, 2]
+    assert bb[0] == np.float32(-1e-7) and bb[-1] == np.float32(1e-7)
+    # G = 1: the lower bound only
+    one = oracle.build_grid("cmp", [2000.0], [3000.0], [1], "inclusive")
+    assert one.shape == (1, 1) and one[0, 0] == np.float32(4.0) / np.float32(4e6)
