@@ -111,8 +111,10 @@ def _uptr(a: np.ndarray):
 class Engine:
     """One device handle: upload a line once, then run searches over midpoints."""
 
-    def __init__(self, device: int = 0):
-        self._lib = lib()
+    def __init__(self, device: int = 0, library: Optional[C.CDLL] = None):
+        # library: another build of the engine (load_library(path)); default
+        # the package's own
+        self._lib = library if library is not None else lib()
         h = C.c_void_p()
         rc = self._lib.hpss_create(device, C.byref(h))
         if rc != HPSS_OK:

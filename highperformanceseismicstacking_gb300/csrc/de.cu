@@ -25,6 +25,8 @@
 // The random stream differs: Philox-4x32-10 (Salmon et al., SC'11), keyed by
 // the seed and countered by (midpoint, sample, individual, draw), instead of
 // curand XORWOW seeded from time(NULL).
+#include <algorithm>
+
 #include "hpss_device.cuh"
 #include "hpss_internal.h"
 
@@ -93,9 +95,6 @@ struct Draws {
     }
 };
 
-constexpr int kDeWarps = 8;
-constexpr int kMaxSlots = kDeMaxPopulation / 32;
-
 // Semblance of one candidate (raw parameters) over the selected traces.
 template <int MODEL, int W>
 __device__ __forceinline__ void de_eval(const DeParams &d, float t0, float m0, uint32_t first,
@@ -143,51 +142,58 @@ __device__ __forceinline__ void de_eval(const DeParams &d, float t0, float m0, u
     *notUsed += nu;
 }
 
-template <int MODEL, int W>
-__global__ void __launch_bounds__(kDeWarps * 32)
-de_kernel(DeParams d, uint32_t nUnits) {
-    const LsParams &a = d.ls;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    constexpr int NP = MODEL == kModelCmp ? 1 : (MODEL == kModelZocrs ? 3 : 2);
-    const uint32_t pop = d.pop;
-    const int slots = (int)((pop + 31) / 32);
+// One thread per individual.  A CTA holds `spc` whole populations of
+// consecutive samples of one midpoint (thread = sample-in-CTA * pop +
+// individual, the reference's thread layout), so every lane works for any
+// population size; the population vectors live in shared memory, where
+// mutation reads the three donors.  Persistent over (midpoint, sample
+// group) units.
+constexpr int kDeThreads = 256;
 
-    // unit = (midpoint, sample); one warp per unit
-    for (uint32_t unit = blockIdx.x * kDeWarps + warp; unit < nUnits;
-         unit += gridDim.x * kDeWarps) {
-        const uint32_t mi = unit / a.S;
-        const uint32_t s = unit % a.S;
+template <int MODEL, int W>
+__global__ void __launch_bounds__(kDeThreads)
+de_kernel(DeParams d, uint32_t spc, uint32_t groups, uint32_t nUnits) {
+    constexpr int NP = MODEL == kModelCmp ? 1 : (MODEL == kModelZocrs ? 3 : 2);
+    const LsParams &a = d.ls;
+    extern __shared__ __align__(16) float deSmem[];
+    const uint32_t pop = d.pop;
+    float *X = deSmem;                           // [spc][pop][NP]
+    float *FX = deSmem + (size_t)spc * pop * NP; // [spc][pop] (final argmax)
+    float *FK = FX + (size_t)spc * pop;          // [spc][pop]
+    __shared__ unsigned long long nuCta;
+    const uint32_t ls = threadIdx.x / pop;       // sample within the CTA
+    const uint32_t ind = threadIdx.x % pop;      // individual
+    const bool member = ls < spc;                // threads past spc * pop only sync
+
+    for (uint32_t unit = blockIdx.x; unit < nUnits; unit += gridDim.x) {
+        const uint32_t mi = unit / groups;
+        const uint32_t s = (unit % groups) * spc + ls;
+        const bool active = member && s < a.S;
         const float m0 = a.m0s[mi];
         const uint32_t first = a.selFirst[mi], cnt = a.selCount[mi];
-        const float t0 = static_cast<float>(s) * a.dt;
-
-        float x[kMaxSlots][NP], fx[kMaxSlots], fxk[kMaxSlots];
+        const float t0 = static_cast<float>(active ? s : 0) * a.dt;
+        float *xs = X + (size_t)(member ? ls : 0) * pop * NP;  // this sample's population
+        float x[NP];
+        float fx = -1.f, fxk = 0.f;
         unsigned notUsed = 0;
+        if (threadIdx.x == 0) nuCta = 0;
         // ---- initial population and its fitness (generation 1)
-#pragma unroll
-        for (int sl = 0; sl < kMaxSlots; sl++) {
-            if (sl >= slots) break;
-            const uint32_t ind = sl * 32 + lane;
+        if (active) {
             Draws rng(d.seedLo, d.seedHi, mi, s, ind, 0);
 #pragma unroll
             for (int j = 0; j < NP; j++) {
-                float r = rng.next();
                 // min + ratio * (max - min) as one fused multiply-add, as the
                 // reference's startPopulations compiles
-                x[sl][j] = __fmaf_rn(r, __fsub_rn(d.hi[j], d.lo[j]), d.lo[j]);
+                x[j] = __fmaf_rn(rng.next(), __fsub_rn(d.hi[j], d.lo[j]), d.lo[j]);
+                xs[ind * NP + j] = x[j];
             }
-            fx[sl] = -1.f;
-            fxk[sl] = 0.f;
-            if (ind < pop) de_eval<MODEL, W>(d, t0, m0, first, cnt, x[sl], &fx[sl], &fxk[sl],
-                                             &notUsed);
+            de_eval<MODEL, W>(d, t0, m0, first, cnt, x, &fx, &fxk, &notUsed);
         }
         // ---- generations 2 .. G
         for (uint32_t gen = 1; gen < d.gens; gen++) {
-            float u[kMaxSlots][NP];
-#pragma unroll
-            for (int sl = 0; sl < kMaxSlots; sl++) {
-                if (sl >= slots) break;
-                const uint32_t ind = sl * 32 + lane;
+            __syncthreads();  // population of the previous generation complete
+            float u[NP];
+            if (active) {
                 Draws rng(d.seedLo, d.seedHi, mi, s, ind, gen);
                 float v[NP];
 #pragma unroll
@@ -196,18 +202,8 @@ de_kernel(DeParams d, uint32_t nUnits) {
                     const uint32_t r1 = (uint32_t)(q1 * (float)(pop - 1));
                     const uint32_t r2 = (uint32_t)(q2 * (float)(pop - 1));
                     const uint32_t r3 = (uint32_t)(q3 * (float)(pop - 1));
-                    float x1 = 0.f, x2 = 0.f, x3 = 0.f;
-#pragma unroll
-                    for (int ss = 0; ss < kMaxSlots; ss++) {
-                        if (ss >= slots) break;
-                        float o1 = __shfl_sync(0xffffffffu, x[ss][j], r1 & 31);
-                        float o2 = __shfl_sync(0xffffffffu, x[ss][j], r2 & 31);
-                        float o3 = __shfl_sync(0xffffffffu, x[ss][j], r3 & 31);
-                        if ((int)(r1 >> 5) == ss) x1 = o1;
-                        if ((int)(r2 >> 5) == ss) x2 = o2;
-                        if ((int)(r3 >> 5) == ss) x3 = o3;
-                    }
-                    float nv = __fmaf_rn(d.F, __fsub_rn(x2, x3), x1);
+                    float nv = __fmaf_rn(d.F, __fsub_rn(xs[r2 * NP + j], xs[r3 * NP + j]),
+                                         xs[r1 * NP + j]);
                     nv = fminf(nv, d.hi[j]);
                     nv = fmaxf(nv, d.lo[j]);
                     v[j] = nv;
@@ -216,72 +212,53 @@ de_kernel(DeParams d, uint32_t nUnits) {
 #pragma unroll
                 for (int j = 0; j < NP; j++) {
                     const float r = rng.next();
-                    u[sl][j] = (r > d.CR && l != (uint32_t)j) ? x[sl][j] : v[j];
+                    u[j] = (r > d.CR && l != (uint32_t)j) ? x[j] : v[j];
                 }
             }
-            // all lanes have read the current population: evaluate and select
-#pragma unroll
-            for (int sl = 0; sl < kMaxSlots; sl++) {
-                if (sl >= slots) break;
-                const uint32_t ind = sl * 32 + lane;
-                if (ind >= pop) continue;
+            __syncthreads();  // every donor read before any replacement
+            if (active) {
                 float fu, fuk;
-                de_eval<MODEL, W>(d, t0, m0, first, cnt, u[sl], &fu, &fuk, &notUsed);
-                if (fu > fx[sl]) {
+                de_eval<MODEL, W>(d, t0, m0, first, cnt, u, &fu, &fuk, &notUsed);
+                if (fu > fx) {
 #pragma unroll
-                    for (int j = 0; j < NP; j++) x[sl][j] = u[sl][j];
-                    fx[sl] = fu;
-                    fxk[sl] = fuk;
+                    for (int j = 0; j < NP; j++) {
+                        x[j] = u[j];
+                        xs[ind * NP + j] = u[j];
+                    }
+                    fx = fu;
+                    fxk = fuk;
                 }
             }
-            __syncwarp();
         }
-        // ---- best individual: strict '>' from -1 in index order
-        float best = -1.f, bestK = 0.f;
-        uint32_t bestI = 0xffffffffu;
-        float bx[NP];
-#pragma unroll
-        for (int j = 0; j < NP; j++) bx[j] = 0.f;
-#pragma unroll
-        for (int sl = 0; sl < kMaxSlots; sl++) {
-            if (sl >= slots) break;
-            const uint32_t ind = sl * 32 + lane;
-            if (ind < pop && fx[sl] > best) {
-                best = fx[sl];
-                bestK = fxk[sl];
-                bestI = ind;
-#pragma unroll
-                for (int j = 0; j < NP; j++) bx[j] = x[sl][j];
+        // ---- best individual per sample: strict '>' from -1 in index order
+        if (member) {
+            FX[ls * pop + ind] = fx;
+            FK[ls * pop + ind] = fxk;
+        }
+        __syncthreads();
+        if (MODEL == kModelOct && notUsed) atomicAdd(&nuCta, (unsigned long long)notUsed);
+        if (active && ind == 0) {
+            float best = -1.f, bestK = 0.f;
+            uint32_t bi = 0xffffffffu;
+            for (uint32_t i = 0; i < pop; i++) {
+                const float f = FX[ls * pop + i];
+                if (f > best) {
+                    best = f;
+                    bestK = FK[ls * pop + i];
+                    bi = i;
+                }
             }
-        }
-#pragma unroll
-        for (int o = 16; o; o >>= 1) {
-            float os = __shfl_xor_sync(0xffffffffu, best, o);
-            float ok = __shfl_xor_sync(0xffffffffu, bestK, o);
-            uint32_t oi = __shfl_xor_sync(0xffffffffu, bestI, o);
-            float ox[NP];
-#pragma unroll
-            for (int j = 0; j < NP; j++) ox[j] = __shfl_xor_sync(0xffffffffu, bx[j], o);
-            if (better(os, oi, best, bestI)) {
-                best = os;
-                bestK = ok;
-                bestI = oi;
-#pragma unroll
-                for (int j = 0; j < NP; j++) bx[j] = ox[j];
-            }
-        }
-        // not-used count (OCT)
-#pragma unroll
-        for (int o = 16; o; o >>= 1) notUsed += __shfl_xor_sync(0xffffffffu, notUsed, o);
-        if (lane == 0) {
             float *out = a.out + (size_t)mi * (2 + NP) * a.S;
             out[s] = best;
             out[a.S + s] = bestK;
 #pragma unroll
-            for (int j = 0; j < NP; j++) out[(size_t)(2 + j) * a.S + s] = bx[j];
-            if (MODEL == kModelOct && a.notUsed && notUsed) atomicAdd(a.notUsed + mi,
-                                                                       (unsigned long long)notUsed);
+            for (int j = 0; j < NP; j++)
+                out[(size_t)(2 + j) * a.S + s] = bi != 0xffffffffu ? xs[bi * NP + j] : 0.f;
         }
+        __syncthreads();
+        if (MODEL == kModelOct && threadIdx.x == 0 && a.notUsed && nuCta)
+            atomicAdd(a.notUsed + mi, nuCta);
+        __syncthreads();  // shared memory reused by the next unit
     }
 }
 
@@ -339,32 +316,49 @@ __global__ void de_select_oct_kernel(DeParams d, const uint32_t *candFirst,
     if (threadIdx.x == 0) selCount[mi] = shCount;
 }
 
-template <int MODEL>
-cudaError_t launch_de_model(const DeParams &d, uint32_t grid, uint32_t nUnits, cudaStream_t st) {
-    switch (d.ls.w) {
-#define HPSS_DE_CASE(WV)                                                       \
-    case WV:                                                                   \
-        de_kernel<MODEL, WV><<<grid, kDeWarps * 32, 0, st>>>(d, nUnits);       \
-        break;
-        HPSS_DE_CASE(1)
-        HPSS_DE_CASE(3)
-        HPSS_DE_CASE(5)
-        HPSS_DE_CASE(7)
-        HPSS_DE_CASE(9)
-        HPSS_DE_CASE(11)
-#undef HPSS_DE_CASE
-        default:
-            de_kernel<MODEL, 0><<<grid, kDeWarps * 32, 0, st>>>(d, nUnits);
-            break;
-    }
+size_t de_smem_bytes(uint32_t spc, uint32_t pop, int np) {
+    return (size_t)spc * pop * (np + 2) * sizeof(float);
+}
+
+template <int MODEL, int W>
+cudaError_t launch_de_w(const DeParams &d, uint32_t numSms, uint32_t spc, uint32_t threads,
+                        uint32_t groups, uint64_t units, size_t smem, cudaStream_t st) {
+    int perSm = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, de_kernel<MODEL, W>,
+                                                                  (int)threads, smem);
+    if (e != cudaSuccess) return e;
+    const uint32_t grid =
+        (uint32_t)std::min<uint64_t>(units, (uint64_t)numSms * (uint64_t)std::max(perSm, 1));
+    de_kernel<MODEL, W><<<grid, threads, smem, st>>>(d, spc, groups, (uint32_t)units);
     return cudaGetLastError();
 }
 
-cudaError_t launch_de(const DeParams &d, int model, uint32_t grid, uint32_t nUnits,
-                      cudaStream_t st) {
-    if (model == kModelCmp) return launch_de_model<kModelCmp>(d, grid, nUnits, st);
-    if (model == kModelZocrs) return launch_de_model<kModelZocrs>(d, grid, nUnits, st);
-    return launch_de_model<kModelOct>(d, grid, nUnits, st);
+template <int MODEL>
+cudaError_t launch_de_model(const DeParams &d, uint32_t numSms, cudaStream_t st) {
+    constexpr int NP = MODEL == kModelCmp ? 1 : (MODEL == kModelZocrs ? 3 : 2);
+    const uint32_t pop = d.pop;
+    const uint32_t spc = pop >= (uint32_t)kDeThreads ? 1u : kDeThreads / pop;
+    const uint32_t threads = ((spc * pop + 31) / 32) * 32;
+    const uint32_t groups = (d.ls.S + spc - 1) / spc;
+    const uint64_t units = (uint64_t)d.ls.nM0 * groups;
+    if (units == 0) return cudaSuccess;
+    if (units > 0xffffffffull) return cudaErrorInvalidConfiguration;
+    const size_t smem = de_smem_bytes(spc, pop, NP);
+    switch (d.ls.w) {
+        case 1: return launch_de_w<MODEL, 1>(d, numSms, spc, threads, groups, units, smem, st);
+        case 3: return launch_de_w<MODEL, 3>(d, numSms, spc, threads, groups, units, smem, st);
+        case 5: return launch_de_w<MODEL, 5>(d, numSms, spc, threads, groups, units, smem, st);
+        case 7: return launch_de_w<MODEL, 7>(d, numSms, spc, threads, groups, units, smem, st);
+        case 9: return launch_de_w<MODEL, 9>(d, numSms, spc, threads, groups, units, smem, st);
+        case 11: return launch_de_w<MODEL, 11>(d, numSms, spc, threads, groups, units, smem, st);
+        default: return launch_de_w<MODEL, 0>(d, numSms, spc, threads, groups, units, smem, st);
+    }
+}
+
+cudaError_t launch_de(const DeParams &d, int model, uint32_t numSms, cudaStream_t st) {
+    if (model == kModelCmp) return launch_de_model<kModelCmp>(d, numSms, st);
+    if (model == kModelZocrs) return launch_de_model<kModelZocrs>(d, numSms, st);
+    return launch_de_model<kModelOct>(d, numSms, st);
 }
 
 cudaError_t launch_de_select_oct(const DeParams &d, const uint32_t *candFirst,

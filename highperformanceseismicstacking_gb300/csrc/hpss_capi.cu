@@ -517,9 +517,7 @@ hpss_status de_impl(hpss_handle h, const float *d_m0s, uint32_t nM0, uint32_t po
     const uint64_t units = (uint64_t)nM0 * h->S;
     if (units > 0xffffffffull)
         return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "too many (midpoint, sample) units");
-    const uint64_t ctas = (units + 7) / 8;
-    const uint32_t grid = (uint32_t)std::min<uint64_t>(ctas, (uint64_t)num_sms(h) * 8);
-    HPSS_CUDA_TRY(h, launch_de(d, h->model, grid, (uint32_t)units, h->stream));
+    HPSS_CUDA_TRY(h, launch_de(d, h->model, (uint32_t)num_sms(h), h->stream));
     HPSS_CUDA_TRY(h, cudaEventRecord(h->ev2, h->stream));
     if (stats || sync) {
         HPSS_CUDA_TRY(h, cudaStreamSynchronize(h->stream));

@@ -153,8 +153,7 @@ cudaError_t launch_convert_storage(const float *src, uint16_t *dst,
                                    uint32_t stride, int storage,
                                    cudaStream_t st);
 size_t tuned_smem_bytes();
-cudaError_t launch_de(const DeParams &d, int model, uint32_t grid, uint32_t nUnits,
-                      cudaStream_t st);
+cudaError_t launch_de(const DeParams &d, int model, uint32_t numSms, cudaStream_t st);
 cudaError_t launch_sf(const LsParams &p, int model, uint32_t grid, uint32_t nUnits,
                       cudaStream_t st);
 cudaError_t launch_sf_select_oct(const LsParams &p, const uint32_t *candFirst,

@@ -21,6 +21,8 @@
 
 #include <cuda_fp16.h>
 
+#include <type_traits>
+
 #include "hpss_device.cuh"
 #include "hpss_internal.h"
 
@@ -52,13 +54,17 @@ struct TunedSmem {
 // window of the tile [t0a, t0b] and the chunk parameter box.  Conservative by
 // one sample each side; rounded to multiples of 4 samples (16 B) for vector
 // copies.  len = 0 if no window of the tile/chunk can lie inside the trace.
+// *full (optional): every window of the tile and chunk box lies inside the
+// trace (for ZO-CRS also: every squared time is positive), judged on the same
+// conservative bounds, so the evaluation may skip the per-candidate checks.
 template <int MODEL>
 __device__ __forceinline__ void trace_span(const LsParams &a, const float *cb,
                                            float m0, float t0a, float t0b,
                                            float m, float hsq, int *lo,
-                                           int *len) {
+                                           int *len, bool *full = nullptr) {
     const int S = (int)a.S, tau = a.tau;
     int kmin, kmax;
+    bool positive = true;
     if (MODEL == kModelCmp) {
         // t increases with t0 and with c
         kmin = window_index(cmp_time(t0a, cb[0], hsq), a.dt).k - 1;
@@ -77,8 +83,10 @@ __device__ __forceinline__ void trace_span(const LsParams &a, const float *cb,
         if (thi < 0.f) {
             *lo = 0;
             *len = 0;
+            if (full) *full = false;
             return;
         }
+        positive = tlo > 1e-4f * thi;
         // relative slack for the different summation order of the kernel
         tlo = fmaxf(tlo, 0.f) * 0.9999f;
         thi = thi * 1.0001f;
@@ -87,13 +95,16 @@ __device__ __forceinline__ void trace_span(const LsParams &a, const float *cb,
     } else {
         kmin = tau;
         kmax = S - tau - 2;
+        positive = false;
     }
+    if (full) *full = positive && kmin >= tau && kmax <= S - tau - 2;
     // in-trace windows have tau <= k <= S - tau - 2
     kmin = max(kmin, tau);
     kmax = min(kmax, S - tau - 2);
     if (kmin > kmax) {
         *lo = 0;
         *len = 0;
+        if (full) *full = false;
         return;
     }
     int l = (kmin - tau) & ~3;
@@ -329,8 +340,10 @@ struct __align__(16) TraceMeta2 {
     int base;   // shared-memory index of sample 0 of the trace
     float hsq;  // h * h
     float dm;   // m - m0 (ZO-CRS)
-    int len;    // staged samples (0: skip the trace)
+    int len;    // staged samples | kFullTrace when every window is in the trace
 };
+constexpr int kFullTrace = int(0x80000000u);
+constexpr int kLenMask = 0x7fffffff;
 
 // stage size per CTA for MINB resident CTAs per SM
 template <int MINB>
@@ -428,6 +441,7 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
 
             float2 num[NP][W], lin[NP], den[NP];
             unsigned used[R];
+            unsigned usedFull = 0;  // traces evaluated on the FULL path
 #pragma unroll
             for (int q = 0; q < NP; q++) {
 #pragma unroll
@@ -442,11 +456,12 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
                 const uint32_t q = q0 + threadIdx.x;
                 int lo = 0, len = 0;
                 float tm = 0.f, thsq = 0.f;
+                bool full = false;
                 if (q < cnt) {
                     const uint32_t ti = a.selIdx ? a.selIdx[first + q] : first + q;
                     tm = a.mid[ti];
                     thsq = a.hsq[ti];
-                    trace_span<MODEL>(a, cbl, m0, t0a, t0b, tm, thsq, &lo, &len);
+                    trace_span<MODEL>(a, cbl, m0, t0a, t0b, tm, thsq, &lo, &len, &full);
                 }
                 int incl = len;
 #pragma unroll
@@ -479,7 +494,7 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
                     md.base = off - lo;
                     md.hsq = thsq;
                     md.dm = tm - m0;
-                    md.len = len;
+                    md.len = len | (full ? kFullTrace : 0);
                     sm.meta[slot] = md;
                     sm.lo[slot] = lo;
                     sm.ti[slot] = (int)(a.selIdx ? a.selIdx[first + q] : first + q);
@@ -496,13 +511,14 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
                     if (a.samples16 == nullptr) {
                         const float4 *src = reinterpret_cast<const float4 *>(
                             a.samples + (size_t)sm.ti[j] * a.stride + lo_j);
-                        for (int v = lane; v < (md.len >> 2); v += 32) dst[v] = __ldg(src + v);
+                        for (int v = lane; v < ((md.len & kLenMask) >> 2); v += 32)
+                            dst[v] = __ldg(src + v);
                     } else {
                         // 16-bit storage: 4 samples per 8-byte load, widened to FP32
                         const uint2 *src = reinterpret_cast<const uint2 *>(
                             a.samples16 + (size_t)sm.ti[j] * a.stride + lo_j);
                         const float sc = a.storage == 2 ? a.scale[sm.ti[j]] : 1.f;
-                        for (int v = lane; v < (md.len >> 2); v += 32) {
+                        for (int v = lane; v < ((md.len & kLenMask) >> 2); v += 32) {
                             const uint2 q = __ldg(src + v);
                             dst[v] = a.storage == 2
                                          ? make_float4(half_bits_to_float(q.x & 0xffffu) * sc,
@@ -517,9 +533,12 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
                     }
                 }
                 __syncthreads();
-#pragma unroll 2
-                for (int j = 0; j < nkeep; j++) {
-                    const TraceMeta2 md = sm.meta[j];
+                // One trace for all candidates of the thread.  FULL: every
+                // window lies inside the trace (trace_span's conservative
+                // bounds), so the range test, the zero-pad redirect, the
+                // clamp and the per-candidate count are skipped.
+                auto evalTrace = [&](const TraceMeta2 &md, int j, auto fullTag) {
+                    constexpr bool FULL = decltype(fullTag)::value;
                     int bo[R];
                     float fr[R];
 #pragma unroll
@@ -538,7 +557,7 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
                             t2 = __ffma2_rn(cq, hsq2, __ffma2_rn(bd, dm2, __fmul2_rn(x, x)));
                         }
                         float2 t;
-                        if (MODEL == kModelCmp) {
+                        if (MODEL == kModelCmp || FULL) {
                             t = f2(sqrtf(t2.x), sqrtf(t2.y));
                         } else {
                             t = f2(sqrtf(fmaxf(t2.x, 0.f)), sqrtf(fmaxf(t2.y, 0.f)));
@@ -558,20 +577,25 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
                             const int r = 2 * qq + h;
                             // k - tau (ti >= 2^23, inf: far out of range)
                             const int km = __float_as_int(h ? rk.y : rk.x) - magicTau;
-                            // k - tau >= 0 && k + tau + 1 < S as one unsigned compare
-                            bool in = (unsigned)km < winSpan;
-                            if (MODEL != kModelCmp) in = in && (h ? t2.y : t2.x) >= 0;
-                            int b = in ? md.base + km : 0;
-#ifdef HPSS_CHECKED
-                            if (in && (b < md.base + sm.lo[j] ||
-                                       b > md.base + sm.lo[j] + md.len - (W + 1)))
-                                atomicOr(a.errorWord, kErrSmemBounds);
-#endif
-                            bo[r] = (int)min((unsigned)b, (unsigned)kLastBase);
-                            // out-of-trace windows read the zero pad: u = 0 for
-                            // any finite fraction, so the fraction needs no select
                             fr[r] = h ? fq.y : fq.x;
-                            used[r] += in ? 1u : 0u;
+                            if (FULL) {
+                                bo[r] = md.base + km;
+                            } else {
+                                // k - tau >= 0 && k + tau + 1 < S as one unsigned compare
+                                bool in = (unsigned)km < winSpan;
+                                if (MODEL != kModelCmp) in = in && (h ? t2.y : t2.x) >= 0;
+                                const int b = in ? md.base + km : 0;
+#ifdef HPSS_CHECKED
+                                if (in && (b < md.base + sm.lo[j] ||
+                                           b > md.base + sm.lo[j] + (md.len & kLenMask) - (W + 1)))
+                                    atomicOr(a.errorWord, kErrSmemBounds);
+#endif
+                                // out-of-trace windows read the zero pad: u = 0
+                                // for any finite fraction, so the fraction
+                                // needs no select
+                                bo[r] = (int)min((unsigned)b, (unsigned)kLastBase);
+                                used[r] += in ? 1u : 0u;
+                            }
                         }
                     }
 #pragma unroll
@@ -590,6 +614,39 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
                             if (EXACT_STACK) lin[qq] = __fadd2_rn(lin[qq], u);
                             den[qq] = __ffma2_rn(u, u, den[qq]);
                         }
+                    }
+                };
+#pragma unroll 2
+                for (int j = 0; j < nkeep; j++) {
+                    const TraceMeta2 md = sm.meta[j];
+#ifdef HPSS_CHECKED
+                    // the span bounds must hold for every candidate: compare
+                    // with the checked evaluation (counts, window positions)
+                    if (md.len < 0) {
+                        // recompute the positions of the FULL path and test them
+                        for (int r = 0; r < R; r++) {
+                            float t2;
+                            if (MODEL == kModelCmp) {
+                                t2 = __fmaf_rn(cc[r], md.hsq, __fmul_rn(t0, t0));
+                            } else {
+                                t2 = zocrs_t2(t0, cc[r], c1[r], c2[r], md.dm, md.hsq);
+                            }
+                            const float ti = __fmul_rn(sqrtf(fmaxf(t2, 0.f)), rdt);
+                            const int k = (int)ti;
+                            const int b = md.base + k - tau;
+                            if ((MODEL != kModelCmp && !(t2 > 0.f)) ||
+                                (unsigned)(k - tau) >= winSpan ||
+                                b < md.base + sm.lo[j] ||
+                                b > md.base + sm.lo[j] + (md.len & kLenMask) - (W + 1))
+                                atomicOr(a.errorWord, kErrSmemBounds);
+                        }
+                    }
+#endif
+                    if (md.len < 0) {
+                        evalTrace(md, j, std::true_type{});
+                        usedFull++;
+                    } else {
+                        evalTrace(md, j, std::false_type{});
                     }
                 }
                 q0 += nfit;
@@ -610,7 +667,7 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
                         for (int jj = 0; jj < W; jj++) ls += nm[jj];
                     }
                     float sembl, stack;
-                    reduce_semblance(nm, ls, h ? den[qq].y : den[qq].x, W, used[r], &sembl,
+                    reduce_semblance(nm, ls, h ? den[qq].y : den[qq].x, W, used[r] + usedFull, &sembl,
                                      &stack);
                     const uint32_t p = chunk * a.chunkSize + warp * R + r;
                     if (valid[r]) top2_offer(sembl, best, second);
