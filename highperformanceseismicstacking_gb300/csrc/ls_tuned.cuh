@@ -537,10 +537,12 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
                 // window lies inside the trace (trace_span's conservative
                 // bounds), so the range test, the zero-pad redirect, the
                 // clamp and the per-candidate count are skipped.
-                auto evalTrace = [&](const TraceMeta2 &md, int j, auto fullTag) {
+                struct Win {
+                    int bo[R];    // shared-memory index of each window's first sample
+                    float fr[R];  // interpolation fraction
+                };
+                auto windowsOf = [&](const TraceMeta2 &md, int j, auto fullTag, Win &wn) {
                     constexpr bool FULL = decltype(fullTag)::value;
-                    int bo[R];
-                    float fr[R];
 #pragma unroll
                     for (int qq = 0; qq < NP; qq++) {
                         // traveltime of both candidates of the pair, the
@@ -577,9 +579,9 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
                             const int r = 2 * qq + h;
                             // k - tau (ti >= 2^23, inf: far out of range)
                             const int km = __float_as_int(h ? rk.y : rk.x) - magicTau;
-                            fr[r] = h ? fq.y : fq.x;
+                            wn.fr[r] = h ? fq.y : fq.x;
                             if (FULL) {
-                                bo[r] = md.base + km;
+                                wn.bo[r] = md.base + km;
                             } else {
                                 // k - tau >= 0 && k + tau + 1 < S as one unsigned compare
                                 bool in = (unsigned)km < winSpan;
@@ -593,16 +595,18 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
                                 // out-of-trace windows read the zero pad: u = 0
                                 // for any finite fraction, so the fraction
                                 // needs no select
-                                bo[r] = (int)min((unsigned)b, (unsigned)kLastBase);
+                                wn.bo[r] = (int)min((unsigned)b, (unsigned)kLastBase);
                                 used[r] += in ? 1u : 0u;
                             }
                         }
                     }
+                };
+                auto tapsOf = [&](const Win &wn) {
 #pragma unroll
                     for (int qq = 0; qq < NP; qq++) {
-                        const float *ya = sm.y + bo[2 * qq];
-                        const float *yb = sm.y + bo[2 * qq + 1];
-                        const float2 fq = f2(fr[2 * qq], fr[2 * qq + 1]);
+                        const float *ya = sm.y + wn.bo[2 * qq];
+                        const float *yb = sm.y + wn.bo[2 * qq + 1];
+                        const float2 fq = f2(wn.fr[2 * qq], wn.fr[2 * qq + 1]);
                         float2 y1 = f2(ya[0], yb[0]);
 #pragma unroll
                         for (int jj = 0; jj < W; jj++) {
@@ -616,38 +620,63 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
                         }
                     }
                 };
-#pragma unroll 2
-                for (int j = 0; j < nkeep; j++) {
-                    const TraceMeta2 md = sm.meta[j];
 #ifdef HPSS_CHECKED
-                    // the span bounds must hold for every candidate: compare
-                    // with the checked evaluation (counts, window positions)
-                    if (md.len < 0) {
-                        // recompute the positions of the FULL path and test them
-                        for (int r = 0; r < R; r++) {
-                            float t2;
-                            if (MODEL == kModelCmp) {
-                                t2 = __fmaf_rn(cc[r], md.hsq, __fmul_rn(t0, t0));
-                            } else {
-                                t2 = zocrs_t2(t0, cc[r], c1[r], c2[r], md.dm, md.hsq);
-                            }
-                            const float ti = __fmul_rn(sqrtf(fmaxf(t2, 0.f)), rdt);
-                            const int k = (int)ti;
-                            const int b = md.base + k - tau;
-                            if ((MODEL != kModelCmp && !(t2 > 0.f)) ||
-                                (unsigned)(k - tau) >= winSpan ||
-                                b < md.base + sm.lo[j] ||
-                                b > md.base + sm.lo[j] + (md.len & kLenMask) - (W + 1))
-                                atomicOr(a.errorWord, kErrSmemBounds);
+                // the span bounds must hold for every candidate of a FULL trace:
+                // recompute its window positions with the scalar arithmetic
+                auto checkFull = [&](const TraceMeta2 &md, int j) {
+                    if (md.len >= 0) return;
+                    for (int r = 0; r < R; r++) {
+                        float t2;
+                        if (MODEL == kModelCmp) {
+                            t2 = __fmaf_rn(cc[r], md.hsq, __fmul_rn(t0, t0));
+                        } else {
+                            t2 = zocrs_t2(t0, cc[r], c1[r], c2[r], md.dm, md.hsq);
+                        }
+                        const float ti = __fmul_rn(sqrtf(fmaxf(t2, 0.f)), rdt);
+                        const int k = (int)ti;
+                        const int b = md.base + k - tau;
+                        if ((MODEL != kModelCmp && !(t2 > 0.f)) ||
+                            (unsigned)(k - tau) >= winSpan || b < md.base + sm.lo[j] ||
+                            b > md.base + sm.lo[j] + (md.len & kLenMask) - (W + 1))
+                            atomicOr(a.errorWord, kErrSmemBounds);
+                    }
+                };
+#endif
+                // Traces in order.  Two consecutive FULL traces (the common
+                // case) are handled together: both traces' window positions
+                // first, then the taps of the first and of the second, which
+                // gives the scheduler two independent traveltime chains.
+                for (int j = 0; j < nkeep;) {
+                    const TraceMeta2 mA = sm.meta[j];
+                    if (j + 1 < nkeep) {
+                        const TraceMeta2 mB = sm.meta[j + 1];
+                        if ((mA.len & mB.len) < 0) {
+#ifdef HPSS_CHECKED
+                            checkFull(mA, j);
+                            checkFull(mB, j + 1);
+#endif
+                            Win wA, wB;
+                            windowsOf(mA, j, std::true_type{}, wA);
+                            windowsOf(mB, j + 1, std::true_type{}, wB);
+                            tapsOf(wA);
+                            tapsOf(wB);
+                            usedFull += 2;
+                            j += 2;
+                            continue;
                         }
                     }
+#ifdef HPSS_CHECKED
+                    checkFull(mA, j);
 #endif
-                    if (md.len < 0) {
-                        evalTrace(md, j, std::true_type{});
+                    Win wn;
+                    if (mA.len < 0) {
+                        windowsOf(mA, j, std::true_type{}, wn);
                         usedFull++;
                     } else {
-                        evalTrace(md, j, std::false_type{});
+                        windowsOf(mA, j, std::false_type{}, wn);
                     }
+                    tapsOf(wn);
+                    j++;
                 }
                 q0 += nfit;
             }
