@@ -54,9 +54,10 @@ def parse():
                     help="midpoints of the DE side measurement (0: skip)")
     ap.add_argument("--no-storage-side", action="store_true",
                     help="skip the BF16 / FP16 storage side measurement")
-    ap.add_argument("--zocrs-cmps", type=int, default=8,
+    ap.add_argument("--zocrs-cmps", type=int, default=32,
                     help="midpoints of the ZO-CRS line measured beside the main workload "
-                         "(0 = skip)")
+                         "(0 = skip); 32 midpoints = 1504 (midpoint, tile) units, about five "
+                         "waves of the persistent grid, so the last partial wave is small")
     return ap.parse_args()
 
 

@@ -40,7 +40,7 @@ struct hpss_handle_s : public Handle {
         size_t bytes = 0;
     };
     Buf params, chunkBounds, selFirst, selCount, selIdx, candFirst, candCount,
-        notUsed, errWord, m0s, out, octCands, prior;
+        notUsed, errWord, m0s, out, octCands, prior, octPartial;
     std::vector<float> octCandsHost;
     std::map<std::string, int> variantCache;  // autotuner decisions
     int lastVariant = -1;
@@ -351,8 +351,7 @@ hpss_status linear_search_impl(hpss_handle h, const float *d_m0s, uint32_t nM0,
     // the chunk size (8 warps x candidates per thread).
     const bool pairKernel = tuned && h->model != HPSS_MODEL_OCT &&
                             lp.w <= 15 && h->stride + 8 <= (uint32_t)tuned_stage_floats_min();
-    const bool branchyKernel = tuned && h->model == HPSS_MODEL_OCT &&
-                               lp.w <= 15 && h->stride + 8 <= (uint32_t)tuned_stage_floats();
+    const bool octKernel = tuned && h->model == HPSS_MODEL_OCT && lp.w <= 15;
     auto setChunks = [&](int perThread) -> cudaError_t {
         lp.chunkSize = kTunedWarps * perThread;
         lp.nChunks = (lp.P + lp.chunkSize - 1) / lp.chunkSize;
@@ -370,6 +369,13 @@ hpss_status linear_search_impl(hpss_handle h, const float *d_m0s, uint32_t nM0,
     lp.nearTies = reinterpret_cast<unsigned long long *>(static_cast<char *>(h->errWord.p) + 8);
     HPSS_CUDA_TRY(h, cudaMemsetAsync(lp.notUsed, 0, nM0 * sizeof(unsigned long long), h->stream));
     HPSS_CUDA_TRY(h, cudaMemsetAsync(lp.errorWord, 0, 16, h->stream));
+
+    uint32_t octParts = 1;
+    if (octKernel) {
+        // per-part best / runner-up of the OCT kernel
+        octParts = oct_parts(lp, (uint32_t)num_sms(h));
+        HPSS_CUDA_TRY(h, ensure(h, h->octPartial, oct_partial_bytes(nM0, h->S, octParts)));
+    }
 
     HPSS_CUDA_TRY(h, cudaEventRecord(h->ev0, h->stream));
     rc = run_selection(h, d_m0s, nM0, lp);
@@ -398,9 +404,9 @@ hpss_status linear_search_impl(hpss_handle h, const float *d_m0s, uint32_t nM0,
     }
     if (pairKernel) {
         HPSS_CUDA_TRY(h, launchPair(variant, (uint32_t)units));
-    } else if (branchyKernel) {
-        const uint32_t grid = (uint32_t)std::min<uint64_t>(units, (uint64_t)num_sms(h) * 2);
-        HPSS_CUDA_TRY(h, launch_ls_tuned_oct(lp, grid, tiles, (uint32_t)units, h->stream, 0));
+    } else if (octKernel) {
+        HPSS_CUDA_TRY(h, launch_ls_oct(lp, (uint32_t)num_sms(h), h->octPartial.p, octParts,
+                                       h->stream));
     } else {
         HPSS_CUDA_TRY(h, launch_ls_plain(lp, h->stream));
     }
@@ -606,7 +612,7 @@ hpss_status hpss_destroy(hpss_handle h) {
     free_gather(h);
     for (auto *b : {&h->params, &h->chunkBounds, &h->selFirst, &h->selCount, &h->selIdx,
                     &h->candFirst, &h->candCount, &h->notUsed, &h->errWord, &h->m0s,
-                    &h->out, &h->octCands, &h->prior})
+                    &h->out, &h->octCands, &h->prior, &h->octPartial})
         release(h, *b);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);

@@ -63,23 +63,32 @@ __device__ __forceinline__ int oct_displaced_midpoint(float h, float h0,
                                                       float t0, float m0,
                                                       float c, float slope,
                                                       float *mh) {
-    const float h0sq = __fmul_rn(h0, h0);
     const float theta = __fmul_rn(t0, slope);
-    const float gamma = 2 * sqrtf(__fmaf_rn(h, h, h0sq));
+    // h*h + h0*h0 and h*h - h0*h0: the product h*h is rounded on its own and
+    // the h0 product is fused (fractional half-offsets tell the forms apart)
+    const float gamma = 2 * sqrtf(__fmaf_rn(h0, h0, __fmul_rn(h, h)));
     const float tn0_sq = oct_tn0_sq(t0, c, h0);
     const float theta_sq = __fmul_rn(theta, theta);
     const float gamma_sq = __fmul_rn(gamma, gamma);
     const float tn0_quad = __fmul_rn(tn0_sq, tn0_sq);
     const float p16 = __fmul_rn(
         __fmul_rn(__fmul_rn(__fmul_rn(__fmul_rn(16.f, h), h), h0), h0), theta_sq);
-    float arg = __fmaf_rn(__fmul_rn(tn0_quad, theta_sq), gamma_sq,
-                          __fmul_rn(tn0_quad, tn0_quad));
+    // tq^2 + tq ts gs + 16 h^2 h0^2 ts^2 as the reference's OCT kernel rounds
+    // it: tq ts gs as products, tq^2 fused onto them, the last product fused;
+    // then ts gs + 2 tq as a plain add (matched against every entry of the
+    // reference kernel's semblance tables on the OCT fixtures)
+    float arg = __fmaf_rn(tn0_quad, tn0_quad, __fmul_rn(__fmul_rn(tn0_quad, theta_sq), gamma_sq));
     arg = __fmaf_rn(p16, theta_sq, arg);
     if (arg < 0) return DE_NEG_SQRT;
-    arg = __fadd_rn(__fmaf_rn(theta_sq, gamma_sq, __fmul_rn(2.f, tn0_quad)),
+    arg = __fadd_rn(__fadd_rn(__fmul_rn(theta_sq, gamma_sq), __fmul_rn(2.f, tn0_quad)),
                     __fmul_rn(2.f, sqrtf(arg)));
     if (arg == 0) return DE_DIV_ZERO;
-    *mh = __fadd_rn(m0, __fmul_rn(__fmul_rn(2.f, theta), __fmaf_rn(h, h, -h0sq)) / sqrtf(arg));
+    // m0 + 2 theta (h^2 - h0^2) / sqrt(.): the reference's fast-math build
+    // divides by multiplying with the approximate reciprocal and fuses that
+    // product with the add of m0 -- fma(2 theta dif, rcp(sqrt(.)), m0)
+    const float twoTheta = 2.f * theta;
+    const float dif = __fmaf_rn(-h0, h0, __fmul_rn(h, h));
+    *mh = __fmaf_rn(__fmul_rn(twoTheta, dif), __fdividef(1.0f, sqrtf(arg)), m0);
     return DE_OK;
 }
 

@@ -141,9 +141,13 @@ cudaError_t launch_ls_tuned_cmp_exact(const LsParams &p, uint32_t grid, uint32_t
                                       uint32_t nUnits, cudaStream_t st, int variant);
 cudaError_t launch_ls_tuned_zocrs_exact(const LsParams &p, uint32_t grid, uint32_t tiles,
                                         uint32_t nUnits, cudaStream_t st, int variant);
-// Tuned kernel for OCT (4 candidates per thread, branchy window loop).
-cudaError_t launch_ls_tuned_oct(const LsParams &p, uint32_t grid, uint32_t tiles,
-                                uint32_t nUnits, cudaStream_t st, int unused);
+// Tuned kernel for OCT (ls_oct.cu): (midpoint, 32-sample tile, candidate
+// part) units, windows read through L1, parts merged in candidate order.
+// `partial` holds oct_partial_bytes(nM0, S, parts) bytes.
+uint32_t oct_parts(const LsParams &p, uint32_t numSms);
+size_t oct_partial_bytes(uint32_t nM0, uint32_t S, uint32_t parts);
+cudaError_t launch_ls_oct(const LsParams &p, uint32_t numSms, void *partial, uint32_t parts,
+                          cudaStream_t st);
 cudaError_t launch_select_oct(const LsParams &p, const float *cands,
                               uint32_t nCand, uint32_t *selIdx,
                               uint32_t *selCount, const uint32_t *candFirst,
@@ -152,7 +156,6 @@ cudaError_t launch_convert_storage(const float *src, uint16_t *dst,
                                    float *scale, uint32_t nTraces, uint32_t S,
                                    uint32_t stride, int storage,
                                    cudaStream_t st);
-size_t tuned_smem_bytes();
 cudaError_t launch_de(const DeParams &d, int model, uint32_t numSms, cudaStream_t st);
 cudaError_t launch_sf(const LsParams &p, int model, uint32_t grid, uint32_t nUnits,
                       cudaStream_t st);

@@ -1,0 +1,257 @@
+// ls_oct.cu -- the tuned linear-search kernel for the OCT traveltime.
+//
+// OCT differs from CMP / ZO-CRS in where the time goes: per (sample,
+// candidate, trace) the displaced midpoint (oct/common.cuh:7-35) and, for the
+// traces that pass |m - mh| <= apm, the OCT time (:37-94) cost a few square
+// roots and divisions each, while most traces of the wide OCT aperture fail
+// the test and read no samples at all.  Staging trace spans in shared memory
+// does not pay here (the spans are whole traces and mostly unused), so this
+// kernel reads the windows it needs through L1:
+//
+//  * lane = t0 sample (32 consecutive samples per warp): neighbouring lanes
+//    have nearly the same displaced midpoint and window position, so the skip
+//    decisions agree across the warp and the window loads fall on a few
+//    cache lines of one trace row;
+//  * a warp evaluates R candidates per thread (independent chains);
+//  * the candidate range is split into `parts` (CTAs work on (midpoint,
+//    32-sample tile, part) units) so that a call with few midpoints still
+//    fills the GPU; each unit writes the best / runner-up of its part and
+//    merge_parts_kernel combines the parts in candidate order.
+//
+// The per-candidate arithmetic is the plain kernel's (model_time<kModelOct>,
+// window_index, the COMPUTE_SEMBLANCE restatement), in the same trace order,
+// so semblance, stack and chosen candidate equal the plain kernel's.
+#include "hpss_device.cuh"
+#include "hpss_internal.h"
+
+namespace hpss {
+
+constexpr int kOctWarps = 8;
+
+struct PartBest {
+    float best, second, stack;
+    uint32_t p;
+};
+
+template <int W, int R>
+__global__ void __launch_bounds__(kOctWarps * 32)
+ls_oct_kernel(LsParams a, uint32_t tiles, uint32_t parts, uint32_t chunksPerPart,
+              uint32_t nUnits, PartBest *partial) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int S = (int)a.S, tau = a.tau;
+    constexpr int kChunk = kOctWarps * R;
+    __shared__ float shBest[kOctWarps][32], shSecond[kOctWarps][32], shStack[kOctWarps][32];
+    __shared__ uint32_t shP[kOctWarps][32];
+    __shared__ unsigned long long shNu;
+
+    for (uint32_t unit = blockIdx.x; unit < nUnits; unit += gridDim.x) {
+        const uint32_t part = unit % parts;
+        const uint32_t tile = (unit / parts) % tiles;
+        const uint32_t mi = unit / (parts * tiles);
+        const int s = (int)tile * 32 + lane;
+        const int sc = min(s, S - 1);
+        const float t0 = static_cast<float>(sc) * a.dt;
+        const float m0 = a.m0s[mi];
+        const uint32_t first = a.selFirst[mi], cnt = a.selCount[mi];
+        if (threadIdx.x == 0) shNu = 0;
+
+        float best = -1.f, second = -1.f, bestStack = 0.f;
+        uint32_t bestP = 0xffffffffu;
+        unsigned long long notUsed = 0;
+        const uint32_t c0 = part * chunksPerPart;
+        const uint32_t c1 = min(c0 + chunksPerPart, (a.P + kChunk - 1) / kChunk);
+        for (uint32_t chunk = c0; chunk < c1; chunk++) {
+            float cc[R], sl[R];
+            bool valid[R];
+#pragma unroll
+            for (int r = 0; r < R; r++) {
+                const uint32_t p = chunk * kChunk + warp * R + r;
+                valid[r] = p < a.P;
+                const uint32_t pc = valid[r] ? p : a.P - 1;
+                cc[r] = a.params[2 * (size_t)pc];
+                sl[r] = a.params[2 * (size_t)pc + 1];
+            }
+            float num[R][W], lin[R], den[R];
+            unsigned used[R], nu[R];
+#pragma unroll
+            for (int r = 0; r < R; r++) {
+#pragma unroll
+                for (int j = 0; j < W; j++) num[r][j] = 0.f;
+                lin[r] = den[r] = 0.f;
+                used[r] = nu[r] = 0;
+            }
+            for (uint32_t q = 0; q < cnt; q++) {
+                const uint32_t ti = a.selIdx ? a.selIdx[first + q] : first + q;
+                const float m = a.mid[ti], h = a.hoff[ti];
+                const float *tr = a.samples + (size_t)ti * a.stride;
+#pragma unroll
+                for (int r = 0; r < R; r++) {
+                    float t;
+                    const int ok = model_time<kModelOct>(t0, cc[r], sl[r], 0.f, m, h, 0.f, m0,
+                                                         a.apm, a.h0, &t);
+                    if (ok < 0) nu[r]++;
+                    if (ok > 0) {
+                        const WinIdx wi = window_index(t, a.dt);
+                        if (window_in_trace(wi.k, tau, S)) {
+                            const float *y = tr + (wi.k - tau);
+                            float y1 = __ldg(y);
+#pragma unroll
+                            for (int jj = 0; jj < W; jj++) {
+                                const float y0 = y1;
+                                y1 = __ldg(y + jj + 1);
+                                const float u = (y1 - y0) * wi.frac + y0;
+                                num[r][jj] += u;
+                                lin[r] += u;
+                                den[r] += u * u;
+                            }
+                            used[r]++;
+                        }
+                    }
+                }
+            }
+#pragma unroll
+            for (int r = 0; r < R; r++) {
+                float sembl, stack;
+                reduce_semblance(num[r], lin[r], den[r], W, used[r], &sembl, &stack);
+                const uint32_t p = chunk * kChunk + warp * R + r;
+                if (valid[r]) {
+                    top2_offer(sembl, best, second);
+                    if (sembl > best) {
+                        best = sembl;
+                        bestStack = stack;
+                        bestP = p;
+                    }
+                    if (s < S) notUsed += nu[r];
+                }
+            }
+        }
+        // ---- merge the warps (candidate order is preserved by better())
+        shBest[warp][lane] = best;
+        shSecond[warp][lane] = second;
+        shStack[warp][lane] = bestStack;
+        shP[warp][lane] = bestP;
+#pragma unroll
+        for (int o = 16; o; o >>= 1) notUsed += __shfl_xor_sync(0xffffffffu, notUsed, o);
+        __syncthreads();
+        if (lane == 0 && notUsed) atomicAdd(&shNu, notUsed);
+        if (warp == 0) {
+            for (int wv = 1; wv < kOctWarps; wv++) {
+                const float os = shBest[wv][lane];
+                const uint32_t op = shP[wv][lane];
+                if (better(os, op, best, bestP)) bestStack = shStack[wv][lane];
+                top2_merge(os, op, shSecond[wv][lane], best, bestP, second);
+            }
+            if (s < S) {
+                PartBest pb;
+                pb.best = best;
+                pb.second = second;
+                pb.stack = bestStack;
+                pb.p = bestP;
+                partial[((size_t)mi * parts + part) * a.S + s] = pb;
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0 && shNu && a.notUsed) atomicAdd(a.notUsed + mi, shNu);
+    }
+}
+
+// Combine the parts of every (midpoint, sample) in candidate order; write the
+// result block and count near-ties.
+__global__ void merge_parts_kernel(LsParams a, uint32_t parts, const PartBest *partial) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool live = i < (uint64_t)a.nM0 * a.S;
+    bool tie = false;
+    if (live) {
+        const uint32_t mi = (uint32_t)(i / a.S), s = (uint32_t)(i % a.S);
+        const int np = a.np;
+        float *out = a.out + (size_t)mi * (2 + np) * a.S;
+        if (a.selCount[mi] == 0) {
+            // reference: midpoint skipped, reset (zero) result
+            for (int r = 0; r < 2 + np; r++) out[(size_t)r * a.S + s] = 0.f;
+        } else {
+            float best = -1.f, second = -1.f, stack = 0.f;
+            uint32_t bp = 0xffffffffu;
+            for (uint32_t k = 0; k < parts; k++) {
+                const PartBest pb = partial[((size_t)mi * parts + k) * a.S + s];
+                if (better(pb.best, pb.p, best, bp)) stack = pb.stack;
+                top2_merge(pb.best, pb.p, pb.second, best, bp, second);
+            }
+            out[s] = best;
+            out[a.S + s] = stack;
+            if (bp != 0xffffffffu) {
+                const float *pr = a.params + (size_t)bp * np;
+                out[2 * a.S + s] = 2 / sqrtf(pr[0]);
+                for (int j = 1; j < np; j++) out[(size_t)(2 + j) * a.S + s] = pr[j];
+            } else {
+                for (int j = 0; j < np; j++) out[(size_t)(2 + j) * a.S + s] = 0.f;
+            }
+            tie = near_tie(best, second);
+        }
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, tie);
+    if ((threadIdx.x & 31) == 0 && m && a.nearTies)
+        atomicAdd(a.nearTies, (unsigned long long)__popc(m));
+}
+
+size_t oct_partial_bytes(uint32_t nM0, uint32_t S, uint32_t parts) {
+    return (size_t)nM0 * parts * S * sizeof(PartBest);
+}
+
+template <int R>
+uint32_t oct_chunks(uint32_t P) {
+    return (P + kOctWarps * R - 1) / (kOctWarps * R);
+}
+
+template <int W, int R>
+cudaError_t launch_oct_w(const LsParams &p, uint32_t numSms, void *partial, uint32_t parts,
+                         cudaStream_t st) {
+    const uint32_t tiles = (p.S + 31) / 32;
+    const uint32_t nChunks = oct_chunks<R>(p.P);
+    const uint32_t chunksPerPart = (nChunks + parts - 1) / parts;
+    const uint64_t units = (uint64_t)p.nM0 * tiles * parts;
+    if (units == 0) return cudaSuccess;
+    if (units > 0xffffffffull) return cudaErrorInvalidConfiguration;
+    int perSm = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, ls_oct_kernel<W, R>,
+                                                                  kOctWarps * 32, 0);
+    if (e != cudaSuccess) return e;
+    const uint32_t grid =
+        (uint32_t)std::min<uint64_t>(units, (uint64_t)numSms * (uint64_t)std::max(perSm, 1));
+    ls_oct_kernel<W, R><<<grid, kOctWarps * 32, 0, st>>>(
+        p, tiles, parts, chunksPerPart, (uint32_t)units, static_cast<PartBest *>(partial));
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    const uint64_t n = (uint64_t)p.nM0 * p.S;
+    merge_parts_kernel<<<(uint32_t)((n + 255) / 256), 256, 0, st>>>(
+        p, parts, static_cast<const PartBest *>(partial));
+    return cudaGetLastError();
+}
+
+// Parts: enough (midpoint, tile, part) units for ~8 waves of the GPU, never
+// more than the candidate chunks.
+uint32_t oct_parts(const LsParams &p, uint32_t numSms) {
+    constexpr int R = 2;
+    const uint32_t tiles = (p.S + 31) / 32;
+    const uint64_t base = (uint64_t)p.nM0 * tiles;
+    const uint64_t want = (uint64_t)numSms * 2 * 8;
+    uint64_t parts = base >= want ? 1 : (want + base - 1) / base;
+    return (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(parts, oct_chunks<R>(p.P)));
+}
+
+cudaError_t launch_ls_oct(const LsParams &p, uint32_t numSms, void *partial, uint32_t parts,
+                          cudaStream_t st) {
+    constexpr int R = 2;
+    switch (p.w) {
+        case 1: return launch_oct_w<1, R>(p, numSms, partial, parts, st);
+        case 3: return launch_oct_w<3, R>(p, numSms, partial, parts, st);
+        case 5: return launch_oct_w<5, R>(p, numSms, partial, parts, st);
+        case 7: return launch_oct_w<7, R>(p, numSms, partial, parts, st);
+        case 9: return launch_oct_w<9, R>(p, numSms, partial, parts, st);
+        case 11: return launch_oct_w<11, R>(p, numSms, partial, parts, st);
+        case 13: return launch_oct_w<13, R>(p, numSms, partial, parts, st);
+        case 15: return launch_oct_w<15, R>(p, numSms, partial, parts, st);
+        default: return cudaErrorNotSupported;
+    }
+}
+
+}  // namespace hpss

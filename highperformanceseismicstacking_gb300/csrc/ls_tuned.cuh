@@ -1,6 +1,6 @@
-// ls_tuned.cuh -- the tuned linear-search kernel (template; instantiated per
-// traveltime model in ls_tuned_{cmp,zocrs,oct}.cu so they compile in
-// parallel).
+// ls_tuned.cuh -- the tuned linear-search kernel for the CMP and ZO-CRS
+// traveltimes (template; instantiated in ls_tuned_{cmp,zocrs}{,_exact}.cu so
+// they compile in parallel; the OCT kernel is ls_oct.cu).
 //
 // Work unit: one midpoint x 32 consecutive t0 samples (lane = sample).  The
 // 8 warps of a CTA split the candidates; candidates are visited in chunks of
@@ -27,28 +27,6 @@
 #include "hpss_internal.h"
 
 namespace hpss {
-
-// Shared-memory budget of one CTA (two CTAs per SM).
-constexpr int kStageFloats = 24576;  // 96 KiB of staged samples
-
-struct TraceMeta {
-    int base;    // shared-memory index of sample 0 of the trace (may be < 0)
-    int lo;      // first staged sample
-    int len;     // staged sample count (0: trace contributes nothing)
-    float m;
-    float h;
-    float hsq;
-};
-
-struct TunedSmem {
-    float y[kStageFloats];
-    TraceMeta meta[kTunedThreads];
-    int warpSum[kTunedWarps];
-    float bestS[kTunedWarps][kTileSamples];
-    float bestK[kTunedWarps][kTileSamples];
-    uint32_t bestP[kTunedWarps][kTileSamples];
-    float bestSec[kTunedWarps][kTileSamples];
-};
 
 // Sample span [lo, lo+len) of trace (m, h, hsq) touched by any in-trace
 // window of the tile [t0a, t0b] and the chunk parameter box.  Conservative by
@@ -112,215 +90,6 @@ __device__ __forceinline__ void trace_span(const LsParams &a, const float *cb,
     int e = min((h + 4) & ~3, (int)a.stride); // exclusive, multiple of 4
     *lo = l;
     *len = e - l;
-}
-
-template <int MODEL, int W, int R>
-__global__ void __launch_bounds__(kTunedThreads, 2)
-ls_tuned_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
-    extern __shared__ __align__(16) unsigned char smemRaw[];
-    TunedSmem &sm = *reinterpret_cast<TunedSmem *>(smemRaw);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int np = a.np;
-    const int S = (int)a.S, tau = a.tau;
-
-    for (uint32_t unit = blockIdx.x; unit < nUnits; unit += gridDim.x) {
-        const uint32_t mi = unit / tiles;
-        const int s0 = (int)(unit % tiles) * kTileSamples;
-        const int s = s0 + lane;
-        const int sc = min(s, S - 1);
-        const float t0 = static_cast<float>(sc) * a.dt;
-        const float t0a = static_cast<float>(s0) * a.dt;
-        const float t0b = static_cast<float>(min(s0 + kTileSamples - 1, S - 1)) * a.dt;
-        const float m0 = a.m0s[mi];
-        const uint32_t first = a.selFirst[mi], cnt = a.selCount[mi];
-        float *out = a.out + (size_t)mi * (2 + np) * a.S;
-
-        if (cnt == 0) {
-            // reference: midpoint skipped, reset (zero) result
-            if (warp < 2 + np && s < S) out[(size_t)warp * a.S + s] = 0.f;
-            continue;
-        }
-
-        float best = -1.f, bestStack = 0.f;
-        uint32_t bestP = 0xffffffffu;
-        float second = -1.f;  // runner-up semblance (near-tie count)
-        unsigned long long notUsed = 0;
-
-        for (uint32_t chunk = 0; chunk < a.nChunks; chunk++) {
-            float cc[R], c1[R], c2[R];
-            bool valid[R];
-#pragma unroll
-            for (int r = 0; r < R; r++) {
-                uint32_t p = chunk * a.chunkSize + warp * R + r;
-                valid[r] = p < a.P;
-                uint32_t pc = valid[r] ? p : a.P - 1;
-                const float *pr = a.params + (size_t)pc * np;
-                cc[r] = pr[0];
-                c1[r] = np > 1 ? pr[1] : 0.f;
-                c2[r] = np > 2 ? pr[2] : 0.f;
-            }
-            const float *cb = a.chunkBounds + (size_t)chunk * 2 * np;
-            float cbl[6];
-#pragma unroll
-            for (int j = 0; j < 6; j++) cbl[j] = j < 2 * np ? cb[j] : 0.f;
-
-            float num[R][W];
-            float lin[R], den[R];
-            unsigned used[R], nu[R];
-#pragma unroll
-            for (int r = 0; r < R; r++) {
-#pragma unroll
-                for (int j = 0; j < W; j++) num[r][j] = 0.f;
-                lin[r] = den[r] = 0.f;
-                used[r] = nu[r] = 0;
-            }
-
-            for (uint32_t q0 = 0; q0 < cnt;) {
-                __syncthreads();  // previous block's readers are done
-                // ---- spans of the next (up to 256) traces, prefix offsets
-                const uint32_t q = q0 + threadIdx.x;
-                int lo = 0, len = 0;
-                float tm = 0.f, th = 0.f, thsq = 0.f;
-                uint32_t ti = 0;
-                if (q < cnt) {
-                    ti = a.selIdx ? a.selIdx[first + q] : first + q;
-                    tm = a.mid[ti];
-                    th = a.hoff[ti];
-                    thsq = a.hsq[ti];
-                    trace_span<MODEL>(a, cbl, m0, t0a, t0b, tm, thsq, &lo, &len);
-                }
-                int incl = len;
-#pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    int v = __shfl_up_sync(0xffffffffu, incl, o);
-                    if (lane >= o) incl += v;
-                }
-                if (lane == 31) sm.warpSum[warp] = incl;
-                __syncthreads();
-                int woff = 0;
-#pragma unroll
-                for (int wv = 0; wv < kTunedWarps; wv++)
-                    woff += wv < warp ? sm.warpSum[wv] : 0;
-                const int off = woff + incl - len;
-                const bool fits = (q < cnt) && (off + len <= kStageFloats);
-                const int nfit = __syncthreads_count(fits);
-                if (fits) {
-                    TraceMeta md;
-                    md.base = off - lo;
-                    md.lo = lo;
-                    md.len = len;
-                    md.m = tm;
-                    md.h = th;
-                    md.hsq = thsq;
-                    sm.meta[threadIdx.x] = md;
-                }
-                if (nfit == 0) {
-                    // a single span larger than the stage: cannot happen for
-                    // S <= kStageFloats - 8; flag and stop this midpoint
-                    if (threadIdx.x == 0) atomicOr(a.errorWord, kErrSpanOverflow);
-                    break;
-                }
-                __syncthreads();
-                // ---- stage spans (warp per trace, 16-byte vector loads)
-                for (int j = warp; j < nfit; j += kTunedWarps) {
-                    const TraceMeta md = sm.meta[j];
-                    if (md.len == 0) continue;
-                    const uint32_t tj = a.selIdx ? a.selIdx[first + q0 + j] : first + q0 + j;
-                    const float4 *src = reinterpret_cast<const float4 *>(
-                        a.samples + (size_t)tj * a.stride + md.lo);
-                    float4 *dst = reinterpret_cast<float4 *>(sm.y + md.base + md.lo);
-                    for (int v = lane; v < (md.len >> 2); v += 32) dst[v] = __ldg(src + v);
-                }
-                __syncthreads();
-                // ---- evaluate
-                for (int j = 0; j < nfit; j++) {
-                    const TraceMeta md = sm.meta[j];
-                    if (md.len == 0) continue;
-                    const int lim = md.base + md.lo + md.len - (W + 1);
-#pragma unroll
-                    for (int r = 0; r < R; r++) {
-                        float t;
-                        int ok = model_time<MODEL>(t0, cc[r], c1[r], c2[r], md.m,
-                                                   md.h, md.hsq, m0, a.apm, a.h0, &t);
-                        if (MODEL == kModelOct && ok < 0) nu[r]++;
-                        if (ok > 0) {
-                            WinIdx wi = window_index(t, a.dt);
-                            if (window_in_trace(wi.k, tau, S)) {
-                                int b = md.base + wi.k - tau;
-                                if (b < md.base + md.lo || b > lim) {
-                                    atomicOr(a.errorWord, kErrSmemBounds);
-                                    b = min(max(b, md.base + md.lo), lim);
-                                }
-                                const float *y = sm.y + b;
-                                float y1 = y[0];
-#pragma unroll
-                                for (int jj = 0; jj < W; jj++) {
-                                    float y0 = y1;
-                                    y1 = y[jj + 1];
-                                    float u = (y1 - y0) * wi.frac + y0;
-                                    num[r][jj] += u;
-                                    lin[r] += u;
-                                    den[r] += u * u;
-                                }
-                                used[r]++;
-                            }
-                        }
-                    }
-                }
-                q0 += nfit;
-            }
-
-#pragma unroll
-            for (int r = 0; r < R; r++) {
-                float sembl, stack;
-                reduce_semblance(num[r], lin[r], den[r], W, used[r], &sembl, &stack);
-                const uint32_t p = chunk * a.chunkSize + warp * R + r;
-                if (valid[r]) top2_offer(sembl, best, second);
-                if (valid[r] && sembl > best) {
-                    best = sembl;
-                    bestStack = stack;
-                    bestP = p;
-                }
-                if (valid[r] && s < S) notUsed += nu[r];
-            }
-        }
-
-        // ---- argmax across warps, per sample (lane)
-        sm.bestS[warp][lane] = best;
-        sm.bestK[warp][lane] = bestStack;
-        sm.bestP[warp][lane] = bestP;
-        sm.bestSec[warp][lane] = second;
-        if (MODEL == kModelOct) {
-#pragma unroll
-            for (int o = 16; o; o >>= 1) notUsed += __shfl_xor_sync(0xffffffffu, notUsed, o);
-            if (lane == 0 && notUsed && a.notUsed) atomicAdd(a.notUsed + mi, notUsed);
-        }
-        __syncthreads();
-        if (warp == 0) {
-            for (int wv = 1; wv < kTunedWarps; wv++) {
-                float os = sm.bestS[wv][lane];
-                uint32_t op = sm.bestP[wv][lane];
-                if (better(os, op, best, bestP)) bestStack = sm.bestK[wv][lane];
-                top2_merge(os, op, sm.bestSec[wv][lane], best, bestP, second);
-            }
-            if (a.nearTies) {
-                const unsigned tie = __ballot_sync(0xffffffffu, s < S && near_tie(best, second));
-                if (lane == 0 && tie) atomicAdd(a.nearTies, (unsigned long long)__popc(tie));
-            }
-            if (s < S) {
-                out[s] = best;
-                out[a.S + s] = bestStack;
-                if (bestP != 0xffffffffu) {
-                    const float *pr = a.params + (size_t)bestP * np;
-                    out[2 * a.S + s] = 2 / sqrtf(pr[0]);
-                    for (int j = 1; j < np; j++) out[(size_t)(2 + j) * a.S + s] = pr[j];
-                } else {
-                    for (int j = 0; j < np; j++) out[(size_t)(2 + j) * a.S + s] = 0.f;
-                }
-            }
-        }
-        __syncthreads();
-    }
 }
 
 // ---------------------------------------------------------------------------
@@ -768,35 +537,6 @@ cudaError_t launch_ls_tuned2_model(const LsParams &p, uint32_t grid,
             return cudaErrorNotSupported;
     }
 #undef HPSS_TUNED2_CASE
-}
-
-template <int MODEL, int R>
-cudaError_t launch_ls_tuned_model(const LsParams &p, uint32_t grid,
-                                  uint32_t tiles, uint32_t nUnits,
-                                  cudaStream_t st) {
-    const size_t smem = sizeof(TunedSmem);
-#define HPSS_TUNED_CASE(WV)                                                   \
-    case WV: {                                                                \
-        auto k = ls_tuned_kernel<MODEL, WV, R>;                              \
-        cudaError_t e = cudaFuncSetAttribute(                                 \
-            k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);       \
-        if (e != cudaSuccess) return e;                                       \
-        k<<<grid, kTunedThreads, smem, st>>>(p, tiles, nUnits);              \
-        return cudaGetLastError();                                            \
-    }
-    switch (p.w) {
-        HPSS_TUNED_CASE(1)
-        HPSS_TUNED_CASE(3)
-        HPSS_TUNED_CASE(5)
-        HPSS_TUNED_CASE(7)
-        HPSS_TUNED_CASE(9)
-        HPSS_TUNED_CASE(11)
-        HPSS_TUNED_CASE(13)
-        HPSS_TUNED_CASE(15)
-        default:
-            return cudaErrorNotSupported;
-    }
-#undef HPSS_TUNED_CASE
 }
 
 }  // namespace hpss

@@ -14,8 +14,9 @@ cudaError_t launch_ls_tuned_cmp(const LsParams &p, uint32_t grid, uint32_t tiles
     return launch_ls_tuned2_model<kModelCmp, 2, 2, false>(p, grid, tiles, nUnits, st);
 }
 
-size_t tuned_smem_bytes() { return sizeof(TunedSmem); }
-size_t tuned_stage_floats() { return kStageFloats; }
+// staged floats per CTA of the largest (2 CTAs/SM) and smallest (3 CTAs/SM)
+// shapes: a trace row must fit the stage
+size_t tuned_stage_floats() { return Stage2<2>::kFloats; }
 size_t tuned_stage_floats_min() { return Stage2<3>::kFloats; }
 
 }  // namespace hpss

@@ -162,9 +162,10 @@ class ReferenceKernels:
 
     def linear_search_midpoint(self, model: str, samples, mid, hoff, sel, m0: float, dt: float,
                                tau: int, params: np.ndarray, apm: float = 0.0,
-                               h0: float = 0.0):
+                               h0: float = 0.0, timing: bool = False):
         """computeSemblanceAtGpuForMidpoint (CudaLinearSearchAlgorithm.cu:35-163).
-        Returns (result [(2+np)][S], sembl [S][P], stack [S][P], notUsed [S*P])."""
+        Returns (result [(2+np)][S], sembl [S][P], stack [S][P], notUsed [S*P]),
+        plus the device ms of the evaluation and argmax launches if timing."""
         S = samples.shape[1]
         P = params.shape[0]
         npar = params.shape[1]
@@ -186,6 +187,9 @@ class ReferenceKernels:
         dp = self._dev(np.ascontiguousarray(params, np.float32).ravel())
         g = _grid(S * P)
         gb = _grid(S)
+        e0 = self.torch.cuda.Event(enable_timing=True)
+        e1 = self.torch.cuda.Event(enable_timing=True)
+        e0.record()
         if model == "cmp":
             mod = self.d.module("cmp_linear_search")
             self.d.launch(mod["computeSemblancesForCommonMidPoint"], g, THREADS,
@@ -211,14 +215,18 @@ class ReferenceKernels:
             best = mod["selectBestSemblancesForOffsetContinuationTrajectory"]
         self.d.launch(best, gb, THREADS, [self._ptr(sem), self._ptr(stk), self._ptr(dp),
                                           C.c_uint(P), C.c_uint(S), self._ptr(res)])
-        return (res.cpu().numpy().reshape(2 + npar, S), sem.cpu().numpy().reshape(S, P),
-                stk.cpu().numpy().reshape(S, P), nu.cpu().numpy())
+        e1.record()
+        self.torch.cuda.synchronize()
+        out = (res.cpu().numpy().reshape(2 + npar, S), sem.cpu().numpy().reshape(S, P),
+               stk.cpu().numpy().reshape(S, P), nu.cpu().numpy())
+        return out + (e0.elapsed_time(e1),) if timing else out
 
     def stretch_free_midpoint_cmp(self, samples, hoff, sel, dt: float, tau: int,
-                                  prior: np.ndarray, nmax: int = 10) -> np.ndarray:
+                                  prior: np.ndarray, nmax: int = 10, timing: bool = False):
         """CudaStretchFreeAlgorithm::computeSemblanceAtGpuForMidpoint for CMP
         (the only model its CUDA path runs, CudaStretchFreeAlgorithm.cu:52-66).
-        prior: [S] velocities.  Returns [3][S] (semblance, stack, n)."""
+        prior: [S] velocities.  Returns [3][S] (semblance, stack, n), plus the
+        device ms of the evaluation and argmax launches if timing."""
         S = samples.shape[1]
         nn = 2 * nmax + 1
         sel = np.asarray(sel)
@@ -233,6 +241,9 @@ class ReferenceKernels:
         stk = self.torch.zeros(S * nn, dtype=self.torch.float32, device="cuda")
         res = self.torch.zeros(3 * S, dtype=self.torch.float32, device="cuda")
         mod = self.d.module("cmp_stretch_free")
+        e0 = self.torch.cuda.Event(enable_timing=True)
+        e1 = self.torch.cuda.Event(enable_timing=True)
+        e0.record()
         self.d.launch(mod["computeSemblancesForCommonMidPoint"], _grid(S * nn), THREADS,
                       [self._ptr(smp), self._ptr(dh2), C.c_uint(n), C.c_uint(S), C.c_float(dt),
                        C.c_int(tau), C.c_int(w), self._ptr(dprior), self._ptr(narr),
@@ -240,7 +251,10 @@ class ReferenceKernels:
         best = self.d.module("common_stretch_free")["selectBestSemblances"]
         self.d.launch(best, _grid(S), THREADS, [self._ptr(sem), self._ptr(stk), self._ptr(narr),
                                                 C.c_uint(nn), C.c_uint(S), self._ptr(res)])
-        return res.cpu().numpy().reshape(3, S)
+        e1.record()
+        self.torch.cuda.synchronize()
+        out = res.cpu().numpy().reshape(3, S)
+        return (out, e0.elapsed_time(e1)) if timing else out
 
     def differential_evolution_midpoint(self, model: str, samples, mid, hoff, m0: float,
                                         dt: float, tau: int, lower, upper, pop: int, gens: int,

@@ -14,8 +14,13 @@ to the engine on the same midpoints.  Prints one JSON line per workload.
           one synchronised launch per operator and generation, as the
           reference runs it) against the engine's fused DE launch.
 
+  oct [n] OCT linear search on the OCT DE line's geometry (11 x 5 candidates).
+  sf [n]  CMP stretch-free stack on the CMP production line.
+
     python tests/golden/time_reference_kernels.py ls 40
     python tests/golden/time_reference_kernels.py de 2
+    python tests/golden/time_reference_kernels.py oct 1
+    python tests/golden/time_reference_kernels.py sf 20
 """
 from __future__ import annotations
 
@@ -126,12 +131,93 @@ def time_de(n_mid: int = 2):
         print(json.dumps(line_out))
 
 
+def time_oct(n_mid: int = 1):
+    """OCT linear search (the OCT DE line's geometry, 11 x 5 candidates,
+    h0 = 0): the reference's per-midpoint evaluation + argmax against the
+    engine's plain and tuned kernels on the same midpoints."""
+    from oracle import oracle
+    w = synthetic.WORKLOADS["oct-de"]
+    line = w.make_line(n_cmp=60)
+    lower, upper = synthetic.workload_bounds(w)
+    tau = tau_index(w.tau, line.dt)
+    gran = [11, 5]
+    rk = ref_runner.ReferenceKernels()
+    params = rk.build_grid("oct", lower, upper, gran)
+    cands = oracle.oct_selection_candidates(lower, upper)
+    S = line.samples_per_trace
+    mid = len(line.cdp_midpoints) // 2
+    m0s = np.ascontiguousarray(line.cdp_midpoints[mid:mid + n_mid])
+    ref_ms, ref_evals, ref_out = 0.0, 0.0, []
+    for m0 in m0s:
+        sel = np.nonzero(rk.select("oct", line.midpoints, line.halfoffsets, float(m0), w.apm,
+                                   w.h0, S, float(line.dt), cands))[0]
+        res, _, _, _, ms = rk.linear_search_midpoint("oct", line.samples, line.midpoints,
+                                                     line.halfoffsets, sel, float(m0),
+                                                     float(line.dt), tau, params, w.apm, w.h0,
+                                                     timing=True)
+        ref_ms += ms
+        ref_evals += float(sel.size) * S * params.shape[0]
+        ref_out.append(res)
+    out = {"workload": "oct-ls (OCT DE line geometry, 60 CMPs, 11 x 5 candidates)",
+           "midpoints": int(len(m0s)), "samples": S,
+           "reference": {"ms": ref_ms, "evals": ref_evals, "value": ref_evals / (ref_ms / 1e3)}}
+    with capi.Engine(0) as eng:
+        eng.upload_gather(line.samples, line.midpoints, line.halfoffsets, float(line.dt))
+        eng.set_traveltime("oct", lower, upper, w.apm, w.h0)
+        eng.set_window(tau)
+        for kernel in ("plain", "tuned"):
+            eng.linear_search(m0s, gran, kernel)
+            got, st = eng.linear_search(m0s, gran, kernel)
+            same = float(np.mean(np.isclose(got[:, 2], np.stack(ref_out)[:, 2], rtol=1e-6)))
+            out[kernel] = {"ms": st["kernel_ms"], "evals": st["evals"],
+                           "value": st["evals"] / (st["kernel_ms"] / 1e3),
+                           "velocity_equal_to_reference": same}
+    print(json.dumps(out))
+
+
+def time_sf(n_mid: int = 20):
+    """CMP stretch-free stack (21 n values, window 7) on the CMP production
+    line, prior velocities from the engine's linear search: the reference's
+    per-midpoint evaluation + argmax against the engine's stretch-free."""
+    w = synthetic.WORKLOADS["cmp-production"]
+    line = w.make_line(n_cmp=n_mid)
+    tau = tau_index(w.tau, line.dt)
+    S = line.samples_per_trace
+    m0s = line.cdp_midpoints
+    with capi.Engine(0) as eng:
+        eng.upload_gather(line.samples, line.midpoints, line.halfoffsets, float(line.dt))
+        eng.set_traveltime("cmp", w.lower, w.upper)
+        eng.set_window(tau)
+        ls, _ = eng.linear_search(m0s, w.granularity, "tuned")
+        prior = np.ascontiguousarray(ls[:, 2:3, :])
+        eng.stretch_free(m0s, prior)
+        got, st = eng.stretch_free(m0s, prior)
+    rk = ref_runner.ReferenceKernels()
+    ref_ms, evals, same = 0.0, 0.0, []
+    for i, m0 in enumerate(m0s):
+        sel = np.nonzero(line.midpoints == m0)[0]
+        res, ms = rk.stretch_free_midpoint_cmp(line.samples, line.halfoffsets, sel,
+                                               float(line.dt), tau, prior[i, 0], timing=True)
+        ref_ms += ms
+        evals += float(sel.size) * S * 21
+        same.append(np.array_equal(res, got[i]))
+    print(json.dumps({"workload": "cmp-production stretch-free (21 n)", "midpoints": int(n_mid),
+                      "reference": {"ms": ref_ms, "value": evals / (ref_ms / 1e3)},
+                      "engine": {"ms": st["kernel_ms"], "value": evals / (st["kernel_ms"] / 1e3)},
+                      "identical_to_reference": bool(all(same)),
+                      "speedup_engine_vs_reference": ref_ms / st["kernel_ms"]}))
+
+
 if __name__ == "__main__":
     mode = sys.argv[1] if len(sys.argv) > 1 else "ls"
-    n = int(sys.argv[2]) if len(sys.argv) > 2 else (20 if mode == "ls" else 2)
+    n = int(sys.argv[2]) if len(sys.argv) > 2 else {"ls": 20, "de": 2, "oct": 1, "sf": 20}[mode]
     if mode == "ls":
         time_ls(n)
     elif mode == "de":
         time_de(n)
+    elif mode == "oct":
+        time_oct(n)
+    elif mode == "sf":
+        time_sf(n)
     else:
         raise SystemExit(f"unknown mode {mode}")

@@ -117,11 +117,6 @@ def test_engine_matches_reference_kernels(engine, name, kernel):
         rms = float(np.sqrt(np.mean(z["samples"][sel] ** 2)))
         compare_block(rep, out[i], sem, stk, params, rms)
     rep.check()
-    if model in ("cmp", "zocrs"):
-        # traveltime arithmetic pinned to the reference's: bit-identical results
-        assert frac == 1.0, frac
-    else:
-        # OCT: the rounding order of the OCT formulas is not yet fully pinned
-        # (bit-identical on ~90% of samples; every sample within the parity
-        # tolerances checked above)
-        assert frac >= 0.85, frac
+    # traveltime arithmetic pinned to the reference's (CMP, ZO-CRS and the
+    # OCT displaced midpoint and time): bit-identical results
+    assert frac == 1.0, frac
