@@ -24,13 +24,15 @@ MODELS = {"cmp": 0, "zocrs": 1, "oct": 2}
 STORAGE = {"fp32": 0, "bf16": 1, "fp16": 2}
 KERNELS = {"plain": 0, "tuned": 1, "tuned_exact": 2}
 GRID_MODES = {"reference": 0, "inclusive": 1}
+PREC_FP64_TRAVELTIME, PREC_COMPENSATED = 1, 2
 N_PARAMS = {"cmp": 1, "zocrs": 3, "oct": 2}
 
 # Every symbol include/hpss.h declares.
 EXPORTED = [
     "hpss_create", "hpss_destroy", "hpss_last_error", "hpss_version",
     "hpss_device_count", "hpss_upload_gather", "hpss_set_traveltime",
-    "hpss_set_window", "hpss_set_grid_mode", "hpss_linear_search", "hpss_linear_search_device",
+    "hpss_set_window", "hpss_set_grid_mode", "hpss_set_precision", "hpss_linear_search",
+    "hpss_linear_search_device",
     "hpss_differential_evolution", "hpss_differential_evolution_device",
     "hpss_stretch_free", "hpss_select_traces", "hpss_stream", "hpss_device_bytes",
     "hpss_linear_search_noalloc",
@@ -70,6 +72,7 @@ def load_library(path: Optional[Path] = None) -> C.CDLL:
         "hpss_set_traveltime": (i32, [vp, i32, u32, fp, fp, f32, f32]),
         "hpss_set_window": (i32, [vp, i32]),
         "hpss_set_grid_mode": (i32, [vp, i32]),
+        "hpss_set_precision": (i32, [vp, i32]),
         "hpss_linear_search": (i32, [vp, fp, u32, up, i32, fp, C.POINTER(Stats)]),
         "hpss_linear_search_device": (i32, [vp, vp, u32, up, i32, vp, C.POINTER(Stats)]),
         "hpss_differential_evolution": (i32, [vp, fp, u32, u32, u32, f32, f32, C.c_uint64, fp,
@@ -174,6 +177,13 @@ class Engine:
 
     def set_window(self, tau_index: int):
         self._check(self._lib.hpss_set_window(self.h, int(tau_index)))
+
+    def set_precision(self, fp64_traveltime: bool = False, compensated: bool = False):
+        """Precision modes of the linear search (plain kernel): FP64
+        traveltime (ZO-CRS / OCT) and compensated window sums."""
+        flags = (PREC_FP64_TRAVELTIME if fp64_traveltime else 0) | \
+            (PREC_COMPENSATED if compensated else 0)
+        self._check(self._lib.hpss_set_precision(self.h, flags))
 
     def set_grid_mode(self, mode: str):
         """'reference' (uniform in v, upper bound excluded) or 'inclusive'

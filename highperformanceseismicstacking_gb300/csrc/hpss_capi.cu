@@ -349,9 +349,11 @@ hpss_status linear_search_impl(hpss_handle h, const float *d_m0s, uint32_t nM0,
     // kTunedVariants shapes (candidate pairs per thread x CTAs per SM), OCT the
     // branchy kernel (4 candidates per thread).  The chunk bounds depend on
     // the chunk size (8 warps x candidates per thread).
-    const bool pairKernel = tuned && h->model != HPSS_MODEL_OCT &&
+    // precision modes run on the plain kernel
+    const bool pairKernel = tuned && h->precisionMode == 0 && h->model != HPSS_MODEL_OCT &&
                             lp.w <= 15 && h->stride + 8 <= (uint32_t)tuned_stage_floats_min();
-    const bool octKernel = tuned && h->model == HPSS_MODEL_OCT && lp.w <= 15;
+    const bool octKernel =
+        tuned && h->precisionMode == 0 && h->model == HPSS_MODEL_OCT && lp.w <= 15;
     auto setChunks = [&](int perThread) -> cudaError_t {
         lp.chunkSize = kTunedWarps * perThread;
         lp.nChunks = (lp.P + lp.chunkSize - 1) / lp.chunkSize;
@@ -408,7 +410,7 @@ hpss_status linear_search_impl(hpss_handle h, const float *d_m0s, uint32_t nM0,
         HPSS_CUDA_TRY(h, launch_ls_oct(lp, (uint32_t)num_sms(h), h->octPartial.p, octParts,
                                        h->stream));
     } else {
-        HPSS_CUDA_TRY(h, launch_ls_plain(lp, h->stream));
+        HPSS_CUDA_TRY(h, launch_ls_plain(lp, h->stream, h->precisionMode));
     }
     h->lastVariant = pairKernel ? variant : -1;
     HPSS_CUDA_TRY(h, cudaEventRecord(h->ev2, h->stream));
@@ -732,6 +734,15 @@ hpss_status hpss_set_traveltime(hpss_handle h, int model, uint32_t nParams,
     h->apm = apm;
     h->h0 = model == HPSS_MODEL_OCT ? h0 : 0.f;
     h->octCandsHost.clear();
+    return HPSS_OK;
+}
+
+hpss_status hpss_set_precision(hpss_handle h, int flags) {
+    if (!h) return HPSS_ERR_INVALID_ARGUMENT;
+    if (flags & ~(HPSS_PREC_FP64_TRAVELTIME | HPSS_PREC_COMPENSATED))
+        return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "unknown precision flags");
+    h->precisionMode = (flags & HPSS_PREC_FP64_TRAVELTIME ? kPrecTt64 : 0) |
+                       (flags & HPSS_PREC_COMPENSATED ? kPrecCompensated : 0);
     return HPSS_OK;
 }
 

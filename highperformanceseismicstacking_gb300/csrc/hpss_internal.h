@@ -29,6 +29,10 @@ constexpr int kPlainThreads = 128;
 constexpr int kGridReference = 0;
 constexpr int kGridInclusive = 1;
 
+// Precision modes of the linear search (HPSS_PREC_* of hpss.h).
+constexpr int kPrecTt64 = 1;
+constexpr int kPrecCompensated = 2;
+
 // Near-tie tolerance (HPSS_NEAR_TIE_REL of hpss.h).
 constexpr float kNearTieRel = 1e-4f;
 
@@ -111,6 +115,7 @@ struct Handle {
     float apm = 0, h0 = 0;
     int tau = -1;
     int gridMode = kGridReference;
+    int precisionMode = 0;
     // scratch (grown on demand, owned by the handle)
     void *scratch = nullptr;
     size_t scratchBytes = 0;
@@ -125,7 +130,8 @@ cudaError_t launch_build_grid(int model, int mode, const float *lower, const flo
                               uint32_t P, cudaStream_t st);
 cudaError_t launch_chunk_bounds(const LsParams &p, float *bounds,
                                 cudaStream_t st);
-cudaError_t launch_ls_plain(const LsParams &p, cudaStream_t st);
+// precisionMode: kPrecTt64 | kPrecCompensated (0: the reference's FP32 arithmetic)
+cudaError_t launch_ls_plain(const LsParams &p, cudaStream_t st, int precisionMode = 0);
 // Tuned pair kernel (CMP / ZO-CRS) shapes, `variant`: 0 = 2 candidate pairs
 // per thread, 2 CTAs/SM; 1 = 1 pair, 3 CTAs/SM; 2 = 2 pairs, 3 CTAs/SM
 // (chunk = 8 warps x 2*pairs candidates).  exactStack selects the

@@ -15,7 +15,77 @@
 
 namespace hpss {
 
-template <int MODEL>
+// ---- precision modes (no reference counterpart; plain kernel only) -------
+//
+// kPrecTt64: the ZO-CRS / OCT traveltime is formed in FP64 from the FP32
+//   inputs (square-root arguments, divisions, the displaced midpoint) and
+//   rounded to FP32 once; the window arithmetic stays FP32.
+// kPrecCompensated: when window x selected traces exceeds 4096 terms, the
+//   window sums (numerator per tap, linear sum, denominator) are accumulated
+//   with Neumaier's compensated summation (Neumaier 1974, the improved
+//   Kahan-Babuska sum): sum + compensation, the compensation added once at
+//   the end.
+
+// ZO-CRS time with an FP64 squared time; 0: window skipped (negative square).
+__device__ __forceinline__ int zocrs_time_f64(float t0, float c, float a, float b, float dm,
+                                              float h, float *t) {
+    const double x = (double)t0 + (double)a * (double)dm;
+    const double tmp = x * x + (double)b * (double)dm * (double)dm + (double)c * (double)h * (double)h;
+    if (tmp < 0) return 0;
+    *t = (float)sqrt(tmp);
+    return 1;
+}
+
+// OCT displaced midpoint and time in FP64 (same formulas as
+// oct/common.cuh:7-94); returns as model_time<kModelOct>.
+__device__ __forceinline__ int oct_time_f64(float t0f, float cf, float slopef, float mf, float hf,
+                                            float m0f, float apm, float h0f, float *t) {
+    const double t0 = t0f, c = cf, slope = slopef, m = mf, h = hf, m0 = m0f, h0 = h0f;
+    const double theta = t0 * slope;
+    const double gamma = 2 * sqrt(h * h + h0 * h0);
+    const double tn0_sq = t0 * t0 - c * h0 * h0;
+    const double theta_sq = theta * theta, gamma_sq = gamma * gamma, tn0_quad = tn0_sq * tn0_sq;
+    double arg = tn0_quad * tn0_quad + tn0_quad * theta_sq * gamma_sq +
+                 16 * h * h * h0 * h0 * theta_sq * theta_sq;
+    if (arg < 0) return -1;
+    arg = theta_sq * gamma_sq + 2 * tn0_quad + 2 * sqrt(arg);
+    if (arg == 0) return -1;
+    const double mh = m0 + 2 * theta * (h * h - h0 * h0) / sqrt(arg);
+    if (fabs(m - mh) > (double)apm) return -1;
+    const double w1 = (h + h0) * (h + h0) - (mh - m0) * (mh - m0);
+    const double w2 = (h - h0) * (h - h0) - (mh - m0) * (mh - m0);
+    if (w1 < 0 || w2 < 0) return 0;
+    const double u = sqrt(w1) + sqrt(w2);
+    double th = t0;
+    if (fabs(h) > fabs(h0)) {
+        if (!u) return 0;
+        const double sa = c * h * h + 4 * h * h / (u * u) * tn0_sq;
+        if (sa < 0) return 0;
+        th = sqrt(sa);
+    } else if (fabs(h) < fabs(h0)) {
+        if (!h0) return 0;
+        const double sa = c * h * h + u * u / (4 * h0 * h0) * tn0_sq;
+        if (sa < 0) return 0;
+        th = sqrt(sa);
+    }
+    const double tn_sq = th * th - c * h * h;
+    if (!th || !tn0_sq) return 0;
+    const double ah = (t0 * tn_sq) / (th * tn0_sq) * slope;
+    *t = (float)(th + ah * (m - mh));
+    return 1;
+}
+
+// Neumaier step: s + x with the rounding error of the add kept in comp.
+__device__ __forceinline__ void neumaier(float &s, float &comp, float x) {
+    const float t = __fadd_rn(s, x);
+    comp = __fadd_rn(comp, fabsf(s) >= fabsf(x) ? __fadd_rn(__fsub_rn(s, t), x)
+                                                : __fadd_rn(__fsub_rn(x, t), s));
+    s = t;
+}
+
+constexpr int kCompensateAbove = 4096;  // window x traces terms
+
+template <int MODEL, int MODE>
 __global__ void __launch_bounds__(kPlainThreads)
 ls_plain_kernel(LsParams a) {
     const uint32_t mi = blockIdx.x / a.S;
@@ -47,11 +117,24 @@ ls_plain_kernel(LsParams a) {
         float lin = 0.f, den = 0.f;
         unsigned used = 0, nu = 0;
         for (int j = 0; j < a.w; j++) num[j] = 0.f;
+        // compensated sums (MODE & kPrecCompensated, large windows x traces)
+        constexpr bool kMayComp = (MODE & kPrecCompensated) != 0;
+        const bool comp = kMayComp && (uint64_t)a.w * cnt > (uint64_t)kCompensateAbove;
+        float numc[kMayComp ? kMaxWindow + 1 : 1];
+        float linc = 0.f, denc = 0.f;
+        if (kMayComp)
+            for (int j = 0; j < a.w; j++) numc[j] = 0.f;
         for (uint32_t q = 0; q < cnt; q++) {
             const uint32_t ti = a.selIdx ? a.selIdx[first + q] : first + q;
             float t;
-            int ok = model_time<MODEL>(t0, c, p1, p2, a.mid[ti], a.hoff[ti],
-                                       a.hsq[ti], m0, a.apm, a.h0, &t);
+            int ok;
+            if ((MODE & kPrecTt64) && MODEL == kModelZocrs)
+                ok = zocrs_time_f64(t0, c, p1, p2, a.mid[ti] - m0, a.hoff[ti], &t);
+            else if ((MODE & kPrecTt64) && MODEL == kModelOct)
+                ok = oct_time_f64(t0, c, p1, a.mid[ti], a.hoff[ti], m0, a.apm, a.h0, &t);
+            else
+                ok = model_time<MODEL>(t0, c, p1, p2, a.mid[ti], a.hoff[ti], a.hsq[ti], m0,
+                                       a.apm, a.h0, &t);
             if (ok < 0) {
                 nu++;
                 continue;
@@ -66,12 +149,23 @@ ls_plain_kernel(LsParams a) {
                     float y0 = y1;
                     y1 = tr[k + 1];
                     float u = (y1 - y0) * wi.frac + y0;
-                    num[j] += u;
-                    lin += u;
-                    den += u * u;
+                    if (kMayComp && comp) {
+                        neumaier(num[j], numc[j], u);
+                        neumaier(lin, linc, u);
+                        neumaier(den, denc, __fmul_rn(u, u));
+                    } else {
+                        num[j] += u;
+                        lin += u;
+                        den += u * u;
+                    }
                 }
                 used++;
             }
+        }
+        if (kMayComp && comp) {
+            for (int j = 0; j < a.w; j++) num[j] = __fadd_rn(num[j], numc[j]);
+            lin = __fadd_rn(lin, linc);
+            den = __fadd_rn(den, denc);
         }
         float sembl, stack;
         reduce_semblance(num, lin, den, a.w, used, &sembl, &stack);
@@ -129,19 +223,34 @@ ls_plain_kernel(LsParams a) {
     }
 }
 
-cudaError_t launch_ls_plain(const LsParams &p, cudaStream_t st) {
+template <int MODEL>
+void launch_plain_mode(const LsParams &p, unsigned blocks, int mode, cudaStream_t st) {
+    switch (mode & (kPrecTt64 | kPrecCompensated)) {
+        case 0: ls_plain_kernel<MODEL, 0><<<blocks, kPlainThreads, 0, st>>>(p); break;
+        case kPrecTt64: ls_plain_kernel<MODEL, kPrecTt64><<<blocks, kPlainThreads, 0, st>>>(p); break;
+        case kPrecCompensated:
+            ls_plain_kernel<MODEL, kPrecCompensated><<<blocks, kPlainThreads, 0, st>>>(p);
+            break;
+        default:
+            ls_plain_kernel<MODEL, kPrecTt64 | kPrecCompensated>
+                <<<blocks, kPlainThreads, 0, st>>>(p);
+            break;
+    }
+}
+
+cudaError_t launch_ls_plain(const LsParams &p, cudaStream_t st, int precisionMode) {
     if (p.nM0 == 0 || p.S == 0) return cudaSuccess;
     const uint64_t blocks = (uint64_t)p.nM0 * p.S;
     if (blocks > 0x7fffffffull) return cudaErrorInvalidConfiguration;
     switch (p.np == 1 ? kModelCmp : (p.np == 3 ? kModelZocrs : kModelOct)) {
         case kModelCmp:
-            ls_plain_kernel<kModelCmp><<<(unsigned)blocks, kPlainThreads, 0, st>>>(p);
+            launch_plain_mode<kModelCmp>(p, (unsigned)blocks, precisionMode, st);
             break;
         case kModelZocrs:
-            ls_plain_kernel<kModelZocrs><<<(unsigned)blocks, kPlainThreads, 0, st>>>(p);
+            launch_plain_mode<kModelZocrs>(p, (unsigned)blocks, precisionMode, st);
             break;
         default:
-            ls_plain_kernel<kModelOct><<<(unsigned)blocks, kPlainThreads, 0, st>>>(p);
+            launch_plain_mode<kModelOct>(p, (unsigned)blocks, precisionMode, st);
             break;
     }
     return cudaGetLastError();

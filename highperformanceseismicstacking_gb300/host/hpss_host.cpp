@@ -318,6 +318,7 @@ void ComputeAlgorithm::setUp() {
                                                                   : 1e-3f,
                                 storage));
     check(h, hpss_set_grid_mode(h, gridMode));
+    check(h, hpss_set_precision(h, precisionFlags));
     const unsigned np = traveltime->getNumberOfParameters();
     std::vector<float> lo(np), hi(np);
     for (unsigned j = 0; j < np; j++) {
@@ -501,6 +502,7 @@ LinearSearchAlgorithm *Gb300ComputeAlgorithmBuilder::buildLinearSearchAlgorithm(
     auto *alg = new LinearSearchAlgorithm(tt, ctx, threadCount, g, opts.kernel);
     alg->setEngineStorage(opts.storage);
     alg->setEngineGridMode(opts.gridMode);
+    alg->setEnginePrecision(opts.precisionFlags);
     return alg;
 }
 
@@ -612,6 +614,10 @@ Parser::Parser() {
     add("kernel", "Engine kernel: tuned (default), tuned-exact or plain.", false, false, "tuned");
     add("precision", "Amplitude storage on the device: fp32 (default), bf16 or fp16.", false,
         false, "fp32");
+    add("fp64-traveltime", "Linear search: ZO-CRS / OCT traveltime in FP64 (plain kernel).",
+        false, false, "", true);
+    add("compensated-sums", "Linear search: compensated window sums above 4096 terms "
+        "(plain kernel).", false, false, "", true);
     add("grid-mode", "Linear-search grid: reference (default; uniform in v, upper bound "
         "excluded) or inclusive (both bounds, velocity uniform in 4/v^2).", false, false,
         "reference");
@@ -739,6 +745,8 @@ EngineOptions Parser::engineOptions() const {
         else if (p == "fp16") o.storage = HPSS_STORAGE_FP16;
         else throw std::invalid_argument("--precision must be fp32, bf16 or fp16");
     }
+    if (has("fp64-traveltime")) o.precisionFlags |= HPSS_PREC_FP64_TRAVELTIME;
+    if (has("compensated-sums")) o.precisionFlags |= HPSS_PREC_COMPENSATED;
     if (has("grid-mode")) {
         std::string gm = str("grid-mode");
         if (gm == "reference") o.gridMode = HPSS_GRID_REFERENCE;

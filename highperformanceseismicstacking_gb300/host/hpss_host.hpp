@@ -369,6 +369,7 @@ class ComputeAlgorithm {
     // (HPSS_STORAGE_*) and linear-search grid (HPSS_GRID_*), applied by setUp
     void setEngineStorage(int s) { storage = s; }
     void setEngineGridMode(int m) { gridMode = m; }
+    void setEnginePrecision(int flags) { precisionFlags = flags; }
 
   protected:
     void fillStats(const std::vector<float> &m0s, const hpss_stats &st, double perCandidateFactor,
@@ -382,6 +383,7 @@ class ComputeAlgorithm {
     std::unordered_map<int, float> computedStatisticalResults;
     int storage = HPSS_STORAGE_FP32;
     int gridMode = HPSS_GRID_REFERENCE;
+    int precisionFlags = 0;
 };
 
 class LinearSearchAlgorithm : public ComputeAlgorithm {
@@ -452,6 +454,7 @@ struct EngineOptions {
     int kernel = HPSS_KERNEL_TUNED;
     int storage = HPSS_STORAGE_FP32;
     int gridMode = HPSS_GRID_REFERENCE;
+    int precisionFlags = 0;
     uint64_t seed = 0;
     bool seedGiven = false;
     float deF = 0.85f, deCR = 0.5f;

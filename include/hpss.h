@@ -151,6 +151,18 @@ hpss_status hpss_set_traveltime(hpss_handle h, int model, uint32_t nParams,
 #define HPSS_GRID_INCLUSIVE 1
 hpss_status hpss_set_grid_mode(hpss_handle h, int mode);
 
+/* Precision modes of the linear search (no reference counterpart; the
+ * default 0 is the reference's FP32 arithmetic).  FP64_TRAVELTIME forms the
+ * ZO-CRS / OCT traveltime in FP64 (square-root arguments, divisions, the
+ * displaced midpoint) and rounds it to FP32 once; COMPENSATED accumulates
+ * the window sums with Neumaier's compensated summation when window x
+ * selected traces exceeds 4096 terms.  Either flag runs the plain kernel
+ * family (the tuned kernels implement the reference's arithmetic only).
+ * Interpolation stays FP32. */
+#define HPSS_PREC_FP64_TRAVELTIME 1
+#define HPSS_PREC_COMPENSATED 2
+hpss_status hpss_set_precision(hpss_handle h, int flags);
+
 /* Semblance window: tauIndexDisplacement = (int)(tau / dt), window
  * w = 2 * tau + 1 (Gather.cpp:75-76).  w must be <= 31
  * (MAX_WINDOW_SIZE, common/include/gpu/interface.h:10). */
