@@ -33,8 +33,10 @@ struct PartBest {
     uint32_t p;
 };
 
+// Four resident CTAs per SM (64 registers, no spills): the kernel waits on
+// dependent square-root / reciprocal chains, so resident warps pay.
 template <int W, int R>
-__global__ void __launch_bounds__(kOctWarps * 32)
+__global__ void __launch_bounds__(kOctWarps * 32, 4)
 ls_oct_kernel(LsParams a, uint32_t tiles, uint32_t parts, uint32_t chunksPerPart,
               uint32_t nUnits, PartBest *partial) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
