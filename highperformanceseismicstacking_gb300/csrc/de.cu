@@ -150,8 +150,12 @@ __device__ __forceinline__ void de_eval(const DeParams &d, float t0, float m0, u
 // group) units.
 constexpr int kDeThreads = 256;
 
+// OCT: six resident CTAs per SM (40 registers) -- its evaluation waits on
+// long dependent square-root / reciprocal chains, so resident warps pay
+// (3.5 % on the OCT DE workload); CMP / ZO-CRS keep their registers (a
+// 6-CTA bound costs them 10 %).
 template <int MODEL, int W>
-__global__ void __launch_bounds__(kDeThreads)
+__global__ void __launch_bounds__(kDeThreads, MODEL == kModelOct ? 6 : 1)
 de_kernel(DeParams d, uint32_t spc, uint32_t groups, uint32_t nUnits) {
     constexpr int NP = MODEL == kModelCmp ? 1 : (MODEL == kModelZocrs ? 3 : 2);
     const LsParams &a = d.ls;
