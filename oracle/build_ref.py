@@ -11,6 +11,7 @@ Only the .cu files of the hot path are compiled; the reference's host code
 """
 from __future__ import annotations
 
+import concurrent.futures as cf
 import os
 import subprocess
 import sys
@@ -55,20 +56,15 @@ def build(ref_root: str = "/root/reference") -> list:
     nvcc = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
     base = [nvcc, "-fatbin", "-O3", "--use_fast_math",
             "-gencode=arch=compute_103a,code=sm_103a", "-I" + str(ref)]
-    built = []
-    for rel in KERNELS:
-        src = ref / rel
-        out = OUT / fatbin_name(rel)
-        if not out.exists() or out.stat().st_mtime < src.stat().st_mtime:
-            subprocess.run(base + ["-o", str(out), str(src)], check=True)
-        built.append(out)
-    for shim, name in SHIMS.items():
-        src = HERE / shim
-        out = OUT / name
-        if not out.exists() or out.stat().st_mtime < src.stat().st_mtime:
-            subprocess.run(base + ["-o", str(out), str(src)], check=True)
-        built.append(out)
-    return built
+    jobs = [(ref / rel, OUT / fatbin_name(rel)) for rel in KERNELS]
+    jobs += [(HERE / shim, OUT / name) for shim, name in SHIMS.items()]
+    todo = [(src, out) for src, out in jobs
+            if not out.exists() or out.stat().st_mtime < src.stat().st_mtime]
+    with cf.ThreadPoolExecutor(max_workers=max(1, min(8, os.cpu_count() or 1))) as ex:
+        for f in [ex.submit(subprocess.run, base + ["-o", str(out), str(src)], check=True)
+                  for src, out in todo]:
+            f.result()
+    return [out for _, out in jobs]
 
 
 if __name__ == "__main__":
