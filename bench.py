@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--de-cmps", type=int, default=2,
                     help="midpoints of the DE side measurement (0: skip)")
+    ap.add_argument("--per-midpoint-calls", type=int, default=64,
+                    help="one-midpoint calls timed beside the batched call (0: skip)")
     ap.add_argument("--no-storage-side", action="store_true",
                     help="skip the BF16 / FP16 storage side measurement")
     ap.add_argument("--zocrs-cmps", type=int, default=32,
@@ -277,6 +279,39 @@ def storage_side(eng, line, stream, d_m0, n_m0, gran, evals, fp32_out, reps=1):
     return out
 
 
+def per_midpoint_side(eng, stream, d_m0, gran, S, counts, P, batched_out, n_calls):
+    """One midpoint per call, as the reference's ComputeAlgorithm interface
+    computes them (computeSemblanceAndParametersForMidpoint,
+    common/include/semblance/algorithm/ComputeAlgorithm.hpp:29-100): n_calls
+    consecutive device calls of one midpoint each, tuned (its candidates split
+    into ranges so that one midpoint fills the GPU) and plain; evals/s over
+    the calls and whether the tuned blocks equal the batched call's."""
+    import torch
+    n = min(n_calls, d_m0.numel())
+    d_out = torch.empty((n, 2 + eng.np, S), dtype=torch.float32, device=d_m0.device)
+    evals = float(np.sum(np.asarray(counts[:n], np.float64))) * S * P
+    res = {"calls": n}
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for kernel in ("tuned", "plain"):
+        st = eng.linear_search_device(d_m0.data_ptr(), 1, gran, d_out.data_ptr(), kernel,
+                                      stats=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for i in range(n):
+            eng.linear_search_device(d_m0.data_ptr() + 4 * i, 1, gran, d_out[i].data_ptr(),
+                                     kernel)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        res[kernel] = {"value": evals / (ms / 1e3), "ms_per_call": ms / n}
+        if kernel == "tuned":
+            res[kernel]["candidate_parts"] = int(st["candidate_parts"])
+            res[kernel]["identical_to_batched"] = bool(
+                np.array_equal(d_out.cpu().numpy(), batched_out[:n]))
+    res["speedup_tuned_vs_plain"] = res["tuned"]["value"] / res["plain"]["value"]
+    return res
+
+
 # ----------------------------------------------------------------- reference arm
 
 def run_reference(args, world, rank):
@@ -458,6 +493,12 @@ def main():
     exact_ms = e0.elapsed_time(e1) / args.plain_steps
     exact_same = bool(np.array_equal(d_out.cpu().numpy(), plain_out))
 
+    # ---- one midpoint per call (the reference's per-midpoint interface)
+    per_mid = None
+    if args.per_midpoint_calls > 0:
+        per_mid = per_midpoint_side(eng, stream, d_m0, w.granularity, S, counts, P, tuned_out,
+                                    args.per_midpoint_calls)
+
     # ---- 16-bit amplitude storage (tuned kernel), same line
     storage = None
     if not args.no_storage_side:
@@ -552,6 +593,7 @@ def main():
                      "speedup_tuned_vs_plain": value / plain_value,
                      "tuned_vs_plain": agreement},
            "storage_modes": storage,
+           "per_midpoint_calls": per_mid,
            "near_ties": {"samples": near_ties, "of": int(len(m0s)) * S,
                          "rel_tolerance": 1e-4},
            "tuned_exact": {"value": evals / (exact_ms / 1e3), "ms_per_step": exact_ms,

@@ -43,7 +43,8 @@ class Stats(C.Structure):
     _fields_ = [("evals", C.c_double), ("not_used", C.c_double),
                 ("selected_traces", C.c_double), ("kernel_ms", C.c_double),
                 ("selection_ms", C.c_double), ("device_error", C.c_uint32),
-                ("kernel_variant", C.c_int32), ("near_ties", C.c_double)]
+                ("kernel_variant", C.c_int32), ("near_ties", C.c_double),
+                ("candidate_parts", C.c_uint32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -40,7 +40,9 @@ struct hpss_handle_s : public Handle {
         size_t bytes = 0;
     };
     Buf params, chunkBounds, selFirst, selCount, selIdx, candFirst, candCount,
-        notUsed, errWord, m0s, out, octCands, prior, octPartial;
+        notUsed, errWord, m0s, out, octCands, prior, partial;
+    std::string gridKey;       // grid held in `params` (empty: none)
+    uint32_t boundsChunk = 0;  // chunk size of the bounds in `chunkBounds` (0: none)
     std::vector<float> octCandsHost;
     std::map<std::string, int> variantCache;  // autotuner decisions
     int lastVariant = -1;
@@ -241,8 +243,21 @@ constexpr int kTunedVariants = 3;
 constexpr int kVariantPairs[kTunedVariants] = {2, 1, 2};
 constexpr int kVariantCtasPerSm[kTunedVariants] = {2, 3, 3};
 
-// Autotuner: the first time a (model, window, candidates, samples, fold) key
-// is seen, every variant is timed on a prefix of the work units (results are
+// Candidate parts of the pair kernel: a call whose `base` (midpoint, tile)
+// units fill fewer than four waves of the resident CTAs is split into
+// candidate ranges, at most one per chunk.
+uint32_t pair_parts(uint64_t base, uint32_t nChunks, int numSms, int ctasPerSm) {
+    const uint64_t want = (uint64_t)numSms * (uint64_t)ctasPerSm * 4;
+    if (base == 0 || base >= want) return 1;
+    const uint64_t parts = std::min<uint64_t>((want + base - 1) / base, nChunks);
+    if (parts <= 1) return 1;
+    // equal ranges, none empty
+    const uint32_t per = (uint32_t)((nChunks + parts - 1) / parts);
+    return (nChunks + per - 1) / per;
+}
+
+// Autotuner: the first time a (model, window, candidates, samples, fold,
+// candidate split) key is seen, every variant is timed on a prefix of the work units (results are
 // overwritten by the real launch) and the fastest is cached in the handle.
 // HPSS_LS_VARIANT=<n> forces a variant.
 template <typename SetChunks, typename Launch>
@@ -255,10 +270,16 @@ hpss_status choose_variant(hpss_handle h, const LsParams &lp, uint32_t units, bo
             return HPSS_OK;
         }
     }
+    // calls split into candidate ranges (few midpoints) have their own entry:
+    // the best shape differs from that of a call that fills the GPU by itself
+    const uint32_t split =
+        pair_parts(units, (lp.P + 2 * kTunedWarps * kVariantPairs[0] - 1) /
+                              (2 * kTunedWarps * kVariantPairs[0]),
+                   num_sms(h), kVariantCtasPerSm[0]);
     const std::string key = std::to_string(h->model) + "/" + std::to_string(exactStack) + "/" +
                             std::to_string(lp.w) + "/" +
                             std::to_string(lp.P) + "/" + std::to_string(lp.S) + "/" +
-                            std::to_string(h->meanFold);
+                            std::to_string(h->meanFold) + "/" + std::to_string(split);
     auto it = h->variantCache.find(key);
     if (it != h->variantCache.end()) {
         *out = it->second;
@@ -339,10 +360,30 @@ hpss_status linear_search_impl(hpss_handle h, const float *d_m0s, uint32_t nM0,
     lp.P = (uint32_t)P;
     lp.out = d_out;
 
-    HPSS_CUDA_TRY(h, ensure(h, h->params, P * h->np * sizeof(float)));
+    // The candidate grid (and below the chunk bounds) depend only on the
+    // model, the bounds, the granularity and the grid mode: a call that
+    // repeats the previous call's grid (one midpoint per call) reuses them
+    // from the handle's buffers instead of rebuilding them.
+    std::string gridKey = std::to_string(h->model) + "/" + std::to_string(h->gridMode) + "/" +
+                          std::to_string(h->np) + "/" + std::to_string(P);
+    for (uint32_t j = 0; j < h->np; j++) {
+        uint32_t bits[3];
+        std::memcpy(&bits[0], &low[j], 4);
+        std::memcpy(&bits[1], &inc[j], 4);
+        std::memcpy(&bits[2], &last[j], 4);
+        for (uint32_t b : bits) gridKey += "/" + std::to_string(b);
+        gridKey += "/" + std::to_string(gran[j]);
+    }
+    if (h->gridKey != gridKey) {
+        h->gridKey.clear();
+        h->boundsChunk = 0;
+        HPSS_CUDA_TRY(h, ensure(h, h->params, P * h->np * sizeof(float)));
+        HPSS_CUDA_TRY(h, launch_build_grid(h->model, h->gridMode, low, inc, last, gran,
+                                           static_cast<float *>(h->params.p), (uint32_t)P,
+                                           h->stream));
+        h->gridKey = gridKey;
+    }
     lp.params = static_cast<float *>(h->params.p);
-    HPSS_CUDA_TRY(h, launch_build_grid(h->model, h->gridMode, low, inc, last, gran,
-                                       static_cast<float *>(h->params.p), lp.P, h->stream));
     // candidates per thread of the tuned kernel: 2 * pairs (CMP / ZO-CRS),
     // 4 (OCT); HPSS_LS_PAIRS overrides the pair count (1, 2 or 4)
     // Tuned kernel: CMP / ZO-CRS run the branch-free pair kernel in one of
@@ -354,46 +395,80 @@ hpss_status linear_search_impl(hpss_handle h, const float *d_m0s, uint32_t nM0,
                             lp.w <= 15 && h->stride + 8 <= (uint32_t)tuned_stage_floats_min();
     const bool octKernel =
         tuned && h->precisionMode == 0 && h->model == HPSS_MODEL_OCT && lp.w <= 15;
+    // chunk bounds (read by the pair kernel only), rebuilt when the chunk size
+    // or the grid changed
     auto setChunks = [&](int perThread) -> cudaError_t {
         lp.chunkSize = kTunedWarps * perThread;
         lp.nChunks = (lp.P + lp.chunkSize - 1) / lp.chunkSize;
-        cudaError_t e = ensure(h, h->chunkBounds, (size_t)lp.nChunks * 2 * h->np * sizeof(float));
-        if (e != cudaSuccess) return e;
+        if (h->boundsChunk != lp.chunkSize) {
+            h->boundsChunk = 0;
+            cudaError_t e =
+                ensure(h, h->chunkBounds, (size_t)lp.nChunks * 2 * h->np * sizeof(float));
+            if (e != cudaSuccess) return e;
+            e = launch_chunk_bounds(lp, static_cast<float *>(h->chunkBounds.p), h->stream);
+            if (e != cudaSuccess) return e;
+            h->boundsChunk = lp.chunkSize;
+        }
         lp.chunkBounds = static_cast<float *>(h->chunkBounds.p);
-        return launch_chunk_bounds(lp, static_cast<float *>(h->chunkBounds.p), h->stream);
+        return cudaSuccess;
     };
-    HPSS_CUDA_TRY(h, setChunks(4));
-    HPSS_CUDA_TRY(h, ensure(h, h->notUsed, nM0 * sizeof(unsigned long long)));
-    // error word at byte 0, near-tie counter at byte 8
-    HPSS_CUDA_TRY(h, ensure(h, h->errWord, 16));
-    lp.notUsed = static_cast<unsigned long long *>(h->notUsed.p);
-    lp.errorWord = static_cast<uint32_t *>(h->errWord.p);
-    lp.nearTies = reinterpret_cast<unsigned long long *>(static_cast<char *>(h->errWord.p) + 8);
-    HPSS_CUDA_TRY(h, cudaMemsetAsync(lp.notUsed, 0, nM0 * sizeof(unsigned long long), h->stream));
-    HPSS_CUDA_TRY(h, cudaMemsetAsync(lp.errorWord, 0, 16, h->stream));
+    // counters, cleared by one memset: error word at byte 0, near-tie counter
+    // at byte 8, the per-midpoint notUsed counts from byte 16
+    HPSS_CUDA_TRY(h, ensure(h, h->notUsed, 16 + nM0 * sizeof(unsigned long long)));
+    char *counters = static_cast<char *>(h->notUsed.p);
+    lp.errorWord = reinterpret_cast<uint32_t *>(counters);
+    lp.nearTies = reinterpret_cast<unsigned long long *>(counters + 8);
+    lp.notUsed = reinterpret_cast<unsigned long long *>(counters + 16);
+    HPSS_CUDA_TRY(h, cudaMemsetAsync(counters, 0, 16 + nM0 * sizeof(unsigned long long),
+                                     h->stream));
 
+    const uint32_t tiles = (h->S + kTileSamples - 1) / kTileSamples;
+    const uint64_t units = (uint64_t)nM0 * tiles;
     uint32_t octParts = 1;
     if (octKernel) {
         // per-part best / runner-up of the OCT kernel
         octParts = oct_parts(lp, (uint32_t)num_sms(h));
-        HPSS_CUDA_TRY(h, ensure(h, h->octPartial, oct_partial_bytes(nM0, h->S, octParts)));
+        HPSS_CUDA_TRY(h, ensure(h, h->partial, oct_partial_bytes(nM0, h->S, octParts)));
+    } else if (pairKernel) {
+        // per-part best / runner-up of a split pair-kernel call, for the
+        // largest split of any shape (allocated before the timed region)
+        uint32_t maxParts = 1;
+        for (int v = 0; v < kTunedVariants; v++) {
+            const uint32_t chunk = kTunedWarps * 2 * kVariantPairs[v];
+            maxParts = std::max(maxParts, pair_parts(units, (lp.P + chunk - 1) / chunk,
+                                                     num_sms(h), kVariantCtasPerSm[v]));
+        }
+        if (maxParts > 1)
+            HPSS_CUDA_TRY(h, ensure(h, h->partial, (size_t)nM0 * maxParts * h->S * sizeof(PartBest)));
     }
 
     HPSS_CUDA_TRY(h, cudaEventRecord(h->ev0, h->stream));
     rc = run_selection(h, d_m0s, nM0, lp);
     if (rc != HPSS_OK) return rc;
     HPSS_CUDA_TRY(h, cudaEventRecord(h->ev1, h->stream));
-    const uint32_t tiles = (h->S + kTileSamples - 1) / kTileSamples;
-    const uint64_t units = (uint64_t)nM0 * tiles;
     if (units > 0xffffffffull)
         return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "too many (midpoint, tile) units");
-    auto launchPair = [&](int variant, uint32_t nUnits) -> cudaError_t {
+    // nBase (midpoint, tile) units, each split into the shape's candidate
+    // parts; a split launch of all units is followed by the ordered merge
+    uint32_t lastParts = 1;
+    auto launchPair = [&](int variant, uint32_t nBase) -> cudaError_t {
+        LsParams q = lp;
+        q.parts = pair_parts(units, lp.nChunks, num_sms(h), kVariantCtasPerSm[variant]);
+        q.chunksPerPart = (lp.nChunks + q.parts - 1) / q.parts;
+        q.partial = static_cast<PartBest *>(h->partial.p);
+        lastParts = q.parts;
+        const uint64_t nUnits = (uint64_t)nBase * q.parts;
+        if (nUnits > 0xffffffffull) return cudaErrorInvalidConfiguration;
         const uint32_t grid = (uint32_t)std::min<uint64_t>(
             nUnits, (uint64_t)num_sms(h) * kVariantCtasPerSm[variant]);
-        return h->model == HPSS_MODEL_CMP
-                   ? launch_ls_tuned_cmp(lp, grid, tiles, nUnits, h->stream, variant, exactStack)
-                   : launch_ls_tuned_zocrs(lp, grid, tiles, nUnits, h->stream, variant,
-                                           exactStack);
+        cudaError_t e =
+            h->model == HPSS_MODEL_CMP
+                ? launch_ls_tuned_cmp(q, grid, tiles, (uint32_t)nUnits, h->stream, variant,
+                                      exactStack)
+                : launch_ls_tuned_zocrs(q, grid, tiles, (uint32_t)nUnits, h->stream, variant,
+                                        exactStack);
+        if (e != cudaSuccess || q.parts == 1 || nBase != units) return e;
+        return launch_merge_parts(q, q.parts, q.partial, h->stream);
     };
     int variant = 0;
     if (pairKernel) {
@@ -407,7 +482,7 @@ hpss_status linear_search_impl(hpss_handle h, const float *d_m0s, uint32_t nM0,
     if (pairKernel) {
         HPSS_CUDA_TRY(h, launchPair(variant, (uint32_t)units));
     } else if (octKernel) {
-        HPSS_CUDA_TRY(h, launch_ls_oct(lp, (uint32_t)num_sms(h), h->octPartial.p, octParts,
+        HPSS_CUDA_TRY(h, launch_ls_oct(lp, (uint32_t)num_sms(h), h->partial.p, octParts,
                                        h->stream));
     } else {
         HPSS_CUDA_TRY(h, launch_ls_plain(lp, h->stream, h->precisionMode));
@@ -443,6 +518,7 @@ hpss_status linear_search_impl(hpss_handle h, const float *d_m0s, uint32_t nM0,
             stats->selection_ms = ms;
             stats->device_error = err;
             stats->kernel_variant = h->lastVariant;
+            stats->candidate_parts = pairKernel ? lastParts : octKernel ? octParts : 1;
         }
         if (err)
             return set_error(h, HPSS_ERR_DEVICE_CHECK,
@@ -614,7 +690,7 @@ hpss_status hpss_destroy(hpss_handle h) {
     free_gather(h);
     for (auto *b : {&h->params, &h->chunkBounds, &h->selFirst, &h->selCount, &h->selIdx,
                     &h->candFirst, &h->candCount, &h->notUsed, &h->errWord, &h->m0s,
-                    &h->out, &h->octCands, &h->prior, &h->octPartial})
+                    &h->out, &h->octCands, &h->prior, &h->partial})
         release(h, *b);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);

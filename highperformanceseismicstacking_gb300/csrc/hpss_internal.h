@@ -42,6 +42,12 @@ constexpr uint32_t kErrSpanOverflow = 1u << 1;
 constexpr uint32_t kErrTimeout = 1u << 2;
 
 // Everything a linear-search (or stretch-free) launch reads and writes.
+// Best / runner-up of one candidate range for one (midpoint, sample).
+struct PartBest {
+    float best, second, stack;
+    uint32_t p;
+};
+
 struct LsParams {
     // whole line, resident
     const float *samples;     // [nTraces][stride] FP32 (when storage = FP32)
@@ -80,6 +86,14 @@ struct LsParams {
     // stretch-free: prior parameters [nM0][np][S] (raw), n range
     const float *prior;
     int nmax;
+    // candidate split of the tuned pair kernel: the chunks are cut into
+    // `parts` contiguous ranges of chunksPerPart chunks; with parts > 1 every
+    // (midpoint, tile, part) unit writes its range's best / runner-up to
+    // `partial` ([nM0][parts][S]) and launch_merge_parts writes the result
+    // block.  parts = 1: one unit per (midpoint, tile), written directly.
+    uint32_t parts = 1;
+    uint32_t chunksPerPart = 0;
+    PartBest *partial = nullptr;
 };
 
 // Differential evolution launch (de.cu).
@@ -154,6 +168,10 @@ uint32_t oct_parts(const LsParams &p, uint32_t numSms);
 size_t oct_partial_bytes(uint32_t nM0, uint32_t S, uint32_t parts);
 cudaError_t launch_ls_oct(const LsParams &p, uint32_t numSms, void *partial, uint32_t parts,
                           cudaStream_t st);
+// Combine `parts` candidate ranges of every (midpoint, sample) in candidate
+// order and write the result block [nM0][2+np][S]; counts near-ties.
+cudaError_t launch_merge_parts(const LsParams &p, uint32_t parts, const PartBest *partial,
+                               cudaStream_t st);
 cudaError_t launch_select_oct(const LsParams &p, const float *cands,
                               uint32_t nCand, uint32_t *selIdx,
                               uint32_t *selCount, const uint32_t *candFirst,

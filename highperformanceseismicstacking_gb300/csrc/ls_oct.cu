@@ -28,11 +28,6 @@ namespace hpss {
 
 constexpr int kOctWarps = 8;
 
-struct PartBest {
-    float best, second, stack;
-    uint32_t p;
-};
-
 // Four resident CTAs per SM (64 registers, no spills): the kernel waits on
 // dependent square-root / reciprocal chains, so resident warps pay.
 template <int W, int R>
@@ -158,7 +153,7 @@ ls_oct_kernel(LsParams a, uint32_t tiles, uint32_t parts, uint32_t chunksPerPart
 }
 
 // Combine the parts of every (midpoint, sample) in candidate order; write the
-// result block and count near-ties.
+// result block and count near-ties (also used by the pair kernel's split).
 __global__ void merge_parts_kernel(LsParams a, uint32_t parts, const PartBest *partial) {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const bool live = i < (uint64_t)a.nM0 * a.S;
@@ -195,6 +190,14 @@ __global__ void merge_parts_kernel(LsParams a, uint32_t parts, const PartBest *p
         atomicAdd(a.nearTies, (unsigned long long)__popc(m));
 }
 
+cudaError_t launch_merge_parts(const LsParams &p, uint32_t parts, const PartBest *partial,
+                               cudaStream_t st) {
+    const uint64_t n = (uint64_t)p.nM0 * p.S;
+    if (n == 0) return cudaSuccess;
+    merge_parts_kernel<<<(uint32_t)((n + 255) / 256), 256, 0, st>>>(p, parts, partial);
+    return cudaGetLastError();
+}
+
 size_t oct_partial_bytes(uint32_t nM0, uint32_t S, uint32_t parts) {
     return (size_t)nM0 * parts * S * sizeof(PartBest);
 }
@@ -223,10 +226,7 @@ cudaError_t launch_oct_w(const LsParams &p, uint32_t numSms, void *partial, uint
         p, tiles, parts, chunksPerPart, (uint32_t)units, static_cast<PartBest *>(partial));
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    const uint64_t n = (uint64_t)p.nM0 * p.S;
-    merge_parts_kernel<<<(uint32_t)((n + 255) / 256), 256, 0, st>>>(
-        p, parts, static_cast<const PartBest *>(partial));
-    return cudaGetLastError();
+    return launch_merge_parts(p, parts, static_cast<const PartBest *>(partial), st);
 }
 
 // Parts: enough (midpoint, tile, part) units for ~8 waves of the GPU, never

@@ -16,7 +16,12 @@
 // stack too, except where the pair kernel derives the linear sum from the
 // per-tap sums, see EXACT_STACK below).  The argmax over candidates
 // is kept in registers and reduced across warps at the end (lowest index wins
-// ties).  CTAs are persistent over the work units.
+// ties).  CTAs are persistent over the work units.  A call with few
+// midpoints has too few (midpoint, tile) units to fill the GPU (one CMP
+// midpoint of 2000 samples: 63 units for 2-3 CTAs on each of 152 SMs); the
+// host then splits the candidate chunks into `parts` contiguous ranges, a unit
+// becomes (midpoint, tile, part), and the ordered merge of ls_oct.cu combines
+// the parts (lowest candidate index still wins ties).
 #pragma once
 
 #include <cuda_fp16.h>
@@ -168,8 +173,11 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
     if (threadIdx.x < kZeroPad) sm.y[threadIdx.x] = 0.f;
 
     for (uint32_t unit = blockIdx.x; unit < nUnits; unit += gridDim.x) {
-        const uint32_t mi = unit / tiles;
-        const int s0 = (int)(unit % tiles) * kTileSamples;
+        // unit = (midpoint, tile, candidate part), part fastest
+        const uint32_t part = unit % a.parts;
+        const uint32_t mt = unit / a.parts;
+        const uint32_t mi = mt / tiles;
+        const int s0 = (int)(mt % tiles) * kTileSamples;
         const int s = s0 + lane;
         const int sc = min(s, S - 1);
         const float t0 = static_cast<float>(sc) * a.dt;
@@ -182,7 +190,8 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
         float *out = a.out + (size_t)mi * (2 + np) * a.S;
 
         if (cnt == 0) {
-            if (warp < 2 + np && s < S) out[(size_t)warp * a.S + s] = 0.f;
+            // split calls: the merge writes the zero block
+            if (a.parts == 1 && warp < 2 + np && s < S) out[(size_t)warp * a.S + s] = 0.f;
             continue;
         }
 
@@ -190,7 +199,9 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
         uint32_t bestP = 0xffffffffu;
         float second = -1.f;  // runner-up semblance (near-tie count)
 
-        for (uint32_t chunk = 0; chunk < a.nChunks; chunk++) {
+        const uint32_t chunkEnd =
+            a.parts == 1 ? a.nChunks : min((part + 1) * a.chunksPerPart, a.nChunks);
+        for (uint32_t chunk = part * a.chunksPerPart; chunk < chunkEnd; chunk++) {
             float cc[R], c1[R], c2[R];
             bool valid[R];
 #pragma unroll
@@ -490,19 +501,31 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
                 if (better(os, op, best, bestP)) bestStack = sm.bestK[wv][lane];
                 top2_merge(os, op, sm.bestSec[wv][lane], best, bestP, second);
             }
-            if (a.nearTies) {
-                const unsigned tie = __ballot_sync(0xffffffffu, s < S && near_tie(best, second));
-                if (lane == 0 && tie) atomicAdd(a.nearTies, (unsigned long long)__popc(tie));
-            }
-            if (s < S) {
-                out[s] = best;
-                out[a.S + s] = bestStack;
-                if (bestP != 0xffffffffu) {
-                    const float *pr = a.params + (size_t)bestP * np;
-                    out[2 * a.S + s] = 2 / sqrtf(pr[0]);
-                    for (int j = 1; j < np; j++) out[(size_t)(2 + j) * a.S + s] = pr[j];
-                } else {
-                    for (int j = 0; j < np; j++) out[(size_t)(2 + j) * a.S + s] = 0.f;
+            if (a.parts > 1) {
+                // the merge combines the parts, writes the block and counts ties
+                if (s < S) {
+                    PartBest pb;
+                    pb.best = best;
+                    pb.second = second;
+                    pb.stack = bestStack;
+                    pb.p = bestP;
+                    a.partial[((size_t)mi * a.parts + part) * a.S + s] = pb;
+                }
+            } else {
+                if (a.nearTies) {
+                    const unsigned tie = __ballot_sync(0xffffffffu, s < S && near_tie(best, second));
+                    if (lane == 0 && tie) atomicAdd(a.nearTies, (unsigned long long)__popc(tie));
+                }
+                if (s < S) {
+                    out[s] = best;
+                    out[a.S + s] = bestStack;
+                    if (bestP != 0xffffffffu) {
+                        const float *pr = a.params + (size_t)bestP * np;
+                        out[2 * a.S + s] = 2 / sqrtf(pr[0]);
+                        for (int j = 1; j < np; j++) out[(size_t)(2 + j) * a.S + s] = pr[j];
+                    } else {
+                        for (int j = 0; j < np; j++) out[(size_t)(2 + j) * a.S + s] = 0.f;
+                    }
                 }
             }
         }

@@ -95,6 +95,10 @@ typedef struct {
                                  of it (the chosen index may differ from
                                  another FP32 evaluation's there); 0 for
                                  differential evolution and stretch-free */
+    uint32_t candidate_parts; /* tuned linear search: candidate ranges the
+                                 search of each (midpoint, 32-sample tile)
+                                 was split into so that a call with few
+                                 midpoints fills the GPU (1: no split) */
 } hpss_stats;
 
 #define HPSS_NEAR_TIE_REL 1e-4f

@@ -225,3 +225,82 @@ def test_inclusive_grid_zocrs(engine):
     _check_against_oracle("zocrs", line, m0s, plain, lower, upper, gran, tau, apm,
                           grid_mode="inclusive")
     assert engine._lib.hpss_set_grid_mode(engine.h, 7) == -1     # unknown mode
+
+
+@pytest.mark.parametrize("kernel", ["tuned", "tuned_exact"])
+def test_candidate_split_equals_unsplit(engine, kernel):
+    """A call with few midpoints splits the candidates of every (midpoint,
+    32-sample tile) into ranges merged in candidate order, so that it fills
+    the GPU; one-midpoint calls (the reference's per-midpoint interface) give
+    the unsplit batched call's blocks bit for bit, near-tie counts included."""
+    w = synthetic.WORKLOADS["cmp-production"]
+    line = w.make_line(n_cmp=72)
+    tau = 3
+    _setup(engine, line, "cmp", w.lower, w.upper, tau)
+    m0s = line.cdp_midpoints
+    batched, st_b = engine.linear_search(m0s, w.granularity, kernel)
+    assert st_b["candidate_parts"] == 1 and st_b["device_error"] == 0
+    picks = [0, 17, 40, 71]
+    ties = 0.0
+    for i in picks:
+        one, st = engine.linear_search(m0s[i:i + 1], w.granularity, kernel)
+        assert st["candidate_parts"] > 1 and st["device_error"] == 0
+        assert np.array_equal(one[0], batched[i]), i
+        ties += st["near_ties"]
+    few, st_f = engine.linear_search(m0s[picks], w.granularity, kernel)
+    assert 1 < st_f["candidate_parts"] and np.array_equal(few, batched[picks])
+    plain, st_p = engine.linear_search(m0s[picks], w.granularity, "plain")
+    assert ties == st_f["near_ties"] == st_p["near_ties"]
+    if kernel == "tuned_exact":
+        assert np.array_equal(few, plain)
+    else:
+        assert_same_but_stack(few, plain, 1)
+    print(f"{kernel}: one-midpoint calls split into {st['candidate_parts']} candidate ranges, "
+          f"{len(picks)} midpoints into {st_f['candidate_parts']}")
+
+
+def test_candidate_split_zocrs_and_empty_midpoint(engine):
+    """ZO-CRS (three parameters) through the split, and a midpoint without
+    traces inside a split call (its block stays zero)."""
+    line = synthetic.structured_line(n_cmp=24, fold_range=(8, 14), h_max=1500, ns=400,
+                                     dt_us=4000, n_reflectors=4, f=20.0, snr=6.0, seed=5)
+    lower, upper, gran = [1500.0, -1e-3, -1e-7], [4500.0, 1e-3, 1e-7], [6, 5, 9]
+    apm, tau = 60.0, 2
+    _setup(engine, line, "zocrs", lower, upper, tau, apm)
+    m0s = np.concatenate([line.cdp_midpoints[10:12], [np.float32(-5000.0)]])
+    tuned, st = engine.linear_search(m0s, gran, "tuned")
+    exact, st_e = engine.linear_search(m0s, gran, "tuned_exact")
+    plain, st_p = engine.linear_search(m0s, gran, "plain")
+    assert st["candidate_parts"] > 1 and st_e["candidate_parts"] > 1
+    assert st["device_error"] == 0 and st_e["device_error"] == 0
+    assert np.array_equal(exact, plain)
+    assert_same_but_stack(tuned, plain, 3)
+    assert np.all(tuned[-1] == 0) and np.all(exact[-1] == 0)
+    assert st["near_ties"] == st_p["near_ties"]
+
+
+def test_grid_reuse_across_calls(engine, c1_line):
+    """The handle keeps the candidate grid and chunk bounds of its last call
+    and reuses them when the next call has the same grid; a change of bounds,
+    granularity or grid mode rebuilds them.  Every call equals the same call
+    on a fresh handle."""
+    w = synthetic.WORKLOADS["cmp-small"]
+    tau = 2
+    m0s = c1_line.cdp_midpoints[:4]
+    seq = [(w.lower, [101], "reference"), (w.lower, [101], "reference"),
+           (w.lower, [57], "reference"), ([1200.0], [101], "reference"),
+           ([1200.0], [101], "inclusive"), (w.lower, [101], "reference")]
+    _setup(engine, c1_line, "cmp", w.lower, w.upper, tau)
+    try:
+        for lower, gran, mode in seq:
+            engine.set_traveltime("cmp", lower, w.upper)
+            engine.set_grid_mode(mode)
+            for kernel in ("tuned", "plain"):
+                got, st = engine.linear_search(m0s, gran, kernel)
+                with capi.Engine(0) as fresh:
+                    _setup(fresh, c1_line, "cmp", lower, w.upper, tau)
+                    fresh.set_grid_mode(mode)
+                    want, _ = fresh.linear_search(m0s, gran, kernel)
+                assert np.array_equal(got, want), (lower, gran, mode, kernel)
+    finally:
+        engine.set_grid_mode("reference")
