@@ -111,11 +111,20 @@ __device__ __forceinline__ void de_eval(const DeParams &d, float t0, float m0, u
     for (int j = 0; j < (W > 0 ? W : kMaxWindow); j++) num[j] = 0.f;
     float lin = 0.f, den = 0.f;
     unsigned used = 0, nu = 0;
+    // OCT: (t0, candidate) factors once, trace factors from the line's table
+    const OctCand kc = oct_cand(t0, c, p1, MODEL == kModelOct ? a.h0 : 0.f);
     for (uint32_t q = 0; q < cnt; q++) {
         const uint32_t ti = a.selIdx ? a.selIdx[first + q] : first + q;
         float t;
-        int ok = model_time<MODEL>(t0, c, p1, p2, a.mid[ti], a.hoff[ti], a.hsq[ti], m0, a.apm,
+        int ok;
+        if (MODEL == kModelOct) {
+            const float4 tf = __ldg(a.octTab + ti);  // {m, gamma^2, 16h^2h0^2, h^2-h0^2}
+            ok = oct_model_time(kc, tf.y, tf.z, tf.w, t0, c, p1, tf.x, a.hoff[ti], m0, a.apm,
+                                a.h0, &t);
+        } else {
+            ok = model_time<MODEL>(t0, c, p1, p2, a.mid[ti], a.hoff[ti], a.hsq[ti], m0, a.apm,
                                    a.h0, &t);
+        }
         if (ok < 0) {
             nu++;
             continue;

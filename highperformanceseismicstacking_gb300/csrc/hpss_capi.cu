@@ -41,6 +41,9 @@ struct hpss_handle_s : public Handle {
     };
     Buf params, chunkBounds, selFirst, selCount, selIdx, candFirst, candCount,
         notUsed, errWord, m0s, out, octCands, prior, partial;
+    Buf octTab;                // OCT per-trace factors of the line (octTabH0)
+    bool octTabValid = false;
+    float octTabH0 = 0.f;
     std::string gridKey;       // grid held in `params` (empty: none)
     uint32_t boundsChunk = 0;  // chunk size of the bounds in `chunkBounds` (0: none)
     std::vector<float> octCandsHost;
@@ -120,6 +123,7 @@ void free_gather(hpss_handle h) {
     fr(reinterpret_cast<void *&>(h->dHoff), n * sizeof(float));
     fr(reinterpret_cast<void *&>(h->dHsq), n * sizeof(float));
     h->gatherReady = false;
+    h->octTabValid = false;
 }
 
 int model_params(int model) {
@@ -228,6 +232,25 @@ void fill_line_params(hpss_handle h, LsParams &lp) {
     lp.np = (int)h->np;
     lp.apm = h->apm;
     lp.h0 = h->h0;
+}
+
+// OCT: the per-trace factor table of the resident line for the current h0,
+// built on the handle's stream at the first OCT call after an upload or an
+// h0 change.
+cudaError_t use_oct_table(hpss_handle h, LsParams &lp) {
+    if (h->model != HPSS_MODEL_OCT) return cudaSuccess;
+    if (!h->octTabValid || h->octTabH0 != h->h0) {
+        h->octTabValid = false;
+        cudaError_t e = ensure(h, h->octTab, (size_t)h->nTraces * sizeof(float4));
+        if (e != cudaSuccess) return e;
+        e = launch_oct_trace_table(h->dMid, h->dHoff, h->nTraces, h->h0,
+                                   static_cast<float4 *>(h->octTab.p), h->stream);
+        if (e != cudaSuccess) return e;
+        h->octTabValid = true;
+        h->octTabH0 = h->h0;
+    }
+    lp.octTab = static_cast<const float4 *>(h->octTab.p);
+    return cudaSuccess;
 }
 
 int num_sms(hpss_handle h) {
@@ -359,6 +382,7 @@ hpss_status linear_search_impl(hpss_handle h, const float *d_m0s, uint32_t nM0,
     lp.nM0 = nM0;
     lp.P = (uint32_t)P;
     lp.out = d_out;
+    HPSS_CUDA_TRY(h, use_oct_table(h, lp));
 
     // The candidate grid (and below the chunk bounds) depend only on the
     // model, the bounds, the granularity and the grid mode: a call that
@@ -544,6 +568,7 @@ hpss_status de_impl(hpss_handle h, const float *d_m0s, uint32_t nM0, uint32_t po
     d.ls.m0s = d_m0s;
     d.ls.nM0 = nM0;
     d.ls.out = d_out;
+    HPSS_CUDA_TRY(h, use_oct_table(h, d.ls));
     d.pop = pop;
     d.gens = gens;
     d.F = F;
@@ -690,7 +715,7 @@ hpss_status hpss_destroy(hpss_handle h) {
     free_gather(h);
     for (auto *b : {&h->params, &h->chunkBounds, &h->selFirst, &h->selCount, &h->selIdx,
                     &h->candFirst, &h->candCount, &h->notUsed, &h->errWord, &h->m0s,
-                    &h->out, &h->octCands, &h->prior, &h->partial})
+                    &h->out, &h->octCands, &h->prior, &h->partial, &h->octTab})
         release(h, *b);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);

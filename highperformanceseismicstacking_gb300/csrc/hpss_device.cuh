@@ -58,45 +58,80 @@ __device__ __forceinline__ float oct_tn0_sq(float t0, float c, float h0) {
     return __fmaf_rn(t0, t0, -__fmul_rn(__fmul_rn(c, h0), h0));
 }
 
+// The OCT formulas factored by what their terms depend on, each factor
+// rounded exactly as in the one-expression form: per trace (h, h0) and per
+// (t0, candidate).  Kernels that visit many traces per candidate take the
+// trace factors from a table (oct_trace_table_kernel) and the candidate
+// factors out of the trace loop; the values are the same bit for bit.
+struct OctCand {
+    float ts;        // theta^2, theta = t0 * slope
+    float tn0_sq;    // t0^2 - c h0^2
+    float tq;        // tn0_sq^2
+    float tqts;      // tq * theta^2
+    float twoTq;     // 2 tq
+    float twoTheta;  // 2 theta
+};
+__device__ __forceinline__ OctCand oct_cand(float t0, float c, float slope, float h0) {
+    OctCand k;
+    const float theta = __fmul_rn(t0, slope);
+    k.ts = __fmul_rn(theta, theta);
+    k.tn0_sq = oct_tn0_sq(t0, c, h0);
+    k.tq = __fmul_rn(k.tn0_sq, k.tn0_sq);
+    k.tqts = __fmul_rn(k.tq, k.ts);
+    k.twoTq = __fmul_rn(2.f, k.tq);
+    k.twoTheta = 2.f * theta;
+    return k;
+}
+
+// Trace factors of the displaced midpoint: gamma^2 = (2 sqrt(h^2 + h0^2))^2,
+// 16 h^2 h0^2 and h^2 - h0^2 (the product h*h is rounded on its own and the
+// h0 product is fused -- fractional half-offsets tell the forms apart).
+struct OctTrace {
+    float gs, p16h, dif;
+};
+__device__ __forceinline__ OctTrace oct_trace(float h, float h0) {
+    OctTrace f;
+    const float hh = __fmul_rn(h, h);
+    const float gamma = 2 * sqrtf(__fmaf_rn(h0, h0, hh));
+    f.gs = __fmul_rn(gamma, gamma);
+    f.p16h = __fmul_rn(__fmul_rn(__fmul_rn(__fmul_rn(16.f, h), h), h0), h0);
+    f.dif = __fmaf_rn(-h0, h0, hh);
+    return f;
+}
+
+// OCT displaced midpoint (oct/common.cuh:7-35) from its factors.
+__device__ __forceinline__ int oct_mh(const OctCand &k, float gs, float p16h, float dif,
+                                      float m0, float *mh) {
+    // tq^2 + tq ts gs + 16 h^2 h0^2 ts^2 as the reference's OCT kernel rounds
+    // it: tq ts gs as products, tq^2 fused onto them, the last product fused;
+    // then ts gs + 2 tq as a plain add (matched against every entry of the
+    // reference kernel's semblance tables on the OCT fixtures)
+    float arg = __fmaf_rn(k.tq, k.tq, __fmul_rn(k.tqts, gs));
+    arg = __fmaf_rn(__fmul_rn(p16h, k.ts), k.ts, arg);
+    if (arg < 0) return DE_NEG_SQRT;
+    arg = __fadd_rn(__fadd_rn(__fmul_rn(k.ts, gs), k.twoTq), __fmul_rn(2.f, sqrtf(arg)));
+    if (arg == 0) return DE_DIV_ZERO;
+    // m0 + 2 theta (h^2 - h0^2) / sqrt(.): the reference's fast-math build
+    // divides by multiplying with the approximate reciprocal and fuses that
+    // product with the add of m0 -- fma(2 theta dif, rcp(sqrt(.)), m0)
+    *mh = __fmaf_rn(__fmul_rn(k.twoTheta, dif), __fdividef(1.0f, sqrtf(arg)), m0);
+    return DE_OK;
+}
+
 // OCT displaced midpoint (oct/common.cuh:7-35).
 __device__ __forceinline__ int oct_displaced_midpoint(float h, float h0,
                                                       float t0, float m0,
                                                       float c, float slope,
                                                       float *mh) {
-    const float theta = __fmul_rn(t0, slope);
-    // h*h + h0*h0 and h*h - h0*h0: the product h*h is rounded on its own and
-    // the h0 product is fused (fractional half-offsets tell the forms apart)
-    const float gamma = 2 * sqrtf(__fmaf_rn(h0, h0, __fmul_rn(h, h)));
-    const float tn0_sq = oct_tn0_sq(t0, c, h0);
-    const float theta_sq = __fmul_rn(theta, theta);
-    const float gamma_sq = __fmul_rn(gamma, gamma);
-    const float tn0_quad = __fmul_rn(tn0_sq, tn0_sq);
-    const float p16 = __fmul_rn(
-        __fmul_rn(__fmul_rn(__fmul_rn(__fmul_rn(16.f, h), h), h0), h0), theta_sq);
-    // tq^2 + tq ts gs + 16 h^2 h0^2 ts^2 as the reference's OCT kernel rounds
-    // it: tq ts gs as products, tq^2 fused onto them, the last product fused;
-    // then ts gs + 2 tq as a plain add (matched against every entry of the
-    // reference kernel's semblance tables on the OCT fixtures)
-    float arg = __fmaf_rn(tn0_quad, tn0_quad, __fmul_rn(__fmul_rn(tn0_quad, theta_sq), gamma_sq));
-    arg = __fmaf_rn(p16, theta_sq, arg);
-    if (arg < 0) return DE_NEG_SQRT;
-    arg = __fadd_rn(__fadd_rn(__fmul_rn(theta_sq, gamma_sq), __fmul_rn(2.f, tn0_quad)),
-                    __fmul_rn(2.f, sqrtf(arg)));
-    if (arg == 0) return DE_DIV_ZERO;
-    // m0 + 2 theta (h^2 - h0^2) / sqrt(.): the reference's fast-math build
-    // divides by multiplying with the approximate reciprocal and fuses that
-    // product with the add of m0 -- fma(2 theta dif, rcp(sqrt(.)), m0)
-    const float twoTheta = 2.f * theta;
-    const float dif = __fmaf_rn(-h0, h0, __fmul_rn(h, h));
-    *mh = __fmaf_rn(__fmul_rn(twoTheta, dif), __fdividef(1.0f, sqrtf(arg)), m0);
-    return DE_OK;
+    const OctTrace f = oct_trace(h, h0);
+    return oct_mh(oct_cand(t0, c, slope, h0), f.gs, f.p16h, f.dif, m0, mh);
 }
 
-// OCT traveltime at the displaced midpoint (oct/common.cuh:37-94).
-__device__ __forceinline__ int oct_time(float h, float h0, float t0, float m0,
-                                        float m, float mh, float c,
-                                        float slope, float *out) {
-    const float tn0_sq = oct_tn0_sq(t0, c, h0);
+// OCT traveltime at the displaced midpoint (oct/common.cuh:37-94), with
+// tn0_sq = t0^2 - c h0^2 given.
+__device__ __forceinline__ int oct_time_k(float h, float h0, float t0, float tn0_sq, float m0,
+                                          float m, float mh, float c, float slope,
+                                          float *out) {
     const float b = __fsub_rn(mh, m0);
     const float bb = __fmul_rn(b, b);
     const float ap = __fadd_rn(h, h0), am = __fsub_rn(h, h0);
@@ -125,6 +160,26 @@ __device__ __forceinline__ int oct_time(float h, float h0, float t0, float m0,
     return DE_OK;
 }
 
+// OCT traveltime at the displaced midpoint (oct/common.cuh:37-94).
+__device__ __forceinline__ int oct_time(float h, float h0, float t0, float m0,
+                                        float m, float mh, float c,
+                                        float slope, float *out) {
+    return oct_time_k(h, h0, t0, oct_tn0_sq(t0, c, h0), m0, m, mh, c, slope, out);
+}
+
+// OCT traveltime of one trace for the candidate factors k (candidate c,
+// slope), trace factors f and midpoint m, half-offset h; returns as
+// model_time below.
+__device__ __forceinline__ int oct_model_time(const OctCand &k, float gs, float p16h, float dif,
+                                              float t0, float c, float slope, float m, float h,
+                                              float m0, float apm, float h0, float *t) {
+    float mh;
+    int e = oct_mh(k, gs, p16h, dif, m0, &mh);
+    if (e != DE_OK || fabsf(m - mh) > apm) return -1;
+    e = oct_time_k(h, h0, t0, k.tn0_sq, m0, m, mh, c, slope, t);
+    return e == DE_OK ? 1 : 0;
+}
+
 // Traveltime of one trace for one candidate, dispatching on the model.
 // Returns: 1 = time valid, 0 = window skipped (ZO-CRS negative square,
 // OCT computeTime error), -1 = trace not used (OCT displaced midpoint error
@@ -142,11 +197,9 @@ __device__ __forceinline__ int model_time(float t0, float c, float p1,
         float dm = m - m0;
         return zocrs_time(t0, c, p1, p2, dm, h_sq, t) ? 1 : 0;
     } else {
-        float mh;
-        int e = oct_displaced_midpoint(h, h0, t0, m0, c, p1, &mh);
-        if (e != DE_OK || fabsf(m - mh) > apm) return -1;
-        e = oct_time(h, h0, t0, m0, m, mh, c, p1, t);
-        return e == DE_OK ? 1 : 0;
+        const OctTrace f = oct_trace(h, h0);
+        return oct_model_time(oct_cand(t0, c, p1, h0), f.gs, f.p16h, f.dif, t0, c, p1, m, h, m0,
+                              apm, h0, t);
     }
 }
 

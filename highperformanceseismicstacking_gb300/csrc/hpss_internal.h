@@ -94,6 +94,9 @@ struct LsParams {
     uint32_t parts = 1;
     uint32_t chunksPerPart = 0;
     PartBest *partial = nullptr;
+    // OCT: per-trace factors {m, gamma^2, 16 h^2 h0^2, h^2 - h0^2} for the
+    // line's h0 (launch_oct_trace_table); read by the OCT tuned and DE kernels
+    const float4 *octTab = nullptr;
 };
 
 // Differential evolution launch (de.cu).
@@ -168,6 +171,9 @@ uint32_t oct_parts(const LsParams &p, uint32_t numSms);
 size_t oct_partial_bytes(uint32_t nM0, uint32_t S, uint32_t parts);
 cudaError_t launch_ls_oct(const LsParams &p, uint32_t numSms, void *partial, uint32_t parts,
                           cudaStream_t st);
+// Per-trace factors of the OCT formulas for half-offset h0 (ls_oct.cu).
+cudaError_t launch_oct_trace_table(const float *mid, const float *hoff, uint32_t n, float h0,
+                                   float4 *tab, cudaStream_t st);
 // Combine `parts` candidate ranges of every (midpoint, sample) in candidate
 // order and write the result block [nM0][2+np][S]; counts near-ties.
 cudaError_t launch_merge_parts(const LsParams &p, uint32_t parts, const PartBest *partial,

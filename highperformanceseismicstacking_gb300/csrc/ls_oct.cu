@@ -20,7 +20,9 @@
 //
 // The per-candidate arithmetic is the plain kernel's (model_time<kModelOct>,
 // window_index, the COMPUTE_SEMBLANCE restatement), in the same trace order,
-// so semblance, stack and chosen candidate equal the plain kernel's.
+// so semblance, stack and chosen candidate equal the plain kernel's; the OCT
+// formulas take their per-trace factors from the line's factor table and
+// their (t0, candidate) factors from registers (the same roundings).
 #include "hpss_device.cuh"
 #include "hpss_internal.h"
 
@@ -59,6 +61,7 @@ ls_oct_kernel(LsParams a, uint32_t tiles, uint32_t parts, uint32_t chunksPerPart
         const uint32_t c1 = min(c0 + chunksPerPart, (a.P + kChunk - 1) / kChunk);
         for (uint32_t chunk = c0; chunk < c1; chunk++) {
             float cc[R], sl[R];
+            OctCand kc[R];  // (t0, candidate) factors, out of the trace loop
             bool valid[R];
 #pragma unroll
             for (int r = 0; r < R; r++) {
@@ -67,6 +70,7 @@ ls_oct_kernel(LsParams a, uint32_t tiles, uint32_t parts, uint32_t chunksPerPart
                 const uint32_t pc = valid[r] ? p : a.P - 1;
                 cc[r] = a.params[2 * (size_t)pc];
                 sl[r] = a.params[2 * (size_t)pc + 1];
+                kc[r] = oct_cand(t0, cc[r], sl[r], a.h0);
             }
             float num[R][W], lin[R], den[R];
             unsigned used[R], nu[R];
@@ -79,13 +83,14 @@ ls_oct_kernel(LsParams a, uint32_t tiles, uint32_t parts, uint32_t chunksPerPart
             }
             for (uint32_t q = 0; q < cnt; q++) {
                 const uint32_t ti = a.selIdx ? a.selIdx[first + q] : first + q;
-                const float m = a.mid[ti], h = a.hoff[ti];
+                const float4 tf = __ldg(a.octTab + ti);  // {m, gamma^2, 16h^2h0^2, h^2-h0^2}
+                const float h = a.hoff[ti];
                 const float *tr = a.samples + (size_t)ti * a.stride;
 #pragma unroll
                 for (int r = 0; r < R; r++) {
                     float t;
-                    const int ok = model_time<kModelOct>(t0, cc[r], sl[r], 0.f, m, h, 0.f, m0,
-                                                         a.apm, a.h0, &t);
+                    const int ok = oct_model_time(kc[r], tf.y, tf.z, tf.w, t0, cc[r], sl[r], tf.x,
+                                                  h, m0, a.apm, a.h0, &t);
                     if (ok < 0) nu[r]++;
                     if (ok > 0) {
                         const WinIdx wi = window_index(t, a.dt);
@@ -195,6 +200,21 @@ cudaError_t launch_merge_parts(const LsParams &p, uint32_t parts, const PartBest
     const uint64_t n = (uint64_t)p.nM0 * p.S;
     if (n == 0) return cudaSuccess;
     merge_parts_kernel<<<(uint32_t)((n + 255) / 256), 256, 0, st>>>(p, parts, partial);
+    return cudaGetLastError();
+}
+
+__global__ void oct_trace_table_kernel(const float *mid, const float *hoff, uint32_t n,
+                                       float h0, float4 *tab) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const OctTrace f = oct_trace(hoff[i], h0);
+    tab[i] = make_float4(mid[i], f.gs, f.p16h, f.dif);
+}
+
+cudaError_t launch_oct_trace_table(const float *mid, const float *hoff, uint32_t n, float h0,
+                                   float4 *tab, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    oct_trace_table_kernel<<<(n + 255) / 256, 256, 0, st>>>(mid, hoff, n, h0, tab);
     return cudaGetLastError();
 }
 

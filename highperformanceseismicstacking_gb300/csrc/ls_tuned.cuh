@@ -381,19 +381,26 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
                         }
                     }
                 };
+                // The W + 1 amplitudes of both windows of every pair are loaded
+                // into registers before the taps: the loads of one trace issue
+                // back to back and the taps run without shared-memory waits.
                 auto tapsOf = [&](const Win &wn) {
+                    float2 yv[NP][W + 1];
 #pragma unroll
                     for (int qq = 0; qq < NP; qq++) {
                         const float *ya = sm.y + wn.bo[2 * qq];
                         const float *yb = sm.y + wn.bo[2 * qq + 1];
+#pragma unroll
+                        for (int jj = 0; jj <= W; jj++) yv[qq][jj] = f2(ya[jj], yb[jj]);
+                    }
+#pragma unroll
+                    for (int qq = 0; qq < NP; qq++) {
                         const float2 fq = f2(wn.fr[2 * qq], wn.fr[2 * qq + 1]);
-                        float2 y1 = f2(ya[0], yb[0]);
 #pragma unroll
                         for (int jj = 0; jj < W; jj++) {
-                            const float2 y0 = y1;
-                            y1 = f2(ya[jj + 1], yb[jj + 1]);
-                            const float2 d = __ffma2_rn(y0, kNeg1, y1);   // y1 - y0
-                            const float2 u = __ffma2_rn(d, fq, y0);       // (y1-y0)*f + y0
+                            const float2 y0 = yv[qq][jj];
+                            const float2 d = __ffma2_rn(y0, kNeg1, yv[qq][jj + 1]);  // y1 - y0
+                            const float2 u = __ffma2_rn(d, fq, y0);  // (y1-y0)*f + y0
                             num[qq][jj] = __fadd2_rn(num[qq][jj], u);
                             if (EXACT_STACK) lin[qq] = __fadd2_rn(lin[qq], u);
                             den[qq] = __ffma2_rn(u, u, den[qq]);
