@@ -115,15 +115,32 @@ void free_gather(hpss_handle h) {
         }
         p = nullptr;
     };
-    size_t n = h->nTraces, st = h->stride;
-    fr(reinterpret_cast<void *&>(h->dSamples), n * st * sizeof(float));
-    fr(reinterpret_cast<void *&>(h->dSamples16), n * st * sizeof(uint16_t));
-    fr(reinterpret_cast<void *&>(h->dScale), n * sizeof(float));
-    fr(reinterpret_cast<void *&>(h->dMid), n * sizeof(float));
-    fr(reinterpret_cast<void *&>(h->dHoff), n * sizeof(float));
-    fr(reinterpret_cast<void *&>(h->dHsq), n * sizeof(float));
+    fr(reinterpret_cast<void *&>(h->dSamples), h->capSamples);
+    fr(reinterpret_cast<void *&>(h->dSamples16), h->capSamples16);
+    fr(h->dTraceBuf, h->capTrace);
+    h->dScale = h->dMid = h->dHoff = h->dHsq = nullptr;
+    h->capSamples = h->capSamples16 = h->capTrace = 0;
     h->gatherReady = false;
     h->octTabValid = false;
+}
+
+// Line buffer of at least `bytes`: the current allocation when it is large
+// enough (a re-upload of a line of the same size allocates nothing), else a
+// new one.
+cudaError_t grow_line_buffer(hpss_handle h, void **p, size_t &cap, size_t bytes) {
+    if (bytes == 0) bytes = 16;
+    if (*p && cap >= bytes) return cudaSuccess;
+    if (*p) {
+        cudaFree(*p);
+        h->deviceBytes -= cap;
+        *p = nullptr;
+        cap = 0;
+    }
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) return e;
+    cap = bytes;
+    h->deviceBytes += bytes;
+    return cudaSuccess;
 }
 
 int model_params(int model) {
@@ -218,8 +235,8 @@ void fill_line_params(hpss_handle h, LsParams &lp) {
     lp.samples = h->dSamples;
     // 16-bit copies are read only by the tuned pair kernel's staging; every
     // other kernel reads the FP32 line
-    lp.samples16 = h->dSamples16;
-    lp.scale = h->dScale;
+    lp.samples16 = h->storage != HPSS_STORAGE_FP32 ? h->dSamples16 : nullptr;
+    lp.scale = h->storage != HPSS_STORAGE_FP32 ? h->dScale : nullptr;
     lp.storage = h->storage;
     lp.stride = h->stride;
     lp.S = h->S;
@@ -756,7 +773,8 @@ hpss_status hpss_upload_gather(hpss_handle h, const float *samples,
     }
     cudaSetDevice(h->device);
     cudaStreamSynchronize(h->stream);
-    free_gather(h);
+    h->gatherReady = false;
+    h->octTabValid = false;
     h->nTraces = nTraces;
     h->S = samplesPerTrace;
     h->stride = (samplesPerTrace + 7u) & ~7u;  // 32-byte rows
@@ -773,15 +791,17 @@ hpss_status hpss_upload_gather(hpss_handle h, const float *samples,
     std::vector<float> hsq(nTraces);
     for (uint32_t i = 0; i < nTraces; i++) hsq[i] = halfoffsets[i] * halfoffsets[i];
     const size_t n = nTraces, st = h->stride;
-    auto alloc = [&](void **p, size_t bytes) -> cudaError_t {
-        cudaError_t e = cudaMalloc(p, bytes ? bytes : 16);
-        if (e == cudaSuccess) h->deviceBytes += bytes;
-        return e;
-    };
-    HPSS_CUDA_TRY(h, alloc(reinterpret_cast<void **>(&h->dSamples), n * st * sizeof(float)));
-    HPSS_CUDA_TRY(h, alloc(reinterpret_cast<void **>(&h->dMid), n * sizeof(float)));
-    HPSS_CUDA_TRY(h, alloc(reinterpret_cast<void **>(&h->dHoff), n * sizeof(float)));
-    HPSS_CUDA_TRY(h, alloc(reinterpret_cast<void **>(&h->dHsq), n * sizeof(float)));
+    HPSS_CUDA_TRY(h, grow_line_buffer(h, reinterpret_cast<void **>(&h->dSamples), h->capSamples,
+                                      n * st * sizeof(float)));
+    // mid, hoff, hsq and the 16-bit storage scale: four 256-byte aligned
+    // slices of one buffer
+    const size_t slice = (n * sizeof(float) + 255) & ~size_t(255);
+    HPSS_CUDA_TRY(h, grow_line_buffer(h, &h->dTraceBuf, h->capTrace, 4 * slice));
+    char *tb = static_cast<char *>(h->dTraceBuf);
+    h->dMid = reinterpret_cast<float *>(tb);
+    h->dHoff = reinterpret_cast<float *>(tb + slice);
+    h->dHsq = reinterpret_cast<float *>(tb + 2 * slice);
+    h->dScale = reinterpret_cast<float *>(tb + 3 * slice);
     if (n) {
         if (st != samplesPerTrace)
             HPSS_CUDA_TRY(h, cudaMemsetAsync(h->dSamples, 0, n * st * sizeof(float), h->stream));
@@ -797,8 +817,8 @@ hpss_status hpss_upload_gather(hpss_handle h, const float *samples,
                                          cudaMemcpyHostToDevice, h->stream));
     }
     if (storage != HPSS_STORAGE_FP32) {
-        HPSS_CUDA_TRY(h, alloc(reinterpret_cast<void **>(&h->dSamples16), n * st * sizeof(uint16_t)));
-        HPSS_CUDA_TRY(h, alloc(reinterpret_cast<void **>(&h->dScale), n * sizeof(float)));
+        HPSS_CUDA_TRY(h, grow_line_buffer(h, reinterpret_cast<void **>(&h->dSamples16),
+                                          h->capSamples16, n * st * sizeof(uint16_t)));
         HPSS_CUDA_TRY(h, launch_convert_storage(h->dSamples, h->dSamples16, h->dScale,
                                                 nTraces, samplesPerTrace, h->stride,
                                                 storage, h->stream));

@@ -124,6 +124,10 @@ struct Handle {
     uint16_t *dSamples16 = nullptr;
     float *dScale = nullptr;
     float *dMid = nullptr, *dHoff = nullptr, *dHsq = nullptr;
+    // the per-trace arrays (mid, hoff, hsq, scale) are slices of dTraceBuf;
+    // allocated bytes of the line buffers, kept across uploads that fit
+    void *dTraceBuf = nullptr;
+    size_t capSamples = 0, capSamples16 = 0, capTrace = 0;
     std::vector<float> hMid, hHoff;
     // traveltime
     int model = -1;

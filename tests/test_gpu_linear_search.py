@@ -304,3 +304,35 @@ def test_grid_reuse_across_calls(engine, c1_line):
                 assert np.array_equal(got, want), (lower, gran, mode, kernel)
     finally:
         engine.set_grid_mode("reference")
+
+
+def test_reupload_reuses_line_buffers(engine):
+    """A re-upload keeps the device line buffers when the new line fits them
+    (no allocation for a line of the same size); lines of other sizes,
+    sample counts and storages in between give the results of a fresh
+    handle."""
+    w = synthetic.WORKLOADS["cmp-small"]
+    big = synthetic.cmp_line(n_cmp=8, halfoffsets=list(range(25, 1176, 50)), ns=600,
+                             dt_us=4000, n_reflectors=4, n_multiples=0, f=25.0, snr=10.0, seed=31)
+    small = synthetic.cmp_line(n_cmp=5, halfoffsets=list(range(25, 776, 50)), ns=301,
+                               dt_us=4000, n_reflectors=3, n_multiples=0, f=25.0, snr=10.0, seed=32)
+    tau = 2
+
+    def run(eng, line, storage):
+        eng.upload_gather(line.samples, line.midpoints, line.halfoffsets, float(line.dt),
+                          storage=storage)
+        eng.set_traveltime("cmp", w.lower, w.upper)
+        eng.set_window(tau)
+        return eng.linear_search(line.cdp_midpoints, w.granularity, "tuned")[0]
+
+    with capi.Engine(0) as eng:
+        first = run(eng, big, "fp32")
+        held = eng.device_bytes()
+        again = run(eng, big, "fp32")
+        assert eng.device_bytes() == held
+        assert np.array_equal(first, again)
+        for line, storage in [(small, "fp16"), (big, "bf16"), (small, "fp32"), (big, "fp32")]:
+            got = run(eng, line, storage)
+            with capi.Engine(0) as fresh:
+                want = run(fresh, line, storage)
+            assert np.array_equal(got, want), (line.samples.shape, storage)
