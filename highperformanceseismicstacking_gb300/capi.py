@@ -35,7 +35,7 @@ EXPORTED = [
     "hpss_linear_search_device",
     "hpss_differential_evolution", "hpss_differential_evolution_device",
     "hpss_stretch_free", "hpss_select_traces", "hpss_stream", "hpss_device_bytes",
-    "hpss_linear_search_noalloc",
+    "hpss_linear_search_noalloc", "hpss_linear_search_line",
 ]
 
 
@@ -76,6 +76,8 @@ def load_library(path: Optional[Path] = None) -> C.CDLL:
         "hpss_set_precision": (i32, [vp, i32]),
         "hpss_linear_search": (i32, [vp, fp, u32, up, i32, fp, C.POINTER(Stats)]),
         "hpss_linear_search_device": (i32, [vp, vp, u32, up, i32, vp, C.POINTER(Stats)]),
+        "hpss_linear_search_line": (i32, [vp, fp, fp, fp, u32, u32, f32, i32, fp, u32, up, i32,
+                                          fp, C.POINTER(Stats)]),
         "hpss_differential_evolution": (i32, [vp, fp, u32, u32, u32, f32, f32, C.c_uint64, fp,
                                               C.POINTER(Stats)]),
         "hpss_differential_evolution_device": (i32, [vp, vp, u32, u32, u32, f32, f32,
@@ -199,6 +201,34 @@ class Engine:
         st = Stats()
         self._check(self._lib.hpss_linear_search(self.h, _fptr(m0s), m0s.size, _uptr(g),
                                                   KERNELS[kernel], _fptr(out), C.byref(st)))
+        return out, st.as_dict()
+
+    def linear_search_line(self, samples: np.ndarray, midpoints: np.ndarray,
+                           halfoffsets: np.ndarray, dt: float, m0s, granularity: Sequence[int],
+                           kernel: str = "tuned", storage: str = "fp32",
+                           out: Optional[np.ndarray] = None) -> Tuple[np.ndarray, dict]:
+        """Upload a line and search it in one call, the upload overlapped with
+        the search (hpss_linear_search_line); the traveltime and the window
+        must be set before.  The line stays resident afterwards, as after
+        upload_gather.  `out` (optional): a C-contiguous float32 array of
+        shape (len(m0s), 2 + nParams, S) to write into (e.g. page-locked)."""
+        samples = np.ascontiguousarray(samples, dtype=np.float32)
+        midpoints = np.ascontiguousarray(midpoints, dtype=np.float32)
+        halfoffsets = np.ascontiguousarray(halfoffsets, dtype=np.float32)
+        m0s = np.ascontiguousarray(m0s, dtype=np.float32)
+        n, S = samples.shape
+        g = np.asarray(granularity, np.uint32)
+        shape = (m0s.size, 2 + self.np, S)
+        if out is None:
+            out = np.zeros(shape, np.float32)
+        elif out.shape != shape or out.dtype != np.float32 or not out.flags.c_contiguous:
+            raise ValueError(f"out must be a C-contiguous float32 array of shape {shape}")
+        st = Stats()
+        self._check(self._lib.hpss_linear_search_line(
+            self.h, _fptr(samples), _fptr(midpoints), _fptr(halfoffsets), n, S, C.c_float(dt),
+            STORAGE[storage], _fptr(m0s), m0s.size, _uptr(g), KERNELS[kernel], _fptr(out),
+            C.byref(st)))
+        self.S = S
         return out, st.as_dict()
 
     def linear_search_device(self, d_m0s: int, n_m0: int, granularity, d_out: int,

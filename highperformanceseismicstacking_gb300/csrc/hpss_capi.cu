@@ -49,6 +49,7 @@ struct hpss_handle_s : public Handle {
     std::vector<float> octCandsHost;
     std::map<std::string, int> variantCache;  // autotuner decisions
     int lastVariant = -1;
+    uint32_t lastParts = 1;                    // candidate parts of the last search
     uint32_t meanFold = 0;                     // traces per distinct midpoint
 };
 
@@ -352,9 +353,17 @@ hpss_status choose_variant(hpss_handle h, const LsParams &lp, uint32_t units, bo
     return HPSS_OK;
 }
 
+// A call that is one group of a larger call (hpss_linear_search_line):
+// the counters were cleared once for the whole call and this group's
+// per-midpoint counts start at `m0Offset`.
+struct GroupOfCall {
+    uint32_t m0Offset;
+};
+
 hpss_status linear_search_impl(hpss_handle h, const float *d_m0s, uint32_t nM0,
                                const uint32_t *granularity, int kernel,
-                               float *d_out, hpss_stats *stats, bool sync) {
+                               float *d_out, hpss_stats *stats, bool sync,
+                               const GroupOfCall *group = nullptr) {
     hpss_status rc = check_ready(h);
     if (rc != HPSS_OK) return rc;
     if (!granularity)
@@ -455,13 +464,16 @@ hpss_status linear_search_impl(hpss_handle h, const float *d_m0s, uint32_t nM0,
     };
     // counters, cleared by one memset: error word at byte 0, near-tie counter
     // at byte 8, the per-midpoint notUsed counts from byte 16
-    HPSS_CUDA_TRY(h, ensure(h, h->notUsed, 16 + nM0 * sizeof(unsigned long long)));
+    if (!group) {
+        HPSS_CUDA_TRY(h, ensure(h, h->notUsed, 16 + nM0 * sizeof(unsigned long long)));
+        HPSS_CUDA_TRY(h, cudaMemsetAsync(h->notUsed.p, 0, 16 + nM0 * sizeof(unsigned long long),
+                                         h->stream));
+    }
     char *counters = static_cast<char *>(h->notUsed.p);
     lp.errorWord = reinterpret_cast<uint32_t *>(counters);
     lp.nearTies = reinterpret_cast<unsigned long long *>(counters + 8);
-    lp.notUsed = reinterpret_cast<unsigned long long *>(counters + 16);
-    HPSS_CUDA_TRY(h, cudaMemsetAsync(counters, 0, 16 + nM0 * sizeof(unsigned long long),
-                                     h->stream));
+    lp.notUsed = reinterpret_cast<unsigned long long *>(counters + 16) +
+                 (group ? group->m0Offset : 0);
 
     const uint32_t tiles = (h->S + kTileSamples - 1) / kTileSamples;
     const uint64_t units = (uint64_t)nM0 * tiles;
@@ -513,11 +525,14 @@ hpss_status linear_search_impl(hpss_handle h, const float *d_m0s, uint32_t nM0,
     };
     int variant = 0;
     if (pairKernel) {
+        // the autotuner's timing launches (a prefix of the units) count no
+        // near-ties
+        unsigned long long *ties = lp.nearTies;
+        lp.nearTies = nullptr;
         rc = choose_variant(h, lp, (uint32_t)units, exactStack, setChunks, launchPair, &variant);
+        lp.nearTies = ties;
         if (rc != HPSS_OK) return rc;
         HPSS_CUDA_TRY(h, setChunks(2 * kVariantPairs[variant]));
-        // the timing launches counted near-ties of a prefix
-        HPSS_CUDA_TRY(h, cudaMemsetAsync(lp.nearTies, 0, sizeof(unsigned long long), h->stream));
         HPSS_CUDA_TRY(h, cudaEventRecord(h->ev1, h->stream));
     }
     if (pairKernel) {
@@ -529,6 +544,7 @@ hpss_status linear_search_impl(hpss_handle h, const float *d_m0s, uint32_t nM0,
         HPSS_CUDA_TRY(h, launch_ls_plain(lp, h->stream, h->precisionMode));
     }
     h->lastVariant = pairKernel ? variant : -1;
+    h->lastParts = pairKernel ? lastParts : octKernel ? octParts : 1;
     HPSS_CUDA_TRY(h, cudaEventRecord(h->ev2, h->stream));
 
     if (stats || sync) {
@@ -559,12 +575,160 @@ hpss_status linear_search_impl(hpss_handle h, const float *d_m0s, uint32_t nM0,
             stats->selection_ms = ms;
             stats->device_error = err;
             stats->kernel_variant = h->lastVariant;
-            stats->candidate_parts = pairKernel ? lastParts : octKernel ? octParts : 1;
+            stats->candidate_parts = h->lastParts;
         }
         if (err)
             return set_error(h, HPSS_ERR_DEVICE_CHECK,
                              "device check failed, error word " + std::to_string(err));
     }
+    return HPSS_OK;
+}
+
+// Body of hpss_linear_search_line, after prepare_line: the amplitudes go
+// to the device in kStreamChunks trace ranges on the copy stream, the
+// midpoints are searched in kStreamGroups contiguous groups on the handle's
+// stream, each group waiting only for the chunk that holds the last trace
+// its midpoints can select, and each group's results go back on the copy
+// stream while the next group runs.
+constexpr uint32_t kStreamChunks = 8, kStreamGroups = 8;
+
+cudaError_t copy_line_rows(hpss_handle h, const float *samples, uint32_t a, uint32_t b,
+                           cudaStream_t st);
+
+hpss_status stream_line_and_search(hpss_handle h, const float *samples, const float *m0s,
+                                   uint32_t nM0, const uint32_t *granularity, int kernel,
+                                   float *out, hpss_stats *stats) {
+    if (!h->copyStream)
+        HPSS_CUDA_TRY(h, cudaStreamCreateWithFlags(&h->copyStream, cudaStreamNonBlocking));
+    while (h->streamEvents.size() < kStreamChunks + kStreamGroups) {
+        cudaEvent_t e;
+        HPSS_CUDA_TRY(h, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        h->streamEvents.push_back(e);
+    }
+    if (!h->streamT0) HPSS_CUDA_TRY(h, cudaEventCreate(&h->streamT0));
+    if (!h->streamT1) HPSS_CUDA_TRY(h, cudaEventCreate(&h->streamT1));
+    cudaEvent_t *chunkDone = h->streamEvents.data();
+    cudaEvent_t *groupDone = chunkDone + kStreamChunks;
+    const uint32_t n = h->nTraces;
+    uint32_t bound[kStreamChunks + 1];
+    for (uint32_t k = 0; k <= kStreamChunks; k++)
+        bound[k] = (uint32_t)((uint64_t)n * k / kStreamChunks);
+    if (n && h->stride != h->S)
+        HPSS_CUDA_TRY(h, cudaMemsetAsync(h->dSamples, 0, (size_t)n * h->stride * sizeof(float),
+                                         h->copyStream));
+    for (uint32_t k = 0; k < kStreamChunks; k++) {
+        HPSS_CUDA_TRY(h, copy_line_rows(h, samples, bound[k], bound[k + 1], h->copyStream));
+        HPSS_CUDA_TRY(h, cudaEventRecord(chunkDone[k], h->copyStream));
+    }
+    // every search below waits for the chunks it reads
+    h->gatherReady = true;
+    if (nM0 == 0) {
+        HPSS_CUDA_TRY(h, cudaStreamSynchronize(h->copyStream));
+        HPSS_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+        if (stats) std::memset(stats, 0, sizeof(*stats));
+        return HPSS_OK;
+    }
+    const size_t block = (size_t)(2 + h->np) * h->S;
+    HPSS_CUDA_TRY(h, ensure(h, h->m0s, nM0 * sizeof(float)));
+    HPSS_CUDA_TRY(h, ensure(h, h->out, nM0 * block * sizeof(float)));
+    HPSS_CUDA_TRY(h, ensure(h, h->notUsed, 16 + nM0 * sizeof(unsigned long long)));
+    HPSS_CUDA_TRY(h, cudaMemcpyAsync(h->m0s.p, m0s, nM0 * sizeof(float),
+                                     cudaMemcpyHostToDevice, h->stream));
+    HPSS_CUDA_TRY(h, cudaMemsetAsync(h->notUsed.p, 0, 16 + nM0 * sizeof(unsigned long long),
+                                     h->stream));
+    HPSS_CUDA_TRY(h, cudaEventRecord(h->streamT0, h->stream));
+    // midpoint distance within which a trace can be selected, widened so that
+    // a group never starts before its traces have arrived
+    float hmax = 0.f;
+    for (float v : h->hHoff) hmax = std::max(hmax, std::fabs(v));
+    const float radius = h->model == HPSS_MODEL_CMP ? 0.f
+                         : h->model == HPSS_MODEL_ZOCRS
+                             ? h->apm
+                             : h->apm + std::sqrt(hmax * hmax + h->h0 * h->h0);
+    const uint32_t G = std::min(kStreamGroups, nM0);
+    auto first = [&](uint32_t g) { return (uint32_t)((uint64_t)nM0 * g / G); };
+    auto back = [&](uint32_t g) -> cudaError_t {
+        cudaError_t e = cudaStreamWaitEvent(h->copyStream, groupDone[g], 0);
+        if (e != cudaSuccess) return e;
+        const size_t i0 = first(g), cnt = first(g + 1) - i0;
+        return cudaMemcpyAsync(out + i0 * block, static_cast<float *>(h->out.p) + i0 * block,
+                               cnt * block * sizeof(float), cudaMemcpyDeviceToHost,
+                               h->copyStream);
+    };
+    for (uint32_t g = 0; g < G; g++) {
+        const uint32_t i0 = first(g), i1 = first(g + 1);
+        size_t need = 0;
+        for (uint32_t i = i0; i < i1 && need < n; i++) {
+            const float m0 = m0s[i];
+            if (!std::isfinite(m0)) {
+                need = n;
+                break;
+            }
+            const float reach = m0 + radius + 1e-3f * (std::fabs(m0) + radius) + 1.f;
+            need = std::max<size_t>(
+                need, std::upper_bound(h->hMid.begin(), h->hMid.end(), reach) - h->hMid.begin());
+        }
+        if (need > 0) {
+            uint32_t k = 0;
+            while (bound[k + 1] < need) k++;
+            HPSS_CUDA_TRY(h, cudaStreamWaitEvent(h->stream, chunkDone[k], 0));
+        }
+        const GroupOfCall grp{i0};
+        hpss_status rc = linear_search_impl(h, static_cast<float *>(h->m0s.p) + i0, i1 - i0,
+                                            granularity, kernel,
+                                            static_cast<float *>(h->out.p) + i0 * block, nullptr,
+                                            false, &grp);
+        if (rc != HPSS_OK) return rc;
+        HPSS_CUDA_TRY(h, cudaEventRecord(groupDone[g], h->stream));
+        // the previous group's results return while this group runs
+        if (g > 0) HPSS_CUDA_TRY(h, back(g - 1));
+    }
+    HPSS_CUDA_TRY(h, cudaEventRecord(h->streamT1, h->stream));
+    HPSS_CUDA_TRY(h, back(G - 1));
+    HPSS_CUDA_TRY(h, cudaStreamSynchronize(h->copyStream));
+    HPSS_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    const char *counters = static_cast<const char *>(h->notUsed.p);
+    uint32_t err = 0;
+    unsigned long long ties = 0;
+    HPSS_CUDA_TRY(h, cudaMemcpy(&err, counters, sizeof(err), cudaMemcpyDeviceToHost));
+    HPSS_CUDA_TRY(h, cudaMemcpy(&ties, counters + 8, sizeof(ties), cudaMemcpyDeviceToHost));
+    if (stats) {
+        std::memset(stats, 0, sizeof(*stats));
+        // selected traces of every midpoint, for the evaluation count
+        LsParams lp;
+        fill_line_params(h, lp);
+        lp.m0s = static_cast<float *>(h->m0s.p);
+        lp.nM0 = nM0;
+        hpss_status rc = run_selection(h, lp.m0s, nM0, lp);
+        if (rc != HPSS_OK) return rc;
+        std::vector<uint32_t> cnt(nM0);
+        std::vector<unsigned long long> nu(nM0);
+        HPSS_CUDA_TRY(h, cudaMemcpyAsync(cnt.data(), lp.selCount, nM0 * sizeof(uint32_t),
+                                         cudaMemcpyDeviceToHost, h->stream));
+        HPSS_CUDA_TRY(h, cudaMemcpyAsync(nu.data(), counters + 16,
+                                         nM0 * sizeof(unsigned long long),
+                                         cudaMemcpyDeviceToHost, h->stream));
+        HPSS_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+        double P = 1, sel = 0, nus = 0;
+        for (uint32_t j = 0; j < h->np; j++) P *= granularity[j];
+        for (uint32_t i = 0; i < nM0; i++) {
+            sel += cnt[i];
+            nus += (double)nu[i];
+        }
+        stats->selected_traces = sel;
+        stats->evals = sel * (double)h->S * P;
+        stats->not_used = nus;
+        float ms = 0;
+        cudaEventElapsedTime(&ms, h->streamT0, h->streamT1);
+        stats->kernel_ms = ms;
+        stats->device_error = err;
+        stats->kernel_variant = h->lastVariant;
+        stats->near_ties = (double)ties;
+        stats->candidate_parts = h->lastParts;
+    }
+    if (err)
+        return set_error(h, HPSS_ERR_DEVICE_CHECK,
+                         "device check failed, error word " + std::to_string(err));
     return HPSS_OK;
 }
 
@@ -674,6 +838,100 @@ hpss_status de_impl(hpss_handle h, const float *d_m0s, uint32_t nM0, uint32_t po
     return HPSS_OK;
 }
 
+// A new line, everything but the amplitudes: validation, host geometry,
+// device buffers (grown as needed) and the geometry copies on the handle's
+// stream.  The amplitudes follow with copy_line_rows.
+hpss_status prepare_line(hpss_handle h, const float *samples, const float *midpoints,
+                         const float *halfoffsets, uint32_t nTraces, uint32_t samplesPerTrace,
+                         float dtInSeconds, int storage) {
+    if (nTraces > 0 && (!samples || !midpoints || !halfoffsets))
+        return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "null input array");
+    if (samplesPerTrace == 0 || !(dtInSeconds > 0.f))
+        return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "samplesPerTrace and dt must be > 0");
+    // the tuned kernels take floor(t/dt) through a 2^23 offset add
+    if (samplesPerTrace > (1u << 22))
+        return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "samplesPerTrace must be <= 2^22");
+    if (storage < HPSS_STORAGE_FP32 || storage > HPSS_STORAGE_FP16)
+        return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "unknown storage");
+    for (uint32_t i = 0; i < nTraces; i++) {
+        float m = midpoints[i], o = halfoffsets[i];
+        if (!std::isfinite(m) || !std::isfinite(o))
+            return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "non-finite midpoint or half-offset");
+        if (i > 0) {
+            float pm = midpoints[i - 1], ph = halfoffsets[i - 1];
+            if (m < pm || (m == pm && o < ph))
+                return set_error(h, HPSS_ERR_INVALID_ARGUMENT,
+                                 "traces must be sorted by (midpoint, half-offset)");
+        }
+    }
+    cudaSetDevice(h->device);
+    // earlier work may still read the buffers about to be overwritten
+    cudaStreamSynchronize(h->stream);
+    if (h->copyStream) cudaStreamSynchronize(h->copyStream);
+    h->gatherReady = false;
+    h->octTabValid = false;
+    h->nTraces = nTraces;
+    h->S = samplesPerTrace;
+    h->stride = (samplesPerTrace + 7u) & ~7u;  // 32-byte rows
+    h->dt = dtInSeconds;
+    h->storage = storage;
+    h->hMid.assign(midpoints, midpoints + nTraces);
+    h->hHoff.assign(halfoffsets, halfoffsets + nTraces);
+    {
+        uint32_t distinct = 0;
+        for (uint32_t i = 0; i < nTraces; i++)
+            if (i == 0 || midpoints[i] != midpoints[i - 1]) distinct++;
+        h->meanFold = distinct ? nTraces / distinct : 0;
+    }
+    // h*h in float as the reference's host code; kept in the handle while
+    // its copy is in flight
+    h->hHsq.resize(nTraces);
+    for (uint32_t i = 0; i < nTraces; i++) h->hHsq[i] = halfoffsets[i] * halfoffsets[i];
+    const size_t n = nTraces, st = h->stride;
+    HPSS_CUDA_TRY(h, grow_line_buffer(h, reinterpret_cast<void **>(&h->dSamples), h->capSamples,
+                                      n * st * sizeof(float)));
+    if (storage != HPSS_STORAGE_FP32)
+        HPSS_CUDA_TRY(h, grow_line_buffer(h, reinterpret_cast<void **>(&h->dSamples16),
+                                          h->capSamples16, n * st * sizeof(uint16_t)));
+    // mid, hoff, hsq and the 16-bit storage scale: four 256-byte aligned
+    // slices of one buffer
+    const size_t slice = (n * sizeof(float) + 255) & ~size_t(255);
+    HPSS_CUDA_TRY(h, grow_line_buffer(h, &h->dTraceBuf, h->capTrace, 4 * slice));
+    char *tb = static_cast<char *>(h->dTraceBuf);
+    h->dMid = reinterpret_cast<float *>(tb);
+    h->dHoff = reinterpret_cast<float *>(tb + slice);
+    h->dHsq = reinterpret_cast<float *>(tb + 2 * slice);
+    h->dScale = reinterpret_cast<float *>(tb + 3 * slice);
+    if (n) {
+        HPSS_CUDA_TRY(h, cudaMemcpyAsync(h->dMid, midpoints, n * sizeof(float),
+                                         cudaMemcpyHostToDevice, h->stream));
+        HPSS_CUDA_TRY(h, cudaMemcpyAsync(h->dHoff, halfoffsets, n * sizeof(float),
+                                         cudaMemcpyHostToDevice, h->stream));
+        HPSS_CUDA_TRY(h, cudaMemcpyAsync(h->dHsq, h->hHsq.data(), n * sizeof(float),
+                                         cudaMemcpyHostToDevice, h->stream));
+    }
+    return HPSS_OK;
+}
+
+// Amplitudes of traces [a, b) on stream st: one copy when rows need no
+// padding, a pitched copy otherwise (the padding is zeroed by the caller),
+// then the 16-bit copy of those rows when the storage asks for one.
+cudaError_t copy_line_rows(hpss_handle h, const float *samples, uint32_t a, uint32_t b,
+                           cudaStream_t st) {
+    if (b <= a) return cudaSuccess;
+    const size_t S = h->S, pitch = h->stride, rows = b - a;
+    float *dst = h->dSamples + (size_t)a * pitch;
+    const float *src = samples + (size_t)a * S;
+    cudaError_t e = pitch == S
+                        ? cudaMemcpyAsync(dst, src, rows * S * sizeof(float),
+                                          cudaMemcpyHostToDevice, st)
+                        : cudaMemcpy2DAsync(dst, pitch * sizeof(float), src, S * sizeof(float),
+                                            S * sizeof(float), rows, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess || h->storage == HPSS_STORAGE_FP32) return e;
+    return launch_convert_storage(dst, h->dSamples16 + (size_t)a * pitch, h->dScale + a,
+                                  (uint32_t)rows, h->S, h->stride, h->storage, st);
+}
+
 }  // namespace
 
 namespace hpss {
@@ -737,6 +995,13 @@ hpss_status hpss_destroy(hpss_handle h) {
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
     if (h->ev2) cudaEventDestroy(h->ev2);
+    if (h->copyStream) {
+        cudaStreamSynchronize(h->copyStream);
+        cudaStreamDestroy(h->copyStream);
+    }
+    for (cudaEvent_t e : h->streamEvents) cudaEventDestroy(e);
+    if (h->streamT0) cudaEventDestroy(h->streamT0);
+    if (h->streamT1) cudaEventDestroy(h->streamT1);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
     return HPSS_OK;
@@ -751,79 +1016,13 @@ hpss_status hpss_upload_gather(hpss_handle h, const float *samples,
                                uint32_t nTraces, uint32_t samplesPerTrace,
                                float dtInSeconds, int storage) {
     if (!h) return HPSS_ERR_INVALID_ARGUMENT;
-    if (nTraces > 0 && (!samples || !midpoints || !halfoffsets))
-        return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "null input array");
-    if (samplesPerTrace == 0 || !(dtInSeconds > 0.f))
-        return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "samplesPerTrace and dt must be > 0");
-    // the tuned kernels take floor(t/dt) through a 2^23 offset add
-    if (samplesPerTrace > (1u << 22))
-        return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "samplesPerTrace must be <= 2^22");
-    if (storage < HPSS_STORAGE_FP32 || storage > HPSS_STORAGE_FP16)
-        return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "unknown storage");
-    for (uint32_t i = 0; i < nTraces; i++) {
-        float m = midpoints[i], o = halfoffsets[i];
-        if (!std::isfinite(m) || !std::isfinite(o))
-            return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "non-finite midpoint or half-offset");
-        if (i > 0) {
-            float pm = midpoints[i - 1], ph = halfoffsets[i - 1];
-            if (m < pm || (m == pm && o < ph))
-                return set_error(h, HPSS_ERR_INVALID_ARGUMENT,
-                                 "traces must be sorted by (midpoint, half-offset)");
-        }
-    }
-    cudaSetDevice(h->device);
-    cudaStreamSynchronize(h->stream);
-    h->gatherReady = false;
-    h->octTabValid = false;
-    h->nTraces = nTraces;
-    h->S = samplesPerTrace;
-    h->stride = (samplesPerTrace + 7u) & ~7u;  // 32-byte rows
-    h->dt = dtInSeconds;
-    h->storage = storage;
-    h->hMid.assign(midpoints, midpoints + nTraces);
-    h->hHoff.assign(halfoffsets, halfoffsets + nTraces);
-    {
-        uint32_t distinct = 0;
-        for (uint32_t i = 0; i < nTraces; i++)
-            if (i == 0 || midpoints[i] != midpoints[i - 1]) distinct++;
-        h->meanFold = distinct ? nTraces / distinct : 0;
-    }
-    std::vector<float> hsq(nTraces);
-    for (uint32_t i = 0; i < nTraces; i++) hsq[i] = halfoffsets[i] * halfoffsets[i];
-    const size_t n = nTraces, st = h->stride;
-    HPSS_CUDA_TRY(h, grow_line_buffer(h, reinterpret_cast<void **>(&h->dSamples), h->capSamples,
-                                      n * st * sizeof(float)));
-    // mid, hoff, hsq and the 16-bit storage scale: four 256-byte aligned
-    // slices of one buffer
-    const size_t slice = (n * sizeof(float) + 255) & ~size_t(255);
-    HPSS_CUDA_TRY(h, grow_line_buffer(h, &h->dTraceBuf, h->capTrace, 4 * slice));
-    char *tb = static_cast<char *>(h->dTraceBuf);
-    h->dMid = reinterpret_cast<float *>(tb);
-    h->dHoff = reinterpret_cast<float *>(tb + slice);
-    h->dHsq = reinterpret_cast<float *>(tb + 2 * slice);
-    h->dScale = reinterpret_cast<float *>(tb + 3 * slice);
-    if (n) {
-        if (st != samplesPerTrace)
-            HPSS_CUDA_TRY(h, cudaMemsetAsync(h->dSamples, 0, n * st * sizeof(float), h->stream));
-        HPSS_CUDA_TRY(h, cudaMemcpy2DAsync(h->dSamples, st * sizeof(float), samples,
-                                           samplesPerTrace * sizeof(float),
-                                           samplesPerTrace * sizeof(float), n,
-                                           cudaMemcpyHostToDevice, h->stream));
-        HPSS_CUDA_TRY(h, cudaMemcpyAsync(h->dMid, midpoints, n * sizeof(float),
-                                         cudaMemcpyHostToDevice, h->stream));
-        HPSS_CUDA_TRY(h, cudaMemcpyAsync(h->dHoff, halfoffsets, n * sizeof(float),
-                                         cudaMemcpyHostToDevice, h->stream));
-        HPSS_CUDA_TRY(h, cudaMemcpyAsync(h->dHsq, hsq.data(), n * sizeof(float),
-                                         cudaMemcpyHostToDevice, h->stream));
-    }
-    if (storage != HPSS_STORAGE_FP32) {
-        HPSS_CUDA_TRY(h, grow_line_buffer(h, reinterpret_cast<void **>(&h->dSamples16),
-                                          h->capSamples16, n * st * sizeof(uint16_t)));
-        HPSS_CUDA_TRY(h, launch_convert_storage(h->dSamples, h->dSamples16, h->dScale,
-                                                nTraces, samplesPerTrace, h->stride,
-                                                storage, h->stream));
-    }
-    // the host-side geometry vector `hsq` must outlive the async copy
+    hpss_status rc = prepare_line(h, samples, midpoints, halfoffsets, nTraces, samplesPerTrace,
+                                  dtInSeconds, storage);
+    if (rc != HPSS_OK) return rc;
+    if (nTraces && h->stride != h->S)
+        HPSS_CUDA_TRY(h, cudaMemsetAsync(h->dSamples, 0,
+                                         (size_t)nTraces * h->stride * sizeof(float), h->stream));
+    HPSS_CUDA_TRY(h, copy_line_rows(h, samples, 0, nTraces, h->stream));
     HPSS_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
     h->gatherReady = true;
     return HPSS_OK;
@@ -915,6 +1114,32 @@ hpss_status hpss_linear_search(hpss_handle h, const float *m0s, uint32_t nM0,
                                      cudaMemcpyDeviceToHost, h->stream));
     HPSS_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
     return HPSS_OK;
+}
+
+hpss_status hpss_linear_search_line(hpss_handle h, const float *samples,
+                                    const float *midpoints, const float *halfoffsets,
+                                    uint32_t nTraces, uint32_t samplesPerTrace,
+                                    float dtInSeconds, int storage, const float *m0s,
+                                    uint32_t nM0, const uint32_t *granularity, int kernel,
+                                    float *out, hpss_stats *stats) {
+    if (!h) return HPSS_ERR_INVALID_ARGUMENT;
+    if (nM0 && (!m0s || !out))
+        return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "null host pointer");
+    if (h->model < 0 || h->tau < 0)
+        return set_error(h, HPSS_ERR_NOT_READY,
+                         "traveltime and window must be set before the line");
+    if (!granularity) return set_error(h, HPSS_ERR_LOGIC, "granularity is required");
+    hpss_status rc = prepare_line(h, samples, midpoints, halfoffsets, nTraces, samplesPerTrace,
+                                  dtInSeconds, storage);
+    if (rc != HPSS_OK) return rc;
+    rc = stream_line_and_search(h, samples, m0s, nM0, granularity, kernel, out, stats);
+    if (rc != HPSS_OK) {
+        // leave no half-copied line behind
+        cudaStreamSynchronize(h->copyStream);
+        cudaStreamSynchronize(h->stream);
+        h->gatherReady = false;
+    }
+    return rc;
 }
 
 hpss_status hpss_select_traces(hpss_handle h, const float *m0s, uint32_t nM0,

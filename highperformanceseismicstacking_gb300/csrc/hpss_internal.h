@@ -128,7 +128,12 @@ struct Handle {
     // allocated bytes of the line buffers, kept across uploads that fit
     void *dTraceBuf = nullptr;
     size_t capSamples = 0, capSamples16 = 0, capTrace = 0;
-    std::vector<float> hMid, hHoff;
+    std::vector<float> hMid, hHoff, hHsq;
+    // second stream and events of the streamed line upload
+    // (hpss_linear_search_line): amplitude chunks arrive on copyStream
+    cudaStream_t copyStream = nullptr;
+    std::vector<cudaEvent_t> streamEvents;
+    cudaEvent_t streamT0 = nullptr, streamT1 = nullptr;  // timed span of a streamed call
     // traveltime
     int model = -1;
     uint32_t np = 0;

@@ -183,6 +183,28 @@ hpss_status hpss_linear_search(hpss_handle h, const float *m0s, uint32_t nM0,
                                const uint32_t *granularity, int kernel,
                                float *out, hpss_stats *stats);
 
+/* Upload a line and search it in one call, the upload overlapped with the
+ * search: the amplitudes go to the device in 8 trace ranges on a second
+ * stream while the midpoints are searched in 8 contiguous groups, each group
+ * starting as soon as the traces it can select have arrived, and each
+ * group's results are copied back while the next group runs.  The line
+ * replaces the resident one as hpss_upload_gather would (same arguments and
+ * checks); the traveltime and the window must be set before.  Results,
+ * statistics and errors are those of hpss_upload_gather followed by
+ * hpss_linear_search, except stats->kernel_ms (device time from the first
+ * group's start to the last group's end, copies overlapped) and
+ * stats->selection_ms (0).  Host arrays must stay unchanged until it
+ * returns.  The reference copies the selected traces of every midpoint
+ * before its search (ComputeAlgorithm::copyOnlySelectedTracesToDevice,
+ * common/src/semblance/algorithm/ComputeAlgorithm.cpp:107-153); this call
+ * replaces that per-midpoint copy for a whole line. */
+hpss_status hpss_linear_search_line(hpss_handle h, const float *samples,
+                                    const float *midpoints, const float *halfoffsets,
+                                    uint32_t nTraces, uint32_t samplesPerTrace,
+                                    float dtInSeconds, int storage, const float *m0s,
+                                    uint32_t nM0, const uint32_t *granularity, int kernel,
+                                    float *out, hpss_stats *stats);
+
 /* Same computation with device-resident midpoints and output (d_m0s,
  * d_out are device pointers).  Enqueued on the handle's stream; returns
  * without synchronising.  stats may be NULL (its timing fields are then not

@@ -336,3 +336,51 @@ def test_reupload_reuses_line_buffers(engine):
             with capi.Engine(0) as fresh:
                 want = run(fresh, line, storage)
             assert np.array_equal(got, want), (line.samples.shape, storage)
+
+
+def _line_cases():
+    cmp_line = synthetic.cmp_line(n_cmp=20, halfoffsets=list(range(25, 1176, 50)), ns=301,
+                                  dt_us=4000, n_reflectors=4, n_multiples=0, f=25.0, snr=10.0,
+                                  seed=41)
+    w = synthetic.WORKLOADS["cmp-small"]
+    zl = synthetic.structured_line(n_cmp=30, fold_range=(8, 14), h_max=1000, ns=300,
+                                   dt_us=4000, n_reflectors=4, f=20.0, snr=5.0, seed=42)
+    a, b = synthetic.zocrs_bounds(1414.2136, 2000.0, 90.0, 0.05)
+    ol = synthetic.structured_line(n_cmp=16, fold_range=(4, 8), h_max=800, ns=200,
+                                   dt_us=4000, n_reflectors=3, f=20.0, snr=8.0, seed=43)
+    return [("cmp", cmp_line, w.lower, w.upper, w.granularity, 0.0, 0.0),
+            ("zocrs", zl, [1414.2136, -a, -b], [6324.5553, a, b], [5, 5, 5], 125.0, 0.0),
+            ("oct", ol, [1200.0, -1e-3], [5000.0, 1e-3], [6, 5], 60.0, 300.0)]
+
+
+@pytest.mark.parametrize("storage", ["fp32", "bf16"])
+def test_linear_search_line_equals_upload_then_search(storage):
+    """hpss_linear_search_line (upload streamed in trace ranges, midpoints
+    searched in groups as their traces arrive) gives the blocks and
+    statistics of hpss_upload_gather followed by hpss_linear_search, for all
+    three models, rows with padding (301 samples), calls with more and fewer
+    midpoints than groups and a midpoint outside the line; the line stays
+    resident afterwards."""
+    tau = 2
+    for model, line, lower, upper, gran, apm, h0 in _line_cases():
+        for m0s in (line.cdp_midpoints,
+                    np.concatenate([line.cdp_midpoints[3:5], [np.float32(-777.0)]])):
+            with capi.Engine(0) as ref_eng, capi.Engine(0) as eng:
+                _setup(ref_eng, line, model, lower, upper, tau, apm, h0)
+                ref_eng.upload_gather(line.samples, line.midpoints, line.halfoffsets,
+                                      float(line.dt), storage=storage)
+                want, st_w = ref_eng.linear_search(m0s, gran, "tuned")
+                eng.set_traveltime(model, lower, upper, apm, h0)
+                eng.set_window(tau)
+                got, st = eng.linear_search_line(line.samples, line.midpoints, line.halfoffsets,
+                                                 float(line.dt), m0s, gran, "tuned", storage)
+                assert np.array_equal(got, want), (model, storage, m0s.size)
+                for k in ("evals", "selected_traces", "not_used", "near_ties", "device_error"):
+                    assert st[k] == st_w[k], (model, k, st[k], st_w[k])
+                again, _ = eng.linear_search(m0s, gran, "tuned")
+                assert np.array_equal(again, want)
+                plain, _ = eng.linear_search_line(line.samples, line.midpoints,
+                                                  line.halfoffsets, float(line.dt), m0s, gran,
+                                                  "plain", storage)
+                want_plain, _ = ref_eng.linear_search(m0s, gran, "plain")
+                assert np.array_equal(plain, want_plain), (model, storage, "plain")
