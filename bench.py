@@ -8,9 +8,10 @@ Workload (default): CMP linear search at production size -- 2000 CMPs, fold
   value : device-resident line and midpoints, the tuned kernel, timed with CUDA
           events on the engine's stream (the line, 960 MB, exceeds the 129 MB L2
           so no flush is needed between steps);
-  e2e   : the same step through the public C ABI with host buffers: upload the
-          line from page-locked memory (hpss_upload_gather), search
-          (hpss_linear_search), results copied back to the host;
+  e2e   : the same step through the public C ABI with host buffers, one call of
+          hpss_linear_search_line: the line goes up from page-locked memory in
+          trace ranges while the midpoints whose traces have arrived are
+          searched, and the results come back to a page-locked block;
   plain : the plain one-(sample, candidate)-per-thread FP32 kernel, same line.
 
 `--impl reference` times the reference algorithm on the host CPU (the oracle's
@@ -432,7 +433,10 @@ def main():
         eng.linear_search_device(d_m0.data_ptr(), len(m0s), w.granularity, d_out.data_ptr(),
                                  kernel)
 
-    launches_per_step = 4  # grid, chunk bounds, selection, semblance kernel
+    # per timed step: trace selection + the semblance kernel (the candidate
+    # grid and chunk bounds were built by the warm-up calls and are reused;
+    # the batched call is not split into candidate ranges, so no merge)
+    launches_per_step = 2
     # ---- tuned, device resident
     for _ in range(args.warmup):
         run("tuned")
