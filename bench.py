@@ -210,6 +210,11 @@ def zocrs_side_measure(n_cmp, local):
     storage = storage_side(eng, line, stream, d_m0, len(m0s), w.granularity, evals,
                            outs["tuned"])
     eng.close()
+    # FP32-pipe roofline of the tuned kernel (3w + 5 instructions per eval)
+    props = torch.cuda.get_device_properties(dev)
+    peak = props.multi_processor_count * 128 * float(measured_peaks().get("sm_max_mhz", 2070.0)) * 1e6
+    instr = 3 * (2 * tau + 1) + 5
+    res["tuned"]["roofline_frac"] = res["tuned"]["value"] * instr / peak
     return {"workload": "zocrs-ls", "cmps": int(len(m0s)), "evals": evals,
             "candidates": P, "mean_traces_per_midpoint": evals / P / line.samples_per_trace / len(m0s),
             "tuned": res["tuned"], "plain": res["plain"],

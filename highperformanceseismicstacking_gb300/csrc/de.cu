@@ -111,9 +111,54 @@ __device__ __forceinline__ void de_eval(const DeParams &d, float t0, float m0, u
     for (int j = 0; j < (W > 0 ? W : kMaxWindow); j++) num[j] = 0.f;
     float lin = 0.f, den = 0.f;
     unsigned used = 0, nu = 0;
+    uint32_t q = 0;
+    if (MODEL != kModelOct && W > 0 && !a.selIdx) {
+        // CMP / ZO-CRS: two traces per step -- both traveltimes and both
+        // windows' loads are issued before the sums, which then take the
+        // traces in order (the same sums as one trace at a time)
+        for (; q + 1 < cnt; q += 2) {
+            const uint32_t ti0 = first + q, ti1 = ti0 + 1;
+            float ta = 0.f, tb = 0.f;
+            const bool oka = model_time<MODEL>(t0, c, p1, p2, a.mid[ti0], a.hoff[ti0],
+                                               a.hsq[ti0], m0, a.apm, a.h0, &ta) > 0;
+            const bool okb = model_time<MODEL>(t0, c, p1, p2, a.mid[ti1], a.hoff[ti1],
+                                               a.hsq[ti1], m0, a.apm, a.h0, &tb) > 0;
+            const WinIdx wa = window_index(ta, a.dt), wb = window_index(tb, a.dt);
+            const bool ina = oka && window_in_trace(wa.k, a.tau, (int)a.S);
+            const bool inb = okb && window_in_trace(wb.k, a.tau, (int)a.S);
+            float ya[W > 0 ? W + 1 : 1], yb[W > 0 ? W + 1 : 1];
+            const float *tra = a.samples + (size_t)ti0 * a.stride + (ina ? wa.k - a.tau : 0);
+            const float *trb = a.samples + (size_t)ti1 * a.stride + (inb ? wb.k - a.tau : 0);
+#pragma unroll
+            for (int j = 0; j <= W; j++) {
+                ya[j] = ina ? __ldg(tra + j) : 0.f;
+                yb[j] = inb ? __ldg(trb + j) : 0.f;
+            }
+            if (ina) {
+#pragma unroll
+                for (int j = 0; j < W; j++) {
+                    float u = (ya[j + 1] - ya[j]) * wa.frac + ya[j];
+                    num[j] += u;
+                    lin += u;
+                    den += u * u;
+                }
+                used++;
+            }
+            if (inb) {
+#pragma unroll
+                for (int j = 0; j < W; j++) {
+                    float u = (yb[j + 1] - yb[j]) * wb.frac + yb[j];
+                    num[j] += u;
+                    lin += u;
+                    den += u * u;
+                }
+                used++;
+            }
+        }
+    }
     // OCT: (t0, candidate) factors once, trace factors from the line's table
     const OctCand kc = oct_cand(t0, c, p1, MODEL == kModelOct ? a.h0 : 0.f);
-    for (uint32_t q = 0; q < cnt; q++) {
+    for (; q < cnt; q++) {
         const uint32_t ti = a.selIdx ? a.selIdx[first + q] : first + q;
         float t;
         int ok;
@@ -161,10 +206,12 @@ constexpr int kDeThreads = 256;
 
 // OCT: six resident CTAs per SM (40 registers) -- its evaluation waits on
 // long dependent square-root / reciprocal chains, so resident warps pay
-// (3.5 % on the OCT DE workload); CMP / ZO-CRS keep their registers (a
-// 6-CTA bound costs them 10 %).
+// (3.5 % on the OCT DE workload).  CMP / ZO-CRS: four (64 registers), which
+// their two-trace steps fit without spills (ZO-CRS DE, 2 midpoints: 41.9 ->
+// 38.1 ms; 16 midpoints unchanged; three- or four-trace steps and a 6-CTA
+// bound are slower).
 template <int MODEL, int W>
-__global__ void __launch_bounds__(kDeThreads, MODEL == kModelOct ? 6 : 1)
+__global__ void __launch_bounds__(kDeThreads, MODEL == kModelOct ? 6 : 4)
 de_kernel(DeParams d, uint32_t spc, uint32_t groups, uint32_t nUnits) {
     constexpr int NP = MODEL == kModelCmp ? 1 : (MODEL == kModelZocrs ? 3 : 2);
     const LsParams &a = d.ls;
