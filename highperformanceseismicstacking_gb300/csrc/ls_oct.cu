@@ -12,7 +12,8 @@
 //    have nearly the same displaced midpoint and window position, so the skip
 //    decisions agree across the warp and the window loads fall on a few
 //    cache lines of one trace row;
-//  * a warp evaluates R candidates per thread (independent chains);
+//  * a thread evaluates R candidates (R = 1: resident warps, not chains in
+//    one thread, hide the latency);
 //  * the candidate range is split into `parts` (CTAs work on (midpoint,
 //    32-sample tile, part) units) so that a call with few midpoints still
 //    fills the GPU; each unit writes the best / runner-up of its part and
@@ -30,10 +31,15 @@ namespace hpss {
 
 constexpr int kOctWarps = 8;
 
-// Four resident CTAs per SM (64 registers, no spills): the kernel waits on
-// dependent square-root / reciprocal chains, so resident warps pay.
+// One candidate per thread at five resident CTAs per SM (48 registers, no
+// spills): the kernel waits on dependent square-root / reciprocal chains, so
+// resident warps pay more than independent chains in one thread, and the
+// smaller candidate chunks give small calls more units.  Against two
+// candidates per thread at four CTAs per SM (OCT DE line geometry): 11 x 5
+// candidates 4.07 -> 3.10 ms on one midpoint, 12.1 -> 10.0 ms on four;
+// 41 x 11 candidates 88.6 -> 83.7 ms on four midpoints, within 2 % on one.
 template <int W, int R>
-__global__ void __launch_bounds__(kOctWarps * 32, 4)
+__global__ void __launch_bounds__(kOctWarps * 32, 5)
 ls_oct_kernel(LsParams a, uint32_t tiles, uint32_t parts, uint32_t chunksPerPart,
               uint32_t nUnits, PartBest *partial) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -252,7 +258,7 @@ cudaError_t launch_oct_w(const LsParams &p, uint32_t numSms, void *partial, uint
 // Parts: enough (midpoint, tile, part) units for ~8 waves of the GPU, never
 // more than the candidate chunks.
 uint32_t oct_parts(const LsParams &p, uint32_t numSms) {
-    constexpr int R = 2;
+    constexpr int R = 1;
     const uint32_t tiles = (p.S + 31) / 32;
     const uint64_t base = (uint64_t)p.nM0 * tiles;
     const uint64_t want = (uint64_t)numSms * 2 * 8;
@@ -262,7 +268,7 @@ uint32_t oct_parts(const LsParams &p, uint32_t numSms) {
 
 cudaError_t launch_ls_oct(const LsParams &p, uint32_t numSms, void *partial, uint32_t parts,
                           cudaStream_t st) {
-    constexpr int R = 2;
+    constexpr int R = 1;
     switch (p.w) {
         case 1: return launch_oct_w<1, R>(p, numSms, partial, parts, st);
         case 3: return launch_oct_w<3, R>(p, numSms, partial, parts, st);
