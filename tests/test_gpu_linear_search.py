@@ -384,3 +384,24 @@ def test_linear_search_line_equals_upload_then_search(storage):
                                                   "plain", storage)
                 want_plain, _ = ref_eng.linear_search(m0s, gran, "plain")
                 assert np.array_equal(plain, want_plain), (model, storage, "plain")
+
+
+@pytest.mark.parametrize("ns, tau, tuned_runs", [(16376, 3, True), (16377, 3, False),
+                                                 (2000, 15, False)])
+def test_size_limits_of_the_tuned_kernel(engine, ns, tau, tuned_runs):
+    """Sizes at the tuned kernel's limits: a trace row must fit its shared-
+    memory stage (stride + 8 <= 16384 floats) and the window must be at most
+    15 samples; beyond either the tuned call runs the plain kernel
+    (kernel_variant -1).  Either way the results are the plain kernel's
+    (semblance and chosen parameters bit for bit, stack within parity)."""
+    w = synthetic.WORKLOADS["cmp-small"]
+    line = synthetic.cmp_line(n_cmp=2, halfoffsets=list(range(25, 1176, 50)), ns=ns, dt_us=250,
+                              n_reflectors=6, n_multiples=0, f=25.0, snr=10.0, seed=51)
+    _setup(engine, line, "cmp", w.lower, w.upper, tau)
+    m0s = line.cdp_midpoints
+    tuned, st = engine.linear_search(m0s, [61], "tuned")
+    plain, st_p = engine.linear_search(m0s, [61], "plain")
+    assert st["device_error"] == 0 and st_p["device_error"] == 0
+    assert (st["kernel_variant"] >= 0) == tuned_runs, st["kernel_variant"]
+    assert_same_but_stack(tuned, plain, 1)
+    assert st["near_ties"] == st_p["near_ties"]
