@@ -133,11 +133,55 @@ struct Tuned2Smem {
     int ti[kTunedThreads];
     int warpSum[kTunedWarps];
     int warpKeep[kTunedWarps];
+    int warpLen[kTunedWarps];  // staged floats of the warp's kept traces
     float bestS[kTunedWarps][kTileSamples];
     float bestK[kTunedWarps][kTileSamples];
     uint32_t bestP[kTunedWarps][kTileSamples];
     float bestSec[kTunedWarps][kTileSamples];
+    unsigned long long stageBar;  // mbarrier of the bulk copies of a staging round
 };
+
+// Bulk (TMA) copies of the FP32 trace spans into the stage.  One thread
+// registers the round's byte count on the mbarrier; the lane that owns a
+// span issues one cp.async.bulk for it (16-byte aligned addresses, size a
+// multiple of 16 bytes), which counts its bytes off the same barrier.
+__device__ __forceinline__ uint32_t smem_addr(const void *p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void stage_bar_init(unsigned long long *bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
+}
+__device__ __forceinline__ void stage_bar_expect(unsigned long long *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void stage_bulk_copy(void *dst, const void *src, uint32_t bytes,
+                                                unsigned long long *bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+            "r"(smem_addr(dst)),
+        "l"(src), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
+// true once the barrier's phase `parity` has completed
+__device__ __forceinline__ bool stage_bar_try_wait(unsigned long long *bar, uint32_t parity) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+// Bounded wait for phase `parity`; false when it did not complete in time.
+__device__ __forceinline__ bool stage_bar_wait(unsigned long long *bar, uint32_t parity) {
+    for (uint32_t it = 0; it < (1u << 22); it++)
+        if (stage_bar_try_wait(bar, parity)) return true;
+    return false;
+}
 
 __device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
 
@@ -171,6 +215,9 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
     const int magicTau = 0x4B000000 + tau;                  // bits of 2^23, plus tau
 
     if (threadIdx.x < kZeroPad) sm.y[threadIdx.x] = 0.f;
+    if (threadIdx.x == 0) stage_bar_init(&sm.stageBar);
+    __syncthreads();
+    uint32_t stagePhase = 0;  // parity of the staging barrier's current phase
 
     for (uint32_t unit = blockIdx.x; unit < nUnits; unit += gridDim.x) {
         // unit = (midpoint, tile, candidate part), part fastest
@@ -261,7 +308,11 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
                 // others so the evaluation loop has no per-trace branch
                 const bool keep = fits && len > 0;
                 const unsigned keepMask = __ballot_sync(0xffffffffu, keep);
-                if (lane == 0) sm.warpKeep[warp] = __popc(keepMask);
+                const int keptLen = __reduce_add_sync(0xffffffffu, keep ? len : 0);
+                if (lane == 0) {
+                    sm.warpKeep[warp] = __popc(keepMask);
+                    sm.warpLen[warp] = keptLen;
+                }
                 const int nfit = __syncthreads_count(fits);
                 int slot = __popc(keepMask & ((1u << lane) - 1u));
 #pragma unroll
@@ -284,16 +335,37 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
                     break;
                 }
                 __syncthreads();
-                for (int j = warp; j < nkeep; j += kTunedWarps) {
+                if (a.samples16 == nullptr) {
+                    // FP32: one bulk copy per span on the TMA engine, the
+                    // round's bytes counted off the staging barrier
+                    if (threadIdx.x == 0) {
+                        uint32_t floats = 0;
+#pragma unroll
+                        for (int wv = 0; wv < kTunedWarps; wv++) floats += (uint32_t)sm.warpLen[wv];
+                        stage_bar_expect(&sm.stageBar, floats * 4u);
+                    }
+                    if (keep) {
+                        // the previous round's reads of the stage are ordered
+                        // before the async-proxy writes
+                        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                        const uint32_t ti = a.selIdx ? a.selIdx[first + q] : first + q;
+                        stage_bulk_copy(sm.y + off, a.samples + (size_t)ti * a.stride + lo,
+                                        (uint32_t)len * 4u, &sm.stageBar);
+                    }
+                    const bool ok = stage_bar_wait(&sm.stageBar, stagePhase);
+                    stagePhase ^= 1u;
+                    if (__syncthreads_or(!ok)) {
+                        // copies did not complete in time: report and leave
+                        if (threadIdx.x == 0) atomicOr(a.errorWord, kErrTimeout);
+                        stage_bar_wait(&sm.stageBar, stagePhase ^ 1u);
+                        return;
+                    }
+                }
+                for (int j = warp; j < nkeep && a.samples16 != nullptr; j += kTunedWarps) {
                     const TraceMeta2 md = sm.meta[j];
                     const int lo_j = sm.lo[j];
                     float4 *dst = reinterpret_cast<float4 *>(sm.y + md.base + lo_j);
-                    if (a.samples16 == nullptr) {
-                        const float4 *src = reinterpret_cast<const float4 *>(
-                            a.samples + (size_t)sm.ti[j] * a.stride + lo_j);
-                        for (int v = lane; v < ((md.len & kLenMask) >> 2); v += 32)
-                            dst[v] = __ldg(src + v);
-                    } else {
+                    {
                         // 16-bit storage: 4 samples per 8-byte load, widened to FP32
                         const uint2 *src = reinterpret_cast<const uint2 *>(
                             a.samples16 + (size_t)sm.ti[j] * a.stride + lo_j);
