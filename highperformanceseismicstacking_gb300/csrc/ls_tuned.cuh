@@ -35,8 +35,8 @@ namespace hpss {
 
 // Sample span [lo, lo+len) of trace (m, h, hsq) touched by any in-trace
 // window of the tile [t0a, t0b] and the chunk parameter box.  Conservative by
-// one sample each side; rounded to multiples of `align` samples so that the
-// copy starts and ends on 16-byte boundaries.  len = 0 if no window of the tile/chunk can lie inside the trace.
+// one sample each side; rounded to multiples of 4 samples (16 B) for vector
+// copies.  len = 0 if no window of the tile/chunk can lie inside the trace.
 // *full (optional): every window of the tile and chunk box lies inside the
 // trace (for ZO-CRS also: every squared time is positive), judged on the same
 // conservative bounds, so the evaluation may skip the per-candidate checks.
@@ -44,7 +44,7 @@ template <int MODEL>
 __device__ __forceinline__ void trace_span(const LsParams &a, const float *cb,
                                            float m0, float t0a, float t0b,
                                            float m, float hsq, int *lo,
-                                           int *len, bool *full = nullptr, int align = 4) {
+                                           int *len, bool *full = nullptr) {
     const int S = (int)a.S, tau = a.tau;
     int kmin, kmax;
     bool positive = true;
@@ -90,11 +90,9 @@ __device__ __forceinline__ void trace_span(const LsParams &a, const float *cb,
         if (full) *full = false;
         return;
     }
-    // a multiple of `align` samples at both ends (16-byte copies of FP32 or
-    // 16-bit rows; the row stride is a multiple of 8 samples for 16-bit rows)
-    int l = (kmin - tau) & -align;
-    int h = kmax + tau + 1;                        // last sample read
-    int e = min((h + align) & -align, (int)a.stride);  // exclusive
+    int l = (kmin - tau) & ~3;
+    int h = kmax + tau + 1;                  // last sample read
+    int e = min((h + 4) & ~3, (int)a.stride); // exclusive, multiple of 4
     *lo = l;
     *len = e - l;
 }
@@ -220,7 +218,6 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
     if (threadIdx.x == 0) stage_bar_init(&sm.stageBar);
     __syncthreads();
     uint32_t stagePhase = 0;  // parity of the staging barrier's current phase
-    const bool wide = a.samples16 == nullptr;  // FP32 rows (else 16-bit rows)
 
     for (uint32_t unit = blockIdx.x; unit < nUnits; unit += gridDim.x) {
         // unit = (midpoint, tile, candidate part), part fastest
@@ -291,8 +288,7 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
                     const uint32_t ti = a.selIdx ? a.selIdx[first + q] : first + q;
                     tm = a.mid[ti];
                     thsq = a.hsq[ti];
-                    trace_span<MODEL>(a, cbl, m0, t0a, t0b, tm, thsq, &lo, &len, &full,
-                                      wide ? 4 : 8);
+                    trace_span<MODEL>(a, cbl, m0, t0a, t0b, tm, thsq, &lo, &len, &full);
                 }
                 int incl = len;
 #pragma unroll
@@ -307,12 +303,7 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
                 for (int wv = 0; wv < kTunedWarps; wv++)
                     woff += wv < warp ? sm.warpSum[wv] : 0;
                 const int off = woff + incl - len;
-                // 16-bit rows: the raw spans sit at the top of the stage,
-                // growing down (a span ending at float `end` has its raw copy
-                // at kStage - (end - kZeroPad) / 2), below them nothing is free
-                const bool fits = (q < cnt) &&
-                                  (wide ? off + len <= kStage
-                                        : 3 * (off + len) - kZeroPad <= 2 * kStage);
+                const bool fits = (q < cnt) && (off + len <= kStage);
                 // traces whose span is empty contribute nothing: compact the
                 // others so the evaluation loop has no per-trace branch
                 const bool keep = fits && len > 0;
@@ -344,28 +335,22 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
                     break;
                 }
                 __syncthreads();
-                {
-                    // one bulk copy per span on the TMA engine (FP32 rows into
-                    // the span's place; 16-bit rows raw into the top of the
-                    // stage), the round's bytes counted off the staging barrier
+                if (a.samples16 == nullptr) {
+                    // FP32: one bulk copy per span on the TMA engine, the
+                    // round's bytes counted off the staging barrier
                     if (threadIdx.x == 0) {
                         uint32_t floats = 0;
 #pragma unroll
                         for (int wv = 0; wv < kTunedWarps; wv++) floats += (uint32_t)sm.warpLen[wv];
-                        stage_bar_expect(&sm.stageBar, floats * (wide ? 4u : 2u));
+                        stage_bar_expect(&sm.stageBar, floats * 4u);
                     }
                     if (keep) {
                         // the previous round's reads of the stage are ordered
                         // before the async-proxy writes
                         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                         const uint32_t ti = a.selIdx ? a.selIdx[first + q] : first + q;
-                        if (wide)
-                            stage_bulk_copy(sm.y + off, a.samples + (size_t)ti * a.stride + lo,
-                                            (uint32_t)len * 4u, &sm.stageBar);
-                        else
-                            stage_bulk_copy(sm.y + kStage - (off + len - kZeroPad) / 2,
-                                            a.samples16 + (size_t)ti * a.stride + lo,
-                                            (uint32_t)len * 2u, &sm.stageBar);
+                        stage_bulk_copy(sm.y + off, a.samples + (size_t)ti * a.stride + lo,
+                                        (uint32_t)len * 4u, &sm.stageBar);
                     }
                     const bool ok = stage_bar_wait(&sm.stageBar, stagePhase);
                     stagePhase ^= 1u;
@@ -376,27 +361,27 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
                         return;
                     }
                 }
-                // 16-bit rows: widen the raw spans into their FP32 places
-                for (int j = warp; j < nkeep && !wide; j += kTunedWarps) {
+                for (int j = warp; j < nkeep && a.samples16 != nullptr; j += kTunedWarps) {
                     const TraceMeta2 md = sm.meta[j];
                     const int lo_j = sm.lo[j];
-                    const int len_j = md.len & kLenMask;
-                    const int off_j = md.base + lo_j;
-                    float4 *dst = reinterpret_cast<float4 *>(sm.y + off_j);
-                    const uint2 *src = reinterpret_cast<const uint2 *>(
-                        sm.y + kStage - (off_j + len_j - kZeroPad) / 2);
-                    const float sc = a.storage == 2 ? a.scale[sm.ti[j]] : 1.f;
-                    for (int v = lane; v < (len_j >> 2); v += 32) {
-                        const uint2 q = src[v];
-                        dst[v] = a.storage == 2
-                                     ? make_float4(half_bits_to_float(q.x & 0xffffu) * sc,
-                                                   half_bits_to_float(q.x >> 16) * sc,
-                                                   half_bits_to_float(q.y & 0xffffu) * sc,
-                                                   half_bits_to_float(q.y >> 16) * sc)
-                                     : make_float4(__uint_as_float(q.x << 16),
-                                                   __uint_as_float(q.x & 0xffff0000u),
-                                                   __uint_as_float(q.y << 16),
-                                                   __uint_as_float(q.y & 0xffff0000u));
+                    float4 *dst = reinterpret_cast<float4 *>(sm.y + md.base + lo_j);
+                    {
+                        // 16-bit storage: 4 samples per 8-byte load, widened to FP32
+                        const uint2 *src = reinterpret_cast<const uint2 *>(
+                            a.samples16 + (size_t)sm.ti[j] * a.stride + lo_j);
+                        const float sc = a.storage == 2 ? a.scale[sm.ti[j]] : 1.f;
+                        for (int v = lane; v < ((md.len & kLenMask) >> 2); v += 32) {
+                            const uint2 q = __ldg(src + v);
+                            dst[v] = a.storage == 2
+                                         ? make_float4(half_bits_to_float(q.x & 0xffffu) * sc,
+                                                       half_bits_to_float(q.x >> 16) * sc,
+                                                       half_bits_to_float(q.y & 0xffffu) * sc,
+                                                       half_bits_to_float(q.y >> 16) * sc)
+                                         : make_float4(__uint_as_float(q.x << 16),
+                                                       __uint_as_float(q.x & 0xffff0000u),
+                                                       __uint_as_float(q.y << 16),
+                                                       __uint_as_float(q.y & 0xffff0000u));
+                        }
                     }
                 }
                 __syncthreads();
