@@ -645,8 +645,13 @@ hpss_status stream_line_and_search(hpss_handle h, const float *samples, const fl
                          : h->model == HPSS_MODEL_ZOCRS
                              ? h->apm
                              : h->apm + std::sqrt(hmax * hmax + h->h0 * h->h0);
-    const uint32_t G = std::min(kStreamGroups, nM0);
-    auto first = [&](uint32_t g) { return (uint32_t)((uint64_t)nM0 * g / G); };
+    // groups of ceil(nM0 / kStreamGroups) midpoints, the last one smaller: the
+    // first group is the largest, so the per-call buffers the search grows
+    // (selection, candidate parts) are sized by it and never reallocated
+    // under a later group's launches
+    const uint32_t per = (nM0 + kStreamGroups - 1) / kStreamGroups;
+    const uint32_t G = (nM0 + per - 1) / per;
+    auto first = [&](uint32_t g) { return std::min(g * per, nM0); };
     auto back = [&](uint32_t g) -> cudaError_t {
         cudaError_t e = cudaStreamWaitEvent(h->copyStream, groupDone[g], 0);
         if (e != cudaSuccess) return e;
