@@ -438,10 +438,11 @@ def main():
         eng.linear_search_device(d_m0.data_ptr(), len(m0s), w.granularity, d_out.data_ptr(),
                                  kernel)
 
-    # per timed step: trace selection + the semblance kernel (the candidate
-    # grid and chunk bounds were built by the warm-up calls and are reused;
-    # the batched call is not split into candidate ranges, so no merge)
-    launches_per_step = 2
+    # per timed step: trace selection, the work-queue order of the midpoints
+    # and the semblance kernel (the candidate grid and chunk bounds were built
+    # by the warm-up calls and are reused; the batched call is not split into
+    # candidate ranges, so no merge)
+    launches_per_step = 3
     # ---- tuned, device resident
     for _ in range(args.warmup):
         run("tuned")

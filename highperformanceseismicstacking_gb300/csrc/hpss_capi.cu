@@ -40,7 +40,7 @@ struct hpss_handle_s : public Handle {
         size_t bytes = 0;
     };
     Buf params, chunkBounds, selFirst, selCount, selIdx, candFirst, candCount,
-        notUsed, errWord, m0s, out, octCands, prior, partial;
+        notUsed, errWord, m0s, out, octCands, prior, partial, order;
     Buf octTab;                // OCT per-trace factors of the line (octTabH0)
     bool octTabValid = false;
     float octTabH0 = 0.f;
@@ -462,8 +462,9 @@ hpss_status linear_search_impl(hpss_handle h, const float *d_m0s, uint32_t nM0,
         lp.chunkBounds = static_cast<float *>(h->chunkBounds.p);
         return cudaSuccess;
     };
-    // counters, cleared by one memset: error word at byte 0, near-tie counter
-    // at byte 8, the per-midpoint notUsed counts from byte 16
+    // counters, cleared by one memset: error word at byte 0, the pair
+    // kernel's work-queue counter at byte 4, near-tie counter at byte 8, the
+    // per-midpoint notUsed counts from byte 16
     if (!group) {
         HPSS_CUDA_TRY(h, ensure(h, h->notUsed, 16 + nM0 * sizeof(unsigned long long)));
         HPSS_CUDA_TRY(h, cudaMemsetAsync(h->notUsed.p, 0, 16 + nM0 * sizeof(unsigned long long),
@@ -483,6 +484,9 @@ hpss_status linear_search_impl(hpss_handle h, const float *d_m0s, uint32_t nM0,
         octParts = oct_parts(lp, (uint32_t)num_sms(h));
         HPSS_CUDA_TRY(h, ensure(h, h->partial, oct_partial_bytes(nM0, h->S, octParts)));
     } else if (pairKernel) {
+        // midpoints of the batch by descending selected traces (work-queue order)
+        if (nM0 > 1 && nM0 <= kMaxOrderedMidpoints)
+            HPSS_CUDA_TRY(h, ensure(h, h->order, nM0 * sizeof(uint32_t)));
         // per-part best / runner-up of a split pair-kernel call, for the
         // largest split of any shape (allocated before the timed region)
         uint32_t maxParts = 1;
@@ -504,8 +508,20 @@ hpss_status linear_search_impl(hpss_handle h, const float *d_m0s, uint32_t nM0,
     // nBase (midpoint, tile) units, each split into the shape's candidate
     // parts; a split launch of all units is followed by the ordered merge
     uint32_t lastParts = 1;
+    // work queue of the pair kernel: heaviest midpoints first, units taken
+    // from a counter that every launch starts at zero
+    const bool ordered = pairKernel && nM0 > 1 && nM0 <= kMaxOrderedMidpoints;
+    if (ordered) {
+        HPSS_CUDA_TRY(h, launch_order_by_count(lp.selCount, nM0,
+                                               static_cast<uint32_t *>(h->order.p), h->stream));
+        lp.order = static_cast<const uint32_t *>(h->order.p);
+    }
+    uint32_t *unitCounter = reinterpret_cast<uint32_t *>(static_cast<char *>(h->notUsed.p) + 4);
     auto launchPair = [&](int variant, uint32_t nBase) -> cudaError_t {
         LsParams q = lp;
+        q.unitCounter = unitCounter;
+        cudaError_t e0 = cudaMemsetAsync(unitCounter, 0, sizeof(uint32_t), h->stream);
+        if (e0 != cudaSuccess) return e0;
         q.parts = pair_parts(units, lp.nChunks, num_sms(h), kVariantCtasPerSm[variant]);
         q.chunksPerPart = (lp.nChunks + q.parts - 1) / q.parts;
         q.partial = static_cast<PartBest *>(h->partial.p);
@@ -995,7 +1011,7 @@ hpss_status hpss_destroy(hpss_handle h) {
     free_gather(h);
     for (auto *b : {&h->params, &h->chunkBounds, &h->selFirst, &h->selCount, &h->selIdx,
                     &h->candFirst, &h->candCount, &h->notUsed, &h->errWord, &h->m0s,
-                    &h->out, &h->octCands, &h->prior, &h->partial, &h->octTab})
+                    &h->out, &h->octCands, &h->prior, &h->partial, &h->octTab, &h->order})
         release(h, *b);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);

@@ -94,6 +94,12 @@ struct LsParams {
     uint32_t parts = 1;
     uint32_t chunksPerPart = 0;
     PartBest *partial = nullptr;
+    // work queue of the tuned pair kernel: units are taken from
+    // *unitCounter (zeroed before the launch; nullptr: static round-robin)
+    // and mapped to midpoints through `order` (heaviest first; nullptr:
+    // identity)
+    uint32_t *unitCounter = nullptr;
+    const uint32_t *order = nullptr;
     // OCT: per-trace factors {m, gamma^2, 16 h^2 h0^2, h^2 - h0^2} for the
     // line's h0 (launch_oct_trace_table); read by the OCT tuned and DE kernels
     const float4 *octTab = nullptr;
@@ -183,6 +189,11 @@ cudaError_t launch_ls_oct(const LsParams &p, uint32_t numSms, void *partial, uin
 // Per-trace factors of the OCT formulas for half-offset h0 (ls_oct.cu).
 cudaError_t launch_oct_trace_table(const float *mid, const float *hoff, uint32_t n, float h0,
                                    float4 *tab, cudaStream_t st);
+// order[] = midpoints by descending count[] (select.cu); for up to
+// kMaxOrderedMidpoints midpoints per launch.
+constexpr uint32_t kMaxOrderedMidpoints = 4096;
+cudaError_t launch_order_by_count(const uint32_t *count, uint32_t n, uint32_t *order,
+                                  cudaStream_t st);
 // Combine `parts` candidate ranges of every (midpoint, sample) in candidate
 // order and write the result block [nM0][2+np][S]; counts near-ties.
 cudaError_t launch_merge_parts(const LsParams &p, uint32_t parts, const PartBest *partial,

@@ -139,6 +139,7 @@ struct Tuned2Smem {
     uint32_t bestP[kTunedWarps][kTileSamples];
     float bestSec[kTunedWarps][kTileSamples];
     unsigned long long stageBar;  // mbarrier of the bulk copies of a staging round
+    uint32_t nextUnit;            // work-queue unit handed to the CTA
 };
 
 // Bulk (TMA) copies of the FP32 trace spans into the stage.  One thread
@@ -219,11 +220,20 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
     __syncthreads();
     uint32_t stagePhase = 0;  // parity of the staging barrier's current phase
 
-    for (uint32_t unit = blockIdx.x; unit < nUnits; unit += gridDim.x) {
+    for (uint32_t unit = blockIdx.x;; unit += gridDim.x) {
+        // work queue: the next unit for this CTA (heaviest midpoints first
+        // when the host ordered them), else static round-robin
+        if (a.unitCounter) {
+            __syncthreads();  // every thread has read the previous unit
+            if (threadIdx.x == 0) sm.nextUnit = atomicAdd(a.unitCounter, 1u);
+            __syncthreads();
+            unit = sm.nextUnit;
+        }
+        if (unit >= nUnits) break;
         // unit = (midpoint, tile, candidate part), part fastest
         const uint32_t part = unit % a.parts;
         const uint32_t mt = unit / a.parts;
-        const uint32_t mi = mt / tiles;
+        const uint32_t mi = a.order ? a.order[mt / tiles] : mt / tiles;
         const int s0 = (int)(mt % tiles) * kTileSamples;
         const int s = s0 + lane;
         const int sc = min(s, S - 1);

@@ -55,6 +55,29 @@ __global__ void select_range_kernel(const float *mid, uint32_t n,
     count[i] = b - a;
 }
 
+// Midpoints in descending order of selected traces (ties by index):
+// order[rank(i)] = i with rank(i) = #{j : count[j] > count[i] or
+// (count[j] == count[i] and j < i)}.  Quadratic, for up to a few thousand
+// midpoints (the host sorts only batches up to kMaxOrderedMidpoints).
+__global__ void order_by_count_kernel(const uint32_t *count, uint32_t n, uint32_t *order) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t ci = count[i];
+    uint32_t rank = 0;
+    for (uint32_t j = 0; j < n; j++) {
+        const uint32_t cj = count[j];
+        rank += (cj > ci || (cj == ci && j < i)) ? 1u : 0u;
+    }
+    order[rank] = i;
+}
+
+cudaError_t launch_order_by_count(const uint32_t *count, uint32_t n, uint32_t *order,
+                                  cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    order_by_count_kernel<<<(n + 255) / 256, 256, 0, st>>>(count, n, order);
+    return cudaGetLastError();
+}
+
 // exclusive prefix sum of count[] into first[] (single CTA, any n)
 __global__ void exclusive_scan_kernel(const uint32_t *count, uint32_t *first,
                                       uint32_t n) {
