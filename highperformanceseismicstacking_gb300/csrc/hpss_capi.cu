@@ -480,6 +480,8 @@ hpss_status linear_search_impl(hpss_handle h, const float *d_m0s, uint32_t nM0,
     const uint64_t units = (uint64_t)nM0 * tiles;
     uint32_t octParts = 1;
     if (octKernel) {
+        if (nM0 > 1 && nM0 <= kMaxOrderedMidpoints)
+            HPSS_CUDA_TRY(h, ensure(h, h->order, nM0 * sizeof(uint32_t)));
         // per-part best / runner-up of the OCT kernel
         octParts = oct_parts(lp, (uint32_t)num_sms(h));
         HPSS_CUDA_TRY(h, ensure(h, h->partial, oct_partial_bytes(nM0, h->S, octParts)));
@@ -519,9 +521,6 @@ hpss_status linear_search_impl(hpss_handle h, const float *d_m0s, uint32_t nM0,
     uint32_t *unitCounter = reinterpret_cast<uint32_t *>(static_cast<char *>(h->notUsed.p) + 4);
     auto launchPair = [&](int variant, uint32_t nBase) -> cudaError_t {
         LsParams q = lp;
-        q.unitCounter = unitCounter;
-        cudaError_t e0 = cudaMemsetAsync(unitCounter, 0, sizeof(uint32_t), h->stream);
-        if (e0 != cudaSuccess) return e0;
         q.parts = pair_parts(units, lp.nChunks, num_sms(h), kVariantCtasPerSm[variant]);
         q.chunksPerPart = (lp.nChunks + q.parts - 1) / q.parts;
         q.partial = static_cast<PartBest *>(h->partial.p);
@@ -530,6 +529,12 @@ hpss_status linear_search_impl(hpss_handle h, const float *d_m0s, uint32_t nM0,
         if (nUnits > 0xffffffffull) return cudaErrorInvalidConfiguration;
         const uint32_t grid = (uint32_t)std::min<uint64_t>(
             nUnits, (uint64_t)num_sms(h) * kVariantCtasPerSm[variant]);
+        // more units than resident CTAs: take them from the work queue
+        if (nUnits > grid) {
+            q.unitCounter = unitCounter;
+            cudaError_t e0 = cudaMemsetAsync(unitCounter, 0, sizeof(uint32_t), h->stream);
+            if (e0 != cudaSuccess) return e0;
+        }
         cudaError_t e =
             h->model == HPSS_MODEL_CMP
                 ? launch_ls_tuned_cmp(q, grid, tiles, (uint32_t)nUnits, h->stream, variant,
@@ -554,6 +559,15 @@ hpss_status linear_search_impl(hpss_handle h, const float *d_m0s, uint32_t nM0,
     if (pairKernel) {
         HPSS_CUDA_TRY(h, launchPair(variant, (uint32_t)units));
     } else if (octKernel) {
+        // work queue as for the pair kernel
+        if (nM0 > 1 && nM0 <= kMaxOrderedMidpoints) {
+            HPSS_CUDA_TRY(h, launch_order_by_count(lp.selCount, nM0,
+                                                   static_cast<uint32_t *>(h->order.p),
+                                                   h->stream));
+            lp.order = static_cast<const uint32_t *>(h->order.p);
+        }
+        lp.unitCounter = unitCounter;
+        HPSS_CUDA_TRY(h, cudaMemsetAsync(unitCounter, 0, sizeof(uint32_t), h->stream));
         HPSS_CUDA_TRY(h, launch_ls_oct(lp, (uint32_t)num_sms(h), h->partial.p, octParts,
                                        h->stream));
     } else {

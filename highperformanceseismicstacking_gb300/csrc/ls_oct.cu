@@ -48,11 +48,20 @@ ls_oct_kernel(LsParams a, uint32_t tiles, uint32_t parts, uint32_t chunksPerPart
     __shared__ float shBest[kOctWarps][32], shSecond[kOctWarps][32], shStack[kOctWarps][32];
     __shared__ uint32_t shP[kOctWarps][32];
     __shared__ unsigned long long shNu;
+    __shared__ uint32_t shUnit;
 
-    for (uint32_t unit = blockIdx.x; unit < nUnits; unit += gridDim.x) {
+    for (uint32_t unit = blockIdx.x;; unit += gridDim.x) {
+        // work queue (heaviest midpoints first when ordered), else round-robin
+        if (a.unitCounter) {
+            __syncthreads();  // every thread has read the previous unit
+            if (threadIdx.x == 0) shUnit = atomicAdd(a.unitCounter, 1u);
+            __syncthreads();
+            unit = shUnit;
+        }
+        if (unit >= nUnits) break;
         const uint32_t part = unit % parts;
         const uint32_t tile = (unit / parts) % tiles;
-        const uint32_t mi = unit / (parts * tiles);
+        const uint32_t mi = a.order ? a.order[unit / (parts * tiles)] : unit / (parts * tiles);
         const int s = (int)tile * 32 + lane;
         const int sc = min(s, S - 1);
         const float t0 = static_cast<float>(sc) * a.dt;
@@ -248,8 +257,11 @@ cudaError_t launch_oct_w(const LsParams &p, uint32_t numSms, void *partial, uint
     if (e != cudaSuccess) return e;
     const uint32_t grid =
         (uint32_t)std::min<uint64_t>(units, (uint64_t)numSms * (uint64_t)std::max(perSm, 1));
+    // one wave: every unit has its own CTA, the work queue only adds latency
+    LsParams q = p;
+    if (units <= grid) q.unitCounter = nullptr;
     ls_oct_kernel<W, R><<<grid, kOctWarps * 32, 0, st>>>(
-        p, tiles, parts, chunksPerPart, (uint32_t)units, static_cast<PartBest *>(partial));
+        q, tiles, parts, chunksPerPart, (uint32_t)units, static_cast<PartBest *>(partial));
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     return launch_merge_parts(p, parts, static_cast<const PartBest *>(partial), st);
