@@ -225,8 +225,17 @@ de_kernel(DeParams d, uint32_t spc, uint32_t groups, uint32_t nUnits) {
     const uint32_t ind = threadIdx.x % pop;      // individual
     const bool member = ls < spc;                // threads past spc * pop only sync
 
-    for (uint32_t unit = blockIdx.x; unit < nUnits; unit += gridDim.x) {
-        const uint32_t mi = unit / groups;
+    __shared__ uint32_t nextUnit;
+    for (uint32_t unit = blockIdx.x;; unit += gridDim.x) {
+        // work queue (heaviest midpoints first when ordered), else round-robin
+        if (a.unitCounter) {
+            __syncthreads();  // every thread has read the previous unit
+            if (threadIdx.x == 0) nextUnit = atomicAdd(a.unitCounter, 1u);
+            __syncthreads();
+            unit = nextUnit;
+        }
+        if (unit >= nUnits) break;
+        const uint32_t mi = a.order ? a.order[unit / groups] : unit / groups;
         const uint32_t s = (unit % groups) * spc + ls;
         const bool active = member && s < a.S;
         const float m0 = a.m0s[mi];
@@ -389,7 +398,10 @@ cudaError_t launch_de_w(const DeParams &d, uint32_t numSms, uint32_t spc, uint32
     if (e != cudaSuccess) return e;
     const uint32_t grid =
         (uint32_t)std::min<uint64_t>(units, (uint64_t)numSms * (uint64_t)std::max(perSm, 1));
-    de_kernel<MODEL, W><<<grid, threads, smem, st>>>(d, spc, groups, (uint32_t)units);
+    // one wave: every unit has its own CTA, the work queue only adds latency
+    DeParams q = d;
+    if (units <= grid) q.ls.unitCounter = nullptr;
+    de_kernel<MODEL, W><<<grid, threads, smem, st>>>(q, spc, groups, (uint32_t)units);
     return cudaGetLastError();
 }
 

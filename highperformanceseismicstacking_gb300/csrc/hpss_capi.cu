@@ -796,11 +796,15 @@ hpss_status de_impl(hpss_handle h, const float *d_m0s, uint32_t nM0, uint32_t po
         d.hi[j] = h->upper[j];
     }
     HPSS_CUDA_TRY(h, ensure(h, h->notUsed, nM0 * sizeof(unsigned long long)));
-    HPSS_CUDA_TRY(h, ensure(h, h->errWord, sizeof(uint32_t)));
+    // error word at byte 0, the DE kernel's work-queue counter at byte 8
+    HPSS_CUDA_TRY(h, ensure(h, h->errWord, 16));
     d.ls.notUsed = static_cast<unsigned long long *>(h->notUsed.p);
     d.ls.errorWord = static_cast<uint32_t *>(h->errWord.p);
+    d.ls.unitCounter = reinterpret_cast<uint32_t *>(static_cast<char *>(h->errWord.p) + 8);
     HPSS_CUDA_TRY(h, cudaMemsetAsync(d.ls.notUsed, 0, nM0 * sizeof(unsigned long long), h->stream));
-    HPSS_CUDA_TRY(h, cudaMemsetAsync(d.ls.errorWord, 0, sizeof(uint32_t), h->stream));
+    HPSS_CUDA_TRY(h, cudaMemsetAsync(h->errWord.p, 0, 16, h->stream));
+    const bool ordered = nM0 > 1 && nM0 <= kMaxOrderedMidpoints;
+    if (ordered) HPSS_CUDA_TRY(h, ensure(h, h->order, nM0 * sizeof(uint32_t)));
 
     HPSS_CUDA_TRY(h, cudaEventRecord(h->ev0, h->stream));
     // selection: CMP / ZO-CRS as linear search; OCT with the initial population
@@ -837,6 +841,12 @@ hpss_status de_impl(hpss_handle h, const float *d_m0s, uint32_t nM0, uint32_t po
         HPSS_CUDA_TRY(h, launch_de_select_oct(d, cf, cc, static_cast<uint32_t *>(h->selIdx.p),
                                               static_cast<uint32_t *>(h->selCount.p),
                                               h->stream));
+    }
+    // work queue order: midpoints by descending selected traces
+    if (ordered) {
+        HPSS_CUDA_TRY(h, launch_order_by_count(d.ls.selCount, nM0,
+                                               static_cast<uint32_t *>(h->order.p), h->stream));
+        d.ls.order = static_cast<const uint32_t *>(h->order.p);
     }
     HPSS_CUDA_TRY(h, cudaEventRecord(h->ev1, h->stream));
     const uint64_t units = (uint64_t)nM0 * h->S;
