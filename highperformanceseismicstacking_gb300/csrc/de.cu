@@ -201,7 +201,8 @@ __device__ __forceinline__ void de_eval(const DeParams &d, float t0, float m0, u
 // individual, the reference's thread layout), so every lane works for any
 // population size; the population vectors live in shared memory, where
 // mutation reads the three donors.  Persistent over (midpoint, sample
-// group) units.
+// group) units, taken from a work queue (heaviest midpoints first) when a
+// call has more units than resident CTAs.
 constexpr int kDeThreads = 256;
 
 // OCT: six resident CTAs per SM (40 registers) -- its evaluation waits on

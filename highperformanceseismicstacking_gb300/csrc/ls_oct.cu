@@ -17,7 +17,9 @@
 //  * the candidate range is split into `parts` (CTAs work on (midpoint,
 //    32-sample tile, part) units) so that a call with few midpoints still
 //    fills the GPU; each unit writes the best / runner-up of its part and
-//    merge_parts_kernel combines the parts in candidate order.
+//    merge_parts_kernel combines the parts in candidate order;
+//  * a call with more units than resident CTAs takes them from a work
+//    queue, heaviest midpoints first.
 //
 // The per-candidate arithmetic is the plain kernel's (model_time<kModelOct>,
 // window_index, the COMPUTE_SEMBLANCE restatement), in the same trace order,

@@ -16,7 +16,10 @@
 // stack too, except where the pair kernel derives the linear sum from the
 // per-tap sums, see EXACT_STACK below).  The argmax over candidates
 // is kept in registers and reduced across warps at the end (lowest index wins
-// ties).  CTAs are persistent over the work units.  A call with few
+// ties).  CTAs are persistent over the work units; a call with more units
+// than resident CTAs hands them out from an atomic counter, the midpoints
+// ordered by descending selected traces, so that the heaviest units start
+// first and no CTA idles while others finish.  A call with few
 // midpoints has too few (midpoint, tile) units to fill the GPU (one CMP
 // midpoint of 2000 samples: 63 units for 2-3 CTAs on each of 152 SMs); the
 // host then splits the candidate chunks into `parts` contiguous ranges, a unit
