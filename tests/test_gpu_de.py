@@ -132,3 +132,25 @@ def test_de_oct_selection_from_initial_population(engine):
     # c = 4/v^2 uses the device's fast division: a boundary trace may flip
     assert abs(st["selected_traces"] - want) <= 1
     assert np.all(np.isfinite(de))
+
+
+def test_de_multi_wave_call_maps_units_to_midpoints(engine):
+    """A call with more (midpoint, sample group) units than resident CTAs
+    takes them from the work queue, midpoints ordered by selected traces
+    (uneven fold here); every unit must still work on its own midpoint: with
+    one generation, every reported velocity is one of the initial individuals
+    the counter-based stream gives that midpoint's index."""
+    line = synthetic.structured_line(n_cmp=40, fold_range=(6, 20), h_max=1200, ns=400,
+                                     dt_us=4000, n_reflectors=3, f=20.0, snr=8.0, seed=33)
+    lower, upper = [1000.0], [5040.0]
+    _setup(engine, line, "cmp", lower, upper)
+    m0s = line.cdp_midpoints
+    assert m0s.size == 40
+    seed, pop = 91, 16
+    de, st = engine.differential_evolution(m0s, pop, 1, 0.85, 0.5, seed=seed)
+    assert st["device_error"] == 0
+    S = line.samples_per_trace
+    for i in (0, 7, 23, 39):
+        init = oracle.de_initial_population(seed, i, S, pop, lower, upper)
+        member = np.array([np.any(init[s, :, 0] == de[i, 2, s]) for s in range(S)])
+        assert member.all(), i

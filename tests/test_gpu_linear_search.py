@@ -405,3 +405,31 @@ def test_size_limits_of_the_tuned_kernel(engine, ns, tau, tuned_runs):
     assert (st["kernel_variant"] >= 0) == tuned_runs, st["kernel_variant"]
     assert_same_but_stack(tuned, plain, 1)
     assert st["near_ties"] == st_p["near_ties"]
+
+
+def test_work_queue_multi_wave_calls(engine):
+    """Calls with more units than resident CTAs take them from the work
+    queue: an uneven-fold ZO-CRS line (midpoints ordered by selected traces)
+    and a CMP line of 4200 midpoints (beyond the ordered batch size, queue in
+    midpoint order).  The stack-exact tuned kernel equals the plain kernel bit
+    for bit in both."""
+    zl = synthetic.structured_line(n_cmp=60, fold_range=(4, 30), h_max=1500, ns=600,
+                                   dt_us=4000, n_reflectors=4, f=20.0, snr=6.0, seed=61)
+    a, b = synthetic.zocrs_bounds(1414.2136, 2000.0, 90.0, 0.05)
+    lower, upper, gran = [1414.2136, -a, -b], [6324.5553, a, b], [5, 3, 3]
+    _setup(engine, zl, "zocrs", lower, upper, 2, 125.0)
+    m0s = zl.cdp_midpoints
+    exact, st = engine.linear_search(m0s, gran, "tuned_exact")
+    plain, _ = engine.linear_search(m0s, gran, "plain")
+    assert st["device_error"] == 0 and np.array_equal(exact, plain)
+    cl = synthetic.cmp_line(n_cmp=4200, halfoffsets=[100, 400, 700, 1000], ns=64, dt_us=4000,
+                            n_reflectors=2, n_multiples=0, f=25.0, snr=10.0, seed=62)
+    w = synthetic.WORKLOADS["cmp-small"]
+    _setup(engine, cl, "cmp", w.lower, w.upper, 2)
+    m0s = cl.cdp_midpoints
+    assert m0s.size > 4096
+    exact, st = engine.linear_search(m0s, [21], "tuned_exact")
+    plain, _ = engine.linear_search(m0s, [21], "plain")
+    tuned, _ = engine.linear_search(m0s, [21], "tuned")
+    assert st["device_error"] == 0 and np.array_equal(exact, plain)
+    assert_same_but_stack(tuned, plain, 1)
