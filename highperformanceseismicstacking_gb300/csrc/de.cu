@@ -95,6 +95,8 @@ struct Draws {
     }
 };
 
+__device__ __forceinline__ float2 de_f2(float a, float b) { return make_float2(a, b); }
+
 // Semblance of one candidate (raw parameters) over the selected traces.
 template <int MODEL, int W>
 __device__ __forceinline__ void de_eval(const DeParams &d, float t0, float m0, uint32_t first,
@@ -116,28 +118,65 @@ __device__ __forceinline__ void de_eval(const DeParams &d, float t0, float m0, u
         // CMP / ZO-CRS: two traces per step -- both traveltimes and both
         // windows' loads are issued before the sums, which then take the
         // traces in order (the same sums as one trace at a time)
+        // the two traces' traveltimes, floors and window terms in packed
+        // f32x2 ops (per lane the same IEEE operations as cmp_time /
+        // zocrs_t2 and window_index: t/dt is t*(1/dt) in the fast-math
+        // build, and floor(t/dt) is read from the bits of t/dt + 2^23 added
+        // toward zero, which (int) gives for 0 <= t/dt < 2^23)
+        const float2 c2 = de_f2(c, c), a2 = de_f2(p1, p1), b2 = de_f2(p2, p2);
+        const float t0sq = __fmul_rn(t0, t0);
+        const float2 t02 = de_f2(t0, t0), t0sq2 = de_f2(t0sq, t0sq);
+        const float2 negM02 = de_f2(-m0, -m0);
+        const float rdt = 1.0f / a.dt;
+        const float2 rdt2 = de_f2(rdt, rdt);
+        const float2 kNeg1 = de_f2(-1.f, -1.f);
+        const float2 kMagic2 = de_f2(8388608.f, 8388608.f), kNegMagic2 = de_f2(-8388608.f, -8388608.f);
         for (; q + 1 < cnt; q += 2) {
             const uint32_t ti0 = first + q, ti1 = ti0 + 1;
-            float ta = 0.f, tb = 0.f;
-            const bool oka = model_time<MODEL>(t0, c, p1, p2, a.mid[ti0], a.hoff[ti0],
-                                               a.hsq[ti0], m0, a.apm, a.h0, &ta) > 0;
-            const bool okb = model_time<MODEL>(t0, c, p1, p2, a.mid[ti1], a.hoff[ti1],
-                                               a.hsq[ti1], m0, a.apm, a.h0, &tb) > 0;
-            const WinIdx wa = window_index(ta, a.dt), wb = window_index(tb, a.dt);
-            const bool ina = oka && window_in_trace(wa.k, a.tau, (int)a.S);
-            const bool inb = okb && window_in_trace(wb.k, a.tau, (int)a.S);
+            const float2 hsq2 = de_f2(a.hsq[ti0], a.hsq[ti1]);
+            float2 tt2;
+            if (MODEL == kModelCmp) {
+                tt2 = __ffma2_rn(c2, hsq2, t0sq2);
+            } else {
+                const float2 dm2 = __fadd2_rn(de_f2(a.mid[ti0], a.mid[ti1]), negM02);  // m - m0
+                const float2 x2 = __ffma2_rn(a2, dm2, t02);
+                const float2 bd2 = __fmul2_rn(b2, dm2);
+                tt2 = __ffma2_rn(c2, hsq2, __ffma2_rn(bd2, dm2, __fmul2_rn(x2, x2)));
+            }
+            // ZO-CRS: a negative squared time skips the window
+            const bool oka = MODEL == kModelCmp || tt2.x >= 0.f;
+            const bool okb = MODEL == kModelCmp || tt2.y >= 0.f;
+            const float2 t2 = MODEL == kModelCmp
+                                  ? de_f2(sqrtf(tt2.x), sqrtf(tt2.y))
+                                  : de_f2(sqrtf(fmaxf(tt2.x, 0.f)), sqrtf(fmaxf(tt2.y, 0.f)));
+            const float2 ti2 = __fmul2_rn(t2, rdt2);
+            const float2 rk = __fadd2_rz(ti2, kMagic2);
+            const float2 fq = __ffma2_rn(__fadd2_rn(rk, kNegMagic2), kNeg1, ti2);  // frac
+            const int ka = __float_as_int(rk.x) - 0x4B000000;
+            const int kb = __float_as_int(rk.y) - 0x4B000000;
+            const bool ina = oka && window_in_trace(ka, a.tau, (int)a.S);
+            const bool inb = okb && window_in_trace(kb, a.tau, (int)a.S);
             float ya[W > 0 ? W + 1 : 1], yb[W > 0 ? W + 1 : 1];
-            const float *tra = a.samples + (size_t)ti0 * a.stride + (ina ? wa.k - a.tau : 0);
-            const float *trb = a.samples + (size_t)ti1 * a.stride + (inb ? wb.k - a.tau : 0);
+            const float *tra = a.samples + (size_t)ti0 * a.stride + (ina ? ka - a.tau : 0);
+            const float *trb = a.samples + (size_t)ti1 * a.stride + (inb ? kb - a.tau : 0);
 #pragma unroll
             for (int j = 0; j <= W; j++) {
                 ya[j] = ina ? __ldg(tra + j) : 0.f;
                 yb[j] = inb ? __ldg(trb + j) : 0.f;
             }
+            // window terms of both traces: (y1 - y0) * frac + y0 per lane
+            float2 u2[W > 0 ? W : 1];
+#pragma unroll
+            for (int j = 0; j < W; j++) {
+                const float2 y0 = de_f2(ya[j], yb[j]);
+                const float2 d2 = __ffma2_rn(y0, kNeg1, de_f2(ya[j + 1], yb[j + 1]));
+                u2[j] = __ffma2_rn(d2, fq, y0);
+            }
+            // the sums take trace ti0, then trace ti1
             if (ina) {
 #pragma unroll
                 for (int j = 0; j < W; j++) {
-                    float u = (ya[j + 1] - ya[j]) * wa.frac + ya[j];
+                    const float u = u2[j].x;
                     num[j] += u;
                     lin += u;
                     den += u * u;
@@ -147,7 +186,7 @@ __device__ __forceinline__ void de_eval(const DeParams &d, float t0, float m0, u
             if (inb) {
 #pragma unroll
                 for (int j = 0; j < W; j++) {
-                    float u = (yb[j + 1] - yb[j]) * wb.frac + yb[j];
+                    const float u = u2[j].y;
                     num[j] += u;
                     lin += u;
                     den += u * u;
