@@ -260,10 +260,50 @@ de_kernel(DeParams d, uint32_t spc, uint32_t groups, uint32_t nUnits) {
     float *X = deSmem;                           // [spc][pop][NP]
     float *FX = deSmem + (size_t)spc * pop * NP; // [spc][pop] (final argmax)
     float *FK = FX + (size_t)spc * pop;          // [spc][pop]
+    // OCT: evaluations assigned by slope rank (de_sorted_smem_floats)
+    float *TR = FK + (size_t)spc * pop;                 // [threads][NP] trial vectors
+    float *KEY = TR + (size_t)blockDim.x * NP;          // [threads] sort key
+    float *RES = KEY + blockDim.x;                      // [threads][2] fitness, stack
+    uint32_t *PERM = reinterpret_cast<uint32_t *>(RES + 2 * (size_t)blockDim.x);
     __shared__ unsigned long long nuCta;
     const uint32_t ls = threadIdx.x / pop;       // sample within the CTA
     const uint32_t ind = threadIdx.x % pop;      // individual
     const bool member = ls < spc;                // threads past spc * pop only sync
+
+    // OCT: whether a trace passes the displaced-midpoint test depends on the
+    // candidate (mostly on its slope), and a warp runs the OCT time and
+    // window path for a trace as soon as one lane passes.  So the CTA's
+    // evaluations are dealt by slope rank: thread r evaluates the trial of
+    // the member with the r-th smallest slope (any sample of the CTA), and
+    // the fitness goes back to its owner through shared memory.  Every
+    // trial's fitness is computed exactly as by its owner.  Called by all
+    // threads of the CTA.
+    auto evalSorted = [&](const float *trial, bool active, float s0f, float m0, uint32_t first,
+                          uint32_t cnt, float *f, float *fk, unsigned *notUsed) {
+#pragma unroll
+        for (int j = 0; j < NP; j++) TR[threadIdx.x * NP + j] = trial[j];
+        const float key = active ? trial[NP - 1] : __int_as_float(0x7f800000);  // slope; +inf
+        KEY[threadIdx.x] = key;
+        __syncthreads();
+        uint32_t rank = 0;
+        for (uint32_t t = 0; t < blockDim.x; t++) {
+            const float kt = KEY[t];
+            rank += (kt < key || (kt == key && t < threadIdx.x)) ? 1u : 0u;
+        }
+        PERM[rank] = threadIdx.x;
+        __syncthreads();
+        const uint32_t o = PERM[threadIdx.x];  // the member whose trial this thread evaluates
+        if (KEY[o] != __int_as_float(0x7f800000)) {
+            const float t0o = (s0f + static_cast<float>(o / pop)) * a.dt;
+            float fo, fko;
+            de_eval<MODEL, W>(d, t0o, m0, first, cnt, TR + o * NP, &fo, &fko, notUsed);
+            RES[2 * o] = fo;
+            RES[2 * o + 1] = fko;
+        }
+        __syncthreads();
+        *f = RES[2 * threadIdx.x];
+        *fk = RES[2 * threadIdx.x + 1];
+    };
 
     __shared__ uint32_t nextUnit;
     for (uint32_t unit = blockIdx.x;; unit += gridDim.x) {
@@ -281,6 +321,7 @@ de_kernel(DeParams d, uint32_t spc, uint32_t groups, uint32_t nUnits) {
         const float m0 = a.m0s[mi];
         const uint32_t first = a.selFirst[mi], cnt = a.selCount[mi];
         const float t0 = static_cast<float>(active ? s : 0) * a.dt;
+        const float s0f = static_cast<float>((unit % groups) * spc);  // the CTA's first sample
         float *xs = X + (size_t)(member ? ls : 0) * pop * NP;  // this sample's population
         float x[NP];
         float fx = -1.f, fxk = 0.f;
@@ -296,12 +337,21 @@ de_kernel(DeParams d, uint32_t spc, uint32_t groups, uint32_t nUnits) {
                 x[j] = __fmaf_rn(rng.next(), __fsub_rn(d.hi[j], d.lo[j]), d.lo[j]);
                 xs[ind * NP + j] = x[j];
             }
-            de_eval<MODEL, W>(d, t0, m0, first, cnt, x, &fx, &fxk, &notUsed);
+            if (MODEL != kModelOct) de_eval<MODEL, W>(d, t0, m0, first, cnt, x, &fx, &fxk, &notUsed);
+        } else {
+#pragma unroll
+            for (int j = 0; j < NP; j++) x[j] = d.lo[j];
+        }
+        if (MODEL == kModelOct) {
+            evalSorted(x, active, s0f, m0, first, cnt, &fx, &fxk, &notUsed);
+            if (!active) fx = -1.f;
         }
         // ---- generations 2 .. G
         for (uint32_t gen = 1; gen < d.gens; gen++) {
             __syncthreads();  // population of the previous generation complete
             float u[NP];
+#pragma unroll
+            for (int j = 0; j < NP; j++) u[j] = x[j];
             if (active) {
                 Draws rng(d.seedLo, d.seedHi, mi, s, ind, gen);
                 float v[NP];
@@ -325,9 +375,10 @@ de_kernel(DeParams d, uint32_t spc, uint32_t groups, uint32_t nUnits) {
                 }
             }
             __syncthreads();  // every donor read before any replacement
+            float fu = -1.f, fuk = 0.f;
+            if (MODEL == kModelOct) evalSorted(u, active, s0f, m0, first, cnt, &fu, &fuk, &notUsed);
             if (active) {
-                float fu, fuk;
-                de_eval<MODEL, W>(d, t0, m0, first, cnt, u, &fu, &fuk, &notUsed);
+                if (MODEL != kModelOct) de_eval<MODEL, W>(d, t0, m0, first, cnt, u, &fu, &fuk, &notUsed);
                 if (fu > fx) {
 #pragma unroll
                     for (int j = 0; j < NP; j++) {
@@ -455,7 +506,10 @@ cudaError_t launch_de_model(const DeParams &d, uint32_t numSms, cudaStream_t st)
     const uint64_t units = (uint64_t)d.ls.nM0 * groups;
     if (units == 0) return cudaSuccess;
     if (units > 0xffffffffull) return cudaErrorInvalidConfiguration;
-    const size_t smem = de_smem_bytes(spc, pop, NP);
+    // OCT adds the slope-sorted evaluation's regions: trial vectors, keys,
+    // fitness / stack pairs and the permutation, one each per thread
+    const size_t smem = de_smem_bytes(spc, pop, NP) +
+                        (MODEL == kModelOct ? (size_t)threads * (NP + 4) * sizeof(float) : 0);
     switch (d.ls.w) {
         case 1: return launch_de_w<MODEL, 1>(d, numSms, spc, threads, groups, units, smem, st);
         case 3: return launch_de_w<MODEL, 3>(d, numSms, spc, threads, groups, units, smem, st);
