@@ -15,12 +15,14 @@ to the engine on the same midpoints.  Prints one JSON line per workload.
           reference runs it) against the engine's fused DE launch.
 
   oct [n] OCT linear search on the OCT DE line's geometry (11 x 5 candidates).
+  zocrs [n] ZO-CRS linear search on the ZO-CRS line (21 x 21 x 41 candidates).
   sf [n]  CMP stretch-free stack on the CMP production line.
 
     python tests/golden/time_reference_kernels.py ls 40
     python tests/golden/time_reference_kernels.py de 2
     python tests/golden/time_reference_kernels.py oct 1
     python tests/golden/time_reference_kernels.py sf 20
+    python tests/golden/time_reference_kernels.py zocrs 2
 """
 from __future__ import annotations
 
@@ -85,6 +87,53 @@ def time_ls(n_mid: int = 20):
                       "workload": "cmp-production", "algorithm": "linear-search",
                       "midpoints": n_mid, "evals": evals, "kernel_ms": total_ms,
                       "value": evals / (total_ms / 1e3), "unit": "evals/s"}))
+
+
+def time_zocrs(n_mid: int = 2):
+    """ZO-CRS linear search on the ZO-CRS line (1000 CMPs, +-15-CMP aperture,
+    21 x 21 x 41 candidates, window 5): the reference's evaluation + argmax
+    per midpoint (computeSemblancesForZeroOffsetCommonReflectionSurface +
+    selectBest..., CudaLinearSearchAlgorithm.cu:35-163) against the engine's
+    plain and tuned kernels on the same midpoints."""
+    w = synthetic.WORKLOADS["zocrs-ls"]
+    line = w.make_line()
+    lower, upper = synthetic.workload_bounds(w)
+    tau = tau_index(w.tau, line.dt)
+    rk = ref_runner.ReferenceKernels()
+    params = rk.build_grid("zocrs", lower, upper, w.granularity)
+    S = line.samples_per_trace
+    mid = len(line.cdp_midpoints) // 2
+    m0s = np.ascontiguousarray(line.cdp_midpoints[mid:mid + n_mid])
+    ref_ms, ref_evals, ref_out = 0.0, 0.0, []
+    for i, m0 in enumerate(m0s):
+        sel = np.nonzero(rk.select("zocrs", line.midpoints, line.halfoffsets, float(m0), w.apm,
+                                   0.0, S, float(line.dt)))[0]
+        call = lambda: rk.linear_search_midpoint("zocrs", line.samples, line.midpoints,
+                                                 line.halfoffsets, sel, float(m0),
+                                                 float(line.dt), tau, params, w.apm, 0.0,
+                                                 timing=True)
+        if i == 0:
+            call()  # warm-up (module load)
+        res, _, _, _, ms = call()
+        ref_ms += ms
+        ref_evals += float(sel.size) * S * params.shape[0]
+        ref_out.append(res)
+    out = {"workload": "zocrs-ls (1000-CMP ZO-CRS line, 21 x 21 x 41 candidates, window 5)",
+           "midpoints": int(len(m0s)), "samples": S,
+           "reference": {"ms": ref_ms, "evals": ref_evals, "value": ref_evals / (ref_ms / 1e3)}}
+    with capi.Engine(0) as eng:
+        eng.upload_gather(line.samples, line.midpoints, line.halfoffsets, float(line.dt))
+        eng.set_traveltime("zocrs", lower, upper, w.apm)
+        eng.set_window(tau)
+        for kernel in ("plain", "tuned"):
+            eng.linear_search(m0s, w.granularity, kernel)
+            got, st = eng.linear_search(m0s, w.granularity, kernel)
+            same = float(np.mean(np.all(got[:, 2:] == np.stack(ref_out)[:, 2:], axis=1)))
+            out[kernel] = {"ms": st["kernel_ms"], "evals": st["evals"],
+                           "value": st["evals"] / (st["kernel_ms"] / 1e3),
+                           "parameters_equal_to_reference": same,
+                           "speedup_vs_reference": ref_ms / st["kernel_ms"]}
+    print(json.dumps(out))
 
 
 def time_de(n_mid: int = 2):
@@ -210,9 +259,12 @@ def time_sf(n_mid: int = 20):
 
 if __name__ == "__main__":
     mode = sys.argv[1] if len(sys.argv) > 1 else "ls"
-    n = int(sys.argv[2]) if len(sys.argv) > 2 else {"ls": 20, "de": 2, "oct": 1, "sf": 20}[mode]
+    n = int(sys.argv[2]) if len(sys.argv) > 2 else {"ls": 20, "de": 2, "oct": 1, "sf": 20,
+                                                      "zocrs": 2}[mode]
     if mode == "ls":
         time_ls(n)
+    elif mode == "zocrs":
+        time_zocrs(n)
     elif mode == "de":
         time_de(n)
     elif mode == "oct":
