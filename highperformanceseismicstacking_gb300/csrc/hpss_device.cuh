@@ -118,6 +118,19 @@ __device__ __forceinline__ int oct_mh(const OctCand &k, float gs, float p16h, fl
     return DE_OK;
 }
 
+// oct_mh without the early returns: every operation is carried out whatever
+// the error (the codes are the same, and so is *mh when the code is DE_OK),
+// so that a thread can run several of these chains side by side.
+__device__ __forceinline__ int oct_mh_all(const OctCand &k, float gs, float p16h, float dif,
+                                          float m0, float *mh) {
+    float arg = __fmaf_rn(k.tq, k.tq, __fmul_rn(k.tqts, gs));
+    arg = __fmaf_rn(__fmul_rn(p16h, k.ts), k.ts, arg);
+    const float arg2 =
+        __fadd_rn(__fadd_rn(__fmul_rn(k.ts, gs), k.twoTq), __fmul_rn(2.f, sqrtf(arg)));
+    *mh = __fmaf_rn(__fmul_rn(k.twoTheta, dif), __fdividef(1.0f, sqrtf(arg2)), m0);
+    return arg < 0 ? DE_NEG_SQRT : (arg2 == 0 ? DE_DIV_ZERO : DE_OK);
+}
+
 // OCT displaced midpoint (oct/common.cuh:7-35).
 __device__ __forceinline__ int oct_displaced_midpoint(float h, float h0,
                                                       float t0, float m0,

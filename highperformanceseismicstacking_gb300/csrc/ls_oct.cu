@@ -33,15 +33,19 @@ namespace hpss {
 
 constexpr int kOctWarps = 8;
 
-// One candidate per thread at five resident CTAs per SM (48 registers, no
-// spills): the kernel waits on dependent square-root / reciprocal chains, so
-// resident warps pay more than independent chains in one thread, and the
-// smaller candidate chunks give small calls more units.  Against two
-// candidates per thread at four CTAs per SM (OCT DE line geometry): 11 x 5
-// candidates 4.07 -> 3.10 ms on one midpoint, 12.1 -> 10.0 ms on four;
-// 41 x 11 candidates 88.6 -> 83.7 ms on four midpoints, within 2 % on one.
+// One candidate per thread: the kernel waits on dependent square-root /
+// reciprocal chains, so resident warps pay more than candidates in one
+// thread, and the smaller candidate chunks give small calls more units
+// (against two candidates per thread, OCT DE line geometry, 11 x 5
+// candidates: 4.07 -> 3.10 ms on one midpoint, 12.1 -> 10.0 ms on four).
+// The displaced-midpoint tests of kOctMhBatch traces run side by side
+// (independent chains) before the passing traces are taken in order: four
+// CTAs per SM (63 registers, no spills), 3.10 -> 2.77 ms on one midpoint,
+// 9.88 -> 9.05 ms on four, 37.9 -> 34.8 ms on sixteen.
+constexpr int kOctMhBatch = 4;
+
 template <int W, int R>
-__global__ void __launch_bounds__(kOctWarps * 32, 5)
+__global__ void __launch_bounds__(kOctWarps * 32, 4)
 ls_oct_kernel(LsParams a, uint32_t tiles, uint32_t parts, uint32_t chunksPerPart,
               uint32_t nUnits, PartBest *partial) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -98,7 +102,54 @@ ls_oct_kernel(LsParams a, uint32_t tiles, uint32_t parts, uint32_t chunksPerPart
                 lin[r] = den[r] = 0.f;
                 used[r] = nu[r] = 0;
             }
-            for (uint32_t q = 0; q < cnt; q++) {
+            uint32_t q0 = 0;
+            if (R == 1) {
+                // displaced-midpoint tests of kOctMhBatch traces first, then the
+                // passing traces in order (the per-trace loop below, batched)
+                for (; q0 + kOctMhBatch <= cnt; q0 += kOctMhBatch) {
+                    uint32_t tb[kOctMhBatch];
+                    float4 fb[kOctMhBatch];  // {m, gamma^2, 16h^2h0^2, h^2-h0^2}
+                    float mhb[kOctMhBatch];
+                    bool pass[kOctMhBatch];
+#pragma unroll
+                    for (int b = 0; b < kOctMhBatch; b++) {
+                        tb[b] = a.selIdx ? a.selIdx[first + q0 + b] : first + q0 + b;
+                        fb[b] = __ldg(a.octTab + tb[b]);
+                    }
+#pragma unroll
+                    for (int b = 0; b < kOctMhBatch; b++) {
+                        const int e = oct_mh_all(kc[0], fb[b].y, fb[b].z, fb[b].w, m0, &mhb[b]);
+                        pass[b] = e == DE_OK && !(fabsf(fb[b].x - mhb[b]) > a.apm);
+                    }
+#pragma unroll
+                    for (int b = 0; b < kOctMhBatch; b++) {
+                        if (!pass[b]) {
+                            nu[0]++;
+                            continue;
+                        }
+                        float t;
+                        if (oct_time_k(a.hoff[tb[b]], a.h0, t0, kc[0].tn0_sq, m0, fb[b].x, mhb[b],
+                                       cc[0], sl[0], &t) != DE_OK)
+                            continue;
+                        const WinIdx wi = window_index(t, a.dt);
+                        if (window_in_trace(wi.k, tau, S)) {
+                            const float *y = a.samples + (size_t)tb[b] * a.stride + (wi.k - tau);
+                            float y1 = __ldg(y);
+#pragma unroll
+                            for (int jj = 0; jj < W; jj++) {
+                                const float y0 = y1;
+                                y1 = __ldg(y + jj + 1);
+                                const float u = (y1 - y0) * wi.frac + y0;
+                                num[0][jj] += u;
+                                lin[0] += u;
+                                den[0] += u * u;
+                            }
+                            used[0]++;
+                        }
+                    }
+                }
+            }
+            for (uint32_t q = q0; q < cnt; q++) {
                 const uint32_t ti = a.selIdx ? a.selIdx[first + q] : first + q;
                 const float4 tf = __ldg(a.octTab + ti);  // {m, gamma^2, 16h^2h0^2, h^2-h0^2}
                 const float h = a.hoff[ti];
