@@ -97,6 +97,12 @@ struct Draws {
 
 __device__ __forceinline__ float2 de_f2(float a, float b) { return make_float2(a, b); }
 
+// OCT: displaced-midpoint tests run side by side per thread (four at five
+// CTAs per SM: OCT DE 2 midpoints 876 -> 783 ms, 8 midpoints 2919 -> 2704 ms;
+// two at six CTAs 876 / 2768 ms, four at six 905 / 2824 ms, four at four
+// 814 / 3037 ms)
+constexpr int kDeOctBatch = 4;
+
 // Semblance of one candidate (raw parameters) over the selected traces.
 template <int MODEL, int W>
 __device__ __forceinline__ void de_eval(const DeParams &d, float t0, float m0, uint32_t first,
@@ -197,6 +203,52 @@ __device__ __forceinline__ void de_eval(const DeParams &d, float t0, float m0, u
     }
     // OCT: (t0, candidate) factors once, trace factors from the line's table
     const OctCand kc = oct_cand(t0, c, p1, MODEL == kModelOct ? a.h0 : 0.f);
+    if (MODEL == kModelOct && W > 0) {
+        // the displaced-midpoint tests of kDeOctBatch traces side by side
+        // (independent chains), then the passing traces in order
+        for (; q + kDeOctBatch <= cnt; q += kDeOctBatch) {
+            uint32_t tb[kDeOctBatch];
+            float4 fb[kDeOctBatch];  // {m, gamma^2, 16h^2h0^2, h^2-h0^2}
+            float mhb[kDeOctBatch];
+            bool pass[kDeOctBatch];
+#pragma unroll
+            for (int b = 0; b < kDeOctBatch; b++) {
+                tb[b] = a.selIdx ? a.selIdx[first + q + b] : first + q + b;
+                fb[b] = __ldg(a.octTab + tb[b]);
+            }
+#pragma unroll
+            for (int b = 0; b < kDeOctBatch; b++) {
+                const int e = oct_mh_all(kc, fb[b].y, fb[b].z, fb[b].w, m0, &mhb[b]);
+                pass[b] = e == DE_OK && !(fabsf(fb[b].x - mhb[b]) > a.apm);
+            }
+#pragma unroll
+            for (int b = 0; b < kDeOctBatch; b++) {
+                if (!pass[b]) {
+                    nu++;
+                    continue;
+                }
+                float t;
+                if (oct_time_k(a.hoff[tb[b]], a.h0, t0, kc.tn0_sq, m0, fb[b].x, mhb[b], c, p1,
+                               &t) != DE_OK)
+                    continue;
+                const WinIdx wi = window_index(t, a.dt);
+                if (window_in_trace(wi.k, a.tau, (int)a.S)) {
+                    const float *tr = a.samples + (size_t)tb[b] * a.stride + (wi.k - a.tau);
+                    float y1 = __ldg(tr);
+#pragma unroll
+                    for (int j = 0; j < (W > 0 ? W : 1); j++) {
+                        const float y0 = y1;
+                        y1 = __ldg(tr + j + 1);
+                        float u = (y1 - y0) * wi.frac + y0;
+                        num[j] += u;
+                        lin += u;
+                        den += u * u;
+                    }
+                    used++;
+                }
+            }
+        }
+    }
     for (; q < cnt; q++) {
         const uint32_t ti = a.selIdx ? a.selIdx[first + q] : first + q;
         float t;
@@ -244,14 +296,14 @@ __device__ __forceinline__ void de_eval(const DeParams &d, float t0, float m0, u
 // call has more units than resident CTAs.
 constexpr int kDeThreads = 256;
 
-// OCT: six resident CTAs per SM (40 registers) -- its evaluation waits on
-// long dependent square-root / reciprocal chains, so resident warps pay
-// (3.5 % on the OCT DE workload).  CMP / ZO-CRS: four (64 registers), which
+// OCT: five resident CTAs per SM (48 registers) -- its evaluation waits on
+// long dependent square-root / reciprocal chains, so resident warps and the
+// batched displaced-midpoint tests (kDeOctBatch) both pay.  CMP / ZO-CRS: four (64 registers), which
 // their two-trace steps fit without spills (ZO-CRS DE, 2 midpoints: 41.9 ->
 // 38.1 ms; 16 midpoints unchanged; three- or four-trace steps and a 6-CTA
 // bound are slower).
 template <int MODEL, int W>
-__global__ void __launch_bounds__(kDeThreads, MODEL == kModelOct ? 6 : 4)
+__global__ void __launch_bounds__(kDeThreads, MODEL == kModelOct ? 5 : 4)
 de_kernel(DeParams d, uint32_t spc, uint32_t groups, uint32_t nUnits) {
     constexpr int NP = MODEL == kModelCmp ? 1 : (MODEL == kModelZocrs ? 3 : 2);
     const LsParams &a = d.ls;
