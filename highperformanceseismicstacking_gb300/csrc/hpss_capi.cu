@@ -1,4 +1,6 @@
-// hpss_capi.cu -- the C ABI of libhpss_gb300.so (declared in include/hpss.h).
+// hpss_capi.cu -- the C ABI of libhpss_gb300.so (declared in include/hpss.h):
+// handle lifecycle, the resident line, the setters and the extern "C" entry
+// points (the linear search and DE host logic are in ls_host.cu / de_host.cu).
 //
 // Host-side orchestration only: argument checks with the reference's error
 // semantics, device buffers owned by the handle, and the launch sequence
@@ -17,47 +19,17 @@
 #include <string>
 #include <vector>
 
-#include "../../include/hpss.h"
-#include "hpss_internal.h"
-
-namespace hpss {
-cudaError_t launch_select_range(const float *mid, uint32_t n, const float *m0s,
-                                uint32_t nM0, int mode, float apm, float radius,
-                                uint32_t *first, uint32_t *count,
-                                cudaStream_t st);
-cudaError_t launch_exclusive_scan(const uint32_t *count, uint32_t *first,
-                                  uint32_t n, cudaStream_t st);
-size_t tuned_stage_floats();
-size_t tuned_stage_floats_min();
-}  // namespace hpss
+#include "hpss_handle.h"
 
 using namespace hpss;
 
-struct hpss_handle_s : public Handle {
-    // scratch buffers, grown on demand
-    struct Buf {
-        void *p = nullptr;
-        size_t bytes = 0;
-    };
-    Buf params, chunkBounds, selFirst, selCount, selIdx, candFirst, candCount,
-        notUsed, errWord, m0s, out, octCands, prior, partial, order;
-    Buf octTab;                // OCT per-trace factors of the line (octTabH0)
-    bool octTabValid = false;
-    float octTabH0 = 0.f;
-    std::string gridKey;       // grid held in `params` (empty: none)
-    uint32_t boundsChunk = 0;  // chunk size of the bounds in `chunkBounds` (0: none)
-    std::vector<float> octCandsHost;
-    std::map<std::string, int> variantCache;  // autotuner decisions
-    int lastVariant = -1;
-    uint32_t lastParts = 1;                    // candidate parts of the last search
-    uint32_t meanFold = 0;                     // traces per distinct midpoint
-};
 
 namespace {
-
 thread_local std::string g_createError;
-
 const char *kVersion = "hpss-gb300 0.1.0 (sm_103a)";
+}  // namespace
+
+namespace hpss {
 
 struct Fail {
     hpss_status code;
@@ -69,18 +41,6 @@ hpss_status set_error(hpss_handle h, hpss_status code, const std::string &msg) {
     return code;
 }
 
-#define HPSS_CUDA_TRY(h, expr)                                                 \
-    do {                                                                       \
-        cudaError_t _e = (expr);                                               \
-        if (_e != cudaSuccess) {                                               \
-            return set_error(h, _e == cudaErrorMemoryAllocation                \
-                                    ? HPSS_ERR_OUT_OF_MEMORY                   \
-                                    : HPSS_ERR_CUDA,                           \
-                             std::string("CUDA error at ") + __FILE__ + ":" +  \
-                                 std::to_string(__LINE__) + " (" #expr "): " + \
-                                 cudaGetErrorString(_e));                      \
-        }                                                                      \
-    } while (0)
 
 cudaError_t ensure(hpss_handle h, hpss_handle_s::Buf &b, size_t bytes) {
     if (bytes == 0) bytes = 16;
@@ -277,612 +237,6 @@ int num_sms(hpss_handle h) {
     return v > 0 ? v : 1;
 }
 
-// Shapes of the tuned pair kernel: candidate pairs per thread and resident
-// CTAs per SM (more pairs: more independent chains per thread; more CTAs:
-// more warps to hide latency, a smaller shared-memory stage).
-constexpr int kTunedVariants = 3;
-constexpr int kVariantPairs[kTunedVariants] = {2, 1, 2};
-constexpr int kVariantCtasPerSm[kTunedVariants] = {2, 3, 3};
-
-// Candidate parts of the pair kernel: a call whose `base` (midpoint, tile)
-// units fill fewer than four waves of the resident CTAs is split into
-// candidate ranges, at most one per chunk.
-uint32_t pair_parts(uint64_t base, uint32_t nChunks, int numSms, int ctasPerSm) {
-    const uint64_t want = (uint64_t)numSms * (uint64_t)ctasPerSm * 4;
-    if (base == 0 || base >= want) return 1;
-    const uint64_t parts = std::min<uint64_t>((want + base - 1) / base, nChunks);
-    if (parts <= 1) return 1;
-    // equal ranges, none empty
-    const uint32_t per = (uint32_t)((nChunks + parts - 1) / parts);
-    return (nChunks + per - 1) / per;
-}
-
-// Autotuner: the first time a (model, window, candidates, samples, fold,
-// candidate split) key is seen, every variant is timed on a prefix of the work units (results are
-// overwritten by the real launch) and the fastest is cached in the handle.
-// HPSS_LS_VARIANT=<n> forces a variant.
-template <typename SetChunks, typename Launch>
-hpss_status choose_variant(hpss_handle h, const LsParams &lp, uint32_t units, bool exactStack,
-                           SetChunks setChunks, Launch launch, int *out) {
-    if (const char *env = std::getenv("HPSS_LS_VARIANT")) {
-        int v = std::atoi(env);
-        if (v >= 0 && v < kTunedVariants) {
-            *out = v;
-            return HPSS_OK;
-        }
-    }
-    // calls split into candidate ranges (few midpoints) have their own entry:
-    // the best shape differs from that of a call that fills the GPU by itself
-    const uint32_t split =
-        pair_parts(units, (lp.P + 2 * kTunedWarps * kVariantPairs[0] - 1) /
-                              (2 * kTunedWarps * kVariantPairs[0]),
-                   num_sms(h), kVariantCtasPerSm[0]);
-    const std::string key = std::to_string(h->model) + "/" + std::to_string(exactStack) + "/" +
-                            std::to_string(lp.w) + "/" +
-                            std::to_string(lp.P) + "/" + std::to_string(lp.S) + "/" +
-                            std::to_string(h->meanFold) + "/" + std::to_string(split);
-    auto it = h->variantCache.find(key);
-    if (it != h->variantCache.end()) {
-        *out = it->second;
-        return HPSS_OK;
-    }
-    const uint32_t sub = std::min<uint32_t>(units, (uint32_t)num_sms(h) * 12);
-    cudaEvent_t a, b;
-    HPSS_CUDA_TRY(h, cudaEventCreate(&a));
-    HPSS_CUDA_TRY(h, cudaEventCreate(&b));
-    float best = 3.4e38f;
-    int bestV = 0;
-    for (int v = 0; v < kTunedVariants; v++) {
-        HPSS_CUDA_TRY(h, setChunks(2 * kVariantPairs[v]));
-        HPSS_CUDA_TRY(h, launch(v, std::min<uint32_t>(sub, 64)));  // first-launch costs
-        HPSS_CUDA_TRY(h, cudaEventRecord(a, h->stream));
-        HPSS_CUDA_TRY(h, launch(v, sub));
-        HPSS_CUDA_TRY(h, cudaEventRecord(b, h->stream));
-        HPSS_CUDA_TRY(h, cudaEventSynchronize(b));
-        float ms = 0;
-        HPSS_CUDA_TRY(h, cudaEventElapsedTime(&ms, a, b));
-        if (ms < best) {
-            best = ms;
-            bestV = v;
-        }
-    }
-    cudaEventDestroy(a);
-    cudaEventDestroy(b);
-    h->variantCache[key] = bestV;
-    *out = bestV;
-    return HPSS_OK;
-}
-
-// A call that is one group of a larger call (hpss_linear_search_line):
-// the counters were cleared once for the whole call and this group's
-// per-midpoint counts start at `m0Offset`.
-struct GroupOfCall {
-    uint32_t m0Offset;
-};
-
-hpss_status linear_search_impl(hpss_handle h, const float *d_m0s, uint32_t nM0,
-                               const uint32_t *granularity, int kernel,
-                               float *d_out, hpss_stats *stats, bool sync,
-                               const GroupOfCall *group = nullptr) {
-    hpss_status rc = check_ready(h);
-    if (rc != HPSS_OK) return rc;
-    if (!granularity)
-        return set_error(h, HPSS_ERR_LOGIC, "granularity is required");
-    if (kernel != HPSS_KERNEL_PLAIN && kernel != HPSS_KERNEL_TUNED &&
-        kernel != HPSS_KERNEL_TUNED_EXACT)
-        return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "unknown kernel family");
-    const bool tuned = kernel != HPSS_KERNEL_PLAIN;
-    const bool exactStack = kernel == HPSS_KERNEL_TUNED_EXACT;
-    uint64_t P = 1;
-    uint32_t gran[3] = {1, 1, 1};
-    float inc[3] = {0, 0, 0}, low[3] = {0, 0, 0}, last[3] = {0, 0, 0};
-    for (uint32_t j = 0; j < h->np; j++) {
-        if (granularity[j] == 0)
-            return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "granularity must be > 0");
-        gran[j] = granularity[j];
-        P *= granularity[j];
-        if (h->gridMode == kGridReference) {
-            low[j] = h->lower[j];
-            // setupDiscretizationSteps (LinearSearchAlgorithm.cpp:137-139)
-            inc[j] = (h->upper[j] - h->lower[j]) / static_cast<float>(granularity[j]);
-        } else {
-            // inclusive: velocity uniform in c = 4/v^2 from c(lower) to c(upper)
-            float a = h->lower[j], b = h->upper[j];
-            if (j == 0) {
-                a = 4.0f / (h->lower[0] * h->lower[0]);
-                b = 4.0f / (h->upper[0] * h->upper[0]);
-            }
-            low[j] = a;
-            last[j] = b;
-            inc[j] = granularity[j] > 1 ? (b - a) / static_cast<float>(granularity[j] - 1) : 0.f;
-        }
-    }
-    if (P > 0x7fffffffull)
-        return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "too many candidates");
-    if (nM0 == 0) return HPSS_OK;
-    cudaSetDevice(h->device);
-
-    LsParams lp;
-    fill_line_params(h, lp);
-    lp.m0s = d_m0s;
-    lp.nM0 = nM0;
-    lp.P = (uint32_t)P;
-    lp.out = d_out;
-    HPSS_CUDA_TRY(h, use_oct_table(h, lp));
-
-    // The candidate grid (and below the chunk bounds) depend only on the
-    // model, the bounds, the granularity and the grid mode: a call that
-    // repeats the previous call's grid (one midpoint per call) reuses them
-    // from the handle's buffers instead of rebuilding them.
-    std::string gridKey = std::to_string(h->model) + "/" + std::to_string(h->gridMode) + "/" +
-                          std::to_string(h->np) + "/" + std::to_string(P);
-    for (uint32_t j = 0; j < h->np; j++) {
-        uint32_t bits[3];
-        std::memcpy(&bits[0], &low[j], 4);
-        std::memcpy(&bits[1], &inc[j], 4);
-        std::memcpy(&bits[2], &last[j], 4);
-        for (uint32_t b : bits) gridKey += "/" + std::to_string(b);
-        gridKey += "/" + std::to_string(gran[j]);
-    }
-    if (h->gridKey != gridKey) {
-        h->gridKey.clear();
-        h->boundsChunk = 0;
-        HPSS_CUDA_TRY(h, ensure(h, h->params, P * h->np * sizeof(float)));
-        HPSS_CUDA_TRY(h, launch_build_grid(h->model, h->gridMode, low, inc, last, gran,
-                                           static_cast<float *>(h->params.p), (uint32_t)P,
-                                           h->stream));
-        h->gridKey = gridKey;
-    }
-    lp.params = static_cast<float *>(h->params.p);
-    // candidates per thread of the tuned kernel: 2 * pairs (CMP / ZO-CRS),
-    // 4 (OCT); HPSS_LS_PAIRS overrides the pair count (1, 2 or 4)
-    // Tuned kernel: CMP / ZO-CRS run the branch-free pair kernel in one of
-    // kTunedVariants shapes (candidate pairs per thread x CTAs per SM), OCT the
-    // branchy kernel (4 candidates per thread).  The chunk bounds depend on
-    // the chunk size (8 warps x candidates per thread).
-    // precision modes run on the plain kernel
-    const bool pairKernel = tuned && h->precisionMode == 0 && h->model != HPSS_MODEL_OCT &&
-                            lp.w <= 15 && h->stride + 8 <= (uint32_t)tuned_stage_floats_min();
-    const bool octKernel =
-        tuned && h->precisionMode == 0 && h->model == HPSS_MODEL_OCT && lp.w <= 15;
-    // chunk bounds (read by the pair kernel only), rebuilt when the chunk size
-    // or the grid changed
-    auto setChunks = [&](int perThread) -> cudaError_t {
-        lp.chunkSize = kTunedWarps * perThread;
-        lp.nChunks = (lp.P + lp.chunkSize - 1) / lp.chunkSize;
-        if (h->boundsChunk != lp.chunkSize) {
-            h->boundsChunk = 0;
-            cudaError_t e =
-                ensure(h, h->chunkBounds, (size_t)lp.nChunks * 2 * h->np * sizeof(float));
-            if (e != cudaSuccess) return e;
-            e = launch_chunk_bounds(lp, static_cast<float *>(h->chunkBounds.p), h->stream);
-            if (e != cudaSuccess) return e;
-            h->boundsChunk = lp.chunkSize;
-        }
-        lp.chunkBounds = static_cast<float *>(h->chunkBounds.p);
-        return cudaSuccess;
-    };
-    // counters, cleared by one memset: error word at byte 0, the pair
-    // kernel's work-queue counter at byte 4, near-tie counter at byte 8, the
-    // per-midpoint notUsed counts from byte 16
-    if (!group) {
-        HPSS_CUDA_TRY(h, ensure(h, h->notUsed, 16 + nM0 * sizeof(unsigned long long)));
-        HPSS_CUDA_TRY(h, cudaMemsetAsync(h->notUsed.p, 0, 16 + nM0 * sizeof(unsigned long long),
-                                         h->stream));
-    }
-    char *counters = static_cast<char *>(h->notUsed.p);
-    lp.errorWord = reinterpret_cast<uint32_t *>(counters);
-    lp.nearTies = reinterpret_cast<unsigned long long *>(counters + 8);
-    lp.notUsed = reinterpret_cast<unsigned long long *>(counters + 16) +
-                 (group ? group->m0Offset : 0);
-
-    const uint32_t tiles = (h->S + kTileSamples - 1) / kTileSamples;
-    const uint64_t units = (uint64_t)nM0 * tiles;
-    uint32_t octParts = 1;
-    if (octKernel) {
-        if (nM0 > 1 && nM0 <= kMaxOrderedMidpoints)
-            HPSS_CUDA_TRY(h, ensure(h, h->order, nM0 * sizeof(uint32_t)));
-        // per-part best / runner-up of the OCT kernel
-        octParts = oct_parts(lp, (uint32_t)num_sms(h));
-        HPSS_CUDA_TRY(h, ensure(h, h->partial, oct_partial_bytes(nM0, h->S, octParts)));
-    } else if (pairKernel) {
-        // midpoints of the batch by descending selected traces (work-queue order)
-        if (nM0 > 1 && nM0 <= kMaxOrderedMidpoints)
-            HPSS_CUDA_TRY(h, ensure(h, h->order, nM0 * sizeof(uint32_t)));
-        // per-part best / runner-up of a split pair-kernel call, for the
-        // largest split of any shape (allocated before the timed region)
-        uint32_t maxParts = 1;
-        for (int v = 0; v < kTunedVariants; v++) {
-            const uint32_t chunk = kTunedWarps * 2 * kVariantPairs[v];
-            maxParts = std::max(maxParts, pair_parts(units, (lp.P + chunk - 1) / chunk,
-                                                     num_sms(h), kVariantCtasPerSm[v]));
-        }
-        if (maxParts > 1)
-            HPSS_CUDA_TRY(h, ensure(h, h->partial, (size_t)nM0 * maxParts * h->S * sizeof(PartBest)));
-    }
-
-    HPSS_CUDA_TRY(h, cudaEventRecord(h->ev0, h->stream));
-    rc = run_selection(h, d_m0s, nM0, lp);
-    if (rc != HPSS_OK) return rc;
-    HPSS_CUDA_TRY(h, cudaEventRecord(h->ev1, h->stream));
-    if (units > 0xffffffffull)
-        return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "too many (midpoint, tile) units");
-    // nBase (midpoint, tile) units, each split into the shape's candidate
-    // parts; a split launch of all units is followed by the ordered merge
-    uint32_t lastParts = 1;
-    // work queue of the pair kernel: heaviest midpoints first, units taken
-    // from a counter that every launch starts at zero
-    const bool ordered = pairKernel && nM0 > 1 && nM0 <= kMaxOrderedMidpoints;
-    if (ordered) {
-        HPSS_CUDA_TRY(h, launch_order_by_count(lp.selCount, nM0,
-                                               static_cast<uint32_t *>(h->order.p), h->stream));
-        lp.order = static_cast<const uint32_t *>(h->order.p);
-    }
-    uint32_t *unitCounter = reinterpret_cast<uint32_t *>(static_cast<char *>(h->notUsed.p) + 4);
-    auto launchPair = [&](int variant, uint32_t nBase) -> cudaError_t {
-        LsParams q = lp;
-        q.parts = pair_parts(units, lp.nChunks, num_sms(h), kVariantCtasPerSm[variant]);
-        q.chunksPerPart = (lp.nChunks + q.parts - 1) / q.parts;
-        q.partial = static_cast<PartBest *>(h->partial.p);
-        lastParts = q.parts;
-        const uint64_t nUnits = (uint64_t)nBase * q.parts;
-        if (nUnits > 0xffffffffull) return cudaErrorInvalidConfiguration;
-        const uint32_t grid = (uint32_t)std::min<uint64_t>(
-            nUnits, (uint64_t)num_sms(h) * kVariantCtasPerSm[variant]);
-        // more units than resident CTAs: take them from the work queue
-        if (nUnits > grid) {
-            q.unitCounter = unitCounter;
-            cudaError_t e0 = cudaMemsetAsync(unitCounter, 0, sizeof(uint32_t), h->stream);
-            if (e0 != cudaSuccess) return e0;
-        }
-        cudaError_t e =
-            h->model == HPSS_MODEL_CMP
-                ? launch_ls_tuned_cmp(q, grid, tiles, (uint32_t)nUnits, h->stream, variant,
-                                      exactStack)
-                : launch_ls_tuned_zocrs(q, grid, tiles, (uint32_t)nUnits, h->stream, variant,
-                                        exactStack);
-        if (e != cudaSuccess || q.parts == 1 || nBase != units) return e;
-        return launch_merge_parts(q, q.parts, q.partial, h->stream);
-    };
-    int variant = 0;
-    if (pairKernel) {
-        // the autotuner's timing launches (a prefix of the units) count no
-        // near-ties
-        unsigned long long *ties = lp.nearTies;
-        lp.nearTies = nullptr;
-        rc = choose_variant(h, lp, (uint32_t)units, exactStack, setChunks, launchPair, &variant);
-        lp.nearTies = ties;
-        if (rc != HPSS_OK) return rc;
-        HPSS_CUDA_TRY(h, setChunks(2 * kVariantPairs[variant]));
-        HPSS_CUDA_TRY(h, cudaEventRecord(h->ev1, h->stream));
-    }
-    if (pairKernel) {
-        HPSS_CUDA_TRY(h, launchPair(variant, (uint32_t)units));
-    } else if (octKernel) {
-        // work queue as for the pair kernel
-        if (nM0 > 1 && nM0 <= kMaxOrderedMidpoints) {
-            HPSS_CUDA_TRY(h, launch_order_by_count(lp.selCount, nM0,
-                                                   static_cast<uint32_t *>(h->order.p),
-                                                   h->stream));
-            lp.order = static_cast<const uint32_t *>(h->order.p);
-        }
-        lp.unitCounter = unitCounter;
-        HPSS_CUDA_TRY(h, cudaMemsetAsync(unitCounter, 0, sizeof(uint32_t), h->stream));
-        HPSS_CUDA_TRY(h, launch_ls_oct(lp, (uint32_t)num_sms(h), h->partial.p, octParts,
-                                       h->stream));
-    } else {
-        HPSS_CUDA_TRY(h, launch_ls_plain(lp, h->stream, h->precisionMode));
-    }
-    h->lastVariant = pairKernel ? variant : -1;
-    h->lastParts = pairKernel ? lastParts : octKernel ? octParts : 1;
-    HPSS_CUDA_TRY(h, cudaEventRecord(h->ev2, h->stream));
-
-    if (stats || sync) {
-        HPSS_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
-        uint32_t err = 0;
-        unsigned long long ties = 0;
-        HPSS_CUDA_TRY(h, cudaMemcpy(&err, lp.errorWord, sizeof(uint32_t), cudaMemcpyDeviceToHost));
-        HPSS_CUDA_TRY(h, cudaMemcpy(&ties, lp.nearTies, sizeof(ties), cudaMemcpyDeviceToHost));
-        if (stats) {
-            std::memset(stats, 0, sizeof(*stats));
-            stats->near_ties = (double)ties;
-            std::vector<uint32_t> cnt(nM0);
-            std::vector<unsigned long long> nu(nM0);
-            HPSS_CUDA_TRY(h, cudaMemcpy(cnt.data(), lp.selCount, nM0 * sizeof(uint32_t), cudaMemcpyDeviceToHost));
-            HPSS_CUDA_TRY(h, cudaMemcpy(nu.data(), lp.notUsed, nM0 * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
-            double sel = 0, nus = 0;
-            for (uint32_t i = 0; i < nM0; i++) {
-                sel += cnt[i];
-                nus += (double)nu[i];
-            }
-            stats->selected_traces = sel;
-            stats->evals = sel * (double)h->S * (double)P;
-            stats->not_used = nus;
-            float ms = 0;
-            cudaEventElapsedTime(&ms, h->ev1, h->ev2);
-            stats->kernel_ms = ms;
-            cudaEventElapsedTime(&ms, h->ev0, h->ev1);
-            stats->selection_ms = ms;
-            stats->device_error = err;
-            stats->kernel_variant = h->lastVariant;
-            stats->candidate_parts = h->lastParts;
-        }
-        if (err)
-            return set_error(h, HPSS_ERR_DEVICE_CHECK,
-                             "device check failed, error word " + std::to_string(err));
-    }
-    return HPSS_OK;
-}
-
-// Body of hpss_linear_search_line, after prepare_line: the amplitudes go
-// to the device in kStreamChunks trace ranges on the copy stream, the
-// midpoints are searched in kStreamGroups contiguous groups on the handle's
-// stream, each group waiting only for the chunk that holds the last trace
-// its midpoints can select, and each group's results go back on the copy
-// stream while the next group runs.
-constexpr uint32_t kStreamChunks = 8, kStreamGroups = 8;
-
-cudaError_t copy_line_rows(hpss_handle h, const float *samples, uint32_t a, uint32_t b,
-                           cudaStream_t st);
-
-hpss_status stream_line_and_search(hpss_handle h, const float *samples, const float *m0s,
-                                   uint32_t nM0, const uint32_t *granularity, int kernel,
-                                   float *out, hpss_stats *stats) {
-    if (!h->copyStream)
-        HPSS_CUDA_TRY(h, cudaStreamCreateWithFlags(&h->copyStream, cudaStreamNonBlocking));
-    while (h->streamEvents.size() < kStreamChunks + kStreamGroups) {
-        cudaEvent_t e;
-        HPSS_CUDA_TRY(h, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-        h->streamEvents.push_back(e);
-    }
-    if (!h->streamT0) HPSS_CUDA_TRY(h, cudaEventCreate(&h->streamT0));
-    if (!h->streamT1) HPSS_CUDA_TRY(h, cudaEventCreate(&h->streamT1));
-    cudaEvent_t *chunkDone = h->streamEvents.data();
-    cudaEvent_t *groupDone = chunkDone + kStreamChunks;
-    const uint32_t n = h->nTraces;
-    uint32_t bound[kStreamChunks + 1];
-    for (uint32_t k = 0; k <= kStreamChunks; k++)
-        bound[k] = (uint32_t)((uint64_t)n * k / kStreamChunks);
-    if (n && h->stride != h->S)
-        HPSS_CUDA_TRY(h, cudaMemsetAsync(h->dSamples, 0, (size_t)n * h->stride * sizeof(float),
-                                         h->copyStream));
-    for (uint32_t k = 0; k < kStreamChunks; k++) {
-        HPSS_CUDA_TRY(h, copy_line_rows(h, samples, bound[k], bound[k + 1], h->copyStream));
-        HPSS_CUDA_TRY(h, cudaEventRecord(chunkDone[k], h->copyStream));
-    }
-    // every search below waits for the chunks it reads
-    h->gatherReady = true;
-    if (nM0 == 0) {
-        HPSS_CUDA_TRY(h, cudaStreamSynchronize(h->copyStream));
-        HPSS_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
-        if (stats) std::memset(stats, 0, sizeof(*stats));
-        return HPSS_OK;
-    }
-    const size_t block = (size_t)(2 + h->np) * h->S;
-    HPSS_CUDA_TRY(h, ensure(h, h->m0s, nM0 * sizeof(float)));
-    HPSS_CUDA_TRY(h, ensure(h, h->out, nM0 * block * sizeof(float)));
-    HPSS_CUDA_TRY(h, ensure(h, h->notUsed, 16 + nM0 * sizeof(unsigned long long)));
-    HPSS_CUDA_TRY(h, cudaMemcpyAsync(h->m0s.p, m0s, nM0 * sizeof(float),
-                                     cudaMemcpyHostToDevice, h->stream));
-    HPSS_CUDA_TRY(h, cudaMemsetAsync(h->notUsed.p, 0, 16 + nM0 * sizeof(unsigned long long),
-                                     h->stream));
-    HPSS_CUDA_TRY(h, cudaEventRecord(h->streamT0, h->stream));
-    // midpoint distance within which a trace can be selected, widened so that
-    // a group never starts before its traces have arrived
-    float hmax = 0.f;
-    for (float v : h->hHoff) hmax = std::max(hmax, std::fabs(v));
-    const float radius = h->model == HPSS_MODEL_CMP ? 0.f
-                         : h->model == HPSS_MODEL_ZOCRS
-                             ? h->apm
-                             : h->apm + std::sqrt(hmax * hmax + h->h0 * h->h0);
-    // groups of ceil(nM0 / kStreamGroups) midpoints, the last one smaller: the
-    // first group is the largest, so the per-call buffers the search grows
-    // (selection, candidate parts) are sized by it and never reallocated
-    // under a later group's launches
-    const uint32_t per = (nM0 + kStreamGroups - 1) / kStreamGroups;
-    const uint32_t G = (nM0 + per - 1) / per;
-    auto first = [&](uint32_t g) { return std::min(g * per, nM0); };
-    auto back = [&](uint32_t g) -> cudaError_t {
-        cudaError_t e = cudaStreamWaitEvent(h->copyStream, groupDone[g], 0);
-        if (e != cudaSuccess) return e;
-        const size_t i0 = first(g), cnt = first(g + 1) - i0;
-        return cudaMemcpyAsync(out + i0 * block, static_cast<float *>(h->out.p) + i0 * block,
-                               cnt * block * sizeof(float), cudaMemcpyDeviceToHost,
-                               h->copyStream);
-    };
-    for (uint32_t g = 0; g < G; g++) {
-        const uint32_t i0 = first(g), i1 = first(g + 1);
-        size_t need = 0;
-        for (uint32_t i = i0; i < i1 && need < n; i++) {
-            const float m0 = m0s[i];
-            if (!std::isfinite(m0)) {
-                need = n;
-                break;
-            }
-            const float reach = m0 + radius + 1e-3f * (std::fabs(m0) + radius) + 1.f;
-            need = std::max<size_t>(
-                need, std::upper_bound(h->hMid.begin(), h->hMid.end(), reach) - h->hMid.begin());
-        }
-        if (need > 0) {
-            uint32_t k = 0;
-            while (bound[k + 1] < need) k++;
-            HPSS_CUDA_TRY(h, cudaStreamWaitEvent(h->stream, chunkDone[k], 0));
-        }
-        const GroupOfCall grp{i0};
-        hpss_status rc = linear_search_impl(h, static_cast<float *>(h->m0s.p) + i0, i1 - i0,
-                                            granularity, kernel,
-                                            static_cast<float *>(h->out.p) + i0 * block, nullptr,
-                                            false, &grp);
-        if (rc != HPSS_OK) return rc;
-        HPSS_CUDA_TRY(h, cudaEventRecord(groupDone[g], h->stream));
-        // the previous group's results return while this group runs
-        if (g > 0) HPSS_CUDA_TRY(h, back(g - 1));
-    }
-    HPSS_CUDA_TRY(h, cudaEventRecord(h->streamT1, h->stream));
-    HPSS_CUDA_TRY(h, back(G - 1));
-    HPSS_CUDA_TRY(h, cudaStreamSynchronize(h->copyStream));
-    HPSS_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
-    const char *counters = static_cast<const char *>(h->notUsed.p);
-    uint32_t err = 0;
-    unsigned long long ties = 0;
-    HPSS_CUDA_TRY(h, cudaMemcpy(&err, counters, sizeof(err), cudaMemcpyDeviceToHost));
-    HPSS_CUDA_TRY(h, cudaMemcpy(&ties, counters + 8, sizeof(ties), cudaMemcpyDeviceToHost));
-    if (stats) {
-        std::memset(stats, 0, sizeof(*stats));
-        // selected traces of every midpoint, for the evaluation count
-        LsParams lp;
-        fill_line_params(h, lp);
-        lp.m0s = static_cast<float *>(h->m0s.p);
-        lp.nM0 = nM0;
-        hpss_status rc = run_selection(h, lp.m0s, nM0, lp);
-        if (rc != HPSS_OK) return rc;
-        std::vector<uint32_t> cnt(nM0);
-        std::vector<unsigned long long> nu(nM0);
-        HPSS_CUDA_TRY(h, cudaMemcpyAsync(cnt.data(), lp.selCount, nM0 * sizeof(uint32_t),
-                                         cudaMemcpyDeviceToHost, h->stream));
-        HPSS_CUDA_TRY(h, cudaMemcpyAsync(nu.data(), counters + 16,
-                                         nM0 * sizeof(unsigned long long),
-                                         cudaMemcpyDeviceToHost, h->stream));
-        HPSS_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
-        double P = 1, sel = 0, nus = 0;
-        for (uint32_t j = 0; j < h->np; j++) P *= granularity[j];
-        for (uint32_t i = 0; i < nM0; i++) {
-            sel += cnt[i];
-            nus += (double)nu[i];
-        }
-        stats->selected_traces = sel;
-        stats->evals = sel * (double)h->S * P;
-        stats->not_used = nus;
-        float ms = 0;
-        cudaEventElapsedTime(&ms, h->streamT0, h->streamT1);
-        stats->kernel_ms = ms;
-        stats->device_error = err;
-        stats->kernel_variant = h->lastVariant;
-        stats->near_ties = (double)ties;
-        stats->candidate_parts = h->lastParts;
-    }
-    if (err)
-        return set_error(h, HPSS_ERR_DEVICE_CHECK,
-                         "device check failed, error word " + std::to_string(err));
-    return HPSS_OK;
-}
-
-hpss_status de_impl(hpss_handle h, const float *d_m0s, uint32_t nM0, uint32_t pop,
-                    uint32_t gens, float F, float CR, uint64_t seed, float *d_out,
-                    hpss_stats *stats, bool sync) {
-    hpss_status rc = check_ready(h);
-    if (rc != HPSS_OK) return rc;
-    if (pop < 1 || pop > kDeMaxPopulation)
-        return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "population must be in [1, 128]");
-    if (gens < 1) return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "generations must be >= 1");
-    if (nM0 == 0) return HPSS_OK;
-    if (!d_m0s || !d_out) return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "null device pointer");
-    cudaSetDevice(h->device);
-
-    DeParams d{};
-    fill_line_params(h, d.ls);
-    d.ls.m0s = d_m0s;
-    d.ls.nM0 = nM0;
-    d.ls.out = d_out;
-    HPSS_CUDA_TRY(h, use_oct_table(h, d.ls));
-    d.pop = pop;
-    d.gens = gens;
-    d.F = F;
-    d.CR = CR;
-    d.seedLo = (uint32_t)seed;
-    d.seedHi = (uint32_t)(seed >> 32);
-    for (int j = 0; j < 3; j++) {
-        d.lo[j] = h->lower[j];
-        d.hi[j] = h->upper[j];
-    }
-    HPSS_CUDA_TRY(h, ensure(h, h->notUsed, nM0 * sizeof(unsigned long long)));
-    // error word at byte 0, the DE kernel's work-queue counter at byte 8
-    HPSS_CUDA_TRY(h, ensure(h, h->errWord, 16));
-    d.ls.notUsed = static_cast<unsigned long long *>(h->notUsed.p);
-    d.ls.errorWord = static_cast<uint32_t *>(h->errWord.p);
-    d.ls.unitCounter = reinterpret_cast<uint32_t *>(static_cast<char *>(h->errWord.p) + 8);
-    HPSS_CUDA_TRY(h, cudaMemsetAsync(d.ls.notUsed, 0, nM0 * sizeof(unsigned long long), h->stream));
-    HPSS_CUDA_TRY(h, cudaMemsetAsync(h->errWord.p, 0, 16, h->stream));
-    const bool ordered = nM0 > 1 && nM0 <= kMaxOrderedMidpoints;
-    if (ordered) HPSS_CUDA_TRY(h, ensure(h, h->order, nM0 * sizeof(uint32_t)));
-
-    HPSS_CUDA_TRY(h, cudaEventRecord(h->ev0, h->stream));
-    // selection: CMP / ZO-CRS as linear search; OCT with the initial population
-    HPSS_CUDA_TRY(h, ensure(h, h->selFirst, nM0 * sizeof(uint32_t)));
-    HPSS_CUDA_TRY(h, ensure(h, h->selCount, nM0 * sizeof(uint32_t)));
-    d.ls.selFirst = static_cast<uint32_t *>(h->selFirst.p);
-    d.ls.selCount = static_cast<uint32_t *>(h->selCount.p);
-    d.ls.selIdx = nullptr;
-    if (h->model != HPSS_MODEL_OCT) {
-        HPSS_CUDA_TRY(h, launch_select_range(h->dMid, h->nTraces, d_m0s, nM0,
-                                             h->model == HPSS_MODEL_CMP ? 0 : 1, h->apm, 0.f,
-                                             static_cast<uint32_t *>(h->selFirst.p),
-                                             static_cast<uint32_t *>(h->selCount.p), h->stream));
-    } else {
-        float hmax = 0.f;
-        for (float v : h->hHoff) hmax = std::max(hmax, std::fabs(v));
-        float radius = (h->apm + std::sqrt(hmax * hmax + h->h0 * h->h0)) * 1.001f + 1.0f;
-        HPSS_CUDA_TRY(h, ensure(h, h->candFirst, nM0 * sizeof(uint32_t)));
-        HPSS_CUDA_TRY(h, ensure(h, h->candCount, nM0 * sizeof(uint32_t)));
-        uint32_t *cf = static_cast<uint32_t *>(h->candFirst.p);
-        uint32_t *cc = static_cast<uint32_t *>(h->candCount.p);
-        HPSS_CUDA_TRY(h, launch_select_range(h->dMid, h->nTraces, d_m0s, nM0, 2, h->apm, radius,
-                                             cf, cc, h->stream));
-        HPSS_CUDA_TRY(h, launch_exclusive_scan(cc, static_cast<uint32_t *>(h->selFirst.p), nM0,
-                                               h->stream));
-        std::vector<uint32_t> ccHost(nM0);
-        HPSS_CUDA_TRY(h, cudaMemcpyAsync(ccHost.data(), cc, nM0 * sizeof(uint32_t),
-                                         cudaMemcpyDeviceToHost, h->stream));
-        HPSS_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
-        size_t total = 0;
-        for (uint32_t v : ccHost) total += v;
-        HPSS_CUDA_TRY(h, ensure(h, h->selIdx, total * sizeof(uint32_t)));
-        d.ls.selIdx = static_cast<uint32_t *>(h->selIdx.p);
-        HPSS_CUDA_TRY(h, launch_de_select_oct(d, cf, cc, static_cast<uint32_t *>(h->selIdx.p),
-                                              static_cast<uint32_t *>(h->selCount.p),
-                                              h->stream));
-    }
-    // work queue order: midpoints by descending selected traces
-    if (ordered) {
-        HPSS_CUDA_TRY(h, launch_order_by_count(d.ls.selCount, nM0,
-                                               static_cast<uint32_t *>(h->order.p), h->stream));
-        d.ls.order = static_cast<const uint32_t *>(h->order.p);
-    }
-    HPSS_CUDA_TRY(h, cudaEventRecord(h->ev1, h->stream));
-    const uint64_t units = (uint64_t)nM0 * h->S;
-    if (units > 0xffffffffull)
-        return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "too many (midpoint, sample) units");
-    HPSS_CUDA_TRY(h, launch_de(d, h->model, (uint32_t)num_sms(h), h->stream));
-    HPSS_CUDA_TRY(h, cudaEventRecord(h->ev2, h->stream));
-    if (stats || sync) {
-        HPSS_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
-        if (stats) {
-            std::memset(stats, 0, sizeof(*stats));
-            std::vector<uint32_t> cnt(nM0);
-            std::vector<unsigned long long> nu(nM0);
-            HPSS_CUDA_TRY(h, cudaMemcpy(cnt.data(), d.ls.selCount, nM0 * sizeof(uint32_t),
-                                        cudaMemcpyDeviceToHost));
-            HPSS_CUDA_TRY(h, cudaMemcpy(nu.data(), d.ls.notUsed,
-                                        nM0 * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
-            double sel = 0, nus = 0;
-            for (uint32_t i = 0; i < nM0; i++) {
-                sel += cnt[i];
-                nus += (double)nu[i];
-            }
-            stats->selected_traces = sel;
-            stats->evals = sel * (double)h->S * (double)pop * (double)gens;
-            stats->not_used = nus;
-            float ms = 0;
-            cudaEventElapsedTime(&ms, h->ev1, h->ev2);
-            stats->kernel_ms = ms;
-            cudaEventElapsedTime(&ms, h->ev0, h->ev1);
-            stats->selection_ms = ms;
-            stats->kernel_variant = -1;
-        }
-    }
-    return HPSS_OK;
-}
-
 // A new line, everything but the amplitudes: validation, host geometry,
 // device buffers (grown as needed) and the geometry copies on the handle's
 // stream.  The amplitudes follow with copy_line_rows.
@@ -977,9 +331,6 @@ cudaError_t copy_line_rows(hpss_handle h, const float *samples, uint32_t a, uint
                                   (uint32_t)rows, h->S, h->stride, h->storage, st);
 }
 
-}  // namespace
-
-namespace hpss {
 // error message of a handle-less call, read back with hpss_last_error(NULL)
 void set_thread_error(const std::string &msg) { g_createError = msg; }
 }  // namespace hpss
