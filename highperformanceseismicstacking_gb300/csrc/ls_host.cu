@@ -64,7 +64,10 @@ hpss_status choose_variant(hpss_handle h, const LsParams &lp, uint32_t units, bo
         *out = it->second;
         return HPSS_OK;
     }
-    const uint32_t sub = std::min<uint32_t>(units, (uint32_t)num_sms(h) * 12);
+    // trial prefix: three waves of the 2-CTA shape, two of the 3-CTA shapes
+    // (a ZO-CRS unit of 18081 candidates takes ~0.3 s, so the prefix bounds
+    // the first call's tuning time)
+    const uint32_t sub = std::min<uint32_t>(units, (uint32_t)num_sms(h) * 6);
     cudaEvent_t a, b;
     HPSS_CUDA_TRY(h, cudaEventCreate(&a));
     HPSS_CUDA_TRY(h, cudaEventCreate(&b));
