@@ -8,6 +8,8 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -35,9 +37,15 @@ uint32_t pair_parts(uint64_t base, uint32_t nChunks, int numSms, int ctasPerSm) 
     return (nChunks + per - 1) / per;
 }
 
-// Autotuner: the first time a (model, window, candidates, samples, fold,
-// candidate split) key is seen, every variant is timed on a prefix of the work units (results are
-// overwritten by the real launch) and the fastest is cached in the handle.
+// Autotuner decisions shared by the handles of the process (keys carry the
+// device), so that a handle opened after another one does not tune again.
+std::mutex g_variantMutex;
+std::map<std::string, int> g_variantCache;
+
+// Autotuner: the first time a (device, storage, model, window, candidates,
+// samples, fold, candidate split) key is seen, every variant is timed on a prefix of the work units (results are
+// overwritten by the real launch) and the fastest is cached in the handle
+// and in the process-wide table.
 // HPSS_LS_VARIANT=<n> forces a variant.
 template <typename SetChunks, typename Launch>
 hpss_status choose_variant(hpss_handle h, const LsParams &lp, uint32_t units, bool exactStack,
@@ -55,7 +63,8 @@ hpss_status choose_variant(hpss_handle h, const LsParams &lp, uint32_t units, bo
         pair_parts(units, (lp.P + 2 * kTunedWarps * kVariantPairs[0] - 1) /
                               (2 * kTunedWarps * kVariantPairs[0]),
                    num_sms(h), kVariantCtasPerSm[0]);
-    const std::string key = std::to_string(h->model) + "/" + std::to_string(exactStack) + "/" +
+    const std::string key = std::to_string(h->device) + "/" + std::to_string(h->storage) + "/" +
+                            std::to_string(h->model) + "/" + std::to_string(exactStack) + "/" +
                             std::to_string(lp.w) + "/" +
                             std::to_string(lp.P) + "/" + std::to_string(lp.S) + "/" +
                             std::to_string(h->meanFold) + "/" + std::to_string(split);
@@ -64,13 +73,30 @@ hpss_status choose_variant(hpss_handle h, const LsParams &lp, uint32_t units, bo
         *out = it->second;
         return HPSS_OK;
     }
+    {
+        // decided already by another handle of this process on this device
+        std::lock_guard<std::mutex> lock(g_variantMutex);
+        auto g = g_variantCache.find(key);
+        if (g != g_variantCache.end()) {
+            h->variantCache[key] = g->second;
+            *out = g->second;
+            return HPSS_OK;
+        }
+    }
     // trial prefix: three waves of the 2-CTA shape, two of the 3-CTA shapes
     // (a ZO-CRS unit of 18081 candidates takes ~0.3 s, so the prefix bounds
     // the first call's tuning time)
     const uint32_t sub = std::min<uint32_t>(units, (uint32_t)num_sms(h) * 6);
-    cudaEvent_t a, b;
-    HPSS_CUDA_TRY(h, cudaEventCreate(&a));
-    HPSS_CUDA_TRY(h, cudaEventCreate(&b));
+    struct Events {
+        cudaEvent_t a = nullptr, b = nullptr;
+        ~Events() {
+            if (a) cudaEventDestroy(a);
+            if (b) cudaEventDestroy(b);
+        }
+    } ev;
+    HPSS_CUDA_TRY(h, cudaEventCreate(&ev.a));
+    HPSS_CUDA_TRY(h, cudaEventCreate(&ev.b));
+    cudaEvent_t a = ev.a, b = ev.b;
     float best = 3.4e38f;
     int bestV = 0;
     for (int v = 0; v < kTunedVariants; v++) {
@@ -87,9 +113,11 @@ hpss_status choose_variant(hpss_handle h, const LsParams &lp, uint32_t units, bo
             bestV = v;
         }
     }
-    cudaEventDestroy(a);
-    cudaEventDestroy(b);
     h->variantCache[key] = bestV;
+    {
+        std::lock_guard<std::mutex> lock(g_variantMutex);
+        g_variantCache.emplace(key, bestV);
+    }
     *out = bestV;
     return HPSS_OK;
 }

@@ -433,3 +433,22 @@ def test_work_queue_multi_wave_calls(engine):
     tuned, _ = engine.linear_search(m0s, [21], "tuned")
     assert st["device_error"] == 0 and np.array_equal(exact, plain)
     assert_same_but_stack(tuned, plain, 1)
+
+
+def test_autotuner_decision_shared_across_handles(c1_line):
+    """A handle opened after another one of the same device reuses the
+    shape the first one tuned for the same call (the decision table is
+    shared by the handles of the process); its results equal the first
+    handle's."""
+    w = synthetic.WORKLOADS["cmp-small"]
+    m0s = c1_line.cdp_midpoints
+    with capi.Engine(0) as first:
+        _setup(first, c1_line, "cmp", w.lower, w.upper, 2)
+        want, st0 = first.linear_search(m0s, w.granularity, "tuned")
+    assert st0["kernel_variant"] >= 0
+    for _ in range(3):
+        with capi.Engine(0) as later:
+            _setup(later, c1_line, "cmp", w.lower, w.upper, 2)
+            got, st = later.linear_search(m0s, w.granularity, "tuned")
+        assert st["kernel_variant"] == st0["kernel_variant"]
+        assert np.array_equal(got, want)
