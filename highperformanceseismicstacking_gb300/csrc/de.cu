@@ -103,11 +103,20 @@ __device__ __forceinline__ float2 de_f2(float a, float b) { return make_float2(a
 // 814 / 3037 ms)
 constexpr int kDeOctBatch = 4;
 
+// (t0, slope) box of a warp's OCT evaluations for oct_box_may_pass.
+struct OctBox {
+    float t0Lo, t0Hi, sLo, sHi;
+    bool on;
+};
+
 // Semblance of one candidate (raw parameters) over the selected traces.
+// OCT with box->on: called by all 32 lanes of the warp (a collective over
+// blocks of 32 traces); lanes with ev false take part in the box test only.
 template <int MODEL, int W>
 __device__ __forceinline__ void de_eval(const DeParams &d, float t0, float m0, uint32_t first,
                                         uint32_t cnt, const float *x, float *sembl,
-                                        float *stack, unsigned *notUsed) {
+                                        float *stack, unsigned *notUsed, bool ev = true,
+                                        const OctBox *box = nullptr) {
     const LsParams &a = d.ls;
     const float v = x[0];
     const float c = 4.0f / (v * v);
@@ -203,51 +212,53 @@ __device__ __forceinline__ void de_eval(const DeParams &d, float t0, float m0, u
     }
     // OCT: (t0, candidate) factors once, trace factors from the line's table
     const OctCand kc = oct_cand(t0, c, p1, MODEL == kModelOct ? a.h0 : 0.f);
-    if (MODEL == kModelOct && W > 0) {
+    if constexpr (MODEL == kModelOct && W > 0) {
+      if (box && box->on) {
+        // blocks of 32 traces: lane j tests trace qb + j against the warp's
+        // (t0, slope) box, then the lanes evaluate the traces kept, in order
+        const int lane = threadIdx.x & 31;
+        for (uint32_t qb = 0; qb < cnt; qb += 32) {
+            const uint32_t n = min(32u, cnt - qb);
+            bool keep = false;
+            if ((uint32_t)lane < n) {
+                const uint32_t ti = a.selIdx ? a.selIdx[first + qb + lane] : first + qb + lane;
+                keep = oct_box_may_pass(__ldg(a.octTab + ti), box->sLo, box->sHi, box->t0Lo,
+                                        box->t0Hi, m0, a.apm);
+            }
+            uint32_t mask = __ballot_sync(0xffffffffu, keep);
+            if (ev) nu += n - (uint32_t)__popc(mask);
+            while (mask) {
+                uint32_t tb[kDeOctBatch];
+                bool live[kDeOctBatch];
+                const uint32_t firstBit = (uint32_t)__ffs(mask) - 1;
+#pragma unroll
+                for (int b = 0; b < kDeOctBatch; b++) {
+                    live[b] = mask != 0;
+                    const uint32_t bit = live[b] ? (uint32_t)__ffs(mask) - 1 : firstBit;
+                    if (live[b]) mask &= mask - 1;
+                    tb[b] = a.selIdx ? a.selIdx[first + qb + bit] : first + qb + bit;
+                }
+                if (ev)
+                    oct_eval_batch<W, kDeOctBatch>(a, tb, live, kc, c, p1, t0, m0, num,
+                                                               lin, den, used, nu);
+            }
+        }
+        q = cnt;
+      } else {
         // the displaced-midpoint tests of kDeOctBatch traces side by side
         // (independent chains), then the passing traces in order
         for (; q + kDeOctBatch <= cnt; q += kDeOctBatch) {
             uint32_t tb[kDeOctBatch];
-            float4 fb[kDeOctBatch];  // {m, gamma^2, 16h^2h0^2, h^2-h0^2}
-            float mhb[kDeOctBatch];
-            bool pass[kDeOctBatch];
+            bool live[kDeOctBatch];
 #pragma unroll
             for (int b = 0; b < kDeOctBatch; b++) {
                 tb[b] = a.selIdx ? a.selIdx[first + q + b] : first + q + b;
-                fb[b] = __ldg(a.octTab + tb[b]);
+                live[b] = true;
             }
-#pragma unroll
-            for (int b = 0; b < kDeOctBatch; b++) {
-                const int e = oct_mh_all(kc, fb[b].y, fb[b].z, fb[b].w, m0, &mhb[b]);
-                pass[b] = e == DE_OK && !(fabsf(fb[b].x - mhb[b]) > a.apm);
-            }
-#pragma unroll
-            for (int b = 0; b < kDeOctBatch; b++) {
-                if (!pass[b]) {
-                    nu++;
-                    continue;
-                }
-                float t;
-                if (oct_time_k(a.hoff[tb[b]], a.h0, t0, kc.tn0_sq, m0, fb[b].x, mhb[b], c, p1,
-                               &t) != DE_OK)
-                    continue;
-                const WinIdx wi = window_index(t, a.dt);
-                if (window_in_trace(wi.k, a.tau, (int)a.S)) {
-                    const float *tr = a.samples + (size_t)tb[b] * a.stride + (wi.k - a.tau);
-                    float y1 = __ldg(tr);
-#pragma unroll
-                    for (int j = 0; j < (W > 0 ? W : 1); j++) {
-                        const float y0 = y1;
-                        y1 = __ldg(tr + j + 1);
-                        float u = (y1 - y0) * wi.frac + y0;
-                        num[j] += u;
-                        lin += u;
-                        den += u * u;
-                    }
-                    used++;
-                }
-            }
+            oct_eval_batch<W, kDeOctBatch>(a, tb, live, kc, c, p1, t0, m0, num, lin,
+                                                       den, used, nu);
         }
+      }
     }
     for (; q < cnt; q++) {
         const uint32_t ti = a.selIdx ? a.selIdx[first + q] : first + q;
@@ -345,12 +356,33 @@ de_kernel(DeParams d, uint32_t spc, uint32_t groups, uint32_t nUnits) {
         PERM[rank] = threadIdx.x;
         __syncthreads();
         const uint32_t o = PERM[threadIdx.x];  // the member whose trial this thread evaluates
-        if (KEY[o] != __int_as_float(0x7f800000)) {
-            const float t0o = (s0f + static_cast<float>(o / pop)) * a.dt;
+        const bool ev = KEY[o] != __int_as_float(0x7f800000);
+        const float t0o = (s0f + static_cast<float>(o / pop)) * a.dt;
+        // the warp's (t0, slope) box for the displaced-midpoint box test
+        // (h0 = 0; t0 = 0 fails every test by itself and stays out)
+        OctBox box;
+        const bool inBox = ev && t0o > 0.f;
+        const float inf = __int_as_float(0x7f800000);
+        box.t0Lo = inBox ? t0o : inf;
+        box.t0Hi = inBox ? t0o : -inf;
+        box.sLo = inBox ? TR[o * NP + NP - 1] : inf;
+        box.sHi = inBox ? TR[o * NP + NP - 1] : -inf;
+#pragma unroll
+        for (int sh = 16; sh; sh >>= 1) {
+            box.t0Lo = fminf(box.t0Lo, __shfl_xor_sync(0xffffffffu, box.t0Lo, sh));
+            box.t0Hi = fmaxf(box.t0Hi, __shfl_xor_sync(0xffffffffu, box.t0Hi, sh));
+            box.sLo = fminf(box.sLo, __shfl_xor_sync(0xffffffffu, box.sLo, sh));
+            box.sHi = fmaxf(box.sHi, __shfl_xor_sync(0xffffffffu, box.sHi, sh));
+        }
+        box.on = MODEL == kModelOct && W > 0 && a.octBox && a.h0 == 0.f && box.t0Lo >= kOctBoxMinT0 &&
+                 box.t0Hi >= box.t0Lo;
+        if (box.on || ev) {
             float fo, fko;
-            de_eval<MODEL, W>(d, t0o, m0, first, cnt, TR + o * NP, &fo, &fko, notUsed);
-            RES[2 * o] = fo;
-            RES[2 * o + 1] = fko;
+            de_eval<MODEL, W>(d, t0o, m0, first, cnt, TR + o * NP, &fo, &fko, notUsed, ev, &box);
+            if (ev) {
+                RES[2 * o] = fo;
+                RES[2 * o + 1] = fko;
+            }
         }
         __syncthreads();
         *f = RES[2 * threadIdx.x];

@@ -228,6 +228,10 @@ cudaError_t use_oct_table(hpss_handle h, LsParams &lp) {
         h->octTabH0 = h->h0;
     }
     lp.octTab = static_cast<const float4 *>(h->octTab.p);
+    // HPSS_OCT_BOX_TEST=0 turns the displaced-midpoint box test off (every
+    // trace through the per-sample test; same results, for A/B checks)
+    const char *box = std::getenv("HPSS_OCT_BOX_TEST");
+    lp.octBox = !(box && box[0] == '0');
     return cudaSuccess;
 }
 

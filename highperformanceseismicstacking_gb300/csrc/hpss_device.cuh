@@ -287,4 +287,84 @@ __device__ __forceinline__ bool near_tie(float best, float second) {
     return best > 0.f && second >= 0.f && best - second <= kNearTieRel * fmaxf(best, 1e-3f);
 }
 
+// Displaced-midpoint test for a box of (t0, slope) at once, h0 = 0.  There
+// the OCT formula (oct/common.cuh:7-35) reduces to
+//     mh - m0 = 2 s h^2 / (t0 + sqrt(t0^2 + 4 s^2 h^2))
+// (sqrt(arg2) = t0 (t0 + sqrt(t0^2 + 4 s^2 h^2)) in real arithmetic), which
+// increases with the slope s and, for a fixed s, moves toward 0 as t0 grows.
+// So over t0 in [t0Lo, t0Hi] and s in [sLo, sHi] mh lies between its values
+// at two corners, and a trace whose midpoint is farther than apm from that
+// whole interval fails the per-(t0, candidate) test of every member of the
+// box: a warp counts it as not used without evaluating it lane by lane.  The
+// margin covers the FP32 roundings of both forms (relative 1e-4 of the
+// displacement, 1e-5 of the coordinates; the two FP32 evaluations differ
+// from the real value by a few ulps).  The exact per-lane test still decides
+// every trace the box keeps, so results and not-used counts are those of the
+// per-lane test.  Used with t0Lo >= kOctBoxMinT0 (the FP32 terms of the
+// reference's form stay normal there); t0 = 0 fails the exact test anyway
+// (division by zero) and stays out of the box.  tf = {m, gamma^2 (= 4 h^2),
+// 16 h^2 h0^2, h^2 - h0^2 (= h^2)} from the line's factor table.
+constexpr float kOctBoxMinT0 = 1e-4f;
+__device__ __forceinline__ bool oct_box_may_pass(const float4 &tf, float sLo, float sHi,
+                                                 float t0Lo, float t0Hi, float m0, float apm) {
+    const float tForHi = sHi > 0.f ? t0Lo : t0Hi;
+    const float tForLo = sLo > 0.f ? t0Hi : t0Lo;
+    const float hi = 2.f * sHi * tf.w / (tForHi + sqrtf(fmaf(tForHi, tForHi, sHi * sHi * tf.y)));
+    const float lo = 2.f * sLo * tf.w / (tForLo + sqrtf(fmaf(tForLo, tForLo, sLo * sLo * tf.y)));
+    const float marg = 1e-4f * fmaxf(fabsf(lo), fabsf(hi)) +
+                       1e-5f * (fabsf(m0) + fabsf(tf.x)) + 1e-3f;
+    // NaN anywhere keeps the trace
+    return !((m0 + lo) - marg > tf.x + apm || (m0 + hi) + marg < tf.x - apm);
+}
+
+// B traces of one thread's OCT candidate (factors kc, c = 4/v^2, slope):
+// the displaced-midpoint tests side by side (independent chains), then time
+// and window of the passing traces in order, as COMPUTE_SEMBLANCE
+// (interface.h:26-44).  live[b] false: padding, neither evaluated nor
+// counted.
+template <int W, int B>
+__device__ __forceinline__ void oct_eval_batch(const LsParams &a, const uint32_t (&tb)[B],
+                                               const bool (&live)[B], const OctCand &kc,
+                                               float c, float slope, float t0, float m0,
+                                               float (&num)[W], float &lin, float &den,
+                                               unsigned &used, unsigned &nu) {
+    float4 fb[B];  // {m, gamma^2, 16h^2h0^2, h^2-h0^2}
+    float mhb[B];
+    bool pass[B];
+#pragma unroll
+    for (int b = 0; b < B; b++) fb[b] = __ldg(a.octTab + tb[b]);
+#pragma unroll
+    for (int b = 0; b < B; b++) {
+        const int e = oct_mh_all(kc, fb[b].y, fb[b].z, fb[b].w, m0, &mhb[b]);
+        pass[b] = e == DE_OK && !(fabsf(fb[b].x - mhb[b]) > a.apm);
+    }
+#pragma unroll
+    for (int b = 0; b < B; b++) {
+        if (!live[b]) continue;
+        if (!pass[b]) {
+            nu++;
+            continue;
+        }
+        float t;
+        if (oct_time_k(a.hoff[tb[b]], a.h0, t0, kc.tn0_sq, m0, fb[b].x, mhb[b], c, slope, &t) !=
+            DE_OK)
+            continue;
+        const WinIdx wi = window_index(t, a.dt);
+        if (window_in_trace(wi.k, a.tau, (int)a.S)) {
+            const float *y = a.samples + (size_t)tb[b] * a.stride + (wi.k - a.tau);
+            float y1 = __ldg(y);
+#pragma unroll
+            for (int jj = 0; jj < W; jj++) {
+                const float y0 = y1;
+                y1 = __ldg(y + jj + 1);
+                const float u = (y1 - y0) * wi.frac + y0;
+                num[jj] += u;
+                lin += u;
+                den += u * u;
+            }
+            used++;
+        }
+    }
+}
+
 }  // namespace hpss

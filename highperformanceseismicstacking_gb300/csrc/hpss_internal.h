@@ -103,6 +103,9 @@ struct LsParams {
     // OCT: per-trace factors {m, gamma^2, 16 h^2 h0^2, h^2 - h0^2} for the
     // line's h0 (launch_oct_trace_table); read by the OCT tuned and DE kernels
     const float4 *octTab = nullptr;
+    // OCT with h0 = 0: warps drop traces by the displaced-midpoint box test
+    // (oct_box_may_pass) before the per-sample test
+    bool octBox = false;
 };
 
 // Differential evolution launch (de.cu).

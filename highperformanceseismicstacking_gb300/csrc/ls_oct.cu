@@ -74,6 +74,12 @@ ls_oct_kernel(LsParams a, uint32_t tiles, uint32_t parts, uint32_t chunksPerPart
         const float m0 = a.m0s[mi];
         const uint32_t first = a.selFirst[mi], cnt = a.selCount[mi];
         if (threadIdx.x == 0) shNu = 0;
+        // t0 range of the warp's samples for the displaced-midpoint box test
+        // (oct_box_may_pass; the sample t0 = 0 fails every displaced-midpoint
+        // test by itself: division by zero)
+        const int sa = max((int)tile * 32, 1), sb = min((int)tile * 32 + 31, S - 1);
+        const float t0a = static_cast<float>(sa) * a.dt, t0b = static_cast<float>(sb) * a.dt;
+        const bool tileTest = a.octBox && a.h0 == 0.f && t0a >= kOctBoxMinT0 && sa <= sb;
 
         float best = -1.f, second = -1.f, bestStack = 0.f;
         uint32_t bestP = 0xffffffffu;
@@ -103,50 +109,48 @@ ls_oct_kernel(LsParams a, uint32_t tiles, uint32_t parts, uint32_t chunksPerPart
                 used[r] = nu[r] = 0;
             }
             uint32_t q0 = 0;
-            if (R == 1) {
+            if (R == 1 && tileTest) {
+                // blocks of 32 traces: lane j tests trace qb + j for the whole
+                // warp, then the warp evaluates the traces kept, in order
+                for (uint32_t qb = 0; qb < cnt; qb += 32) {
+                    const uint32_t n = min(32u, cnt - qb);
+                    bool keep = false;
+                    if ((uint32_t)lane < n) {
+                        const uint32_t ti = a.selIdx ? a.selIdx[first + qb + lane] : first + qb + lane;
+                        keep = oct_box_may_pass(__ldg(a.octTab + ti), sl[0], sl[0], t0a, t0b, m0,
+                                                a.apm);
+                    }
+                    uint32_t mask = __ballot_sync(0xffffffffu, keep);
+                    nu[0] += n - (uint32_t)__popc(mask);
+                    while (mask) {
+                        uint32_t tb[kOctMhBatch];
+                        bool live[kOctMhBatch];
+                        const uint32_t firstBit = (uint32_t)__ffs(mask) - 1;
+#pragma unroll
+                        for (int b = 0; b < kOctMhBatch; b++) {
+                            live[b] = mask != 0;
+                            const uint32_t bit = live[b] ? (uint32_t)__ffs(mask) - 1 : firstBit;
+                            if (live[b]) mask &= mask - 1;
+                            tb[b] = a.selIdx ? a.selIdx[first + qb + bit] : first + qb + bit;
+                        }
+                        oct_eval_batch<W, kOctMhBatch>(a, tb, live, kc[0], cc[0], sl[0], t0, m0, num[0],
+                                                       lin[0], den[0], used[0], nu[0]);
+                    }
+                }
+                q0 = cnt;
+            } else if (R == 1) {
                 // displaced-midpoint tests of kOctMhBatch traces first, then the
                 // passing traces in order (the per-trace loop below, batched)
                 for (; q0 + kOctMhBatch <= cnt; q0 += kOctMhBatch) {
                     uint32_t tb[kOctMhBatch];
-                    float4 fb[kOctMhBatch];  // {m, gamma^2, 16h^2h0^2, h^2-h0^2}
-                    float mhb[kOctMhBatch];
-                    bool pass[kOctMhBatch];
+                    bool live[kOctMhBatch];
 #pragma unroll
                     for (int b = 0; b < kOctMhBatch; b++) {
                         tb[b] = a.selIdx ? a.selIdx[first + q0 + b] : first + q0 + b;
-                        fb[b] = __ldg(a.octTab + tb[b]);
+                        live[b] = true;
                     }
-#pragma unroll
-                    for (int b = 0; b < kOctMhBatch; b++) {
-                        const int e = oct_mh_all(kc[0], fb[b].y, fb[b].z, fb[b].w, m0, &mhb[b]);
-                        pass[b] = e == DE_OK && !(fabsf(fb[b].x - mhb[b]) > a.apm);
-                    }
-#pragma unroll
-                    for (int b = 0; b < kOctMhBatch; b++) {
-                        if (!pass[b]) {
-                            nu[0]++;
-                            continue;
-                        }
-                        float t;
-                        if (oct_time_k(a.hoff[tb[b]], a.h0, t0, kc[0].tn0_sq, m0, fb[b].x, mhb[b],
-                                       cc[0], sl[0], &t) != DE_OK)
-                            continue;
-                        const WinIdx wi = window_index(t, a.dt);
-                        if (window_in_trace(wi.k, tau, S)) {
-                            const float *y = a.samples + (size_t)tb[b] * a.stride + (wi.k - tau);
-                            float y1 = __ldg(y);
-#pragma unroll
-                            for (int jj = 0; jj < W; jj++) {
-                                const float y0 = y1;
-                                y1 = __ldg(y + jj + 1);
-                                const float u = (y1 - y0) * wi.frac + y0;
-                                num[0][jj] += u;
-                                lin[0] += u;
-                                den[0] += u * u;
-                            }
-                            used[0]++;
-                        }
-                    }
+                    oct_eval_batch<W, kOctMhBatch>(a, tb, live, kc[0], cc[0], sl[0], t0, m0, num[0],
+                                                   lin[0], den[0], used[0], nu[0]);
                 }
             }
             for (uint32_t q = q0; q < cnt; q++) {
