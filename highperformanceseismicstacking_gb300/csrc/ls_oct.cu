@@ -12,14 +12,17 @@
 //    have nearly the same displaced midpoint and window position, so the skip
 //    decisions agree across the warp and the window loads fall on a few
 //    cache lines of one trace row;
-//  * a thread evaluates R candidates (R = 1: resident warps, not chains in
-//    one thread, hide the latency);
-//  * the candidate range is split into `parts` (CTAs work on (midpoint,
-//    32-sample tile, part) units) so that a call with few midpoints still
-//    fills the GPU; each unit writes the best / runner-up of its part and
-//    merge_parts_kernel combines the parts in candidate order;
-//  * a call with more units than resident CTAs takes them from a work
-//    queue, heaviest midpoints first.
+//  * a thread evaluates one candidate at a time (resident warps, not chains
+//    in one thread, hide the latency);
+//  * the candidate range is split into `parts` ((midpoint, 32-sample tile,
+//    part) units) so that a call with few midpoints still fills the GPU, and
+//    every unit into warp units (one per warp slot, see ls_oct_kernel); each
+//    warp unit writes the best / runner-up of its candidates and
+//    merge_parts_kernel combines them in candidate order;
+//  * a call with more units than resident CTAs takes the warp units from a
+//    work queue, heaviest midpoints first;
+//  * with h0 = 0 a warp drops, per block of 32 traces, those no sample of
+//    its tile can pass (oct_box_may_pass) before the per-sample tests.
 //
 // The per-candidate arithmetic is the plain kernel's (model_time<kModelOct>,
 // window_index, the COMPUTE_SEMBLANCE restatement), in the same trace order,
@@ -44,27 +47,34 @@ constexpr int kOctWarps = 8;
 // 9.88 -> 9.05 ms on four, 37.9 -> 34.8 ms on sixteen.
 constexpr int kOctMhBatch = 4;
 
-template <int W, int R>
+// Warp units: a (midpoint, 32-sample tile, candidate part) unit is split
+// into kOctWarps warp units, warp slot k taking candidates chunk * kOctWarps + k
+// of the part's chunks; every warp unit writes its own best / runner-up
+// (partial[mi][part][slot][S]) and merge_parts_kernel combines all of them
+// in candidate order.  Warps never wait for each other: the candidates keep
+// different numbers of traces (their slopes decide the displaced-midpoint
+// tests), and a CTA-wide merge per unit would hold every warp until the
+// slowest one is done.  Warp units are taken from the work queue one warp
+// at a time; without the queue CTA b's warps take the slots of units b,
+// b + grid, ... (the warps of a CTA read the same trace rows).
+template <int W>
 __global__ void __launch_bounds__(kOctWarps * 32, 4)
 ls_oct_kernel(LsParams a, uint32_t tiles, uint32_t parts, uint32_t chunksPerPart,
-              uint32_t nUnits, PartBest *partial) {
+              uint32_t nWarpUnits, PartBest *partial) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int S = (int)a.S, tau = a.tau;
-    constexpr int kChunk = kOctWarps * R;
-    __shared__ float shBest[kOctWarps][32], shSecond[kOctWarps][32], shStack[kOctWarps][32];
-    __shared__ uint32_t shP[kOctWarps][32];
-    __shared__ unsigned long long shNu;
-    __shared__ uint32_t shUnit;
-
-    for (uint32_t unit = blockIdx.x;; unit += gridDim.x) {
-        // work queue (heaviest midpoints first when ordered), else round-robin
+    const uint32_t nChunks = (a.P + kOctWarps - 1) / kOctWarps;
+    for (uint32_t k = 0;; k++) {
+        uint32_t wu;
         if (a.unitCounter) {
-            __syncthreads();  // every thread has read the previous unit
-            if (threadIdx.x == 0) shUnit = atomicAdd(a.unitCounter, 1u);
-            __syncthreads();
-            unit = shUnit;
+            uint32_t got = 0;
+            if (lane == 0) got = atomicAdd(a.unitCounter, 1u);
+            wu = __shfl_sync(0xffffffffu, got, 0);
+        } else {
+            wu = (blockIdx.x + k * gridDim.x) * kOctWarps + warp;
         }
-        if (unit >= nUnits) break;
+        if (wu >= nWarpUnits) break;
+        const uint32_t slot = wu % kOctWarps, unit = wu / kOctWarps;
         const uint32_t part = unit % parts;
         const uint32_t tile = (unit / parts) % tiles;
         const uint32_t mi = a.order ? a.order[unit / (parts * tiles)] : unit / (parts * tiles);
@@ -73,7 +83,6 @@ ls_oct_kernel(LsParams a, uint32_t tiles, uint32_t parts, uint32_t chunksPerPart
         const float t0 = static_cast<float>(sc) * a.dt;
         const float m0 = a.m0s[mi];
         const uint32_t first = a.selFirst[mi], cnt = a.selCount[mi];
-        if (threadIdx.x == 0) shNu = 0;
         // t0 range of the warp's samples for the displaced-midpoint box test
         // (oct_box_may_pass; the sample t0 = 0 fails every displaced-midpoint
         // test by itself: division by zero)
@@ -85,31 +94,19 @@ ls_oct_kernel(LsParams a, uint32_t tiles, uint32_t parts, uint32_t chunksPerPart
         uint32_t bestP = 0xffffffffu;
         unsigned long long notUsed = 0;
         const uint32_t c0 = part * chunksPerPart;
-        const uint32_t c1 = min(c0 + chunksPerPart, (a.P + kChunk - 1) / kChunk);
+        const uint32_t c1 = min(c0 + chunksPerPart, nChunks);
         for (uint32_t chunk = c0; chunk < c1; chunk++) {
-            float cc[R], sl[R];
-            OctCand kc[R];  // (t0, candidate) factors, out of the trace loop
-            bool valid[R];
+            const uint32_t p = chunk * kOctWarps + slot;
+            if (p >= a.P) break;
+            const float cc = a.params[2 * (size_t)p];
+            const float sl = a.params[2 * (size_t)p + 1];
+            const OctCand kc = oct_cand(t0, cc, sl, a.h0);  // (t0, candidate) factors
+            float num[W];
 #pragma unroll
-            for (int r = 0; r < R; r++) {
-                const uint32_t p = chunk * kChunk + warp * R + r;
-                valid[r] = p < a.P;
-                const uint32_t pc = valid[r] ? p : a.P - 1;
-                cc[r] = a.params[2 * (size_t)pc];
-                sl[r] = a.params[2 * (size_t)pc + 1];
-                kc[r] = oct_cand(t0, cc[r], sl[r], a.h0);
-            }
-            float num[R][W], lin[R], den[R];
-            unsigned used[R], nu[R];
-#pragma unroll
-            for (int r = 0; r < R; r++) {
-#pragma unroll
-                for (int j = 0; j < W; j++) num[r][j] = 0.f;
-                lin[r] = den[r] = 0.f;
-                used[r] = nu[r] = 0;
-            }
-            uint32_t q0 = 0;
-            if (R == 1 && tileTest) {
+            for (int j = 0; j < W; j++) num[j] = 0.f;
+            float lin = 0.f, den = 0.f;
+            unsigned used = 0, nu = 0;
+            if (tileTest) {
                 // blocks of 32 traces: lane j tests trace qb + j for the whole
                 // warp, then the warp evaluates the traces kept, in order
                 for (uint32_t qb = 0; qb < cnt; qb += 32) {
@@ -117,115 +114,73 @@ ls_oct_kernel(LsParams a, uint32_t tiles, uint32_t parts, uint32_t chunksPerPart
                     bool keep = false;
                     if ((uint32_t)lane < n) {
                         const uint32_t ti = a.selIdx ? a.selIdx[first + qb + lane] : first + qb + lane;
-                        keep = oct_box_may_pass(__ldg(a.octTab + ti), sl[0], sl[0], t0a, t0b, m0,
-                                                a.apm);
+                        keep = oct_box_may_pass(__ldg(a.octTab + ti), sl, sl, t0a, t0b, m0, a.apm);
                     }
                     uint32_t mask = __ballot_sync(0xffffffffu, keep);
-                    nu[0] += n - (uint32_t)__popc(mask);
+                    nu += n - (uint32_t)__popc(mask);
                     while (mask) {
                         uint32_t tb[kOctMhBatch];
                         bool live[kOctMhBatch];
                         const uint32_t firstBit = (uint32_t)__ffs(mask) - 1;
 #pragma unroll
-                        for (int b = 0; b < kOctMhBatch; b++) {
-                            live[b] = mask != 0;
-                            const uint32_t bit = live[b] ? (uint32_t)__ffs(mask) - 1 : firstBit;
-                            if (live[b]) mask &= mask - 1;
-                            tb[b] = a.selIdx ? a.selIdx[first + qb + bit] : first + qb + bit;
+                        for (int bb = 0; bb < kOctMhBatch; bb++) {
+                            live[bb] = mask != 0;
+                            const uint32_t bit = live[bb] ? (uint32_t)__ffs(mask) - 1 : firstBit;
+                            if (live[bb]) mask &= mask - 1;
+                            tb[bb] = a.selIdx ? a.selIdx[first + qb + bit] : first + qb + bit;
                         }
-                        oct_eval_batch<W, kOctMhBatch>(a, tb, live, kc[0], cc[0], sl[0], t0, m0, num[0],
-                                                       lin[0], den[0], used[0], nu[0]);
+                        oct_eval_batch<W, kOctMhBatch>(a, tb, live, kc, cc, sl, t0, m0, num, lin,
+                                                       den, used, nu);
                     }
                 }
-                q0 = cnt;
-            } else if (R == 1) {
-                // displaced-midpoint tests of kOctMhBatch traces first, then the
-                // passing traces in order (the per-trace loop below, batched)
-                for (; q0 + kOctMhBatch <= cnt; q0 += kOctMhBatch) {
+            } else {
+                // displaced-midpoint tests of kOctMhBatch traces side by side,
+                // then the passing traces in order; the rest one by one
+                uint32_t q = 0;
+                for (; q + kOctMhBatch <= cnt; q += kOctMhBatch) {
                     uint32_t tb[kOctMhBatch];
                     bool live[kOctMhBatch];
 #pragma unroll
-                    for (int b = 0; b < kOctMhBatch; b++) {
-                        tb[b] = a.selIdx ? a.selIdx[first + q0 + b] : first + q0 + b;
-                        live[b] = true;
+                    for (int bb = 0; bb < kOctMhBatch; bb++) {
+                        tb[bb] = a.selIdx ? a.selIdx[first + q + bb] : first + q + bb;
+                        live[bb] = true;
                     }
-                    oct_eval_batch<W, kOctMhBatch>(a, tb, live, kc[0], cc[0], sl[0], t0, m0, num[0],
-                                                   lin[0], den[0], used[0], nu[0]);
+                    oct_eval_batch<W, kOctMhBatch>(a, tb, live, kc, cc, sl, t0, m0, num, lin, den,
+                                                   used, nu);
+                }
+                for (; q < cnt; q++) {
+                    uint32_t tb[kOctMhBatch];
+                    bool live[kOctMhBatch];
+#pragma unroll
+                    for (int bb = 0; bb < kOctMhBatch; bb++) {
+                        tb[bb] = a.selIdx ? a.selIdx[first + q] : first + q;
+                        live[bb] = bb == 0;
+                    }
+                    oct_eval_batch<W, kOctMhBatch>(a, tb, live, kc, cc, sl, t0, m0, num, lin, den,
+                                                   used, nu);
                 }
             }
-            for (uint32_t q = q0; q < cnt; q++) {
-                const uint32_t ti = a.selIdx ? a.selIdx[first + q] : first + q;
-                const float4 tf = __ldg(a.octTab + ti);  // {m, gamma^2, 16h^2h0^2, h^2-h0^2}
-                const float h = a.hoff[ti];
-                const float *tr = a.samples + (size_t)ti * a.stride;
-#pragma unroll
-                for (int r = 0; r < R; r++) {
-                    float t;
-                    const int ok = oct_model_time(kc[r], tf.y, tf.z, tf.w, t0, cc[r], sl[r], tf.x,
-                                                  h, m0, a.apm, a.h0, &t);
-                    if (ok < 0) nu[r]++;
-                    if (ok > 0) {
-                        const WinIdx wi = window_index(t, a.dt);
-                        if (window_in_trace(wi.k, tau, S)) {
-                            const float *y = tr + (wi.k - tau);
-                            float y1 = __ldg(y);
-#pragma unroll
-                            for (int jj = 0; jj < W; jj++) {
-                                const float y0 = y1;
-                                y1 = __ldg(y + jj + 1);
-                                const float u = (y1 - y0) * wi.frac + y0;
-                                num[r][jj] += u;
-                                lin[r] += u;
-                                den[r] += u * u;
-                            }
-                            used[r]++;
-                        }
-                    }
-                }
+            float sembl, stack;
+            reduce_semblance(num, lin, den, W, used, &sembl, &stack);
+            top2_offer(sembl, best, second);
+            if (sembl > best) {
+                best = sembl;
+                bestStack = stack;
+                bestP = p;
             }
-#pragma unroll
-            for (int r = 0; r < R; r++) {
-                float sembl, stack;
-                reduce_semblance(num[r], lin[r], den[r], W, used[r], &sembl, &stack);
-                const uint32_t p = chunk * kChunk + warp * R + r;
-                if (valid[r]) {
-                    top2_offer(sembl, best, second);
-                    if (sembl > best) {
-                        best = sembl;
-                        bestStack = stack;
-                        bestP = p;
-                    }
-                    if (s < S) notUsed += nu[r];
-                }
-            }
+            if (s < S) notUsed += nu;
         }
-        // ---- merge the warps (candidate order is preserved by better())
-        shBest[warp][lane] = best;
-        shSecond[warp][lane] = second;
-        shStack[warp][lane] = bestStack;
-        shP[warp][lane] = bestP;
+        if (s < S) {
+            PartBest pb;
+            pb.best = best;
+            pb.second = second;
+            pb.stack = bestStack;
+            pb.p = bestP;
+            partial[(((size_t)mi * parts + part) * kOctWarps + slot) * a.S + s] = pb;
+        }
 #pragma unroll
         for (int o = 16; o; o >>= 1) notUsed += __shfl_xor_sync(0xffffffffu, notUsed, o);
-        __syncthreads();
-        if (lane == 0 && notUsed) atomicAdd(&shNu, notUsed);
-        if (warp == 0) {
-            for (int wv = 1; wv < kOctWarps; wv++) {
-                const float os = shBest[wv][lane];
-                const uint32_t op = shP[wv][lane];
-                if (better(os, op, best, bestP)) bestStack = shStack[wv][lane];
-                top2_merge(os, op, shSecond[wv][lane], best, bestP, second);
-            }
-            if (s < S) {
-                PartBest pb;
-                pb.best = best;
-                pb.second = second;
-                pb.stack = bestStack;
-                pb.p = bestP;
-                partial[((size_t)mi * parts + part) * a.S + s] = pb;
-            }
-        }
-        __syncthreads();
-        if (threadIdx.x == 0 && shNu && a.notUsed) atomicAdd(a.notUsed + mi, shNu);
+        if (lane == 0 && notUsed && a.notUsed) atomicAdd(a.notUsed + mi, notUsed);
     }
 }
 
@@ -291,7 +246,7 @@ cudaError_t launch_oct_trace_table(const float *mid, const float *hoff, uint32_t
 }
 
 size_t oct_partial_bytes(uint32_t nM0, uint32_t S, uint32_t parts) {
-    return (size_t)nM0 * parts * S * sizeof(PartBest);
+    return (size_t)nM0 * parts * kOctWarps * S * sizeof(PartBest);
 }
 
 template <int R>
@@ -299,17 +254,17 @@ uint32_t oct_chunks(uint32_t P) {
     return (P + kOctWarps * R - 1) / (kOctWarps * R);
 }
 
-template <int W, int R>
+template <int W>
 cudaError_t launch_oct_w(const LsParams &p, uint32_t numSms, void *partial, uint32_t parts,
                          cudaStream_t st) {
     const uint32_t tiles = (p.S + 31) / 32;
-    const uint32_t nChunks = oct_chunks<R>(p.P);
+    const uint32_t nChunks = oct_chunks<1>(p.P);
     const uint32_t chunksPerPart = (nChunks + parts - 1) / parts;
     const uint64_t units = (uint64_t)p.nM0 * tiles * parts;
     if (units == 0) return cudaSuccess;
-    if (units > 0xffffffffull) return cudaErrorInvalidConfiguration;
+    if (units * kOctWarps > 0xffffffffull) return cudaErrorInvalidConfiguration;
     int perSm = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, ls_oct_kernel<W, R>,
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, ls_oct_kernel<W>,
                                                                   kOctWarps * 32, 0);
     if (e != cudaSuccess) return e;
     const uint32_t grid =
@@ -317,11 +272,12 @@ cudaError_t launch_oct_w(const LsParams &p, uint32_t numSms, void *partial, uint
     // one wave: every unit has its own CTA, the work queue only adds latency
     LsParams q = p;
     if (units <= grid) q.unitCounter = nullptr;
-    ls_oct_kernel<W, R><<<grid, kOctWarps * 32, 0, st>>>(
-        q, tiles, parts, chunksPerPart, (uint32_t)units, static_cast<PartBest *>(partial));
+    ls_oct_kernel<W><<<grid, kOctWarps * 32, 0, st>>>(
+        q, tiles, parts, chunksPerPart, (uint32_t)(units * kOctWarps),
+        static_cast<PartBest *>(partial));
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    return launch_merge_parts(p, parts, static_cast<const PartBest *>(partial), st);
+    return launch_merge_parts(p, parts * kOctWarps, static_cast<const PartBest *>(partial), st);
 }
 
 // Parts: enough (midpoint, tile, part) units for ~8 waves of the GPU, never
@@ -337,16 +293,15 @@ uint32_t oct_parts(const LsParams &p, uint32_t numSms) {
 
 cudaError_t launch_ls_oct(const LsParams &p, uint32_t numSms, void *partial, uint32_t parts,
                           cudaStream_t st) {
-    constexpr int R = 1;
     switch (p.w) {
-        case 1: return launch_oct_w<1, R>(p, numSms, partial, parts, st);
-        case 3: return launch_oct_w<3, R>(p, numSms, partial, parts, st);
-        case 5: return launch_oct_w<5, R>(p, numSms, partial, parts, st);
-        case 7: return launch_oct_w<7, R>(p, numSms, partial, parts, st);
-        case 9: return launch_oct_w<9, R>(p, numSms, partial, parts, st);
-        case 11: return launch_oct_w<11, R>(p, numSms, partial, parts, st);
-        case 13: return launch_oct_w<13, R>(p, numSms, partial, parts, st);
-        case 15: return launch_oct_w<15, R>(p, numSms, partial, parts, st);
+        case 1: return launch_oct_w<1>(p, numSms, partial, parts, st);
+        case 3: return launch_oct_w<3>(p, numSms, partial, parts, st);
+        case 5: return launch_oct_w<5>(p, numSms, partial, parts, st);
+        case 7: return launch_oct_w<7>(p, numSms, partial, parts, st);
+        case 9: return launch_oct_w<9>(p, numSms, partial, parts, st);
+        case 11: return launch_oct_w<11>(p, numSms, partial, parts, st);
+        case 13: return launch_oct_w<13>(p, numSms, partial, parts, st);
+        case 15: return launch_oct_w<15>(p, numSms, partial, parts, st);
         default: return cudaErrorNotSupported;
     }
 }
