@@ -103,20 +103,18 @@ __device__ __forceinline__ float2 de_f2(float a, float b) { return make_float2(a
 // 814 / 3037 ms)
 constexpr int kDeOctBatch = 4;
 
-// (t0, slope) box of a warp's OCT evaluations for oct_box_may_pass.
-struct OctBox {
-    float t0Lo, t0Hi, sLo, sHi;
-    bool on;
-};
+// threads of a DE CTA (kDeThreads below), for the per-warp box slots
+constexpr int kDeThreadsMax = 256;
 
 // Semblance of one candidate (raw parameters) over the selected traces.
-// OCT with box->on: called by all 32 lanes of the warp (a collective over
-// blocks of 32 traces); lanes with ev false take part in the box test only.
+// OCT with boxMode: called by all 32 lanes of the warp (the warp's
+// displaced-midpoint box and the tests over blocks of 32 traces are
+// collectives); lanes with ev false take part in those only.
 template <int MODEL, int W>
 __device__ __forceinline__ void de_eval(const DeParams &d, float t0, float m0, uint32_t first,
                                         uint32_t cnt, const float *x, float *sembl,
                                         float *stack, unsigned *notUsed, bool ev = true,
-                                        const OctBox *box = nullptr) {
+                                        bool boxMode = false) {
     const LsParams &a = d.ls;
     const float v = x[0];
     const float c = 4.0f / (v * v);
@@ -213,17 +211,24 @@ __device__ __forceinline__ void de_eval(const DeParams &d, float t0, float m0, u
     // OCT: (t0, candidate) factors once, trace factors from the line's table
     const OctCand kc = oct_cand(t0, c, p1, MODEL == kModelOct ? a.h0 : 0.f);
     if constexpr (MODEL == kModelOct && W > 0) {
-      if (box && box->on) {
+      __shared__ float deBox[kDeThreadsMax / 32][4];  // each warp's displaced-midpoint box
+      volatile float *boxSlot = deBox[threadIdx.x >> 5];
+      bool boxOn = false;
+      if (boxMode) {
+          const OctWarpBox box = oct_warp_box(a.octBox, ev, t0, p1, kc, a.h0);
+          boxOn = box.on;
+          if (boxOn) oct_box_store(boxSlot, box);
+      }
+      if (boxOn) {
         // blocks of 32 traces: lane j tests trace qb + j against the warp's
-        // (t0, slope) box, then the lanes evaluate the traces kept, in order
+        // displaced-midpoint box, then the lanes evaluate the traces kept, in order
         const int lane = threadIdx.x & 31;
         for (uint32_t qb = 0; qb < cnt; qb += 32) {
             const uint32_t n = min(32u, cnt - qb);
             bool keep = false;
             if ((uint32_t)lane < n) {
                 const uint32_t ti = a.selIdx ? a.selIdx[first + qb + lane] : first + qb + lane;
-                keep = oct_box_may_pass(__ldg(a.octTab + ti), box->sLo, box->sHi, box->t0Lo,
-                                        box->t0Hi, m0, a.apm);
+                keep = oct_box_keep(a, ti, boxSlot, m0);
             }
             uint32_t mask = __ballot_sync(0xffffffffu, keep);
             if (ev) nu += n - (uint32_t)__popc(mask);
@@ -244,6 +249,8 @@ __device__ __forceinline__ void de_eval(const DeParams &d, float t0, float m0, u
             }
         }
         q = cnt;
+      } else if (!ev) {
+        q = cnt;  // a lane without an evaluation only joins the warp's box
       } else {
         // the displaced-midpoint tests of kDeOctBatch traces side by side
         // (independent chains), then the passing traces in order
@@ -305,7 +312,7 @@ __device__ __forceinline__ void de_eval(const DeParams &d, float t0, float m0, u
 // mutation reads the three donors.  Persistent over (midpoint, sample
 // group) units, taken from a work queue (heaviest midpoints first) when a
 // call has more units than resident CTAs.
-constexpr int kDeThreads = 256;
+constexpr int kDeThreads = kDeThreadsMax;
 
 // OCT: five resident CTAs per SM (48 registers) -- its evaluation waits on
 // long dependent square-root / reciprocal chains, so resident warps and the
@@ -358,27 +365,11 @@ de_kernel(DeParams d, uint32_t spc, uint32_t groups, uint32_t nUnits) {
         const uint32_t o = PERM[threadIdx.x];  // the member whose trial this thread evaluates
         const bool ev = KEY[o] != __int_as_float(0x7f800000);
         const float t0o = (s0f + static_cast<float>(o / pop)) * a.dt;
-        // the warp's (t0, slope) box for the displaced-midpoint box test
-        // (h0 = 0; t0 = 0 fails every test by itself and stays out)
-        OctBox box;
-        const bool inBox = ev && t0o > 0.f;
-        const float inf = __int_as_float(0x7f800000);
-        box.t0Lo = inBox ? t0o : inf;
-        box.t0Hi = inBox ? t0o : -inf;
-        box.sLo = inBox ? TR[o * NP + NP - 1] : inf;
-        box.sHi = inBox ? TR[o * NP + NP - 1] : -inf;
-#pragma unroll
-        for (int sh = 16; sh; sh >>= 1) {
-            box.t0Lo = fminf(box.t0Lo, __shfl_xor_sync(0xffffffffu, box.t0Lo, sh));
-            box.t0Hi = fmaxf(box.t0Hi, __shfl_xor_sync(0xffffffffu, box.t0Hi, sh));
-            box.sLo = fminf(box.sLo, __shfl_xor_sync(0xffffffffu, box.sLo, sh));
-            box.sHi = fmaxf(box.sHi, __shfl_xor_sync(0xffffffffu, box.sHi, sh));
-        }
-        box.on = MODEL == kModelOct && W > 0 && a.octBox && a.h0 == 0.f && box.t0Lo >= kOctBoxMinT0 &&
-                 box.t0Hi >= box.t0Lo;
-        if (box.on || ev) {
+        // OCT: all lanes enter when the box test is on (warp collectives)
+        const bool boxMode = MODEL == kModelOct && W > 0 && a.octBox;
+        if (boxMode || ev) {
             float fo, fko;
-            de_eval<MODEL, W>(d, t0o, m0, first, cnt, TR + o * NP, &fo, &fko, notUsed, ev, &box);
+            de_eval<MODEL, W>(d, t0o, m0, first, cnt, TR + o * NP, &fo, &fko, notUsed, ev, boxMode);
             if (ev) {
                 RES[2 * o] = fo;
                 RES[2 * o + 1] = fko;

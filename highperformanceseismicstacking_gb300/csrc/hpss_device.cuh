@@ -317,6 +317,98 @@ __device__ __forceinline__ bool oct_box_may_pass(const float4 &tf, float sLo, fl
     return !((m0 + lo) - marg > tf.x + apm || (m0 + hi) + marg < tf.x - apm);
 }
 
+// The same test for any h0.  With A = h^2 + h0^2, D = h^2 - h0^2 the
+// reference's radicand satisfies tq^2 + tq ts gs + 16 h^2 h0^2 ts^2 =
+// (tq + 2 theta^2 A)^2 - 4 theta^4 D^2 (gs = 4A, ts = theta^2), so
+// sqrt(arg2) = sqrt(T^2 + 4 theta^2 H^2) + sqrt(T^2 + 4 theta^2 L^2) with
+// T = t0^2 - c h0^2, H = max(|h|, |h0|), L = min(|h|, |h0|), and
+//     mh - m0 = sign(D) G,  G = 2 theta |D| / sqrt(arg2).
+// G increases with theta = t0 * slope and, for a fixed theta, moves toward 0
+// as |T| grows, so over theta in [thLo, thHi] and |T| in [tLo, tHi] it lies
+// between two corner values.  The box is taken over the lanes' own theta and
+// T (the values their per-sample tests use); T must keep one sign and
+// |T| >= kOctBoxMinT (the reference's tq^2 term stays normal), else the warp
+// runs without the test.  H^2 and L^2 come from h and h0 directly (from the
+// table, gs/2 - 2|D| would lose L^2 to cancellation when |h0| << |h|); D is
+// the table's, as in the reference's numerator; margin as oct_box_may_pass.
+constexpr float kOctBoxMinT = 1e-8f;
+__device__ __forceinline__ float oct_box_g(float th, float T, float ad, float h4, float l4) {
+    const float th2 = th * th;
+    return 2.f * th * ad / (sqrtf(fmaf(T, T, th2 * h4)) + sqrtf(fmaf(T, T, th2 * l4)));
+}
+__device__ __forceinline__ bool oct_box_may_pass_h0(const float4 &tf, float h, float h0,
+                                                    float thLo, float thHi, float tLo, float tHi,
+                                                    float m0, float apm) {
+    const float ad = fabsf(tf.w);
+    const float hh = h * h, hh0 = h0 * h0;
+    const float h4 = 4.f * fmaxf(hh, hh0), l4 = 4.f * fminf(hh, hh0);
+    const float gHi = oct_box_g(thHi, thHi > 0.f ? tLo : tHi, ad, h4, l4);
+    const float gLo = oct_box_g(thLo, thLo > 0.f ? tHi : tLo, ad, h4, l4);
+    const float lo = tf.w >= 0.f ? gLo : -gHi, hi = tf.w >= 0.f ? gHi : -gLo;
+    const float marg = 1e-4f * fmaxf(fabsf(lo), fabsf(hi)) +
+                       1e-5f * (fabsf(m0) + fabsf(tf.x)) + 1e-3f;
+    return !((m0 + lo) - marg > tf.x + apm || (m0 + hi) + marg < tf.x - apm);
+}
+
+// A warp's box for the displaced-midpoint test: h0 = 0 -- t0 and slope
+// ranges of the members with t0 > 0 (t0 = 0 fails the per-sample test by
+// itself: division by zero); otherwise theta and |T| ranges of the members.
+// Called by all 32 lanes; member: the lane's evaluation counts.
+struct OctWarpBox {
+    bool on, h0zero;
+    float aLo, aHi, bLo, bHi;  // h0 = 0: t0, slope; else theta, |T|
+};
+__device__ __forceinline__ OctWarpBox oct_warp_box(bool enable, bool member, float t0,
+                                                   float slope, const OctCand &kc, float h0) {
+    const float inf = __int_as_float(0x7f800000);
+    OctWarpBox r;
+    r.h0zero = h0 == 0.f;
+    const bool in = member && (!r.h0zero || t0 > 0.f);
+    const float a = r.h0zero ? t0 : 0.5f * kc.twoTheta;
+    const float b = r.h0zero ? slope : kc.tn0_sq;
+    r.aLo = in ? a : inf;
+    r.aHi = in ? a : -inf;
+    r.bLo = in ? b : inf;
+    r.bHi = in ? b : -inf;
+#pragma unroll
+    for (int sh = 16; sh; sh >>= 1) {
+        r.aLo = fminf(r.aLo, __shfl_xor_sync(0xffffffffu, r.aLo, sh));
+        r.aHi = fmaxf(r.aHi, __shfl_xor_sync(0xffffffffu, r.aHi, sh));
+        r.bLo = fminf(r.bLo, __shfl_xor_sync(0xffffffffu, r.bLo, sh));
+        r.bHi = fmaxf(r.bHi, __shfl_xor_sync(0xffffffffu, r.bHi, sh));
+    }
+    if (r.h0zero) {
+        r.on = enable && r.aLo >= kOctBoxMinT0 && r.aHi >= r.aLo;
+    } else {
+        if (r.bHi < 0.f) {  // T < 0 throughout: |T| in [-bHi, -bLo]
+            const float t = -r.bLo;
+            r.bLo = -r.bHi;
+            r.bHi = t;
+        }
+        r.on = enable && r.aHi >= r.aLo && r.bLo >= kOctBoxMinT && r.bHi >= r.bLo;
+    }
+    return r;
+}
+// Box test of trace ti (factor table entry and half-offset) for a warp.  The
+// box {aLo, aHi, bLo, bHi} is read from the warp's slot in shared memory
+// (volatile: reloaded at each test instead of held in registers through the
+// trace loop).
+__device__ __forceinline__ void oct_box_store(volatile float *slot, const OctWarpBox &r) {
+    slot[0] = r.aLo;
+    slot[1] = r.aHi;
+    slot[2] = r.bLo;
+    slot[3] = r.bHi;
+    __syncwarp();
+}
+__device__ __forceinline__ bool oct_box_keep(const LsParams &a, uint32_t ti,
+                                             const volatile float *slot, float m0) {
+    const float4 tf = __ldg(a.octTab + ti);
+    const float aLo = slot[0], aHi = slot[1], bLo = slot[2], bHi = slot[3];
+    return a.h0 == 0.f ? oct_box_may_pass(tf, bLo, bHi, aLo, aHi, m0, a.apm)
+                       : oct_box_may_pass_h0(tf, __ldg(a.hoff + ti), a.h0, aLo, aHi, bLo, bHi,
+                                             m0, a.apm);
+}
+
 // B traces of one thread's OCT candidate (factors kc, c = 4/v^2, slope):
 // the displaced-midpoint tests side by side (independent chains), then time
 // and window of the passing traces in order, as COMPUTE_SEMBLANCE

@@ -21,8 +21,8 @@
 //    merge_parts_kernel combines them in candidate order;
 //  * a call with more units than resident CTAs takes the warp units from a
 //    work queue, heaviest midpoints first;
-//  * with h0 = 0 a warp drops, per block of 32 traces, those no sample of
-//    its tile can pass (oct_box_may_pass) before the per-sample tests.
+//  * a warp drops, per block of 32 traces, those no sample of its tile can
+//    pass (oct_warp_box / oct_box_keep) before the per-sample tests.
 //
 // The per-candidate arithmetic is the plain kernel's (model_time<kModelOct>,
 // window_index, the COMPUTE_SEMBLANCE restatement), in the same trace order,
@@ -64,6 +64,7 @@ ls_oct_kernel(LsParams a, uint32_t tiles, uint32_t parts, uint32_t chunksPerPart
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int S = (int)a.S, tau = a.tau;
     const uint32_t nChunks = (a.P + kOctWarps - 1) / kOctWarps;
+    __shared__ float shBox[kOctWarps][4];  // each warp's displaced-midpoint box
     for (uint32_t k = 0;; k++) {
         uint32_t wu;
         if (a.unitCounter) {
@@ -83,12 +84,6 @@ ls_oct_kernel(LsParams a, uint32_t tiles, uint32_t parts, uint32_t chunksPerPart
         const float t0 = static_cast<float>(sc) * a.dt;
         const float m0 = a.m0s[mi];
         const uint32_t first = a.selFirst[mi], cnt = a.selCount[mi];
-        // t0 range of the warp's samples for the displaced-midpoint box test
-        // (oct_box_may_pass; the sample t0 = 0 fails every displaced-midpoint
-        // test by itself: division by zero)
-        const int sa = max((int)tile * 32, 1), sb = min((int)tile * 32 + 31, S - 1);
-        const float t0a = static_cast<float>(sa) * a.dt, t0b = static_cast<float>(sb) * a.dt;
-        const bool tileTest = a.octBox && a.h0 == 0.f && t0a >= kOctBoxMinT0 && sa <= sb;
 
         float best = -1.f, second = -1.f, bestStack = 0.f;
         uint32_t bestP = 0xffffffffu;
@@ -101,12 +96,19 @@ ls_oct_kernel(LsParams a, uint32_t tiles, uint32_t parts, uint32_t chunksPerPart
             const float cc = a.params[2 * (size_t)p];
             const float sl = a.params[2 * (size_t)p + 1];
             const OctCand kc = oct_cand(t0, cc, sl, a.h0);  // (t0, candidate) factors
+            // the warp's displaced-midpoint box (oct_warp_box)
+            bool boxOn;
+            {
+                const OctWarpBox box = oct_warp_box(a.octBox, true, t0, sl, kc, a.h0);
+                boxOn = box.on;
+                if (boxOn) oct_box_store(shBox[warp], box);
+            }
             float num[W];
 #pragma unroll
             for (int j = 0; j < W; j++) num[j] = 0.f;
             float lin = 0.f, den = 0.f;
             unsigned used = 0, nu = 0;
-            if (tileTest) {
+            if (boxOn) {
                 // blocks of 32 traces: lane j tests trace qb + j for the whole
                 // warp, then the warp evaluates the traces kept, in order
                 for (uint32_t qb = 0; qb < cnt; qb += 32) {
@@ -114,7 +116,7 @@ ls_oct_kernel(LsParams a, uint32_t tiles, uint32_t parts, uint32_t chunksPerPart
                     bool keep = false;
                     if ((uint32_t)lane < n) {
                         const uint32_t ti = a.selIdx ? a.selIdx[first + qb + lane] : first + qb + lane;
-                        keep = oct_box_may_pass(__ldg(a.octTab + ti), sl, sl, t0a, t0b, m0, a.apm);
+                        keep = oct_box_keep(a, ti, shBox[warp], m0);
                     }
                     uint32_t mask = __ballot_sync(0xffffffffu, keep);
                     nu += n - (uint32_t)__popc(mask);

@@ -156,16 +156,17 @@ def test_de_multi_wave_call_maps_units_to_midpoints(engine):
         assert member.all(), i
 
 
-@pytest.mark.parametrize("slope", [1e-3, 5e-3])
-def test_de_oct_box_test_keeps_results(engine, monkeypatch, slope):
-    """OCT DE with h0 = 0: warps drop traces by the displaced-midpoint box
-    test (the (t0, slope) range of their evaluations) before the per-sample
-    test.  Blocks and not-used counts equal those with the box test off
-    (HPSS_OCT_BOX_TEST=0: every trace through the per-sample test)."""
+@pytest.mark.parametrize("slope,h0", [(1e-3, 0.0), (5e-3, 0.0), (1e-3, 500.0), (5e-3, 1000.0)])
+def test_de_oct_box_test_keeps_results(engine, monkeypatch, slope, h0):
+    """OCT DE: warps drop traces by the displaced-midpoint box test (the
+    range of their evaluations' t0 and slope, or theta and t0^2 - c h0^2)
+    before the per-sample test.  Blocks and not-used counts equal those with
+    the box test off (HPSS_OCT_BOX_TEST=0: every trace through the
+    per-sample test)."""
     line = synthetic.structured_line(n_cmp=24, fold_range=(6, 12), h_max=2500, ns=400,
                                      dt_us=2000, n_reflectors=4, f=20.0, snr=8.0, seed=14)
     lower, upper = [1200.0, -slope], [5000.0, slope]
-    _setup(engine, line, "oct", lower, upper, apm=150.0, h0=0.0)
+    _setup(engine, line, "oct", lower, upper, apm=150.0, h0=h0)
     m0s = line.cdp_midpoints[2::5]
     de, st = engine.differential_evolution(m0s, 32, 12, 0.5, 0.9, seed=4)
     monkeypatch.setenv("HPSS_OCT_BOX_TEST", "0")

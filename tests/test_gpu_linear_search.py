@@ -165,18 +165,22 @@ def test_oct_small_line(engine, h0):
     _check_against_oracle("oct", line, m0s, plain, lower, upper, gran, tau, apm, h0, cands)
 
 
-@pytest.mark.parametrize("slope,dt_us", [(5e-3, 2000), (2e-4, 1000), (2e-2, 4000)])
-def test_oct_tile_test_keeps_per_sample_results(engine, slope, dt_us):
-    """With h0 = 0 the OCT kernel drops, per 32-sample tile, the traces whose
-    midpoint is farther than apm from every displaced midpoint the tile can
-    reach; the rest go through the per-sample test.  Blocks and not-used
-    counts equal the plain kernel's (every trace through the per-sample
-    test) on wide apertures, steep and shallow slopes and fine sampling."""
+@pytest.mark.parametrize("slope,dt_us,h0", [(5e-3, 2000, 0.0), (2e-4, 1000, 0.0),
+                                             (2e-2, 4000, 0.0), (5e-3, 2000, 500.0),
+                                             (1e-3, 1000, 1000.0), (2e-2, 4000, 0.5)])
+def test_oct_tile_test_keeps_per_sample_results(engine, slope, dt_us, h0):
+    """The OCT kernel drops, per 32-sample tile and candidate, the traces
+    whose midpoint is farther than apm from every displaced midpoint the
+    tile can reach; the rest go through the per-sample test.  Blocks and
+    not-used counts equal the plain kernel's (every trace through the
+    per-sample test) on wide apertures, steep and shallow slopes, fine
+    sampling, h0 = 0 and h0 > 0 (tiles where t0^2 - c h0^2 changes sign run
+    without the test)."""
     line = synthetic.structured_line(n_cmp=24, fold_range=(6, 12), h_max=2500, ns=400,
                                      dt_us=dt_us, n_reflectors=4, f=20.0, snr=8.0, seed=13)
     lower, upper, gran = [1200.0, -slope], [5000.0, slope], [5, 9]
     apm, tau = 150.0, 2
-    _setup(engine, line, "oct", lower, upper, tau, apm, 0.0)
+    _setup(engine, line, "oct", lower, upper, tau, apm, h0)
     m0s = line.cdp_midpoints[1::3]
     plain, st_p = engine.linear_search(m0s, gran, "plain")
     tuned, st_t = engine.linear_search(m0s, gran, "tuned")
