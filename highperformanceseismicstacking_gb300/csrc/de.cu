@@ -580,7 +580,7 @@ cudaError_t launch_de_model(const DeParams &d, uint32_t numSms, cudaStream_t st)
     const uint32_t groups = (d.ls.S + spc - 1) / spc;
     const uint64_t units = (uint64_t)d.ls.nM0 * groups;
     if (units == 0) return cudaSuccess;
-    if (units > 0xffffffffull) return cudaErrorInvalidConfiguration;
+    if (units > 0x7fffffffull) return cudaErrorInvalidConfiguration;
     // OCT adds the slope-sorted evaluation's regions: trial vectors, keys,
     // fitness / stack pairs and the permutation, one each per thread
     const size_t smem = de_smem_bytes(spc, pop, NP) +

@@ -95,7 +95,8 @@ hpss_status de_impl(hpss_handle h, const float *d_m0s, uint32_t nM0, uint32_t po
     }
     HPSS_CUDA_TRY(h, cudaEventRecord(h->ev1, h->stream));
     const uint64_t units = (uint64_t)nM0 * h->S;
-    if (units > 0xffffffffull)
+    // unit indices (and a work-queue counter past the last unit) stay below 2^31
+    if (units > 0x7fffffffull)
         return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "too many (midpoint, sample) units");
     HPSS_CUDA_TRY(h, launch_de(d, h->model, (uint32_t)num_sms(h), h->stream));
     HPSS_CUDA_TRY(h, cudaEventRecord(h->ev2, h->stream));

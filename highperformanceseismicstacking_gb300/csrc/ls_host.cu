@@ -267,7 +267,8 @@ hpss_status linear_search_impl(hpss_handle h, const float *d_m0s, uint32_t nM0,
     rc = run_selection(h, d_m0s, nM0, lp);
     if (rc != HPSS_OK) return rc;
     HPSS_CUDA_TRY(h, cudaEventRecord(h->ev1, h->stream));
-    if (units > 0xffffffffull)
+    // unit indices (and a work-queue counter past the last unit) stay below 2^31
+    if (units > 0x7fffffffull)
         return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "too many (midpoint, tile) units");
     // nBase (midpoint, tile) units, each split into the shape's candidate
     // parts; a split launch of all units is followed by the ordered merge
@@ -288,7 +289,7 @@ hpss_status linear_search_impl(hpss_handle h, const float *d_m0s, uint32_t nM0,
         q.partial = static_cast<PartBest *>(h->partial.p);
         lastParts = q.parts;
         const uint64_t nUnits = (uint64_t)nBase * q.parts;
-        if (nUnits > 0xffffffffull) return cudaErrorInvalidConfiguration;
+        if (nUnits > 0x7fffffffull) return cudaErrorInvalidConfiguration;
         const uint32_t grid = (uint32_t)std::min<uint64_t>(
             nUnits, (uint64_t)num_sms(h) * kVariantCtasPerSm[variant]);
         // more units than resident CTAs: take them from the work queue

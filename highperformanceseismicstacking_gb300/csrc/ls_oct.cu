@@ -264,7 +264,8 @@ cudaError_t launch_oct_w(const LsParams &p, uint32_t numSms, void *partial, uint
     const uint32_t chunksPerPart = (nChunks + parts - 1) / parts;
     const uint64_t units = (uint64_t)p.nM0 * tiles * parts;
     if (units == 0) return cudaSuccess;
-    if (units * kOctWarps > 0xffffffffull) return cudaErrorInvalidConfiguration;
+    // warp-unit indices (and the queue counter past the last unit) stay below 2^31
+    if (units * kOctWarps > 0x7fffffffull) return cudaErrorInvalidConfiguration;
     int perSm = 0;
     cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, ls_oct_kernel<W>,
                                                                   kOctWarps * 32, 0);
