@@ -596,7 +596,8 @@ def main():
            "ms_per_step": total_ms / args.steps, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
            "config": {"workload": w.name, "model": w.model, "algorithm": w.algorithm,
-                      "cmps": int(len(all_m0)) * world, "cmps_per_gpu": int(len(all_m0)), "fold": int(np.max(counts)) if len(counts) else 0,
+                      "cmps": int(len(all_m0)) * world, "cmps_per_gpu": int(len(all_m0)),
+                      "fold": int(np.max(counts)) if len(counts) else 0,
                       "samples": S, "candidates": P, "window": wsz,
                       "evals_per_step": evals_all, "storage": "fp32", "kernel": "tuned",
                       "kernel_variant": variant,

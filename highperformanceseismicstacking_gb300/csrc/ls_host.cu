@@ -43,9 +43,9 @@ std::mutex g_variantMutex;
 std::map<std::string, int> g_variantCache;
 
 // Autotuner: the first time a (device, storage, model, window, candidates,
-// samples, fold, candidate split) key is seen, every variant is timed on a prefix of the work units (results are
-// overwritten by the real launch) and the fastest is cached in the handle
-// and in the process-wide table.
+// samples, fold, candidate split) key is seen, every variant is timed on a
+// prefix of the work units (results are overwritten by the real launch) and
+// the fastest is cached in the handle and in the process-wide table.
 // HPSS_LS_VARIANT=<n> forces a variant.
 template <typename SetChunks, typename Launch>
 hpss_status choose_variant(hpss_handle h, const LsParams &lp, uint32_t units, bool exactStack,
@@ -351,8 +351,10 @@ hpss_status linear_search_impl(hpss_handle h, const float *d_m0s, uint32_t nM0,
             stats->near_ties = (double)ties;
             std::vector<uint32_t> cnt(nM0);
             std::vector<unsigned long long> nu(nM0);
-            HPSS_CUDA_TRY(h, cudaMemcpy(cnt.data(), lp.selCount, nM0 * sizeof(uint32_t), cudaMemcpyDeviceToHost));
-            HPSS_CUDA_TRY(h, cudaMemcpy(nu.data(), lp.notUsed, nM0 * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+            HPSS_CUDA_TRY(h, cudaMemcpy(cnt.data(), lp.selCount, nM0 * sizeof(uint32_t),
+                                        cudaMemcpyDeviceToHost));
+            HPSS_CUDA_TRY(h, cudaMemcpy(nu.data(), lp.notUsed, nM0 * sizeof(unsigned long long),
+                                        cudaMemcpyDeviceToHost));
             double sel = 0, nus = 0;
             for (uint32_t i = 0; i < nM0; i++) {
                 sel += cnt[i];

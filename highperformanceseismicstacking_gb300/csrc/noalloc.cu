@@ -161,8 +161,8 @@ extern "C" hpss_status hpss_linear_search_noalloc(
                                                               nTraces);
     if (e == cudaSuccess) e = cudaGetLastError();
     if (e == cudaSuccess)
-        e = launch_build_grid(model, kGridReference, low, inc, nullptr, gran, reinterpret_cast<float *>(w + kOffParams),
-                              lp.P, st);
+        e = launch_build_grid(model, kGridReference, low, inc, nullptr, gran,
+                              reinterpret_cast<float *>(w + kOffParams), lp.P, st);
     if (e == cudaSuccess)
         e = launch_chunk_bounds(lp, reinterpret_cast<float *>(w + kOffBounds), st);
     if (e == cudaSuccess)
