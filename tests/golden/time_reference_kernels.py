@@ -15,12 +15,15 @@ to the engine on the same midpoints.  Prints one JSON line per workload.
           reference runs it) against the engine's fused DE launch.
 
   oct [n] OCT linear search on the OCT DE line's geometry (11 x 5 candidates).
+  (de and oct take an optional third argument: the OCT reference half-offset
+  h0, default the workload's 0 m.)
   zocrs [n] ZO-CRS linear search on the ZO-CRS line (21 x 21 x 41 candidates).
   sf [n]  CMP stretch-free stack on the CMP production line.
 
     python tests/golden/time_reference_kernels.py ls 40
     python tests/golden/time_reference_kernels.py de 2
     python tests/golden/time_reference_kernels.py oct 1
+    python tests/golden/time_reference_kernels.py oct 1 500
     python tests/golden/time_reference_kernels.py sf 20
     python tests/golden/time_reference_kernels.py zocrs 2
 """
@@ -136,11 +139,12 @@ def time_zocrs(n_mid: int = 2):
     print(json.dumps(out))
 
 
-def time_de(n_mid: int = 2):
+def time_de(n_mid: int = 2, oct_h0=None):
     rk = ref_runner.ReferenceKernels()
     ops = "common_differential_evolution_f05cr09"
     for name in ("zocrs-de", "oct-de"):
         w = synthetic.WORKLOADS[name]
+        h0 = float(oct_h0) if (name == "oct-de" and oct_h0 is not None) else w.h0
         line = w.make_line()
         lower, upper = synthetic.workload_bounds(w)
         tau = tau_index(w.tau, line.dt)
@@ -155,18 +159,18 @@ def time_de(n_mid: int = 2):
             res, ms, n_sel = rk.differential_evolution_midpoint(
                 w.model, line.samples, line.midpoints, line.halfoffsets, float(m0),
                 float(line.dt), tau, lower, upper, w.population, w.generations, seed=11 + i,
-                apm=w.apm, h0=w.h0, sel=sel, operators=ops)
+                apm=w.apm, h0=h0, sel=sel, operators=ops)
             ref_ms += ms
             ref_best.append(res[0])
             ref_evals += float(n_sel) * S * w.population * w.generations
         with capi.Engine(0) as eng:
             eng.upload_gather(line.samples, line.midpoints, line.halfoffsets, float(line.dt))
-            eng.set_traveltime(w.model, lower, upper, w.apm, w.h0)
+            eng.set_traveltime(w.model, lower, upper, w.apm, h0)
             eng.set_window(tau)
             eng.differential_evolution(m0s, w.population, 2, w.de_f, w.de_cr, seed=1)
             got, st = eng.differential_evolution(m0s, w.population, w.generations, w.de_f,
                                                  w.de_cr, seed=7)
-        line_out = {"workload": name, "algorithm": "differential-evolution",
+        line_out = {"workload": name, "algorithm": "differential-evolution", "h0": h0,
                     "midpoints": int(len(m0s)), "samples": S, "population": w.population,
                     "generations": w.generations,
                     "reference": {"ms": ref_ms,
@@ -180,12 +184,13 @@ def time_de(n_mid: int = 2):
         print(json.dumps(line_out))
 
 
-def time_oct(n_mid: int = 1):
+def time_oct(n_mid: int = 1, h0=None):
     """OCT linear search (the OCT DE line's geometry, 11 x 5 candidates,
-    h0 = 0): the reference's per-midpoint evaluation + argmax against the
+    h0 = 0 unless given): the reference's per-midpoint evaluation + argmax against the
     engine's plain and tuned kernels on the same midpoints."""
     from oracle import oracle
     w = synthetic.WORKLOADS["oct-de"]
+    h0 = w.h0 if h0 is None else float(h0)
     line = w.make_line(n_cmp=60)
     lower, upper = synthetic.workload_bounds(w)
     tau = tau_index(w.tau, line.dt)
@@ -199,20 +204,20 @@ def time_oct(n_mid: int = 1):
     ref_ms, ref_evals, ref_out = 0.0, 0.0, []
     for m0 in m0s:
         sel = np.nonzero(rk.select("oct", line.midpoints, line.halfoffsets, float(m0), w.apm,
-                                   w.h0, S, float(line.dt), cands))[0]
+                                   h0, S, float(line.dt), cands))[0]
         res, _, _, _, ms = rk.linear_search_midpoint("oct", line.samples, line.midpoints,
                                                      line.halfoffsets, sel, float(m0),
-                                                     float(line.dt), tau, params, w.apm, w.h0,
+                                                     float(line.dt), tau, params, w.apm, h0,
                                                      timing=True)
         ref_ms += ms
         ref_evals += float(sel.size) * S * params.shape[0]
         ref_out.append(res)
-    out = {"workload": "oct-ls (OCT DE line geometry, 60 CMPs, 11 x 5 candidates)",
+    out = {"workload": "oct-ls (OCT DE line geometry, 60 CMPs, 11 x 5 candidates)", "h0": h0,
            "midpoints": int(len(m0s)), "samples": S,
            "reference": {"ms": ref_ms, "evals": ref_evals, "value": ref_evals / (ref_ms / 1e3)}}
     with capi.Engine(0) as eng:
         eng.upload_gather(line.samples, line.midpoints, line.halfoffsets, float(line.dt))
-        eng.set_traveltime("oct", lower, upper, w.apm, w.h0)
+        eng.set_traveltime("oct", lower, upper, w.apm, h0)
         eng.set_window(tau)
         for kernel in ("plain", "tuned"):
             eng.linear_search(m0s, gran, kernel)
@@ -266,9 +271,9 @@ if __name__ == "__main__":
     elif mode == "zocrs":
         time_zocrs(n)
     elif mode == "de":
-        time_de(n)
+        time_de(n, float(sys.argv[3]) if len(sys.argv) > 3 else None)
     elif mode == "oct":
-        time_oct(n)
+        time_oct(n, float(sys.argv[3]) if len(sys.argv) > 3 else None)
     elif mode == "sf":
         time_sf(n)
     else:
