@@ -366,10 +366,14 @@ __device__ __forceinline__ OctWarpBox oct_warp_box(bool enable, bool member, flo
     const bool in = member && (!r.h0zero || t0 > 0.f);
     const float a = r.h0zero ? t0 : 0.5f * kc.twoTheta;
     const float b = r.h0zero ? slope : kc.tn0_sq;
+    // a NaN member (none with validated inputs) would pass every per-sample
+    // test while fminf / fmaxf leave it out of the box: no box then
+    const bool nan = in && (a != a || b != b);
     r.aLo = in ? a : inf;
     r.aHi = in ? a : -inf;
     r.bLo = in ? b : inf;
     r.bHi = in ? b : -inf;
+    enable = enable && !__any_sync(0xffffffffu, nan);
 #pragma unroll
     for (int sh = 16; sh; sh >>= 1) {
         r.aLo = fminf(r.aLo, __shfl_xor_sync(0xffffffffu, r.aLo, sh));
