@@ -39,8 +39,8 @@ uint32_t pair_parts(uint64_t base, uint32_t nChunks, int numSms, int ctasPerSm) 
 
 // Autotuner decisions shared by the handles of the process (keys carry the
 // device), so that a handle opened after another one does not tune again.
-std::mutex g_variantMutex;
-std::map<std::string, int> g_variantCache;
+static std::mutex g_variantMutex;
+static std::map<std::string, int> g_variantCache;
 
 // Autotuner: the first time a (device, storage, model, window, candidates,
 // samples, fold, candidate split) key is seen, every variant is timed on a
