@@ -187,7 +187,7 @@ hpss_status run_selection(hpss_handle h, const float *d_m0s, uint32_t nM0,
     HPSS_CUDA_TRY(h, launch_select_oct(lp, static_cast<const float *>(h->octCands.p),
                                        (uint32_t)(h->octCandsHost.size() / 2),
                                        static_cast<uint32_t *>(h->selIdx.p), count,
-                                       cf, cc, h->stream));
+                                       cf, cc, (uint64_t)total, h->stream));
     return HPSS_OK;
 }
 

@@ -201,10 +201,11 @@ cudaError_t launch_order_by_count(const uint32_t *count, uint32_t n, uint32_t *o
 // order and write the result block [nM0][2+np][S]; counts near-ties.
 cudaError_t launch_merge_parts(const LsParams &p, uint32_t parts, const PartBest *partial,
                                cudaStream_t st);
+// total: sum of candCount (the selIdx slots, p.selFirst their prefix).
 cudaError_t launch_select_oct(const LsParams &p, const float *cands,
                               uint32_t nCand, uint32_t *selIdx,
                               uint32_t *selCount, const uint32_t *candFirst,
-                              const uint32_t *candCount, cudaStream_t st);
+                              const uint32_t *candCount, uint64_t total, cudaStream_t st);
 cudaError_t launch_convert_storage(const float *src, uint16_t *dst,
                                    float *scale, uint32_t nTraces, uint32_t S,
                                    uint32_t stride, int storage,

@@ -101,67 +101,100 @@ cudaError_t launch_chunk_bounds(const LsParams &p, float *bounds,
 
 // OCT trace selection (oct/linear_search.cu:155-192): a trace is used for m0
 // if some (t0 sample, sampled candidate) gives a valid displaced midpoint
-// within apm of the trace's midpoint.  One warp per candidate trace, lanes
-// over the sampled candidates, early exit on the first hit; then an
-// order-preserving compaction of the selected trace indices per midpoint.
-// candFirst/candCount: per-midpoint range of traces that can pass at all
-// (|m - m0| <= apm + sqrt(h^2 + h0^2), prefiltered on the host).
-__global__ void select_oct_kernel(LsParams a, const float *cands,
-                                  uint32_t nCand, const uint32_t *candFirst,
-                                  const uint32_t *candCount, uint32_t *selIdx,
-                                  uint32_t *selCount) {
-    const uint32_t mi = blockIdx.x;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int nWarps = blockDim.x >> 5;
-    const float m0 = a.m0s[mi];
-    const uint32_t first = candFirst[mi], count = candCount[mi];
-    const uint32_t outBase = a.selFirst[mi];
-    __shared__ uint32_t shCount;
-    __shared__ uint32_t shFlags[256];
-    if (threadIdx.x == 0) shCount = 0;
-    __syncthreads();
-    // process candidate traces in rounds of nWarps, keeping output order
-    for (uint32_t base = 0; base < count; base += nWarps) {
-        uint32_t q = base + warp;
-        bool used = false;
-        if (q < count) {
-            uint32_t ti = first + q;
-            float m = a.mid[ti], h = a.hoff[ti];
-            for (uint32_t s = 0; s < a.S && !used; s++) {
-                float t0 = static_cast<float>(s) * a.dt;
-                for (uint32_t p0 = 0; p0 < nCand && !used; p0 += 32) {
-                    uint32_t p = p0 + lane;
-                    bool hit = false;
-                    if (p < nCand) {
-                        float mh;
-                        int e = oct_displaced_midpoint(h, a.h0, t0, m0,
-                                                       cands[2 * p],
-                                                       cands[2 * p + 1], &mh);
-                        hit = (e == DE_OK && fabsf(m - mh) <= a.apm);
-                    }
-                    used = __any_sync(0xffffffffu, hit);
-                }
-            }
-        }
-        if (lane == 0) shFlags[warp] = used ? 1u : 0u;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            for (int w = 0; w < nWarps && base + w < count; w++) {
-                if (shFlags[w]) selIdx[outBase + shCount++] = first + base + w;
-            }
-        }
-        __syncthreads();
+// within apm of the trace's midpoint.  candFirst/candCount: per-midpoint
+// range of traces that can pass at all (|m - m0| <= apm + sqrt(h^2 + h0^2),
+// prefiltered on the host); a.selFirst: exclusive prefix of candCount, the
+// midpoint's slots in selIdx.
+//
+// Pass 1: one warp per (midpoint, candidate trace) slot over the whole GPU
+// (a trace that is not selected runs every sample and candidate, so the
+// slots are spread over all SMs rather than one CTA per midpoint), lanes
+// over the sampled candidates, early exit on the first hit; the 0 / 1 flag
+// goes to the slot in selIdx.
+__global__ void select_oct_flags_kernel(LsParams a, const float *cands, uint32_t nCand,
+                                        const uint32_t *candFirst, uint64_t total,
+                                        uint32_t *selIdx) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t g = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (g >= total) return;  // whole warps
+    // the slot's midpoint: the last mi with selFirst[mi] <= g (midpoints
+    // without candidates share their successor's offset)
+    uint32_t lo = 0, hi = a.nM0;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) / 2;
+        if ((uint64_t)a.selFirst[mid] <= g) lo = mid;
+        else hi = mid;
     }
-    if (threadIdx.x == 0) selCount[mi] = shCount;
+    const uint32_t mi = lo;
+    const uint32_t ti = candFirst[mi] + (uint32_t)(g - a.selFirst[mi]);
+    const float m0 = a.m0s[mi];
+    const float m = a.mid[ti], h = a.hoff[ti];
+    bool used = false;
+    for (uint32_t s = 0; s < a.S && !used; s++) {
+        const float t0 = static_cast<float>(s) * a.dt;
+        for (uint32_t p0 = 0; p0 < nCand && !used; p0 += 32) {
+            const uint32_t p = p0 + lane;
+            bool hit = false;
+            if (p < nCand) {
+                float mh;
+                const int e = oct_displaced_midpoint(h, a.h0, t0, m0, cands[2 * p],
+                                                     cands[2 * p + 1], &mh);
+                hit = (e == DE_OK && fabsf(m - mh) <= a.apm);
+            }
+            used = __any_sync(0xffffffffu, hit);
+        }
+    }
+    if (lane == 0) selIdx[g] = used ? 1u : 0u;
+}
+
+// Pass 2: order-preserving compaction of every midpoint's flags into its
+// selected trace indices, in place: the flags of a chunk of 256 slots are
+// all read before any index of the chunk is written, and an index lands at
+// or before its flag's slot, never in a later chunk.
+constexpr int kCompactThreads = 256;
+__global__ void __launch_bounds__(kCompactThreads)
+select_oct_compact_kernel(LsParams a, const uint32_t *candFirst, const uint32_t *candCount,
+                          uint32_t *selIdx, uint32_t *selCount) {
+    const uint32_t mi = blockIdx.x;
+    const uint32_t base = a.selFirst[mi], count = candCount[mi], first = candFirst[mi];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    constexpr int kWarps = kCompactThreads / 32;
+    __shared__ uint32_t shWarp[kWarps];
+    uint32_t done = 0;
+    for (uint32_t c = 0; c < count; c += kCompactThreads) {
+        const uint32_t q = c + threadIdx.x;
+        const bool f = q < count && selIdx[base + q] != 0u;
+        const uint32_t bal = __ballot_sync(0xffffffffu, f);
+        if (lane == 0) shWarp[warp] = (uint32_t)__popc(bal);
+        __syncthreads();  // every flag of the chunk read
+        uint32_t before = done, chunk = 0;
+        for (int w = 0; w < kWarps; w++) {
+            if (w < warp) before += shWarp[w];
+            chunk += shWarp[w];
+        }
+        before += (uint32_t)__popc(bal & ((1u << lane) - 1u));
+        if (f) selIdx[base + before] = first + q;
+        done += chunk;
+        __syncthreads();  // shWarp read by every thread before the next chunk
+    }
+    if (threadIdx.x == 0) selCount[mi] = done;
 }
 
 cudaError_t launch_select_oct(const LsParams &p, const float *cands,
                               uint32_t nCand, uint32_t *selIdx,
                               uint32_t *selCount, const uint32_t *candFirst,
-                              const uint32_t *candCount, cudaStream_t st) {
+                              const uint32_t *candCount, uint64_t total, cudaStream_t st) {
     if (p.nM0 == 0) return cudaSuccess;
-    select_oct_kernel<<<p.nM0, 256, 0, st>>>(p, cands, nCand, candFirst,
-                                             candCount, selIdx, selCount);
+    if (total > 0) {
+        const uint64_t blocks = (total * 32 + 255) / 256;
+        if (blocks > 0x7fffffffull) return cudaErrorInvalidConfiguration;
+        select_oct_flags_kernel<<<(uint32_t)blocks, 256, 0, st>>>(p, cands, nCand, candFirst,
+                                                                  total, selIdx);
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    select_oct_compact_kernel<<<p.nM0, kCompactThreads, 0, st>>>(p, candFirst, candCount,
+                                                                  selIdx, selCount);
     return cudaGetLastError();
 }
 
