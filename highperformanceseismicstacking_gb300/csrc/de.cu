@@ -501,54 +501,46 @@ de_kernel(DeParams d, uint32_t spc, uint32_t groups, uint32_t nUnits) {
 // (selectTracesForOffsetContinuationTrajectoryAndDifferentialEvolution,
 // oct/differential_evolution.cu:130-168): a trace is used if any (sample,
 // initial individual) gives a valid displaced midpoint within apm.  The
-// initial individuals are regenerated from the counter-based stream.
-__global__ void de_select_oct_kernel(DeParams d, const uint32_t *candFirst,
-                                     const uint32_t *candCount, uint32_t *selIdx,
-                                     uint32_t *selCount) {
+// initial individuals are regenerated from the counter-based stream.  One
+// warp per (midpoint, candidate trace) slot over the whole GPU writes a 0 / 1
+// flag into the slot (d.ls.selFirst: the prefix of candCount); the flags are
+// then compacted in order (launch_select_compact).
+__global__ void de_select_oct_flags_kernel(DeParams d, const uint32_t *candFirst,
+                                           uint64_t total, uint32_t *selIdx) {
     const LsParams &a = d.ls;
-    const uint32_t mi = blockIdx.x;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int nWarps = blockDim.x >> 5;
-    const float m0 = a.m0s[mi];
-    const uint32_t first = candFirst[mi], count = candCount[mi];
-    const uint32_t outBase = a.selFirst[mi];
-    __shared__ uint32_t shCount;
-    __shared__ uint32_t shFlags[32];
-    if (threadIdx.x == 0) shCount = 0;
-    __syncthreads();
-    for (uint32_t base = 0; base < count; base += nWarps) {
-        const uint32_t q = base + warp;
-        bool used = false;
-        if (q < count) {
-            const uint32_t ti = first + q;
-            const float m = a.mid[ti], h = a.hoff[ti];
-            for (uint32_t s = 0; s < a.S && !used; s++) {
-                const float t0 = static_cast<float>(s) * a.dt;
-                for (uint32_t i0 = 0; i0 < d.pop && !used; i0 += 32) {
-                    const uint32_t ind = i0 + lane;
-                    bool hit = false;
-                    if (ind < d.pop) {
-                        Draws rng(d.seedLo, d.seedHi, mi, s, ind, 0);
-                        float v = __fmaf_rn(rng.next(), __fsub_rn(d.hi[0], d.lo[0]), d.lo[0]);
-                        float sl = __fmaf_rn(rng.next(), __fsub_rn(d.hi[1], d.lo[1]), d.lo[1]);
-                        float c = 4.0f / (v * v);
-                        float mh;
-                        int e = oct_displaced_midpoint(h, a.h0, t0, m0, c, sl, &mh);
-                        hit = (e == DE_OK && fabsf(m - mh) <= a.apm);
-                    }
-                    used = __any_sync(0xffffffffu, hit);
-                }
-            }
-        }
-        if (lane == 0) shFlags[warp] = used ? 1u : 0u;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            for (int w = 0; w < nWarps && base + w < count; w++)
-                if (shFlags[w]) selIdx[outBase + shCount++] = first + base + w;
-        }
-        __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const uint64_t g = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (g >= total) return;  // whole warps
+    // the slot's midpoint: the last mi with selFirst[mi] <= g
+    uint32_t lo = 0, hi = a.nM0;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) / 2;
+        if ((uint64_t)a.selFirst[mid] <= g) lo = mid;
+        else hi = mid;
     }
-    if (threadIdx.x == 0) selCount[mi] = shCount;
+    const uint32_t mi = lo;
+    const uint32_t ti = candFirst[mi] + (uint32_t)(g - a.selFirst[mi]);
+    const float m0 = a.m0s[mi];
+    const float m = a.mid[ti], h = a.hoff[ti];
+    bool used = false;
+    for (uint32_t s = 0; s < a.S && !used; s++) {
+        const float t0 = static_cast<float>(s) * a.dt;
+        for (uint32_t i0 = 0; i0 < d.pop && !used; i0 += 32) {
+            const uint32_t ind = i0 + lane;
+            bool hit = false;
+            if (ind < d.pop) {
+                Draws rng(d.seedLo, d.seedHi, mi, s, ind, 0);
+                const float v = __fmaf_rn(rng.next(), __fsub_rn(d.hi[0], d.lo[0]), d.lo[0]);
+                const float sl = __fmaf_rn(rng.next(), __fsub_rn(d.hi[1], d.lo[1]), d.lo[1]);
+                const float c = 4.0f / (v * v);
+                float mh;
+                const int e = oct_displaced_midpoint(h, a.h0, t0, m0, c, sl, &mh);
+                hit = (e == DE_OK && fabsf(m - mh) <= a.apm);
+            }
+            used = __any_sync(0xffffffffu, hit);
+        }
+    }
+    if (lane == 0) selIdx[g] = used ? 1u : 0u;
 }
 
 size_t de_smem_bytes(uint32_t spc, uint32_t pop, int np) {
@@ -604,10 +596,17 @@ cudaError_t launch_de(const DeParams &d, int model, uint32_t numSms, cudaStream_
 
 cudaError_t launch_de_select_oct(const DeParams &d, const uint32_t *candFirst,
                                  const uint32_t *candCount, uint32_t *selIdx,
-                                 uint32_t *selCount, cudaStream_t st) {
+                                 uint32_t *selCount, uint64_t total, cudaStream_t st) {
     if (d.ls.nM0 == 0) return cudaSuccess;
-    de_select_oct_kernel<<<d.ls.nM0, 256, 0, st>>>(d, candFirst, candCount, selIdx, selCount);
-    return cudaGetLastError();
+    if (total > 0) {
+        const uint64_t blocks = (total * 32 + 255) / 256;
+        if (blocks > 0x7fffffffull) return cudaErrorInvalidConfiguration;
+        de_select_oct_flags_kernel<<<(uint32_t)blocks, 256, 0, st>>>(d, candFirst, total,
+                                                                     selIdx);
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    return launch_select_compact(d.ls, candFirst, candCount, selIdx, selCount, st);
 }
 
 }  // namespace hpss

@@ -85,7 +85,7 @@ hpss_status de_impl(hpss_handle h, const float *d_m0s, uint32_t nM0, uint32_t po
         d.ls.selIdx = static_cast<uint32_t *>(h->selIdx.p);
         HPSS_CUDA_TRY(h, launch_de_select_oct(d, cf, cc, static_cast<uint32_t *>(h->selIdx.p),
                                               static_cast<uint32_t *>(h->selCount.p),
-                                              h->stream));
+                                              (uint64_t)total, h->stream));
     }
     // work queue order: midpoints by descending selected traces
     if (ordered) {

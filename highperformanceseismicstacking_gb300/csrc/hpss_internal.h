@@ -201,6 +201,12 @@ cudaError_t launch_order_by_count(const uint32_t *count, uint32_t n, uint32_t *o
 // order and write the result block [nM0][2+np][S]; counts near-ties.
 cudaError_t launch_merge_parts(const LsParams &p, uint32_t parts, const PartBest *partial,
                                cudaStream_t st);
+// Order-preserving compaction of 0 / 1 flags in selIdx (slots p.selFirst[mi]
+// .. + candCount[mi]) into the selected trace indices candFirst[mi] + q, in
+// place; selCount[mi] = their number (ls_common.cu).
+cudaError_t launch_select_compact(const LsParams &p, const uint32_t *candFirst,
+                                  const uint32_t *candCount, uint32_t *selIdx,
+                                  uint32_t *selCount, cudaStream_t st);
 // total: sum of candCount (the selIdx slots, p.selFirst their prefix).
 cudaError_t launch_select_oct(const LsParams &p, const float *cands,
                               uint32_t nCand, uint32_t *selIdx,
@@ -218,6 +224,6 @@ cudaError_t launch_sf_select_oct(const LsParams &p, const uint32_t *candFirst,
                                  uint32_t *selCount, cudaStream_t st);
 cudaError_t launch_de_select_oct(const DeParams &d, const uint32_t *candFirst,
                                  const uint32_t *candCount, uint32_t *selIdx,
-                                 uint32_t *selCount, cudaStream_t st);
+                                 uint32_t *selCount, uint64_t total, cudaStream_t st);
 
 }  // namespace hpss

@@ -193,6 +193,13 @@ cudaError_t launch_select_oct(const LsParams &p, const float *cands,
         const cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
+    return launch_select_compact(p, candFirst, candCount, selIdx, selCount, st);
+}
+
+cudaError_t launch_select_compact(const LsParams &p, const uint32_t *candFirst,
+                                  const uint32_t *candCount, uint32_t *selIdx,
+                                  uint32_t *selCount, cudaStream_t st) {
+    if (p.nM0 == 0) return cudaSuccess;
     select_oct_compact_kernel<<<p.nM0, kCompactThreads, 0, st>>>(p, candFirst, candCount,
                                                                   selIdx, selCount);
     return cudaGetLastError();
