@@ -53,22 +53,29 @@ def _stale(out: Path, deps) -> bool:
     return any(Path(d).stat().st_mtime > t for d in deps)
 
 
-def build_engine(force: bool = False, extra_flags=()) -> Path:
-    """Compile every csrc/*.cu for sm_103a and link libhpss_gb300.so."""
-    BUILD_DIR.mkdir(exist_ok=True)
-    LIB_DIR.mkdir(exist_ok=True)
+def build_engine(force: bool = False, extra_flags=(), flavour: str = "") -> Path:
+    """Compile every csrc/*.cu for sm_103a and link libhpss_gb300.so.
+
+    ``flavour`` names a separate build with ``extra_flags`` (objects in
+    _build/<flavour>/, library in lib/<flavour>/), e.g. the bounds-checked
+    build ``build_engine(extra_flags=["-DHPSS_CHECKED"], flavour="checked")``;
+    the default build is unaffected."""
+    bdir = BUILD_DIR / flavour if flavour else BUILD_DIR
+    ldir = LIB_DIR / flavour if flavour else LIB_DIR
+    bdir.mkdir(parents=True, exist_ok=True)
+    ldir.mkdir(parents=True, exist_ok=True)
     sources = sorted(CSRC.glob("*.cu"))
     headers = list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h")) + list((ROOT / "include").glob("*.h"))
     objs = []
     jobs = []
     for src in sources:
-        obj = BUILD_DIR / (src.stem + ".o")
+        obj = bdir / (src.stem + ".o")
         objs.append(obj)
         if force or _stale(obj, [src, *headers]):
             jobs.append([nvcc(), *NVCC_FLAGS, *extra_flags, "-c", str(src), "-o", str(obj)])
     with cf.ThreadPoolExecutor(max_workers=max(2, os.cpu_count() or 2)) as ex:
         list(ex.map(_run, jobs))
-    lib = LIB_DIR / LIB_NAME
+    lib = ldir / LIB_NAME
     if force or jobs or _stale(lib, objs):
         _run([nvcc(), ARCH, "-shared", "-o", str(lib), *map(str, objs), "-lcudart"])
     return lib

@@ -35,7 +35,7 @@ EXPORTED = [
     "hpss_linear_search_device",
     "hpss_differential_evolution", "hpss_differential_evolution_device",
     "hpss_stretch_free", "hpss_select_traces", "hpss_stream", "hpss_device_bytes",
-    "hpss_linear_search_noalloc", "hpss_linear_search_line",
+    "hpss_linear_search_noalloc", "hpss_noalloc_device_error", "hpss_linear_search_line",
 ]
 
 
@@ -88,6 +88,7 @@ def load_library(path: Optional[Path] = None) -> C.CDLL:
         "hpss_device_bytes": (C.c_size_t, [vp]),
         "hpss_linear_search_noalloc": (i32, [i32, vp, u32, vp, vp, u32, u32, f32, i32, fp, fp,
                                              up, f32, vp, u32, vp, vp]),
+        "hpss_noalloc_device_error": (i32, [vp, up]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

@@ -6,10 +6,11 @@
 // cuda/src/semblance/kernel/common/differential_evolution.cu and the
 // {cmp,zocrs,oct}/differential_evolution.cu evaluators).  Here the whole run
 // -- initialisation, and per generation mutation, crossover, semblance
-// evaluation and selection -- is ONE launch: a warp owns the population of one
-// sample (individual i lives in lane i % 32, slot i / 32), so mutation reads
-// other individuals with warp shuffles and nothing round-trips through global
-// memory between operators.
+// evaluation and selection -- is ONE launch: one thread per individual
+// (consecutive threads are the individuals of one sample, the reference's
+// thread layout), a CTA holds the whole populations of consecutive samples in
+// shared memory, mutation reads the donors from there, and nothing
+// round-trips through global memory between operators.
 //
 // Operator semantics follow the reference:
 //  * init: x_j = min_j + U * (max_j - min_j), U in (0, 1]   (startPopulations)

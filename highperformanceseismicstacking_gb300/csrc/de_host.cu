@@ -64,24 +64,11 @@ hpss_status de_impl(hpss_handle h, const float *d_m0s, uint32_t nM0, uint32_t po
                                              static_cast<uint32_t *>(h->selFirst.p),
                                              static_cast<uint32_t *>(h->selCount.p), h->stream));
     } else {
-        float hmax = 0.f;
-        for (float v : h->hHoff) hmax = std::max(hmax, std::fabs(v));
-        float radius = (h->apm + std::sqrt(hmax * hmax + h->h0 * h->h0)) * 1.001f + 1.0f;
-        HPSS_CUDA_TRY(h, ensure(h, h->candFirst, nM0 * sizeof(uint32_t)));
-        HPSS_CUDA_TRY(h, ensure(h, h->candCount, nM0 * sizeof(uint32_t)));
-        uint32_t *cf = static_cast<uint32_t *>(h->candFirst.p);
-        uint32_t *cc = static_cast<uint32_t *>(h->candCount.p);
-        HPSS_CUDA_TRY(h, launch_select_range(h->dMid, h->nTraces, d_m0s, nM0, 2, h->apm, radius,
-                                             cf, cc, h->stream));
-        HPSS_CUDA_TRY(h, launch_exclusive_scan(cc, static_cast<uint32_t *>(h->selFirst.p), nM0,
-                                               h->stream));
-        std::vector<uint32_t> ccHost(nM0);
-        HPSS_CUDA_TRY(h, cudaMemcpyAsync(ccHost.data(), cc, nM0 * sizeof(uint32_t),
-                                         cudaMemcpyDeviceToHost, h->stream));
-        HPSS_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
-        size_t total = 0;
-        for (uint32_t v : ccHost) total += v;
-        HPSS_CUDA_TRY(h, ensure(h, h->selIdx, total * sizeof(uint32_t)));
+        uint64_t total = 0;
+        rc = oct_candidate_slots(h, d_m0s, nM0, static_cast<uint32_t *>(h->selFirst.p), &total);
+        if (rc != HPSS_OK) return rc;
+        const uint32_t *cf = static_cast<const uint32_t *>(h->candFirst.p);
+        const uint32_t *cc = static_cast<const uint32_t *>(h->candCount.p);
         d.ls.selIdx = static_cast<uint32_t *>(h->selIdx.p);
         HPSS_CUDA_TRY(h, launch_de_select_oct(d, cf, cc, static_cast<uint32_t *>(h->selIdx.p),
                                               static_cast<uint32_t *>(h->selCount.p),

@@ -137,6 +137,41 @@ void build_oct_selection_candidates(hpss_handle h) {
     }
 }
 
+// OCT selection, the step shared by the linear search, DE and stretch-free:
+// only traces with |m - m0| <= apm + sqrt(hmax^2 + h0^2) can pass (the
+// displaced midpoint formula, oct/common.cuh:26-32, divides
+// 2*theta*(h^2-h0^2) by a root no smaller than 2*|theta|*sqrt(h^2+h0^2)),
+// widened for rounding: a contiguous run of the sorted line per midpoint
+// (candFirst / candCount).  Each midpoint gets that many slots of selIdx, at
+// offsets `first` (exclusive prefix sum, 32-bit: a total of 2^32 slots or
+// more is rejected); selIdx is grown to the total.
+hpss_status oct_candidate_slots(hpss_handle h, const float *d_m0s, uint32_t nM0,
+                                uint32_t *first, uint64_t *total) {
+    float hmax = 0.f;
+    for (float v : h->hHoff) hmax = std::max(hmax, std::fabs(v));
+    float radius = (h->apm + std::sqrt(hmax * hmax + h->h0 * h->h0)) * 1.001f + 1.0f;
+    HPSS_CUDA_TRY(h, ensure(h, h->candFirst, nM0 * sizeof(uint32_t)));
+    HPSS_CUDA_TRY(h, ensure(h, h->candCount, nM0 * sizeof(uint32_t)));
+    uint32_t *cf = static_cast<uint32_t *>(h->candFirst.p);
+    uint32_t *cc = static_cast<uint32_t *>(h->candCount.p);
+    HPSS_CUDA_TRY(h, launch_select_range(h->dMid, h->nTraces, d_m0s, nM0, 2,
+                                         h->apm, radius, cf, cc, h->stream));
+    HPSS_CUDA_TRY(h, launch_exclusive_scan(cc, first, nM0, h->stream));
+    std::vector<uint32_t> ccHost(nM0);
+    HPSS_CUDA_TRY(h, cudaMemcpyAsync(ccHost.data(), cc, nM0 * sizeof(uint32_t),
+                                     cudaMemcpyDeviceToHost, h->stream));
+    HPSS_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    uint64_t t = 0;
+    for (uint32_t v : ccHost) t += v;
+    if (t > 0xffffffffull)
+        return set_error(h, HPSS_ERR_INVALID_ARGUMENT,
+                         "OCT selection: 2^32 or more candidate trace slots in one call; "
+                         "split the midpoints into smaller calls");
+    HPSS_CUDA_TRY(h, ensure(h, h->selIdx, t * sizeof(uint32_t)));
+    *total = t;
+    return HPSS_OK;
+}
+
 // Device-side selection for nM0 midpoints (d_m0s on the device).  Leaves
 // LsParams' selFirst / selCount / selIdx filled.
 hpss_status run_selection(hpss_handle h, const float *d_m0s, uint32_t nM0,
@@ -154,28 +189,11 @@ hpss_status run_selection(hpss_handle h, const float *d_m0s, uint32_t nM0,
                                              h->apm, 0.f, first, count, h->stream));
         return HPSS_OK;
     }
-    // OCT: |mh - m0| <= sqrt(h^2 + h0^2) for any candidate (the displaced
-    // midpoint formula, oct/common.cuh:26-32, divides 2*theta*(h^2-h0^2) by a
-    // root no smaller than 2*|theta|*sqrt(h^2+h0^2)), so only traces with
-    // |m - m0| <= apm + sqrt(hmax^2 + h0^2) can pass; widened for rounding.
-    float hmax = 0.f;
-    for (float v : h->hHoff) hmax = std::max(hmax, std::fabs(v));
-    float radius = (h->apm + std::sqrt(hmax * hmax + h->h0 * h->h0)) * 1.001f + 1.0f;
-    HPSS_CUDA_TRY(h, ensure(h, h->candFirst, nM0 * sizeof(uint32_t)));
-    HPSS_CUDA_TRY(h, ensure(h, h->candCount, nM0 * sizeof(uint32_t)));
-    uint32_t *cf = static_cast<uint32_t *>(h->candFirst.p);
-    uint32_t *cc = static_cast<uint32_t *>(h->candCount.p);
-    HPSS_CUDA_TRY(h, launch_select_range(h->dMid, h->nTraces, d_m0s, nM0, 2,
-                                         h->apm, radius, cf, cc, h->stream));
-    // capacity per midpoint = its candidate count; offsets by prefix sum
-    HPSS_CUDA_TRY(h, launch_exclusive_scan(cc, first, nM0, h->stream));
-    std::vector<uint32_t> ccHost(nM0);
-    HPSS_CUDA_TRY(h, cudaMemcpyAsync(ccHost.data(), cc, nM0 * sizeof(uint32_t),
-                                     cudaMemcpyDeviceToHost, h->stream));
-    HPSS_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
-    size_t total = 0;
-    for (uint32_t v : ccHost) total += v;
-    HPSS_CUDA_TRY(h, ensure(h, h->selIdx, total * sizeof(uint32_t)));
+    uint64_t total = 0;
+    hpss_status rc = oct_candidate_slots(h, d_m0s, nM0, first, &total);
+    if (rc != HPSS_OK) return rc;
+    const uint32_t *cf = static_cast<const uint32_t *>(h->candFirst.p);
+    const uint32_t *cc = static_cast<const uint32_t *>(h->candCount.p);
     if (h->octCandsHost.empty()) build_oct_selection_candidates(h);
     HPSS_CUDA_TRY(h, ensure(h, h->octCands, h->octCandsHost.size() * sizeof(float)));
     HPSS_CUDA_TRY(h, cudaMemcpyAsync(h->octCands.p, h->octCandsHost.data(),
@@ -642,24 +660,11 @@ hpss_status hpss_stretch_free(hpss_handle h, const float *m0s, uint32_t nM0,
                                              static_cast<uint32_t *>(h->selFirst.p),
                                              static_cast<uint32_t *>(h->selCount.p), h->stream));
     } else {
-        float hmax = 0.f;
-        for (float v : h->hHoff) hmax = std::max(hmax, std::fabs(v));
-        float radius = (h->apm + std::sqrt(hmax * hmax + h->h0 * h->h0)) * 1.001f + 1.0f;
-        HPSS_CUDA_TRY(h, ensure(h, h->candFirst, nM0 * sizeof(uint32_t)));
-        HPSS_CUDA_TRY(h, ensure(h, h->candCount, nM0 * sizeof(uint32_t)));
-        uint32_t *cf = static_cast<uint32_t *>(h->candFirst.p);
-        uint32_t *cc = static_cast<uint32_t *>(h->candCount.p);
-        HPSS_CUDA_TRY(h, launch_select_range(h->dMid, h->nTraces, d_m0s, nM0, 2, h->apm, radius,
-                                             cf, cc, h->stream));
-        HPSS_CUDA_TRY(h, launch_exclusive_scan(cc, static_cast<uint32_t *>(h->selFirst.p), nM0,
-                                               h->stream));
-        std::vector<uint32_t> ccHost(nM0);
-        HPSS_CUDA_TRY(h, cudaMemcpyAsync(ccHost.data(), cc, nM0 * sizeof(uint32_t),
-                                         cudaMemcpyDeviceToHost, h->stream));
-        HPSS_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
-        size_t total = 0;
-        for (uint32_t v : ccHost) total += v;
-        HPSS_CUDA_TRY(h, ensure(h, h->selIdx, total * sizeof(uint32_t)));
+        uint64_t total = 0;
+        rc = oct_candidate_slots(h, d_m0s, nM0, static_cast<uint32_t *>(h->selFirst.p), &total);
+        if (rc != HPSS_OK) return rc;
+        const uint32_t *cf = static_cast<const uint32_t *>(h->candFirst.p);
+        const uint32_t *cc = static_cast<const uint32_t *>(h->candCount.p);
         lp.selIdx = static_cast<uint32_t *>(h->selIdx.p);
         HPSS_CUDA_TRY(h, launch_sf_select_oct(lp, cf, cc, static_cast<uint32_t *>(h->selIdx.p),
                                               static_cast<uint32_t *>(h->selCount.p),

@@ -54,6 +54,11 @@ hpss_status set_error(hpss_handle h, hpss_status code, const std::string &msg);
 cudaError_t ensure(hpss_handle h, hpss_handle_s::Buf &b, size_t bytes);
 void release(hpss_handle h, hpss_handle_s::Buf &b);
 hpss_status check_ready(hpss_handle h);
+// OCT: the candidate traces of each midpoint (h->candFirst / candCount), their
+// slot offsets in selIdx (`first`) and selIdx sized for them (`total` slots,
+// rejected at 2^32 or more).
+hpss_status oct_candidate_slots(hpss_handle h, const float *d_m0s, uint32_t nM0,
+                                uint32_t *first, uint64_t *total);
 // Trace selection of nM0 device midpoints into the handle's buffers (lp's
 // selFirst / selCount / selIdx are set).
 hpss_status run_selection(hpss_handle h, const float *d_m0s, uint32_t nM0, LsParams &lp);

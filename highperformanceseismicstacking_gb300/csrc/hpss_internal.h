@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <cstdlib>
 #include <string>
 #include <vector>
 
@@ -106,7 +107,24 @@ struct LsParams {
     // OCT with h0 = 0: warps drop traces by the displaced-midpoint box test
     // (oct_box_may_pass) before the per-sample test
     bool octBox = false;
+#ifdef HPSS_CHECKED
+    // checked builds only: bytes armed on the tuned kernel's staging barrier
+    // beyond what its copies deliver, so that the bounded wait runs out and
+    // the kernel reports kErrTimeout (a drill of the timeout path; 0 = off)
+    uint32_t stageDrillBytes = 0;
+#endif
 };
+
+// Checked builds: the staging-timeout drill from the environment variable
+// HPSS_STAGE_DRILL (extra bytes, rounded down to 16); no-op otherwise.
+inline void set_stage_drill(LsParams &p) {
+#ifdef HPSS_CHECKED
+    const char *v = std::getenv("HPSS_STAGE_DRILL");
+    p.stageDrillBytes = v ? (uint32_t)(std::strtoul(v, nullptr, 10) & 0xfff0ul) : 0u;
+#else
+    (void)p;
+#endif
+}
 
 // Differential evolution launch (de.cu).
 struct DeParams {

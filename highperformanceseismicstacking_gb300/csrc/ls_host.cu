@@ -237,6 +237,7 @@ hpss_status linear_search_impl(hpss_handle h, const float *d_m0s, uint32_t nM0,
     lp.nearTies = reinterpret_cast<unsigned long long *>(counters + 8);
     lp.notUsed = reinterpret_cast<unsigned long long *>(counters + 16) +
                  (group ? group->m0Offset : 0);
+    set_stage_drill(lp);
 
     const uint32_t tiles = (h->S + kTileSamples - 1) / kTileSamples;
     const uint64_t units = (uint64_t)nM0 * tiles;
@@ -372,6 +373,10 @@ hpss_status linear_search_impl(hpss_handle h, const float *d_m0s, uint32_t nM0,
             stats->kernel_variant = h->lastVariant;
             stats->candidate_parts = h->lastParts;
         }
+        if (err & kErrTimeout)
+            return set_error(h, HPSS_ERR_TIMEOUT,
+                             "staging copies did not complete in time, error word " +
+                                 std::to_string(err));
         if (err)
             return set_error(h, HPSS_ERR_DEVICE_CHECK,
                              "device check failed, error word " + std::to_string(err));

@@ -180,9 +180,11 @@ __device__ __forceinline__ bool stage_bar_try_wait(unsigned long long *bar, uint
         : "memory");
     return done != 0;
 }
-// Bounded wait for phase `parity`; false when it did not complete in time.
-__device__ __forceinline__ bool stage_bar_wait(unsigned long long *bar, uint32_t parity) {
-    for (uint32_t it = 0; it < (1u << 22); it++)
+// Bounded wait for phase `parity`; false when it did not complete within
+// `limit` polls.
+__device__ __forceinline__ bool stage_bar_wait(unsigned long long *bar, uint32_t parity,
+                                               uint32_t limit) {
+    for (uint32_t it = 0; it < limit; it++)
         if (stage_bar_try_wait(bar, parity)) return true;
     return false;
 }
@@ -217,6 +219,15 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
     const float2 kMagic2 = f2(8388608.f, 8388608.f);      // 2^23
     const float2 kNegMagic2 = f2(-8388608.f, -8388608.f);
     const int magicTau = 0x4B000000 + tau;                  // bits of 2^23, plus tau
+
+#ifdef HPSS_CHECKED
+    const uint32_t drillBytes = a.stageDrillBytes;
+#else
+    constexpr uint32_t drillBytes = 0;
+#endif
+    // polls of the staging barrier before a round counts as timed out (the
+    // timeout drill of checked builds gives up sooner)
+    const uint32_t waitLimit = drillBytes ? (1u << 12) : (1u << 22);
 
     if (threadIdx.x < kZeroPad) sm.y[threadIdx.x] = 0.f;
     if (threadIdx.x == 0) stage_bar_init(&sm.stageBar);
@@ -355,7 +366,7 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
                         uint32_t floats = 0;
 #pragma unroll
                         for (int wv = 0; wv < kTunedWarps; wv++) floats += (uint32_t)sm.warpLen[wv];
-                        stage_bar_expect(&sm.stageBar, floats * 4u);
+                        stage_bar_expect(&sm.stageBar, floats * 4u + drillBytes);
                     }
                     if (keep) {
                         // the previous round's reads of the stage are ordered
@@ -365,12 +376,13 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
                         stage_bulk_copy(sm.y + off, a.samples + (size_t)ti * a.stride + lo,
                                         (uint32_t)len * 4u, &sm.stageBar);
                     }
-                    const bool ok = stage_bar_wait(&sm.stageBar, stagePhase);
+                    const bool ok = stage_bar_wait(&sm.stageBar, stagePhase, waitLimit);
                     stagePhase ^= 1u;
                     if (__syncthreads_or(!ok)) {
-                        // copies did not complete in time: report and leave
+                        // copies did not complete in time: report, wait (again
+                        // bounded) for this CTA's copies in flight, and leave
                         if (threadIdx.x == 0) atomicOr(a.errorWord, kErrTimeout);
-                        stage_bar_wait(&sm.stageBar, stagePhase ^ 1u);
+                        stage_bar_wait(&sm.stageBar, stagePhase ^ 1u, waitLimit);
                         return;
                     }
                 }

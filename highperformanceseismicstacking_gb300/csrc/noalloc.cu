@@ -16,7 +16,8 @@
 // one array and it keeps the previous call's contents: this file clears what
 // must start at zero on every call, and calls whose work overlaps on the GPU
 // (different streams, or different host threads on the same device) race on
-// it -- serialise them.
+// it -- serialise them.  The kernels' device error word is part of that
+// array too: hpss_noalloc_device_error reads it once the call has finished.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -67,6 +68,30 @@ hpss_status fail(hpss_status code, const std::string &msg) {
     return code;
 }
 
+// Device address of the scratch array on the current device, looked up
+// once per device with that device current (the array's name in host code is
+// only a host-side stand-in).  The address is kept for the life of the
+// process: it is not valid across cudaDeviceReset, after which this library
+// must not be called again on that device.
+hpss_status scratch_of_current_device(int *devOut, void **base) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return fail(HPSS_ERR_CUDA, cudaGetErrorString(e));
+    if (dev < 0 || dev >= kMaxDevices) return fail(HPSS_ERR_NO_DEVICE, "device index too large");
+    std::lock_guard<std::mutex> lock(g_mu);
+    if (!g_scratchAddr[dev]) {
+        e = cudaGetSymbolAddress(&g_scratchAddr[dev], g_noallocScratch);
+        if (e != cudaSuccess) {
+            g_scratchAddr[dev] = nullptr;
+            return fail(HPSS_ERR_CUDA,
+                        std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+        }
+    }
+    *devOut = dev;
+    *base = g_scratchAddr[dev];
+    return HPSS_OK;
+}
+
 __global__ void square_kernel(const float *h, float *hsq, uint32_t n) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) hsq[i] = h[i] * h[i];  // float h*h, as the reference's host code
@@ -110,22 +135,10 @@ extern "C" hpss_status hpss_linear_search_noalloc(
                     "traces <= 1048576");
 
     int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return fail(HPSS_ERR_CUDA, cudaGetErrorString(e));
-    if (dev < 0 || dev >= kMaxDevices) return fail(HPSS_ERR_NO_DEVICE, "device index too large");
     void *base = nullptr;
-    {
-        std::lock_guard<std::mutex> lock(g_mu);
-        if (!g_scratchAddr[dev]) {
-            e = cudaGetSymbolAddress(&g_scratchAddr[dev], g_noallocScratch);
-            if (e != cudaSuccess) {
-                g_scratchAddr[dev] = nullptr;
-                return fail(HPSS_ERR_CUDA, std::string("cudaGetSymbolAddress: ") +
-                                               cudaGetErrorString(e));
-            }
-        }
-        base = g_scratchAddr[dev];
-    }
+    hpss_status rc = scratch_of_current_device(&dev, &base);
+    if (rc != HPSS_OK) return rc;
+    cudaError_t e = cudaSuccess;
     uint32_t *w = static_cast<uint32_t *>(base);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
 
@@ -152,6 +165,7 @@ extern "C" hpss_status hpss_linear_search_noalloc(
     lp.selCount = w + kOffCount;
     lp.out = d_out;
     lp.errorWord = w + kOffErr;
+    set_stage_drill(lp);
 
     // the error word keeps the previous call's value: clear it
     e = cudaMemsetAsync(lp.errorWord, 0, sizeof(uint32_t), st);
@@ -184,6 +198,25 @@ extern "C" hpss_status hpss_linear_search_noalloc(
     } else {
         e = launch_ls_plain(lp, st);
     }
+    if (e != cudaSuccess) return fail(HPSS_ERR_CUDA, cudaGetErrorString(e));
+    return HPSS_OK;
+}
+
+// The allocating entry points report the kernels' device error word in
+// hpss_stats.device_error; the allocation-free search is asynchronous and has
+// no statistics, so its word (it lives in the shared scratch array) is read
+// here: after the stream has finished the call, one 4-byte copy to the
+// caller's host variable.  No allocation.
+extern "C" hpss_status hpss_noalloc_device_error(void *stream, uint32_t *word) {
+    if (!word) return fail(HPSS_ERR_INVALID_ARGUMENT, "null output pointer");
+    int dev = 0;
+    void *base = nullptr;
+    hpss_status rc = scratch_of_current_device(&dev, &base);
+    if (rc != HPSS_OK) return rc;
+    cudaError_t e = cudaStreamSynchronize(static_cast<cudaStream_t>(stream));
+    if (e == cudaSuccess)
+        e = cudaMemcpy(word, static_cast<uint32_t *>(base) + kOffErr, sizeof(uint32_t),
+                       cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return fail(HPSS_ERR_CUDA, cudaGetErrorString(e));
     return HPSS_OK;
 }

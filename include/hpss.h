@@ -51,6 +51,16 @@ typedef int hpss_status;
 #define HPSS_ERR_TIMEOUT (-7)
 #define HPSS_ERR_DEVICE_CHECK (-8)
 
+/* Bits of the device error word (hpss_stats.device_error,
+ * hpss_noalloc_device_error).  A synchronous call that sees TIMEOUT returns
+ * HPSS_ERR_TIMEOUT, any other bit HPSS_ERR_DEVICE_CHECK; its outputs are then
+ * not valid. */
+#define HPSS_DEVERR_SMEM_BOUNDS 1u   /* shared-memory index out of its span
+                                        (bounds-checked builds only) */
+#define HPSS_DEVERR_SPAN_OVERFLOW 2u /* a trace span larger than the stage */
+#define HPSS_DEVERR_TIMEOUT 4u       /* staging copies did not complete
+                                        within the bounded wait */
+
 /* traveltime_t (common/include/capability.h:3-7). */
 #define HPSS_MODEL_CMP 0
 #define HPSS_MODEL_ZOCRS 1
@@ -274,7 +284,11 @@ size_t hpss_device_bytes(hpss_handle h);
  * rejected with HPSS_ERR_INVALID_ARGUMENT).  The first call on a device looks
  * the scratch up (make it before any stream capture).  Calls share the
  * scratch: calls that overlap on the GPU race.  Enqueued on `stream`
- * (cudaStream_t; NULL = default stream); errors via hpss_last_error(NULL).
+ * (cudaStream_t; NULL = default stream); errors found on the host via
+ * hpss_last_error(NULL); errors found by the kernels (the device error word,
+ * hpss_stats.device_error of the allocating calls) via
+ * hpss_noalloc_device_error.  The scratch address is looked up once per
+ * device and kept: do not call it on a device after cudaDeviceReset.
  * Same results as hpss_linear_search with the tuned kernel. */
 hpss_status hpss_linear_search_noalloc(
     int model, const float *d_samples, uint32_t stride, const float *d_midpoints,
@@ -282,6 +296,13 @@ hpss_status hpss_linear_search_noalloc(
     float dtInSeconds, int tauIndexDisplacement, const float *lower,
     const float *upper, const uint32_t *granularity, float apm,
     const float *d_m0s, uint32_t nM0, float *d_out, void *stream);
+
+/* Device error word of the last hpss_linear_search_noalloc call on the
+ * current device (no counterpart in the reference): waits for `stream` and
+ * copies the word into *word (0 = none; bits as hpss_stats.device_error).
+ * The word is cleared at the start of every call, so read it before the next
+ * call.  Allocates nothing. */
+hpss_status hpss_noalloc_device_error(void *stream, uint32_t *word);
 
 #ifdef __cplusplus
 }

@@ -8,6 +8,8 @@ with the target fixed to sm_103a.
 
 Only the .cu files of the hot path are compiled; the reference's host code
 (boost, SPITS) is not.  Run: python oracle/build_ref.py [reference_root]
+(default: $HPSS_REFERENCE_ROOT, else the path in default_root()); where the
+tree is absent nothing is built and the prebuilt fatbins are used.
 """
 from __future__ import annotations
 
@@ -48,8 +50,14 @@ def fatbin_name(rel: str, tag: str = "") -> str:
     return "_".join(parts) + tag + ".fatbin"
 
 
-def build(ref_root: str = "/root/reference") -> list:
-    ref = Path(ref_root)
+def default_root() -> str:
+    """The reference source tree: $HPSS_REFERENCE_ROOT, else the checkout
+    this recipe was written against."""
+    return os.environ.get("HPSS_REFERENCE_ROOT", "/root/reference")
+
+
+def build(ref_root: str = None) -> list:
+    ref = Path(ref_root or default_root())
     if not ref.exists():
         return []
     OUT.mkdir(exist_ok=True)
@@ -68,5 +76,5 @@ def build(ref_root: str = "/root/reference") -> list:
 
 
 if __name__ == "__main__":
-    for p in build(sys.argv[1] if len(sys.argv) > 1 else "/root/reference"):
+    for p in build(sys.argv[1] if len(sys.argv) > 1 else None):
         print(p)

@@ -52,6 +52,23 @@ void oracle_ls_eval_f64(int model, const float *samples, uint32_t stride,
                         double *sembl, double *stack, double *not_used,
                         int nthreads);
 
+/* The same evaluation on the t0 samples sidx[0..nS) only (all candidates):
+ * tables [nS][P]. */
+void oracle_ls_eval_samples_f32(int model, const float *samples,
+                                uint32_t stride, uint32_t S, float dt, int tau,
+                                const float *mid, const float *hoff,
+                                const uint32_t *sel, uint32_t nsel, float m0,
+                                float apm, float h0, const float *params,
+                                uint32_t P, const uint32_t *sidx, uint32_t nS,
+                                float *sembl, float *stack, int nthreads);
+void oracle_ls_eval_samples_f64(int model, const float *samples,
+                                uint32_t stride, uint32_t S, float dt, int tau,
+                                const float *mid, const float *hoff,
+                                const uint32_t *sel, uint32_t nsel, float m0,
+                                float apm, float h0, const float *params,
+                                uint32_t P, const uint32_t *sidx, uint32_t nS,
+                                double *sembl, double *stack, int nthreads);
+
 /* Argmax over candidates with the reference's strict '>' scan from -1
  * (lowest index wins ties; NaN never wins).  best_idx[s] = -1 if none.
  * Follows selectBestSemblancesFor* (cuda/src/semblance/kernel/cmp/

@@ -40,6 +40,8 @@ def lib():
         _lib.oracle_sf_eval_f64.argtypes = common + [fp, i32, dp, dp, dp, i32]
         _lib.oracle_eval_raw_f32.argtypes = common + [fp, u32, fp, fp, i32]
         _lib.oracle_eval_raw_f64.argtypes = common + [fp, u32, dp, dp, i32]
+        _lib.oracle_ls_eval_samples_f32.argtypes = common + [fp, u32, up, u32, fp, fp, i32]
+        _lib.oracle_ls_eval_samples_f64.argtypes = common + [fp, u32, up, u32, dp, dp, i32]
         _lib.oracle_argmax_f32.argtypes = [fp, u32, u32, C.POINTER(C.c_int32)]
         _lib.oracle_argmax_f64.argtypes = [dp, u32, u32, C.POINTER(C.c_int32)]
         _lib.oracle_build_grid.argtypes = [i32, fp, fp, up, fp]
@@ -139,6 +141,30 @@ def ls_eval(model: str, samples: np.ndarray, mid, hoff, sel, m0: float, dt: floa
        sel.size, C.c_float(m0), C.c_float(apm), C.c_float(h0), _f(params), P, cv(sembl),
        cv(stack), cv(nu), nthreads)
     return sembl, stack, nu
+
+
+def ls_eval_samples(model: str, samples: np.ndarray, mid, hoff, sel, m0: float, dt: float,
+                    tau: int, params: np.ndarray, sidx, apm: float = 0.0, h0: float = 0.0,
+                    precision: str = "f32", nthreads: int = 0):
+    """ls_eval on the t0 samples sidx only: semblance and stack [len(sidx)][P]."""
+    samples = np.ascontiguousarray(samples, np.float32)
+    mid = np.ascontiguousarray(mid, np.float32)
+    hoff = np.ascontiguousarray(hoff, np.float32)
+    sel = np.ascontiguousarray(sel, np.uint32)
+    params = np.ascontiguousarray(params, np.float32)
+    sidx = np.ascontiguousarray(sidx, np.uint32)
+    S = samples.shape[1]
+    P = params.shape[0]
+    dtype = np.float32 if precision == "f32" else np.float64
+    sembl = np.zeros((sidx.size, P), dtype)
+    stack = np.zeros((sidx.size, P), dtype)
+    fn = lib().oracle_ls_eval_samples_f32 if precision == "f32" else \
+        lib().oracle_ls_eval_samples_f64
+    cv = _f if precision == "f32" else _d
+    fn(MODELS[model], _f(samples), S, S, C.c_float(dt), tau, _f(mid), _f(hoff), _u(sel),
+       sel.size, C.c_float(m0), C.c_float(apm), C.c_float(h0), _f(params), P, _u(sidx),
+       sidx.size, cv(sembl), cv(stack), nthreads)
+    return sembl, stack
 
 
 def argmax(sembl: np.ndarray) -> np.ndarray:

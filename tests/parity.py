@@ -7,8 +7,11 @@ interpolation fraction and changes the semblance by ~1e-5 .. 1e-4 relative,
 and, when a window lies exactly at a trace edge, includes or drops one trace
 (a discrete jump).  So results are judged by distributions:
 
-* chosen semblance: relative error (floor 1e-3) at the 99.9th percentile
-  <= SEMBL_P999, and samples off by more than 1e-3 absolute <= JUMP_FRAC;
+* chosen semblance: samples off by more than 1e-3 absolute (window-edge
+  jumps) <= JUMP_FRAC; over the other samples the relative error (floor
+  1e-3) at the 99.9th percentile <= SEMBL_P999 x index_scale(S): the
+  traveltime's rounding moves t/dt by an ulp of t/dt, so the tolerance grows
+  with the largest sample index (1 up to 512 samples, 4 at 2000);
 * chosen candidate: identical except where the two best candidates of the
   oracle's own table are within NEAR_TIE relative (near-ties), counted;
   other disagreements <= FAR_FRAC of the samples (window-edge jumps);
@@ -30,8 +33,18 @@ FAR_FRAC = 2e-3
 STACK_P999 = 1e-3
 
 
+def index_scale(S: int, model: str = "cmp") -> float:
+    """ulp of the largest window index of an S-sample trace over that of a
+    512-sample trace (at least 1); twice that for OCT, whose time is some 40
+    FP32 operations with square roots and divisions (two FP32 evaluations of
+    it differ by more ulps than the CMP / ZO-CRS forms)."""
+    s = max(1.0, float(2 ** int(np.ceil(np.log2(max(S, 1))))) / 512.0)
+    return 2.0 * s if model == "oct" else s
+
+
 @dataclasses.dataclass
 class Report:
+    sembl_p999: float = SEMBL_P999
     samples: int = 0
     mismatches: int = 0
     near_ties: int = 0
@@ -44,7 +57,7 @@ class Report:
         rel = np.concatenate(self.sembl_rel) if self.sembl_rel else np.zeros(1)
         se = np.concatenate(self.stack_err) if self.stack_err else np.zeros(1)
         n = max(self.samples, 1)
-        assert np.quantile(rel, 0.999) <= SEMBL_P999, np.quantile(rel, 0.999)
+        assert np.quantile(rel, 0.999) <= self.sembl_p999, np.quantile(rel, 0.999)
         assert self.jumps <= JUMP_FRAC * n, (self.jumps, n)
         assert self.far <= FAR_FRAC * n, (self.far, n)
         assert np.quantile(se, 0.999) <= STACK_P999, np.quantile(se, 0.999)
@@ -79,8 +92,9 @@ def compare_block(rep: Report, got: np.ndarray, sem: np.ndarray, stk: np.ndarray
     g0 = got[0].astype(np.float64)
     r0 = ref[0].astype(np.float64)
     rel = np.abs(g0 - r0) / np.maximum(np.abs(r0), 1e-3)
-    rep.sembl_rel.append(rel)
-    rep.jumps += int(np.sum(np.abs(g0 - r0) > 1e-3))
+    jump = np.abs(g0 - r0) > 1e-3
+    rep.sembl_rel.append(rel[~jump])
+    rep.jumps += int(np.sum(jump))
     gi = chosen_index(params, got)
     same = gi == idx
     rows = np.arange(S)

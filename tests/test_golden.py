@@ -15,7 +15,7 @@ import numpy as np
 import pytest
 
 from oracle import oracle
-from parity import Report, assert_same_but_stack, compare_block
+from parity import Report, assert_same_but_stack, compare_block, index_scale
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
 CASES = sorted(p.stem[4:] for p in GOLDEN.glob("ref_*.npz"))
@@ -23,7 +23,34 @@ CASES = sorted(p.stem[4:] for p in GOLDEN.glob("ref_*.npz"))
 
 def load(name):
     z = np.load(GOLDEN / f"ref_{name}.npz")
-    return {k: z[k] for k in z.files}
+    d = {k: z[k] for k in z.files}
+    if "samples16" in d:  # FP16-valued amplitudes, stored as FP16
+        d["samples"] = d.pop("samples16").astype(np.float32)
+    return d
+
+
+# Oracle comparisons of a fixture cost P x S x selected traces evaluations
+# per midpoint; above this many the oracle runs on a fixed subset of the
+# samples (every one of them is still compared bit for bit with the
+# reference's results by the GPU test).
+ORACLE_EVALS_MAX = 3e8
+
+
+def oracle_tables(z, i, m0, sel):
+    """Oracle semblance / stack tables of midpoint i and the sample indices
+    they cover (all samples, or an evenly spaced subset for large cases)."""
+    model = str(z["model"])
+    S = z["samples"].shape[1]
+    P = z["params"].shape[0]
+    args = (model, z["samples"], z["midpoints"], z["halfoffsets"], sel, float(m0),
+            float(z["dt"]), int(z["tau"]), z["params"])
+    if float(P) * S * sel.size <= ORACLE_EVALS_MAX:
+        sem, stk, nu = oracle.ls_eval(*args, float(z["apm"]), float(z["h0"]))
+        return sem, stk, nu, np.arange(S)
+    n = max(8, int(ORACLE_EVALS_MAX / (float(P) * sel.size)))
+    sidx = np.unique(np.linspace(0, S - 1, n).astype(np.uint32))
+    sem, stk = oracle.ls_eval_samples(*args, sidx, float(z["apm"]), float(z["h0"]))
+    return sem, stk, None, sidx
 
 
 def selection(z, m0):
@@ -40,7 +67,8 @@ def selection(z, m0):
 
 
 def test_fixtures_present():
-    assert set(CASES) >= {"cmp", "zocrs", "oct_h0_0", "oct_h0_300"}
+    assert set(CASES) >= {"cmp", "zocrs", "oct_h0_0", "oct_h0_300", "oct_h0_500",
+                          "oct_h0_1000", "cmp_production_w7", "zocrs_full_grid"}
 
 
 @pytest.mark.parametrize("name", CASES)
@@ -60,19 +88,20 @@ def test_oracle_matches_reference_kernels(name):
     z = load(name)
     model = str(z["model"])
     params = z["params"]
-    rep = Report()
+    rep = Report(sembl_p999=index_scale(z["samples"].shape[1], model) * Report.sembl_p999)
     for i, m0 in enumerate(z["m0s"]):
         sel = selection(z, m0).astype(np.uint32)
         if sel.size == 0:
             assert np.all(z["results"][i] == 0)
             continue
-        sem, stk, nu = oracle.ls_eval(model, z["samples"], z["midpoints"], z["halfoffsets"], sel,
-                                      float(m0), float(z["dt"]), int(z["tau"]), params,
-                                      float(z["apm"]), float(z["h0"]))
+        sem, stk, nu, sidx = oracle_tables(z, i, m0, sel)
         rms = float(np.sqrt(np.mean(z["samples"][sel] ** 2)))
-        compare_block(rep, z["results"][i], sem, stk, params, rms)
+        compare_block(rep, z["results"][i][:, sidx], sem, stk, params, rms)
         if model == "oct":
-            assert float(nu.sum()) == z["not_used"][i]
+            # IEEE FP32 (the oracle) against the fast-math build (the
+            # reference): a trace within rounding of the aperture may flip;
+            # the engine's count is checked for equality on the GPU
+            assert abs(float(nu.sum()) - z["not_used"][i]) <= max(2.0, 1e-5 * z["not_used"][i])
     rep.check()
 
 
@@ -106,16 +135,14 @@ def test_engine_matches_reference_kernels(engine, name, kernel):
     # every sample: the reference's chosen candidate and values within the
     # parity tolerances (tests/parity.py), judged against the reference's table
     params = z["params"]
-    rep = Report()
+    rep = Report(sembl_p999=index_scale(z["samples"].shape[1], model) * Report.sembl_p999)
     for i, m0 in enumerate(z["m0s"]):
         sel = selection(z, m0).astype(np.uint32)
         if sel.size == 0:
             continue
-        sem, stk, _ = oracle.ls_eval(model, z["samples"], z["midpoints"], z["halfoffsets"], sel,
-                                     float(m0), float(z["dt"]), int(z["tau"]), params,
-                                     float(z["apm"]), float(z["h0"]))
+        sem, stk, _, sidx = oracle_tables(z, i, m0, sel)
         rms = float(np.sqrt(np.mean(z["samples"][sel] ** 2)))
-        compare_block(rep, out[i], sem, stk, params, rms)
+        compare_block(rep, out[i][:, sidx], sem, stk, params, rms)
     rep.check()
     # traveltime arithmetic pinned to the reference's (CMP, ZO-CRS and the
     # OCT displaced midpoint and time): bit-identical results

@@ -116,22 +116,38 @@ def test_de_zocrs_small_line(engine):
 
 
 def test_de_oct_selection_from_initial_population(engine):
+    """OCT DE selects a trace if any sample's initial individual reaches it
+    (oct/differential_evolution.cu selectTraces...): the engine's count per
+    midpoint equals the oracle's on the same initial population.  The device
+    forms c = 4/v^2 with the fast-math division, so a trace whose test sits
+    within rounding of the aperture may flip: a midpoint is well-conditioned
+    when the oracle's count is unchanged with every velocity moved by
+    +-5e-7 (c by ~1e-6, well above the division's error); those must match
+    exactly, the others within one trace."""
     line = synthetic.structured_line(n_cmp=10, fold_range=(4, 8), h_max=800, ns=120,
                                      dt_us=4000, n_reflectors=3, f=20.0, snr=8.0, seed=51)
     lower, upper = [1200.0, -1e-3], [5000.0, 1e-3]
     apm, h0, seed, pop = 50.0, 300.0, 9, 8
     _setup(engine, line, "oct", lower, upper, apm=apm, h0=h0)
-    m0s = line.cdp_midpoints[3:6]
-    de, st = engine.differential_evolution(m0s, pop, 3, 0.5, 0.9, seed=seed)
     S = line.samples_per_trace
-    want = 0
-    for i, m0 in enumerate(m0s):
-        init = oracle.de_initial_population(seed, i, S, pop, lower, upper)
-        want += int(oracle.select_oct_per_sample(line.midpoints, line.halfoffsets, m0, apm, h0,
-                                                 S, float(line.dt), init).sum())
-    # c = 4/v^2 uses the device's fast division: a boundary trace may flip
-    assert abs(st["selected_traces"] - want) <= 1
-    assert np.all(np.isfinite(de))
+    exact = 0
+    for m0 in line.cdp_midpoints[2:8]:
+        de, st = engine.differential_evolution([m0], pop, 3, 0.5, 0.9, seed=seed)
+        assert np.all(np.isfinite(de))
+        init = oracle.de_initial_population(seed, 0, S, pop, lower, upper)
+        counts = []
+        for f in (1.0, 1.0 - 5e-7, 1.0 + 5e-7):
+            pert = init.copy()
+            pert[..., 0] = (pert[..., 0].astype(np.float64) * f).astype(np.float32)
+            counts.append(int(oracle.select_oct_per_sample(
+                line.midpoints, line.halfoffsets, m0, apm, h0, S, float(line.dt),
+                pert).sum()))
+        if len(set(counts)) == 1:
+            assert st["selected_traces"] == counts[0], m0
+            exact += 1
+        else:
+            assert abs(st["selected_traces"] - counts[0]) <= 1, m0
+    assert exact >= 4
 
 
 def test_de_multi_wave_call_maps_units_to_midpoints(engine):

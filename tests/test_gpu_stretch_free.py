@@ -35,18 +35,27 @@ def _check_sf(out, sem, stk, nmax, near_tie=1e-4):
     assert far <= 0.002 * S, far
 
 
-def test_cmp_stretch_free_matches_reference_kernels(engine):
-    z = np.load(GOLDEN / "ref_cmp.npz")
+SF_FIXTURES = sorted(p.stem[4:] for p in GOLDEN.glob("ref_*.npz")
+                     if "sf_results" in np.load(p).files)
+
+
+@pytest.mark.parametrize("name", SF_FIXTURES)
+def test_cmp_stretch_free_matches_reference_kernels(engine, name):
+    """The reference's CMP stretch-free kernels on its own linear-search
+    velocities (window 5 on the small line; window 9 on the production-line
+    slice, whose search ran with window 7)."""
+    from test_golden import load
+    z = load(name)
     engine.upload_gather(z["samples"], z["midpoints"], z["halfoffsets"], float(z["dt"]))
     engine.set_traveltime("cmp", z["lower"], z["upper"])
-    engine.set_window(int(z["tau"]))
+    engine.set_window(int(z["sf_tau"]) if "sf_tau" in z else int(z["tau"]))
     sf = z["sf_results"]
     m0s = z["m0s"][: sf.shape[0]]
     prior = z["results"][: sf.shape[0], 2:3]        # reference LS velocities [nM0][1][S]
     out, st = engine.stretch_free(m0s, prior, 10)
     assert st["evals"] == float(np.sum(z["counts"][: sf.shape[0]])) * sf.shape[2] * 21
     exact = float(np.mean(np.all(out == sf, axis=1)))
-    print(f"stretch-free cmp: bit-identical samples {exact:.6f}")
+    print(f"stretch-free {name}: bit-identical samples {exact:.6f}")
     assert exact == 1.0
 
 

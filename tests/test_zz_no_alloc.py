@@ -6,9 +6,10 @@ pass their own device buffers; the library's scratch is a fixed __device__
 array.  This test (collected last on purpose) calls the entry point through
 the C ABI twice in a row and checks both results against the allocating entry
 point's (hpss_linear_search) -- same kernels, so the tolerance is equality,
-stricter than the parity tolerances of tests/parity.py.  It allocates its own
-buffers with torch; the entry point allocates nothing.  It passes alone in a
-fresh process and after the other tests.
+stricter than the parity tolerances of tests/parity.py -- and reads the
+kernels' device error word back with hpss_noalloc_device_error after each.
+It allocates its own buffers with torch; the entry point allocates nothing.
+It passes alone in a fresh process and after the other tests.
 """
 import ctypes as C
 
@@ -73,6 +74,10 @@ def test_noalloc_matches_allocating_entry_point_twice(model):
             C.c_float(apm), C.c_void_p(d_m0.data_ptr()), m0s.size, C.c_void_p(d_out.data_ptr()),
             None)
         assert rc == 0, lib.hpss_last_error(None)
+        # the kernels' error word (cleared by every call) reads back as 0
+        word = C.c_uint32(0xffffffff)
+        assert lib.hpss_noalloc_device_error(None, C.byref(word)) == 0
+        assert word.value == 0, f"call {call}: device error word {word.value}"
         torch.cuda.synchronize()
         got = d_out.cpu().numpy()
         assert np.array_equal(got, want), f"call {call}"
