@@ -31,7 +31,8 @@ N_PARAMS = {"cmp": 1, "zocrs": 3, "oct": 2}
 EXPORTED = [
     "hpss_create", "hpss_destroy", "hpss_last_error", "hpss_version",
     "hpss_device_count", "hpss_upload_gather", "hpss_set_traveltime",
-    "hpss_set_window", "hpss_set_grid_mode", "hpss_set_precision", "hpss_linear_search",
+    "hpss_set_window", "hpss_set_grid_mode", "hpss_set_precision", "hpss_set_oct_half_offsets",
+    "hpss_linear_search",
     "hpss_linear_search_device",
     "hpss_differential_evolution", "hpss_differential_evolution_device",
     "hpss_stretch_free", "hpss_select_traces", "hpss_stream", "hpss_device_bytes",
@@ -74,6 +75,7 @@ def load_library(path: Optional[Path] = None) -> C.CDLL:
         "hpss_set_window": (i32, [vp, i32]),
         "hpss_set_grid_mode": (i32, [vp, i32]),
         "hpss_set_precision": (i32, [vp, i32]),
+        "hpss_set_oct_half_offsets": (i32, [vp, fp, u32]),
         "hpss_linear_search": (i32, [vp, fp, u32, up, i32, fp, C.POINTER(Stats)]),
         "hpss_linear_search_device": (i32, [vp, vp, u32, up, i32, vp, C.POINTER(Stats)]),
         "hpss_linear_search_line": (i32, [vp, fp, fp, fp, u32, u32, f32, i32, fp, u32, up, i32,
@@ -130,6 +132,7 @@ class Engine:
         self.model = None
         self.S = 0
         self.np = 0
+        self.n_h0 = 0  # OCT target half-offsets of set_oct_half_offsets (0: one h0)
 
     def close(self):
         if self.h:
@@ -179,6 +182,18 @@ class Engine:
         self.model = model
         self.np = N_PARAMS[model]
 
+    def set_oct_half_offsets(self, h0s: Sequence[float]):
+        """OCT over several target half-offsets per call: results come back
+        as [len(h0s) * nM0][...] blocks, h0-major; [] restores the single h0
+        of set_traveltime."""
+        a = np.ascontiguousarray(h0s, np.float32)
+        self._check(self._lib.hpss_set_oct_half_offsets(self.h, _fptr(a) if a.size else None,
+                                                         a.size))
+        self.n_h0 = int(a.size)
+
+    def _blocks(self) -> int:
+        return self.n_h0 if (self.model == "oct" and self.n_h0) else 1
+
     def set_window(self, tau_index: int):
         self._check(self._lib.hpss_set_window(self.h, int(tau_index)))
 
@@ -198,7 +213,7 @@ class Engine:
                       ) -> Tuple[np.ndarray, dict]:
         m0s = np.ascontiguousarray(m0s, dtype=np.float32)
         g = np.asarray(granularity, np.uint32)
-        out = np.zeros((m0s.size, 2 + self.np, self.S), np.float32)
+        out = np.zeros((m0s.size * self._blocks(), 2 + self.np, self.S), np.float32)
         st = Stats()
         self._check(self._lib.hpss_linear_search(self.h, _fptr(m0s), m0s.size, _uptr(g),
                                                   KERNELS[kernel], _fptr(out), C.byref(st)))
@@ -244,7 +259,7 @@ class Engine:
     def differential_evolution(self, m0s, population: int, generations: int, F: float,
                                CR: float, seed: int) -> Tuple[np.ndarray, dict]:
         m0s = np.ascontiguousarray(m0s, dtype=np.float32)
-        out = np.zeros((m0s.size, 2 + self.np, self.S), np.float32)
+        out = np.zeros((m0s.size * self._blocks(), 2 + self.np, self.S), np.float32)
         st = Stats()
         self._check(self._lib.hpss_differential_evolution(
             self.h, _fptr(m0s), m0s.size, population, generations, C.c_float(F),
@@ -255,7 +270,9 @@ class Engine:
                      ) -> Tuple[np.ndarray, dict]:
         m0s = np.ascontiguousarray(m0s, dtype=np.float32)
         params = np.ascontiguousarray(params, dtype=np.float32)
-        out = np.zeros((m0s.size, 3, self.S), np.float32)
+        if params.size != m0s.size * self._blocks() * self.np * self.S:
+            raise ValueError("params must hold [blocks * nM0][nParams][S] values")
+        out = np.zeros((m0s.size * self._blocks(), 3, self.S), np.float32)
         st = Stats()
         self._check(self._lib.hpss_stretch_free(self.h, _fptr(m0s), m0s.size, _fptr(params),
                                                  nmax, _fptr(out), C.byref(st)))
@@ -263,6 +280,6 @@ class Engine:
 
     def select_traces(self, m0s) -> np.ndarray:
         m0s = np.ascontiguousarray(m0s, dtype=np.float32)
-        counts = np.zeros(m0s.size, np.uint32)
+        counts = np.zeros(m0s.size * self._blocks(), np.uint32)
         self._check(self._lib.hpss_select_traces(self.h, _fptr(m0s), m0s.size, _uptr(counts)))
         return counts

@@ -112,10 +112,10 @@ constexpr int kDeThreadsMax = 256;
 // displaced-midpoint box and the tests over blocks of 32 traces are
 // collectives); lanes with ev false take part in those only.
 template <int MODEL, int W>
-__device__ __forceinline__ void de_eval(const DeParams &d, float t0, float m0, uint32_t first,
-                                        uint32_t cnt, const float *x, float *sembl,
-                                        float *stack, unsigned *notUsed, bool ev = true,
-                                        bool boxMode = false) {
+__device__ __forceinline__ void de_eval(const DeParams &d, const OctLine &ol, float t0,
+                                        float m0, uint32_t first, uint32_t cnt, const float *x,
+                                        float *sembl, float *stack, unsigned *notUsed,
+                                        bool ev = true, bool boxMode = false) {
     const LsParams &a = d.ls;
     const float v = x[0];
     const float c = 4.0f / (v * v);
@@ -171,12 +171,24 @@ __device__ __forceinline__ void de_eval(const DeParams &d, float t0, float m0, u
             const bool ina = oka && window_in_trace(ka, a.tau, (int)a.S);
             const bool inb = okb && window_in_trace(kb, a.tau, (int)a.S);
             float ya[W > 0 ? W + 1 : 1], yb[W > 0 ? W + 1 : 1];
-            const float *tra = a.samples + (size_t)ti0 * a.stride + (ina ? ka - a.tau : 0);
-            const float *trb = a.samples + (size_t)ti1 * a.stride + (inb ? kb - a.tau : 0);
+            if (a.samples16) {
+                // 16-bit storage: out-of-trace windows read sample 0 and are
+                // zeroed, as the FP32 form's
+                load_window(a, ti0, ina ? ka - a.tau : 0, ya);
+                load_window(a, ti1, inb ? kb - a.tau : 0, yb);
 #pragma unroll
-            for (int j = 0; j <= W; j++) {
-                ya[j] = ina ? __ldg(tra + j) : 0.f;
-                yb[j] = inb ? __ldg(trb + j) : 0.f;
+                for (int j = 0; j <= W; j++) {
+                    ya[j] = ina ? ya[j] : 0.f;
+                    yb[j] = inb ? yb[j] : 0.f;
+                }
+            } else {
+                const float *tra = a.samples + (size_t)ti0 * a.stride + (ina ? ka - a.tau : 0);
+                const float *trb = a.samples + (size_t)ti1 * a.stride + (inb ? kb - a.tau : 0);
+#pragma unroll
+                for (int j = 0; j <= W; j++) {
+                    ya[j] = ina ? __ldg(tra + j) : 0.f;
+                    yb[j] = inb ? __ldg(trb + j) : 0.f;
+                }
             }
             // window terms of both traces: (y1 - y0) * frac + y0 per lane
             float2 u2[W > 0 ? W : 1];
@@ -210,13 +222,13 @@ __device__ __forceinline__ void de_eval(const DeParams &d, float t0, float m0, u
         }
     }
     // OCT: (t0, candidate) factors once, trace factors from the line's table
-    const OctCand kc = oct_cand(t0, c, p1, MODEL == kModelOct ? a.h0 : 0.f);
+    const OctCand kc = oct_cand(t0, c, p1, MODEL == kModelOct ? ol.h0 : 0.f);
     if constexpr (MODEL == kModelOct && W > 0) {
       __shared__ float deBox[kDeThreadsMax / 32][4];  // each warp's displaced-midpoint box
       volatile float *boxSlot = deBox[threadIdx.x >> 5];
       bool boxOn = false;
       if (boxMode) {
-          const OctWarpBox box = oct_warp_box(a.octBox, ev, t0, p1, kc, a.h0);
+          const OctWarpBox box = oct_warp_box(a.octBox, ev, t0, p1, kc, ol.h0);
           boxOn = box.on;
           if (boxOn) oct_box_store(boxSlot, box);
       }
@@ -229,7 +241,7 @@ __device__ __forceinline__ void de_eval(const DeParams &d, float t0, float m0, u
             bool keep = false;
             if ((uint32_t)lane < n) {
                 const uint32_t ti = a.selIdx ? a.selIdx[first + qb + lane] : first + qb + lane;
-                keep = oct_box_keep(a, ti, boxSlot, m0);
+                keep = oct_box_keep(a, ol, ti, boxSlot, m0);
             }
             uint32_t mask = __ballot_sync(0xffffffffu, keep);
             if (ev) nu += n - (uint32_t)__popc(mask);
@@ -245,7 +257,7 @@ __device__ __forceinline__ void de_eval(const DeParams &d, float t0, float m0, u
                     tb[b] = a.selIdx ? a.selIdx[first + qb + bit] : first + qb + bit;
                 }
                 if (ev)
-                    oct_eval_batch<W, kDeOctBatch>(a, tb, live, kc, c, p1, t0, m0, num,
+                    oct_eval_batch<W, kDeOctBatch>(a, ol, tb, live, kc, c, p1, t0, m0, num,
                                                                lin, den, used, nu);
             }
         }
@@ -263,7 +275,7 @@ __device__ __forceinline__ void de_eval(const DeParams &d, float t0, float m0, u
                 tb[b] = a.selIdx ? a.selIdx[first + q + b] : first + q + b;
                 live[b] = true;
             }
-            oct_eval_batch<W, kDeOctBatch>(a, tb, live, kc, c, p1, t0, m0, num, lin,
+            oct_eval_batch<W, kDeOctBatch>(a, ol, tb, live, kc, c, p1, t0, m0, num, lin,
                                                        den, used, nu);
         }
       }
@@ -273,9 +285,9 @@ __device__ __forceinline__ void de_eval(const DeParams &d, float t0, float m0, u
         float t;
         int ok;
         if (MODEL == kModelOct) {
-            const float4 tf = __ldg(a.octTab + ti);  // {m, gamma^2, 16h^2h0^2, h^2-h0^2}
+            const float4 tf = __ldg(ol.tab + ti);  // {m, gamma^2, 16h^2h0^2, h^2-h0^2}
             ok = oct_model_time(kc, tf.y, tf.z, tf.w, t0, c, p1, tf.x, a.hoff[ti], m0, a.apm,
-                                a.h0, &t);
+                                ol.h0, &t);
         } else {
             ok = model_time<MODEL>(t0, c, p1, p2, a.mid[ti], a.hoff[ti], a.hsq[ti], m0, a.apm,
                                    a.h0, &t);
@@ -287,13 +299,13 @@ __device__ __forceinline__ void de_eval(const DeParams &d, float t0, float m0, u
         if (ok == 0) continue;
         WinIdx wi = window_index(t, a.dt);
         if (window_in_trace(wi.k, a.tau, (int)a.S)) {
-            const float *tr = a.samples + (size_t)ti * a.stride + (wi.k - a.tau);
-            float y1 = __ldg(tr);
+            const int k0 = wi.k - a.tau;
+            float y1 = amp_at(a, ti, k0);
 #pragma unroll
             for (int j = 0; j < (W > 0 ? W : kMaxWindow); j++) {
                 if (W == 0 && j >= w) break;
                 float y0 = y1;
-                y1 = __ldg(tr + j + 1);
+                y1 = amp_at(a, ti, k0 + j + 1);
                 float u = (y1 - y0) * wi.frac + y0;
                 num[j] += u;
                 lin += u;
@@ -349,8 +361,9 @@ de_kernel(DeParams d, uint32_t spc, uint32_t groups, uint32_t nUnits) {
     // the fitness goes back to its owner through shared memory.  Every
     // trial's fitness is computed exactly as by its owner.  Called by all
     // threads of the CTA.
-    auto evalSorted = [&](const float *trial, bool active, float s0f, float m0, uint32_t first,
-                          uint32_t cnt, float *f, float *fk, unsigned *notUsed) {
+    auto evalSorted = [&](const float *trial, bool active, float s0f, float m0,
+                          const OctLine &ol, uint32_t first, uint32_t cnt, float *f, float *fk,
+                          unsigned *notUsed) {
 #pragma unroll
         for (int j = 0; j < NP; j++) TR[threadIdx.x * NP + j] = trial[j];
         const float key = active ? trial[NP - 1] : __int_as_float(0x7f800000);  // slope; +inf
@@ -370,7 +383,8 @@ de_kernel(DeParams d, uint32_t spc, uint32_t groups, uint32_t nUnits) {
         const bool boxMode = MODEL == kModelOct && W > 0 && a.octBox;
         if (boxMode || ev) {
             float fo, fko;
-            de_eval<MODEL, W>(d, t0o, m0, first, cnt, TR + o * NP, &fo, &fko, notUsed, ev, boxMode);
+            de_eval<MODEL, W>(d, ol, t0o, m0, first, cnt, TR + o * NP, &fo, &fko, notUsed, ev,
+                              boxMode);
             if (ev) {
                 RES[2 * o] = fo;
                 RES[2 * o + 1] = fko;
@@ -396,6 +410,8 @@ de_kernel(DeParams d, uint32_t spc, uint32_t groups, uint32_t nUnits) {
         const bool active = member && s < a.S;
         const float m0 = a.m0s[mi];
         const uint32_t first = a.selFirst[mi], cnt = a.selCount[mi];
+        const OctLine ol = oct_line(a, mi);          // OCT: the midpoint's h0 and table
+        const uint32_t mkey = m0_in_block(a, mi);    // random-stream key of the midpoint
         const float t0 = static_cast<float>(active ? s : 0) * a.dt;
         const float s0f = static_cast<float>((unit % groups) * spc);  // the CTA's first sample
         float *xs = X + (size_t)(member ? ls : 0) * pop * NP;  // this sample's population
@@ -405,7 +421,7 @@ de_kernel(DeParams d, uint32_t spc, uint32_t groups, uint32_t nUnits) {
         if (threadIdx.x == 0) nuCta = 0;
         // ---- initial population and its fitness (generation 1)
         if (active) {
-            Draws rng(d.seedLo, d.seedHi, mi, s, ind, 0);
+            Draws rng(d.seedLo, d.seedHi, mkey, s, ind, 0);
 #pragma unroll
             for (int j = 0; j < NP; j++) {
                 // min + ratio * (max - min) as one fused multiply-add, as the
@@ -413,13 +429,14 @@ de_kernel(DeParams d, uint32_t spc, uint32_t groups, uint32_t nUnits) {
                 x[j] = __fmaf_rn(rng.next(), __fsub_rn(d.hi[j], d.lo[j]), d.lo[j]);
                 xs[ind * NP + j] = x[j];
             }
-            if (MODEL != kModelOct) de_eval<MODEL, W>(d, t0, m0, first, cnt, x, &fx, &fxk, &notUsed);
+            if (MODEL != kModelOct)
+                de_eval<MODEL, W>(d, ol, t0, m0, first, cnt, x, &fx, &fxk, &notUsed);
         } else {
 #pragma unroll
             for (int j = 0; j < NP; j++) x[j] = d.lo[j];
         }
         if (MODEL == kModelOct) {
-            evalSorted(x, active, s0f, m0, first, cnt, &fx, &fxk, &notUsed);
+            evalSorted(x, active, s0f, m0, ol, first, cnt, &fx, &fxk, &notUsed);
             if (!active) fx = -1.f;
         }
         // ---- generations 2 .. G
@@ -429,7 +446,7 @@ de_kernel(DeParams d, uint32_t spc, uint32_t groups, uint32_t nUnits) {
 #pragma unroll
             for (int j = 0; j < NP; j++) u[j] = x[j];
             if (active) {
-                Draws rng(d.seedLo, d.seedHi, mi, s, ind, gen);
+                Draws rng(d.seedLo, d.seedHi, mkey, s, ind, gen);
                 float v[NP];
 #pragma unroll
                 for (int j = 0; j < NP; j++) {
@@ -452,9 +469,11 @@ de_kernel(DeParams d, uint32_t spc, uint32_t groups, uint32_t nUnits) {
             }
             __syncthreads();  // every donor read before any replacement
             float fu = -1.f, fuk = 0.f;
-            if (MODEL == kModelOct) evalSorted(u, active, s0f, m0, first, cnt, &fu, &fuk, &notUsed);
+            if (MODEL == kModelOct)
+                evalSorted(u, active, s0f, m0, ol, first, cnt, &fu, &fuk, &notUsed);
             if (active) {
-                if (MODEL != kModelOct) de_eval<MODEL, W>(d, t0, m0, first, cnt, u, &fu, &fuk, &notUsed);
+                if (MODEL != kModelOct)
+                    de_eval<MODEL, W>(d, ol, t0, m0, first, cnt, u, &fu, &fuk, &notUsed);
                 if (fu > fx) {
 #pragma unroll
                     for (int j = 0; j < NP; j++) {
@@ -522,6 +541,8 @@ __global__ void de_select_oct_flags_kernel(DeParams d, const uint32_t *candFirst
     const uint32_t mi = lo;
     const uint32_t ti = candFirst[mi] + (uint32_t)(g - a.selFirst[mi]);
     const float m0 = a.m0s[mi];
+    const float h0 = oct_line(a, mi).h0;
+    const uint32_t mkey = m0_in_block(a, mi);
     const float m = a.mid[ti], h = a.hoff[ti];
     bool used = false;
     for (uint32_t s = 0; s < a.S && !used; s++) {
@@ -530,12 +551,12 @@ __global__ void de_select_oct_flags_kernel(DeParams d, const uint32_t *candFirst
             const uint32_t ind = i0 + lane;
             bool hit = false;
             if (ind < d.pop) {
-                Draws rng(d.seedLo, d.seedHi, mi, s, ind, 0);
+                Draws rng(d.seedLo, d.seedHi, mkey, s, ind, 0);
                 const float v = __fmaf_rn(rng.next(), __fsub_rn(d.hi[0], d.lo[0]), d.lo[0]);
                 const float sl = __fmaf_rn(rng.next(), __fsub_rn(d.hi[1], d.lo[1]), d.lo[1]);
                 const float c = 4.0f / (v * v);
                 float mh;
-                const int e = oct_displaced_midpoint(h, a.h0, t0, m0, c, sl, &mh);
+                const int e = oct_displaced_midpoint(h, h0, t0, m0, c, sl, &mh);
                 hit = (e == DE_OK && fabsf(m - mh) <= a.apm);
             }
             used = __any_sync(0xffffffffu, hit);

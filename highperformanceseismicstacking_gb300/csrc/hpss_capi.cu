@@ -147,9 +147,10 @@ void build_oct_selection_candidates(hpss_handle h) {
 // more is rejected); selIdx is grown to the total.
 hpss_status oct_candidate_slots(hpss_handle h, const float *d_m0s, uint32_t nM0,
                                 uint32_t *first, uint64_t *total) {
-    float hmax = 0.f;
+    float hmax = 0.f, h0max = std::fabs(h->h0);
     for (float v : h->hHoff) hmax = std::max(hmax, std::fabs(v));
-    float radius = (h->apm + std::sqrt(hmax * hmax + h->h0 * h->h0)) * 1.001f + 1.0f;
+    for (float v : h->octH0s) h0max = std::max(h0max, std::fabs(v));
+    float radius = (h->apm + std::sqrt(hmax * hmax + h0max * h0max)) * 1.001f + 1.0f;
     HPSS_CUDA_TRY(h, ensure(h, h->candFirst, nM0 * sizeof(uint32_t)));
     HPSS_CUDA_TRY(h, ensure(h, h->candCount, nM0 * sizeof(uint32_t)));
     uint32_t *cf = static_cast<uint32_t *>(h->candFirst.p);
@@ -211,9 +212,10 @@ hpss_status run_selection(hpss_handle h, const float *d_m0s, uint32_t nM0,
 
 void fill_line_params(hpss_handle h, LsParams &lp) {
     lp = LsParams{};
-    lp.samples = h->dSamples;
-    // 16-bit copies are read only by the tuned pair kernel's staging; every
-    // other kernel reads the FP32 line
+    // the line is resident in one storage only: FP32 rows, or 16-bit rows
+    // (every kernel widens them as it reads; dSamples is then only the
+    // upload's FP32 staging area)
+    lp.samples = h->storage == HPSS_STORAGE_FP32 ? h->dSamples : nullptr;
     lp.samples16 = h->storage != HPSS_STORAGE_FP32 ? h->dSamples16 : nullptr;
     lp.scale = h->storage != HPSS_STORAGE_FP32 ? h->dScale : nullptr;
     lp.storage = h->storage;
@@ -230,22 +232,28 @@ void fill_line_params(hpss_handle h, LsParams &lp) {
     lp.h0 = h->h0;
 }
 
-// OCT: the per-trace factor table of the resident line for the current h0,
-// built on the handle's stream at the first OCT call after an upload or an
-// h0 change.
+// OCT: the per-trace factor tables of the resident line -- one for the
+// current h0, or one per target half-offset of hpss_set_oct_half_offsets,
+// octTabStride entries apart -- built on the handle's stream at the first OCT
+// call after an upload or a change of the half-offsets.
 cudaError_t use_oct_table(hpss_handle h, LsParams &lp) {
     if (h->model != HPSS_MODEL_OCT) return cudaSuccess;
-    if (!h->octTabValid || h->octTabH0 != h->h0) {
+    const std::vector<float> want = h->octH0s.empty() ? std::vector<float>{h->h0} : h->octH0s;
+    if (!h->octTabValid || h->octTabH0s != want) {
         h->octTabValid = false;
-        cudaError_t e = ensure(h, h->octTab, (size_t)h->nTraces * sizeof(float4));
+        cudaError_t e = ensure(h, h->octTab, want.size() * (size_t)h->nTraces * sizeof(float4));
         if (e != cudaSuccess) return e;
-        e = launch_oct_trace_table(h->dMid, h->dHoff, h->nTraces, h->h0,
-                                   static_cast<float4 *>(h->octTab.p), h->stream);
-        if (e != cudaSuccess) return e;
+        for (size_t b = 0; b < want.size(); b++) {
+            e = launch_oct_trace_table(h->dMid, h->dHoff, h->nTraces, want[b],
+                                       static_cast<float4 *>(h->octTab.p) + b * h->nTraces,
+                                       h->stream);
+            if (e != cudaSuccess) return e;
+        }
         h->octTabValid = true;
-        h->octTabH0 = h->h0;
+        h->octTabH0s = want;
     }
     lp.octTab = static_cast<const float4 *>(h->octTab.p);
+    lp.octTabStride = h->nTraces;
     // HPSS_OCT_BOX_TEST=0 turns the displaced-midpoint box test off (every
     // trace through the per-sample test; same results, for A/B checks)
     const char *box = std::getenv("HPSS_OCT_BOX_TEST");
@@ -253,10 +261,39 @@ cudaError_t use_oct_table(hpss_handle h, LsParams &lp) {
     return cudaSuccess;
 }
 
+uint32_t h0_blocks(hpss_handle h) {
+    return h->model == HPSS_MODEL_OCT && !h->octH0s.empty() ? (uint32_t)h->octH0s.size() : 1u;
+}
+
+cudaError_t expand_h0_blocks(hpss_handle h, LsParams &lp) {
+    const uint32_t nb = h0_blocks(h);
+    if (nb == 1 || lp.nM0 == 0) return cudaSuccess;
+    const uint32_t n = lp.nM0;
+    cudaError_t e = ensure(h, h->m0v, (size_t)nb * n * sizeof(float));
+    if (e != cudaSuccess) return e;
+    float *dst = static_cast<float *>(h->m0v.p);
+    for (uint32_t b = 0; b < nb; b++) {
+        e = cudaMemcpyAsync(dst + (size_t)b * n, lp.m0s, n * sizeof(float),
+                            cudaMemcpyDeviceToDevice, h->stream);
+        if (e != cudaSuccess) return e;
+    }
+    lp.m0s = dst;
+    lp.nM0 = nb * n;
+    lp.m0PerH0 = n;
+    lp.h0s = static_cast<const float *>(h->octH0sDev.p);
+    return cudaSuccess;
+}
+
 int num_sms(hpss_handle h) {
     int v = 0;
     cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, h->device);
     return v > 0 ? v : 1;
+}
+
+// Rows of the FP32 staging area of a 16-bit upload (about 64 MB).
+size_t stage_rows(hpss_handle h) {
+    constexpr size_t kStageBytes = size_t(64) << 20;
+    return std::max<size_t>(1, kStageBytes / ((size_t)h->stride * sizeof(float)));
 }
 
 // A new line, everything but the amplitudes: validation, host geometry,
@@ -309,11 +346,18 @@ hpss_status prepare_line(hpss_handle h, const float *samples, const float *midpo
     h->hHsq.resize(nTraces);
     for (uint32_t i = 0; i < nTraces; i++) h->hHsq[i] = halfoffsets[i] * halfoffsets[i];
     const size_t n = nTraces, st = h->stride;
-    HPSS_CUDA_TRY(h, grow_line_buffer(h, reinterpret_cast<void **>(&h->dSamples), h->capSamples,
-                                      n * st * sizeof(float)));
-    if (storage != HPSS_STORAGE_FP32)
+    if (storage == HPSS_STORAGE_FP32) {
+        HPSS_CUDA_TRY(h, grow_line_buffer(h, reinterpret_cast<void **>(&h->dSamples),
+                                          h->capSamples, n * st * sizeof(float)));
+    } else {
+        // 16-bit storage: the line lives in 16-bit rows only; the FP32 rows
+        // pass through a staging area of at most kStageBytes on their way
         HPSS_CUDA_TRY(h, grow_line_buffer(h, reinterpret_cast<void **>(&h->dSamples16),
                                           h->capSamples16, n * st * sizeof(uint16_t)));
+        HPSS_CUDA_TRY(h, grow_line_buffer(h, reinterpret_cast<void **>(&h->dSamples),
+                                          h->capSamples,
+                                          std::min<size_t>(n, stage_rows(h)) * st * sizeof(float)));
+    }
     // mid, hoff, hsq and the 16-bit storage scale: four 256-byte aligned
     // slices of one buffer
     const size_t slice = (n * sizeof(float) + 255) & ~size_t(255);
@@ -334,23 +378,35 @@ hpss_status prepare_line(hpss_handle h, const float *samples, const float *midpo
     return HPSS_OK;
 }
 
-// Amplitudes of traces [a, b) on stream st: one copy when rows need no
-// padding, a pitched copy otherwise (the padding is zeroed by the caller),
-// then the 16-bit copy of those rows when the storage asks for one.
+// Amplitudes of traces [a, b) on stream st.  FP32 storage: one copy into
+// the line when rows need no padding, a pitched copy otherwise (the padding
+// is zeroed by the caller).  16-bit storage: pieces of at most stage_rows
+// rows are copied into the staging area and converted into the 16-bit line
+// (stream order keeps a piece's conversion before the next piece's copy; the
+// converter writes the rows' zero padding itself).
 cudaError_t copy_line_rows(hpss_handle h, const float *samples, uint32_t a, uint32_t b,
                            cudaStream_t st) {
     if (b <= a) return cudaSuccess;
-    const size_t S = h->S, pitch = h->stride, rows = b - a;
-    float *dst = h->dSamples + (size_t)a * pitch;
-    const float *src = samples + (size_t)a * S;
-    cudaError_t e = pitch == S
-                        ? cudaMemcpyAsync(dst, src, rows * S * sizeof(float),
-                                          cudaMemcpyHostToDevice, st)
-                        : cudaMemcpy2DAsync(dst, pitch * sizeof(float), src, S * sizeof(float),
-                                            S * sizeof(float), rows, cudaMemcpyHostToDevice, st);
-    if (e != cudaSuccess || h->storage == HPSS_STORAGE_FP32) return e;
-    return launch_convert_storage(dst, h->dSamples16 + (size_t)a * pitch, h->dScale + a,
-                                  (uint32_t)rows, h->S, h->stride, h->storage, st);
+    const size_t S = h->S, pitch = h->stride;
+    auto copyRows = [&](float *dst, uint32_t r0, size_t rows) {
+        const float *src = samples + (size_t)r0 * S;
+        return pitch == S ? cudaMemcpyAsync(dst, src, rows * S * sizeof(float),
+                                            cudaMemcpyHostToDevice, st)
+                          : cudaMemcpy2DAsync(dst, pitch * sizeof(float), src, S * sizeof(float),
+                                              S * sizeof(float), rows, cudaMemcpyHostToDevice,
+                                              st);
+    };
+    if (h->storage == HPSS_STORAGE_FP32) return copyRows(h->dSamples + (size_t)a * pitch, a, b - a);
+    const uint32_t piece = (uint32_t)stage_rows(h);
+    for (uint32_t r = a; r < b; r += piece) {
+        const uint32_t rows = std::min(piece, b - r);
+        cudaError_t e = copyRows(h->dSamples, r, rows);
+        if (e == cudaSuccess)
+            e = launch_convert_storage(h->dSamples, h->dSamples16 + (size_t)r * pitch,
+                                       h->dScale + r, rows, h->S, h->stride, h->storage, st);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
 // error message of a handle-less call, read back with hpss_last_error(NULL)
@@ -408,7 +464,8 @@ hpss_status hpss_destroy(hpss_handle h) {
     free_gather(h);
     for (auto *b : {&h->params, &h->chunkBounds, &h->selFirst, &h->selCount, &h->selIdx,
                     &h->candFirst, &h->candCount, &h->notUsed, &h->errWord, &h->m0s,
-                    &h->out, &h->octCands, &h->prior, &h->partial, &h->octTab, &h->order})
+                    &h->out, &h->octCands, &h->prior, &h->partial, &h->octTab, &h->order,
+                    &h->octH0sDev, &h->m0v})
         release(h, *b);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
@@ -437,7 +494,7 @@ hpss_status hpss_upload_gather(hpss_handle h, const float *samples,
     hpss_status rc = prepare_line(h, samples, midpoints, halfoffsets, nTraces, samplesPerTrace,
                                   dtInSeconds, storage);
     if (rc != HPSS_OK) return rc;
-    if (nTraces && h->stride != h->S)
+    if (nTraces && h->stride != h->S && storage == HPSS_STORAGE_FP32)
         HPSS_CUDA_TRY(h, cudaMemsetAsync(h->dSamples, 0,
                                          (size_t)nTraces * h->stride * sizeof(float), h->stream));
     HPSS_CUDA_TRY(h, copy_line_rows(h, samples, 0, nTraces, h->stream));
@@ -484,6 +541,27 @@ hpss_status hpss_set_precision(hpss_handle h, int flags) {
     return HPSS_OK;
 }
 
+hpss_status hpss_set_oct_half_offsets(hpss_handle h, const float *h0s, uint32_t nH0) {
+    if (!h) return HPSS_ERR_INVALID_ARGUMENT;
+    if (nH0 > kMaxOctHalfOffsets)
+        return set_error(h, HPSS_ERR_INVALID_ARGUMENT,
+                         "at most " + std::to_string(kMaxOctHalfOffsets) + " half-offsets");
+    if (nH0 && !h0s) return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "null half-offset array");
+    for (uint32_t b = 0; b < nH0; b++)
+        if (!std::isfinite(h0s[b]))
+            return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "half-offsets must be finite");
+    cudaSetDevice(h->device);
+    // earlier calls may still read the device copy
+    HPSS_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    if (nH0) {
+        HPSS_CUDA_TRY(h, ensure(h, h->octH0sDev, nH0 * sizeof(float)));
+        HPSS_CUDA_TRY(h, cudaMemcpy(h->octH0sDev.p, h0s, nH0 * sizeof(float),
+                                    cudaMemcpyHostToDevice));
+    }
+    h->octH0s.assign(h0s, h0s + nH0);
+    return HPSS_OK;
+}
+
 hpss_status hpss_set_grid_mode(hpss_handle h, int mode) {
     if (!h) return HPSS_ERR_INVALID_ARGUMENT;
     if (mode != HPSS_GRID_REFERENCE && mode != HPSS_GRID_INCLUSIVE)
@@ -520,7 +598,7 @@ hpss_status hpss_linear_search(hpss_handle h, const float *m0s, uint32_t nM0,
     if (rc != HPSS_OK) return rc;
     if (nM0 == 0) return HPSS_OK;
     cudaSetDevice(h->device);
-    const size_t outElems = (size_t)nM0 * (2 + h->np) * h->S;
+    const size_t outElems = (size_t)nM0 * h0_blocks(h) * (2 + h->np) * h->S;
     HPSS_CUDA_TRY(h, ensure(h, h->m0s, nM0 * sizeof(float)));
     HPSS_CUDA_TRY(h, ensure(h, h->out, outElems * sizeof(float)));
     HPSS_CUDA_TRY(h, cudaMemcpyAsync(h->m0s.p, m0s, nM0 * sizeof(float),
@@ -547,6 +625,10 @@ hpss_status hpss_linear_search_line(hpss_handle h, const float *samples,
         return set_error(h, HPSS_ERR_NOT_READY,
                          "traveltime and window must be set before the line");
     if (!granularity) return set_error(h, HPSS_ERR_LOGIC, "granularity is required");
+    if (h0_blocks(h) > 1)
+        return set_error(h, HPSS_ERR_INVALID_ARGUMENT,
+                         "several OCT half-offsets: upload the line and call "
+                         "hpss_linear_search instead");
     hpss_status rc = prepare_line(h, samples, midpoints, halfoffsets, nTraces, samplesPerTrace,
                                   dtInSeconds, storage);
     if (rc != HPSS_OK) return rc;
@@ -576,9 +658,10 @@ hpss_status hpss_select_traces(hpss_handle h, const float *m0s, uint32_t nM0,
     fill_line_params(h, lp);
     lp.m0s = static_cast<float *>(h->m0s.p);
     lp.nM0 = nM0;
-    hpss_status rc = run_selection(h, static_cast<float *>(h->m0s.p), nM0, lp);
+    HPSS_CUDA_TRY(h, expand_h0_blocks(h, lp));  // counts [nH0][nM0] for an h0 list
+    hpss_status rc = run_selection(h, lp.m0s, lp.nM0, lp);
     if (rc != HPSS_OK) return rc;
-    HPSS_CUDA_TRY(h, cudaMemcpyAsync(counts, lp.selCount, nM0 * sizeof(uint32_t),
+    HPSS_CUDA_TRY(h, cudaMemcpyAsync(counts, lp.selCount, lp.nM0 * sizeof(uint32_t),
                                      cudaMemcpyDeviceToHost, h->stream));
     HPSS_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
     return HPSS_OK;
@@ -603,7 +686,7 @@ hpss_status hpss_differential_evolution(hpss_handle h, const float *m0s, uint32_
     if (rc != HPSS_OK) return rc;
     if (nM0 == 0) return HPSS_OK;
     cudaSetDevice(h->device);
-    const size_t outElems = (size_t)nM0 * (2 + h->np) * h->S;
+    const size_t outElems = (size_t)nM0 * h0_blocks(h) * (2 + h->np) * h->S;
     HPSS_CUDA_TRY(h, ensure(h, h->m0s, nM0 * sizeof(float)));
     HPSS_CUDA_TRY(h, ensure(h, h->out, outElems * sizeof(float)));
     HPSS_CUDA_TRY(h, cudaMemcpyAsync(h->m0s.p, m0s, nM0 * sizeof(float),
@@ -628,8 +711,8 @@ hpss_status hpss_stretch_free(hpss_handle h, const float *m0s, uint32_t nM0,
     if (!m0s || !params || !out)
         return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "null host pointer");
     cudaSetDevice(h->device);
-    const size_t priorElems = (size_t)nM0 * h->np * h->S;
-    const size_t outElems = (size_t)nM0 * 3 * h->S;
+    const size_t priorElems = (size_t)nM0 * h0_blocks(h) * h->np * h->S;
+    const size_t outElems = (size_t)nM0 * h0_blocks(h) * 3 * h->S;
     HPSS_CUDA_TRY(h, ensure(h, h->m0s, nM0 * sizeof(float)));
     HPSS_CUDA_TRY(h, ensure(h, h->out, outElems * sizeof(float)));
     HPSS_CUDA_TRY(h, ensure(h, h->prior, priorElems * sizeof(float)));
@@ -639,9 +722,12 @@ hpss_status hpss_stretch_free(hpss_handle h, const float *m0s, uint32_t nM0,
                                      cudaMemcpyHostToDevice, h->stream));
     LsParams lp;
     fill_line_params(h, lp);
-    const float *d_m0s = static_cast<float *>(h->m0s.p);
-    lp.m0s = d_m0s;
+    lp.m0s = static_cast<float *>(h->m0s.p);
     lp.nM0 = nM0;
+    // several OCT half-offsets: nH0 blocks of the midpoints, one launch
+    HPSS_CUDA_TRY(h, expand_h0_blocks(h, lp));
+    const float *d_m0s = lp.m0s;
+    nM0 = lp.nM0;
     lp.out = static_cast<float *>(h->out.p);
     lp.prior = static_cast<float *>(h->prior.p);
     lp.nmax = nmax;
@@ -667,7 +753,7 @@ hpss_status hpss_stretch_free(hpss_handle h, const float *m0s, uint32_t nM0,
         const uint32_t *cc = static_cast<const uint32_t *>(h->candCount.p);
         lp.selIdx = static_cast<uint32_t *>(h->selIdx.p);
         HPSS_CUDA_TRY(h, launch_sf_select_oct(lp, cf, cc, static_cast<uint32_t *>(h->selIdx.p),
-                                              static_cast<uint32_t *>(h->selCount.p),
+                                              static_cast<uint32_t *>(h->selCount.p), total,
                                               h->stream));
     }
     HPSS_CUDA_TRY(h, cudaEventRecord(h->ev1, h->stream));

@@ -11,6 +11,8 @@
 // index and selected grid index come out bit-identical.
 #pragma once
 
+#include <cuda_fp16.h>
+
 #include <cstdint>
 
 #include "hpss_internal.h"
@@ -397,6 +399,60 @@ __device__ __forceinline__ OctWarpBox oct_warp_box(bool enable, bool member, flo
 // box {aLo, aHi, bLo, bHi} is read from the warp's slot in shared memory
 // (volatile: reloaded at each test instead of held in registers through the
 // trace loop).
+// The OCT half-offset and factor table of midpoint mi of a launch (one h0,
+// or the h0 block mi falls in).
+struct OctLine {
+    const float4 *tab;  // {m, gamma^2, 16h^2h0^2, h^2-h0^2} per trace
+    float h0;
+};
+__device__ __forceinline__ OctLine oct_line(const LsParams &a, uint32_t mi) {
+    OctLine l;
+    if (a.m0PerH0 == 0) {
+        l.tab = a.octTab;
+        l.h0 = a.h0;
+    } else {
+        const uint32_t b = mi / a.m0PerH0;
+        l.tab = a.octTab + (size_t)b * a.octTabStride;
+        l.h0 = a.h0s[b];
+    }
+    return l;
+}
+// The midpoint's index within its h0 block (keys of the DE random stream, so
+// that a block of a batched call draws what a one-h0 call would).
+__device__ __forceinline__ uint32_t m0_in_block(const LsParams &a, uint32_t mi) {
+    return a.m0PerH0 ? mi % a.m0PerH0 : mi;
+}
+
+// Window amplitudes y[0..n) of trace ti from sample k as FP32: the FP32 row,
+// or the 16-bit row widened (BF16: the high half of an FP32 word; FP16:
+// times the trace's scale).
+__device__ __forceinline__ float amp16(const LsParams &a, uint32_t ti, uint16_t bits) {
+    return a.storage == 2 ? __half2float(__ushort_as_half(bits)) * __ldg(a.scale + ti)
+                          : __uint_as_float((uint32_t)bits << 16);
+}
+template <int N>
+__device__ __forceinline__ void load_window(const LsParams &a, uint32_t ti, int k, float (&y)[N]) {
+    if (a.samples16) {
+        const uint16_t *r = a.samples16 + (size_t)ti * a.stride + k;
+        const float sc = a.storage == 2 ? __ldg(a.scale + ti) : 1.f;
+#pragma unroll
+        for (int j = 0; j < N; j++) {
+            const uint16_t b = __ldg(r + j);
+            y[j] = a.storage == 2 ? __half2float(__ushort_as_half(b)) * sc
+                                  : __uint_as_float((uint32_t)b << 16);
+        }
+    } else {
+        const float *r = a.samples + (size_t)ti * a.stride + k;
+#pragma unroll
+        for (int j = 0; j < N; j++) y[j] = __ldg(r + j);
+    }
+}
+// One amplitude (runtime-sized windows).
+__device__ __forceinline__ float amp_at(const LsParams &a, uint32_t ti, int k) {
+    return a.samples16 ? amp16(a, ti, __ldg(a.samples16 + (size_t)ti * a.stride + k))
+                       : __ldg(a.samples + (size_t)ti * a.stride + k);
+}
+
 __device__ __forceinline__ void oct_box_store(volatile float *slot, const OctWarpBox &r) {
     slot[0] = r.aLo;
     slot[1] = r.aHi;
@@ -404,13 +460,13 @@ __device__ __forceinline__ void oct_box_store(volatile float *slot, const OctWar
     slot[3] = r.bHi;
     __syncwarp();
 }
-__device__ __forceinline__ bool oct_box_keep(const LsParams &a, uint32_t ti,
+__device__ __forceinline__ bool oct_box_keep(const LsParams &a, const OctLine &ol, uint32_t ti,
                                              const volatile float *slot, float m0) {
-    const float4 tf = __ldg(a.octTab + ti);
+    const float4 tf = __ldg(ol.tab + ti);
     const float aLo = slot[0], aHi = slot[1], bLo = slot[2], bHi = slot[3];
-    return a.h0 == 0.f ? oct_box_may_pass(tf, bLo, bHi, aLo, aHi, m0, a.apm)
-                       : oct_box_may_pass_h0(tf, __ldg(a.hoff + ti), a.h0, aLo, aHi, bLo, bHi,
-                                             m0, a.apm);
+    return ol.h0 == 0.f ? oct_box_may_pass(tf, bLo, bHi, aLo, aHi, m0, a.apm)
+                        : oct_box_may_pass_h0(tf, __ldg(a.hoff + ti), ol.h0, aLo, aHi, bLo, bHi,
+                                              m0, a.apm);
 }
 
 // B traces of one thread's OCT candidate (factors kc, c = 4/v^2, slope):
@@ -419,7 +475,8 @@ __device__ __forceinline__ bool oct_box_keep(const LsParams &a, uint32_t ti,
 // (interface.h:26-44).  live[b] false: padding, neither evaluated nor
 // counted.
 template <int W, int B>
-__device__ __forceinline__ void oct_eval_batch(const LsParams &a, const uint32_t (&tb)[B],
+__device__ __forceinline__ void oct_eval_batch(const LsParams &a, const OctLine &ol,
+                                               const uint32_t (&tb)[B],
                                                const bool (&live)[B], const OctCand &kc,
                                                float c, float slope, float t0, float m0,
                                                float (&num)[W], float &lin, float &den,
@@ -428,7 +485,7 @@ __device__ __forceinline__ void oct_eval_batch(const LsParams &a, const uint32_t
     float mhb[B];
     bool pass[B];
 #pragma unroll
-    for (int b = 0; b < B; b++) fb[b] = __ldg(a.octTab + tb[b]);
+    for (int b = 0; b < B; b++) fb[b] = __ldg(ol.tab + tb[b]);
 #pragma unroll
     for (int b = 0; b < B; b++) {
         const int e = oct_mh_all(kc, fb[b].y, fb[b].z, fb[b].w, m0, &mhb[b]);
@@ -442,17 +499,16 @@ __device__ __forceinline__ void oct_eval_batch(const LsParams &a, const uint32_t
             continue;
         }
         float t;
-        if (oct_time_k(a.hoff[tb[b]], a.h0, t0, kc.tn0_sq, m0, fb[b].x, mhb[b], c, slope, &t) !=
+        if (oct_time_k(a.hoff[tb[b]], ol.h0, t0, kc.tn0_sq, m0, fb[b].x, mhb[b], c, slope, &t) !=
             DE_OK)
             continue;
         const WinIdx wi = window_index(t, a.dt);
         if (window_in_trace(wi.k, a.tau, (int)a.S)) {
-            const float *y = a.samples + (size_t)tb[b] * a.stride + (wi.k - a.tau);
-            float y1 = __ldg(y);
+            float y[W + 1];
+            load_window(a, tb[b], wi.k - a.tau, y);
 #pragma unroll
             for (int jj = 0; jj < W; jj++) {
-                const float y0 = y1;
-                y1 = __ldg(y + jj + 1);
+                const float y0 = y[jj], y1 = y[jj + 1];
                 const float u = (y1 - y0) * wi.frac + y0;
                 num[jj] += u;
                 lin += u;

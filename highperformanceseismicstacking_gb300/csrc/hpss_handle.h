@@ -21,9 +21,15 @@ struct hpss_handle_s : public hpss::Handle {
     };
     Buf params, chunkBounds, selFirst, selCount, selIdx, candFirst, candCount,
         notUsed, errWord, m0s, out, octCands, prior, partial, order;
-    Buf octTab;                // OCT per-trace factors of the line (octTabH0)
+    Buf octTab;                // OCT per-trace factors of the line, one table per
+                               // half-offset in octTabH0s
     bool octTabValid = false;
-    float octTabH0 = 0.f;
+    std::vector<float> octTabH0s;
+    // OCT over several target half-offsets (hpss_set_oct_half_offsets):
+    // empty = the single h0 of hpss_set_traveltime
+    std::vector<float> octH0s;
+    Buf octH0sDev;             // octH0s on the device
+    Buf m0v;                   // midpoints of a call repeated per half-offset
     std::string gridKey;       // grid held in `params` (empty: none)
     uint32_t boundsChunk = 0;  // chunk size of the bounds in `chunkBounds` (0: none)
     std::vector<float> octCandsHost;
@@ -64,9 +70,18 @@ hpss_status oct_candidate_slots(hpss_handle h, const float *d_m0s, uint32_t nM0,
 hpss_status run_selection(hpss_handle h, const float *d_m0s, uint32_t nM0, LsParams &lp);
 // The resident line, window and traveltime of the handle as kernel parameters.
 void fill_line_params(hpss_handle h, LsParams &lp);
-// OCT: the per-trace factor table of the line for the current h0 (built on
-// first use after an upload or an h0 change).
+// OCT: the per-trace factor tables of the line for the current h0 or
+// half-offset list (built on first use after an upload or a change).
 cudaError_t use_oct_table(hpss_handle h, LsParams &lp);
+// Result blocks per midpoint of an OCT call: the number of target
+// half-offsets of hpss_set_oct_half_offsets (1 without a list or for
+// CMP / ZO-CRS).
+uint32_t h0_blocks(hpss_handle h);
+// OCT with several target half-offsets: lp.m0s / lp.nM0 (nM0 midpoints)
+// become nH0 * nM0 midpoints in h0 blocks (block b = the midpoints at h0s[b],
+// copied on the device) and lp's block fields are set; otherwise nothing
+// changes.
+cudaError_t expand_h0_blocks(hpss_handle h, LsParams &lp);
 int num_sms(hpss_handle h);
 // Amplitudes of traces [a, b) of a line being uploaded, on stream st.
 cudaError_t copy_line_rows(hpss_handle h, const float *samples, uint32_t a, uint32_t b,

@@ -107,6 +107,13 @@ struct LsParams {
     // OCT with h0 = 0: warps drop traces by the displaced-midpoint box test
     // (oct_box_may_pass) before the per-sample test
     bool octBox = false;
+    // OCT over several target half-offsets in one launch: the launch's nM0
+    // midpoints are blocks of m0PerH0 midpoints, block b taking half-offset
+    // h0s[b] and the factor table octTab + b * octTabStride (oct_line).
+    // m0PerH0 = 0: one half-offset, h0 and octTab.
+    uint32_t m0PerH0 = 0;
+    const float *h0s = nullptr;
+    size_t octTabStride = 0;
 #ifdef HPSS_CHECKED
     // checked builds only: bytes armed on the tuned kernel's staging barrier
     // beyond what its copies deliver, so that the bounded wait runs out and
@@ -136,6 +143,8 @@ struct DeParams {
     float lo[3], hi[3];
 };
 constexpr uint32_t kDeMaxPopulation = 128;
+// Target half-offsets of one OCT call (hpss_set_oct_half_offsets).
+constexpr uint32_t kMaxOctHalfOffsets = 64;
 
 struct Handle {
     int device = 0;
@@ -239,7 +248,7 @@ cudaError_t launch_sf(const LsParams &p, int model, uint32_t grid, uint32_t nUni
                       cudaStream_t st);
 cudaError_t launch_sf_select_oct(const LsParams &p, const uint32_t *candFirst,
                                  const uint32_t *candCount, uint32_t *selIdx,
-                                 uint32_t *selCount, cudaStream_t st);
+                                 uint32_t *selCount, uint64_t total, cudaStream_t st);
 cudaError_t launch_de_select_oct(const DeParams &d, const uint32_t *candFirst,
                                  const uint32_t *candCount, uint32_t *selIdx,
                                  uint32_t *selCount, uint64_t total, cudaStream_t st);

@@ -128,6 +128,7 @@ __global__ void select_oct_flags_kernel(LsParams a, const float *cands, uint32_t
     const uint32_t mi = lo;
     const uint32_t ti = candFirst[mi] + (uint32_t)(g - a.selFirst[mi]);
     const float m0 = a.m0s[mi];
+    const float h0 = oct_line(a, mi).h0;
     const float m = a.mid[ti], h = a.hoff[ti];
     bool used = false;
     for (uint32_t s = 0; s < a.S && !used; s++) {
@@ -137,7 +138,7 @@ __global__ void select_oct_flags_kernel(LsParams a, const float *cands, uint32_t
             bool hit = false;
             if (p < nCand) {
                 float mh;
-                const int e = oct_displaced_midpoint(h, a.h0, t0, m0, cands[2 * p],
+                const int e = oct_displaced_midpoint(h, h0, t0, m0, cands[2 * p],
                                                      cands[2 * p + 1], &mh);
                 hit = (e == DE_OK && fabsf(m - mh) <= a.apm);
             }

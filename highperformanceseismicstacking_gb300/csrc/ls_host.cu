@@ -171,6 +171,12 @@ hpss_status linear_search_impl(hpss_handle h, const float *d_m0s, uint32_t nM0,
     lp.P = (uint32_t)P;
     lp.out = d_out;
     HPSS_CUDA_TRY(h, use_oct_table(h, lp));
+    // OCT over several half-offsets: the midpoints in h0 blocks, one search
+    if (!group) {
+        HPSS_CUDA_TRY(h, expand_h0_blocks(h, lp));
+        d_m0s = lp.m0s;
+        nM0 = lp.nM0;
+    }
 
     // The candidate grid (and below the chunk bounds) depend only on the
     // model, the bounds, the granularity and the grid mode: a call that
@@ -411,7 +417,7 @@ hpss_status stream_line_and_search(hpss_handle h, const float *samples, const fl
     uint32_t bound[kStreamChunks + 1];
     for (uint32_t k = 0; k <= kStreamChunks; k++)
         bound[k] = (uint32_t)((uint64_t)n * k / kStreamChunks);
-    if (n && h->stride != h->S)
+    if (n && h->stride != h->S && h->storage == HPSS_STORAGE_FP32)
         HPSS_CUDA_TRY(h, cudaMemsetAsync(h->dSamples, 0, (size_t)n * h->stride * sizeof(float),
                                          h->copyStream));
     for (uint32_t k = 0; k < kStreamChunks; k++) {

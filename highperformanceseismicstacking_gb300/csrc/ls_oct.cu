@@ -84,6 +84,7 @@ ls_oct_kernel(LsParams a, uint32_t tiles, uint32_t parts, uint32_t chunksPerPart
         const float t0 = static_cast<float>(sc) * a.dt;
         const float m0 = a.m0s[mi];
         const uint32_t first = a.selFirst[mi], cnt = a.selCount[mi];
+        const OctLine ol = oct_line(a, mi);  // the midpoint's h0 and factor table
 
         float best = -1.f, second = -1.f, bestStack = 0.f;
         uint32_t bestP = 0xffffffffu;
@@ -95,11 +96,11 @@ ls_oct_kernel(LsParams a, uint32_t tiles, uint32_t parts, uint32_t chunksPerPart
             if (p >= a.P) break;
             const float cc = a.params[2 * (size_t)p];
             const float sl = a.params[2 * (size_t)p + 1];
-            const OctCand kc = oct_cand(t0, cc, sl, a.h0);  // (t0, candidate) factors
+            const OctCand kc = oct_cand(t0, cc, sl, ol.h0);  // (t0, candidate) factors
             // the warp's displaced-midpoint box (oct_warp_box)
             bool boxOn;
             {
-                const OctWarpBox box = oct_warp_box(a.octBox, true, t0, sl, kc, a.h0);
+                const OctWarpBox box = oct_warp_box(a.octBox, true, t0, sl, kc, ol.h0);
                 boxOn = box.on;
                 if (boxOn) oct_box_store(shBox[warp], box);
             }
@@ -116,7 +117,7 @@ ls_oct_kernel(LsParams a, uint32_t tiles, uint32_t parts, uint32_t chunksPerPart
                     bool keep = false;
                     if ((uint32_t)lane < n) {
                         const uint32_t ti = a.selIdx ? a.selIdx[first + qb + lane] : first + qb + lane;
-                        keep = oct_box_keep(a, ti, shBox[warp], m0);
+                        keep = oct_box_keep(a, ol, ti, shBox[warp], m0);
                     }
                     uint32_t mask = __ballot_sync(0xffffffffu, keep);
                     nu += n - (uint32_t)__popc(mask);
@@ -131,7 +132,7 @@ ls_oct_kernel(LsParams a, uint32_t tiles, uint32_t parts, uint32_t chunksPerPart
                             if (live[bb]) mask &= mask - 1;
                             tb[bb] = a.selIdx ? a.selIdx[first + qb + bit] : first + qb + bit;
                         }
-                        oct_eval_batch<W, kOctMhBatch>(a, tb, live, kc, cc, sl, t0, m0, num, lin,
+                        oct_eval_batch<W, kOctMhBatch>(a, ol, tb, live, kc, cc, sl, t0, m0, num, lin,
                                                        den, used, nu);
                     }
                 }
@@ -147,7 +148,7 @@ ls_oct_kernel(LsParams a, uint32_t tiles, uint32_t parts, uint32_t chunksPerPart
                         tb[bb] = a.selIdx ? a.selIdx[first + q + bb] : first + q + bb;
                         live[bb] = true;
                     }
-                    oct_eval_batch<W, kOctMhBatch>(a, tb, live, kc, cc, sl, t0, m0, num, lin, den,
+                    oct_eval_batch<W, kOctMhBatch>(a, ol, tb, live, kc, cc, sl, t0, m0, num, lin, den,
                                                    used, nu);
                 }
                 for (; q < cnt; q++) {
@@ -158,7 +159,7 @@ ls_oct_kernel(LsParams a, uint32_t tiles, uint32_t parts, uint32_t chunksPerPart
                         tb[bb] = a.selIdx ? a.selIdx[first + q] : first + q;
                         live[bb] = bb == 0;
                     }
-                    oct_eval_batch<W, kOctMhBatch>(a, tb, live, kc, cc, sl, t0, m0, num, lin, den,
+                    oct_eval_batch<W, kOctMhBatch>(a, ol, tb, live, kc, cc, sl, t0, m0, num, lin, den,
                                                    used, nu);
                 }
             }

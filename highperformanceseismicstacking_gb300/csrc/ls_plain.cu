@@ -104,6 +104,7 @@ ls_plain_kernel(LsParams a) {
     }
 
     const float t0 = static_cast<float>(s) * a.dt;
+    const float h0 = MODEL == kModelOct ? oct_line(a, mi).h0 : 0.f;
     float best = -1.f, bestStack = 0.f, second = -1.f;
     uint32_t bestP = 0xffffffffu;
     unsigned long long notUsed = 0;
@@ -131,23 +132,22 @@ ls_plain_kernel(LsParams a) {
             if ((MODE & kPrecTt64) && MODEL == kModelZocrs)
                 ok = zocrs_time_f64(t0, c, p1, p2, a.mid[ti] - m0, a.hoff[ti], &t);
             else if ((MODE & kPrecTt64) && MODEL == kModelOct)
-                ok = oct_time_f64(t0, c, p1, a.mid[ti], a.hoff[ti], m0, a.apm, a.h0, &t);
+                ok = oct_time_f64(t0, c, p1, a.mid[ti], a.hoff[ti], m0, a.apm, h0, &t);
             else
                 ok = model_time<MODEL>(t0, c, p1, p2, a.mid[ti], a.hoff[ti], a.hsq[ti], m0,
-                                       a.apm, a.h0, &t);
+                                       a.apm, h0, &t);
             if (ok < 0) {
                 nu++;
                 continue;
             }
             if (ok == 0) continue;
-            const float *tr = a.samples + (size_t)ti * a.stride;
             WinIdx wi = window_index(t, a.dt);
             if (window_in_trace(wi.k, a.tau, (int)a.S)) {
                 int k = wi.k - a.tau;
-                float y1 = tr[k];
+                float y1 = amp_at(a, ti, k);
                 for (int j = 0; j < a.w; j++, k++) {
                     float y0 = y1;
-                    y1 = tr[k + 1];
+                    y1 = amp_at(a, ti, k + 1);
                     float u = (y1 - y0) * wi.frac + y0;
                     if (kMayComp && comp) {
                         neumaier(num[j], numc[j], u);

@@ -29,6 +29,7 @@ __global__ void __launch_bounds__(kSfWarps * 32) sf_kernel(LsParams a, uint32_t 
         const float m0 = a.m0s[mi];
         const uint32_t first = a.selFirst[mi], cnt = a.selCount[mi];
         const float *prior = a.prior + (size_t)mi * NP * a.S;
+        const float h0 = MODEL == kModelOct ? oct_line(a, mi).h0 : 0.f;
         float best = -1.f, bestK = 0.f;
         uint32_t bestI = 0xffffffffu;
         unsigned nu = 0;
@@ -52,7 +53,7 @@ __global__ void __launch_bounds__(kSfWarps * 32) sf_kernel(LsParams a, uint32_t 
                     const uint32_t ti = a.selIdx ? a.selIdx[first + q] : first + q;
                     float tn;
                     int ok = model_time<MODEL>(t0n, c, p1, p2, a.mid[ti], a.hoff[ti], a.hsq[ti],
-                                               m0, a.apm, a.h0, &tn);
+                                               m0, a.apm, h0, &tn);
                     if (ok < 0) {
                         nu++;
                         continue;
@@ -63,11 +64,11 @@ __global__ void __launch_bounds__(kSfWarps * 32) sf_kernel(LsParams a, uint32_t 
                     const float t = __fmaf_rn(nf, a.dt, tn);
                     WinIdx wi = window_index(t, a.dt);
                     if (window_in_trace(wi.k, a.tau, (int)a.S)) {
-                        const float *tr = a.samples + (size_t)ti * a.stride + (wi.k - a.tau);
-                        float y1 = __ldg(tr);
+                        const int k0 = wi.k - a.tau;
+                        float y1 = amp_at(a, ti, k0);
                         for (int j = 0; j < a.w; j++) {
                             float y0 = y1;
-                            y1 = __ldg(tr + j + 1);
+                            y1 = amp_at(a, ti, k0 + j + 1);
                             float u = (y1 - y0) * wi.frac + y0;
                             num[j] += u;
                             lin += u;
@@ -108,43 +109,45 @@ __global__ void __launch_bounds__(kSfWarps * 32) sf_kernel(LsParams a, uint32_t 
 }
 
 // OCT trace selection with the prior parameters of every sample
-// (selectTracesForOffsetContinuationTrajectory, oct/stretch_free.cu:99-138).
-__global__ void sf_select_oct_kernel(LsParams a, const uint32_t *candFirst,
-                                     const uint32_t *candCount, uint32_t *selIdx,
-                                     uint32_t *selCount) {
-    const uint32_t mi = blockIdx.x;
-    const float m0 = a.m0s[mi];
-    const float *prior = a.prior + (size_t)mi * 2 * a.S;
-    const uint32_t first = candFirst[mi], count = candCount[mi];
-    const uint32_t outBase = a.selFirst[mi];
-    __shared__ uint32_t shCount;
-    __shared__ uint32_t shFlags[256];
-    if (threadIdx.x == 0) shCount = 0;
-    __syncthreads();
-    for (uint32_t base = 0; base < count; base += blockDim.x) {
-        const uint32_t q = base + threadIdx.x;
-        bool used = false;
-        if (q < count) {
-            const uint32_t ti = first + q;
-            const float m = a.mid[ti], h = a.hoff[ti];
-            for (uint32_t s = 0; s < a.S && !used; s++) {
-                const float t0 = static_cast<float>(s) * a.dt;
-                const float v = prior[s];
-                const float c = 4.0f / (v * v);
-                float mh;
-                int e = oct_displaced_midpoint(h, a.h0, t0, m0, c, prior[a.S + s], &mh);
-                used = (e == DE_OK && fabsf(m - mh) <= a.apm);
-            }
-        }
-        shFlags[threadIdx.x] = used ? 1u : 0u;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            for (uint32_t w = 0; w < blockDim.x && base + w < count; w++)
-                if (shFlags[w]) selIdx[outBase + shCount++] = first + base + w;
-        }
-        __syncthreads();
+// (selectTracesForOffsetContinuationTrajectory, oct/stretch_free.cu:99-138):
+// a trace is used if the parameters chosen at any sample s give a valid
+// displaced midpoint within apm at t0 = s dt.  One warp per (midpoint,
+// candidate trace) slot over the whole GPU, lanes over the samples, writes a
+// 0 / 1 flag into the slot (a.selFirst: the prefix of candCount); the flags
+// are then compacted in order (launch_select_compact).
+__global__ void sf_select_oct_flags_kernel(LsParams a, const uint32_t *candFirst,
+                                           uint64_t total, uint32_t *selIdx) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t g = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (g >= total) return;  // whole warps
+    // the slot's midpoint: the last mi with selFirst[mi] <= g
+    uint32_t lo = 0, hi = a.nM0;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) / 2;
+        if ((uint64_t)a.selFirst[mid] <= g) lo = mid;
+        else hi = mid;
     }
-    if (threadIdx.x == 0) selCount[mi] = shCount;
+    const uint32_t mi = lo;
+    const uint32_t ti = candFirst[mi] + (uint32_t)(g - a.selFirst[mi]);
+    const float m0 = a.m0s[mi];
+    const float h0 = oct_line(a, mi).h0;
+    const float *prior = a.prior + (size_t)mi * 2 * a.S;
+    const float m = a.mid[ti], h = a.hoff[ti];
+    bool used = false;
+    for (uint32_t s0 = 0; s0 < a.S && !used; s0 += 32) {
+        const uint32_t s = s0 + lane;
+        bool hit = false;
+        if (s < a.S) {
+            const float t0 = static_cast<float>(s) * a.dt;
+            const float v = prior[s];
+            const float c = 4.0f / (v * v);
+            float mh;
+            const int e = oct_displaced_midpoint(h, h0, t0, m0, c, prior[a.S + s], &mh);
+            hit = e == DE_OK && fabsf(m - mh) <= a.apm;
+        }
+        used = __any_sync(0xffffffffu, hit);
+    }
+    if (lane == 0) selIdx[g] = used ? 1u : 0u;
 }
 
 cudaError_t launch_sf(const LsParams &p, int model, uint32_t grid, uint32_t nUnits,
@@ -160,10 +163,16 @@ cudaError_t launch_sf(const LsParams &p, int model, uint32_t grid, uint32_t nUni
 
 cudaError_t launch_sf_select_oct(const LsParams &p, const uint32_t *candFirst,
                                  const uint32_t *candCount, uint32_t *selIdx,
-                                 uint32_t *selCount, cudaStream_t st) {
+                                 uint32_t *selCount, uint64_t total, cudaStream_t st) {
     if (p.nM0 == 0) return cudaSuccess;
-    sf_select_oct_kernel<<<p.nM0, 256, 0, st>>>(p, candFirst, candCount, selIdx, selCount);
-    return cudaGetLastError();
+    if (total > 0) {
+        const uint64_t blocks = (total * 32 + 255) / 256;
+        if (blocks > 0x7fffffffull) return cudaErrorInvalidConfiguration;
+        sf_select_oct_flags_kernel<<<(uint32_t)blocks, 256, 0, st>>>(p, candFirst, total, selIdx);
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    return launch_select_compact(p, candFirst, candCount, selIdx, selCount, st);
 }
 
 }  // namespace hpss

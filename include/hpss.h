@@ -177,6 +177,20 @@ hpss_status hpss_set_grid_mode(hpss_handle h, int mode);
 #define HPSS_PREC_COMPENSATED 2
 hpss_status hpss_set_precision(hpss_handle h, int flags);
 
+/* OCT over several target half-offsets in one call (no reference
+ * counterpart: the reference holds one h0 per OffsetContinuationTrajectory,
+ * common/src/traveltime/OffsetContinuationTrajectory.cpp:5-25, and runs a
+ * whole job per h0).  With nH0 >= 1 values, every OCT linear search,
+ * differential evolution, stretch-free and trace-selection call over nM0
+ * midpoints computes nH0 x nM0 results in one launch: result blocks (and
+ * stretch-free parameter blocks, selection counts) are laid out
+ * [nH0][nM0][...], block (b, i) being midpoint i at h0s[b] -- exactly what
+ * a call with hpss_set_traveltime(..., h0s[b]) would give, the DE random
+ * stream included.  The h0 of hpss_set_traveltime is then not used; nH0 = 0
+ * restores it.  At most 64 values; CMP and ZO-CRS calls are unaffected;
+ * hpss_linear_search_line rejects OCT lists. */
+hpss_status hpss_set_oct_half_offsets(hpss_handle h, const float *h0s, uint32_t nH0);
+
 /* Semblance window: tauIndexDisplacement = (int)(tau / dt), window
  * w = 2 * tau + 1 (Gather.cpp:75-76).  w must be <= 31
  * (MAX_WINDOW_SIZE, common/include/gpu/interface.h:10). */
