@@ -250,6 +250,168 @@ def de_side_measure(n_cmp, local):
     return out
 
 
+# Algorithmic FP32-pipe instructions per evaluation (one (m0, t0, candidate,
+# selected trace) tuple): 3 per window tap (interpolation with a precomputed
+# slope, numerator add, denominator fma) plus the traveltime -- 2 CMP, 5
+# ZO-CRS, 40 OCT (displaced midpoint and time).  An OCT trace that fails the
+# displaced-midpoint test costs the test alone: 9 (its per-(t0, candidate,
+# trace) operations once the trace-only and candidate-only factors are
+# hoisted).  Stretch-free adds the time shift (1).
+T_MODEL = {"cmp": 2, "zocrs": 5, "oct": 40}
+T_OCT_SKIP = 9
+
+
+def fp32_roofline(model, w, evals, not_used, ms, local, extra_per_eval=0, alg_bytes=None):
+    """FP32-pipe roofline of one launch: algorithmic instructions / time over
+    SMs x 128 lanes x max SM clock; plus the HBM view of its algorithmic
+    bytes when given."""
+    import torch
+    peaks = measured_peaks()
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    peak = sms * 128 * float(peaks.get("sm_max_mhz", 2070.0)) * 1e6
+    used = evals - not_used
+    instr = used * (3 * w + T_MODEL[model] + extra_per_eval) + not_used * T_OCT_SKIP
+    r = {"bound": "fp32", "achieved": instr / (ms / 1e3) / 1e12, "peak": peak / 1e12,
+         "unit": "Tinstr/s", "frac": instr / (ms / 1e3) / peak, "kernel_ms": ms,
+         "instr_per_launch": instr}
+    if alg_bytes is not None:
+        hbm = float(peaks.get("hbm_gbs", 6800.0))
+        gbs = alg_bytes / (ms / 1e3) / 1e9
+        r["hbm"] = {"achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": gbs / hbm,
+                    "bytes_per_launch": alg_bytes}
+    return r
+
+
+def c5_side_measure(n_cmp, local, h0s=(0.0, 500.0, 1000.0), storages=("fp16", "fp32")):
+    """The OCT DE workload as one pipeline on a bounded sample of its
+    midpoints: OCT differential evolution (population 48, 80 generations, F
+    0.5, CR 0.9, window 9) over every target half-offset in ONE launch, then
+    the stretch-free stack (window 9, n in [-10, 10]) over the chosen
+    parameters in one launch; FP16 amplitude storage (the workload's) and
+    FP32 storage for comparison.  Device time from the engine's events."""
+    from highperformanceseismicstacking_gb300 import capi
+    w, line, lower, upper, tau = make_workload("oct-de")
+    mid = len(line.cdp_midpoints) // 2
+    m0s = np.ascontiguousarray(line.cdp_midpoints[mid:mid + n_cmp])
+    S = line.samples_per_trace
+    wsz = 2 * tau + 1
+    out = {"cmps": int(len(m0s)), "h0s": list(h0s), "samples": S, "population": w.population,
+           "generations": w.generations, "window": wsz, "launches_per_pipeline": None}
+    res = {}
+    for storage in storages:
+        with capi.Engine(local) as eng:
+            eng.upload_gather(line.samples, line.midpoints, line.halfoffsets, float(line.dt),
+                              storage=storage)
+            eng.set_traveltime("oct", lower, upper, w.apm, 0.0)
+            eng.set_window(tau)
+            eng.set_oct_half_offsets(list(h0s))
+            eng.differential_evolution(m0s, w.population, 2, w.de_f, w.de_cr, seed=1)
+            de, st = eng.differential_evolution(m0s, w.population, w.generations, w.de_f,
+                                                w.de_cr, seed=7)
+            prior = np.ascontiguousarray(de[:, 2:])
+            sf, st2 = eng.stretch_free(m0s, prior, 10)
+            dev_bytes = eng.device_bytes()
+        sel = st["selected_traces"]
+        bpv = 2 if storage != "fp32" else 4
+        de_bytes = sel * S * bpv + sel * 16
+        r = {"de": {"kernel_ms": st["kernel_ms"], "selection_ms": st["selection_ms"],
+                    "evals": st["evals"], "not_used": st["not_used"],
+                    "value": st["evals"] / (st["kernel_ms"] / 1e3),
+                    "mean_best_semblance": float(np.mean(de[:, 0])),
+                    "roofline": fp32_roofline("oct", wsz, st["evals"], st["not_used"],
+                                              st["kernel_ms"], local, alg_bytes=de_bytes)},
+             "stretch_free": {"kernel_ms": st2["kernel_ms"], "selection_ms": st2["selection_ms"],
+                              "evals": st2["evals"], "not_used": st2["not_used"],
+                              "value": st2["evals"] / (st2["kernel_ms"] / 1e3),
+                              "mean_semblance": float(np.mean(sf[:, 0])),
+                              "roofline": fp32_roofline("oct", wsz, st2["evals"], st2["not_used"],
+                                                        st2["kernel_ms"], local, extra_per_eval=1)},
+             "device_bytes": dev_bytes}
+        r["pipeline_ms"] = (st["kernel_ms"] + st["selection_ms"] + st2["kernel_ms"] +
+                            st2["selection_ms"])
+        res[storage] = (r, de, sf)
+    for storage in storages:
+        out[storage] = res[storage][0]
+    if "fp16" in res and "fp32" in res:
+        d16, d32 = res["fp16"][1], res["fp32"][1]
+        strong = d32[:, 0] > 0.1
+        out["fp16_vs_fp32"] = {
+            "de_median_best_semblance_ratio": float(np.median(d16[:, 0][strong] /
+                                                              d32[:, 0][strong])),
+            "de_speedup": res["fp32"][0]["de"]["kernel_ms"] / res["fp16"][0]["de"]["kernel_ms"]}
+    # per pipeline: DE selection (flags + compaction), DE, stretch-free
+    # selection (flags + compaction), stretch-free
+    out["launches_per_pipeline"] = 6
+    return out
+
+
+def fp64_agreement_side(n_mid, local):
+    """Chosen parameters of every FP32 mode against the FP64 reference on
+    n_mid midpoints of the ZO-CRS line (every sample of each, 21 x 21 x 41
+    candidates, window 5): the FP64 reference is the search with every step
+    in FP64 on the device (HPSS_PREC_FP64).  Per mode, a sample is
+    'agree' (the FP64 choice), 'near_tie' (another candidate whose FP64
+    semblance is within 1e-4 x max(best, 1e-3) of the FP64 best -- evaluated
+    by the FP64 stretch-free pass with n = 0 on both choices) or 'changed'.
+    Modes: FP32 (the reference's arithmetic), FP64 traveltime, compensated
+    sums, both (tuned kernels), and BF16 / FP16 amplitude storage."""
+    import torch
+    from highperformanceseismicstacking_gb300 import capi
+    w, line, lower, upper, tau = make_workload("zocrs-ls")
+    cdp = line.cdp_midpoints
+    pick = np.linspace(40, len(cdp) - 41, n_mid).round().astype(int)
+    m0s = np.ascontiguousarray(cdp[pick])
+    S = line.samples_per_trace
+    gran = w.granularity
+    eng = capi.Engine(local)
+    eng.upload_gather(line.samples, line.midpoints, line.halfoffsets, float(line.dt))
+    eng.set_traveltime(w.model, lower, upper, w.apm, w.h0)
+    eng.set_window(tau)
+    eng.set_precision(fp64=True)
+    t0 = time.perf_counter()
+    ref, st64 = eng.linear_search(m0s, gran, "plain")
+    fp64_s = time.perf_counter() - t0
+
+    def semb64(params):
+        # FP64 semblance of explicit per-sample parameters (raw) at n = 0
+        out, _ = eng.stretch_free(m0s, np.ascontiguousarray(params), 0)
+        return out[:, 0].astype(np.float64)
+
+    s_best = semb64(ref[:, 2:])
+    modes = {"fp32": {}, "fp64_traveltime": {"fp64_traveltime": True},
+             "compensated": {"compensated": True},
+             "fp64_traveltime+compensated": {"fp64_traveltime": True, "compensated": True}}
+    outs = {}
+    for name, kw in modes.items():
+        eng.set_precision(**kw)
+        outs[name], _ = eng.linear_search(m0s, gran, "tuned")
+    eng.set_precision()
+    for storage in ("bf16", "fp16"):
+        eng.upload_gather(line.samples, line.midpoints, line.halfoffsets, float(line.dt),
+                          storage=storage)
+        outs[storage], _ = eng.linear_search(m0s, gran, "tuned")
+    eng.upload_gather(line.samples, line.midpoints, line.halfoffsets, float(line.dt))
+    res = {"midpoints": int(n_mid), "samples": int(n_mid * S), "candidates": int(np.prod(gran)),
+           "fp64_reference_s": fp64_s, "fp64_reference_evals": st64["evals"],
+           "fp64_near_ties": st64["near_ties"], "modes": {}}
+    eng.set_precision(fp64=True)
+    for name, got in outs.items():
+        diff = np.any(got[:, 2:] != ref[:, 2:], axis=1)  # [nM0][S]
+        n = int(diff.sum())
+        near = 0
+        if n:
+            s_alt = semb64(got[:, 2:])
+            tol = 1e-4 * np.maximum(s_best, 1e-3)
+            near = int(np.sum(diff & (s_alt >= s_best - tol)))
+        tot = diff.size
+        res["modes"][name] = {"changed": (n - near) / tot, "near_tie": near / tot,
+                              "agree": 1.0 - n / tot,
+                              "meets_99_9": (n - near) / tot <= 1e-3}
+    eng.set_precision()
+    eng.close()
+    return res
+
+
 def time_call(eng, stream, d_m0, n_m0, gran, d_out, kernel, reps=1):
     """One untimed call (autotuning, first-launch costs), then `reps` calls
     timed with CUDA events on the engine's stream; ms per call."""

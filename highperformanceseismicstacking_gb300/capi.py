@@ -24,7 +24,7 @@ MODELS = {"cmp": 0, "zocrs": 1, "oct": 2}
 STORAGE = {"fp32": 0, "bf16": 1, "fp16": 2}
 KERNELS = {"plain": 0, "tuned": 1, "tuned_exact": 2}
 GRID_MODES = {"reference": 0, "inclusive": 1}
-PREC_FP64_TRAVELTIME, PREC_COMPENSATED = 1, 2
+PREC_FP64_TRAVELTIME, PREC_COMPENSATED, PREC_FP64 = 1, 2, 4
 N_PARAMS = {"cmp": 1, "zocrs": 3, "oct": 2}
 
 # Every symbol include/hpss.h declares.
@@ -197,11 +197,12 @@ class Engine:
     def set_window(self, tau_index: int):
         self._check(self._lib.hpss_set_window(self.h, int(tau_index)))
 
-    def set_precision(self, fp64_traveltime: bool = False, compensated: bool = False):
-        """Precision modes of the linear search (plain kernel): FP64
-        traveltime (ZO-CRS / OCT) and compensated window sums."""
+    def set_precision(self, fp64_traveltime: bool = False, compensated: bool = False,
+                      fp64: bool = False):
+        """Precision modes of the linear search: FP64 traveltime (ZO-CRS /
+        OCT), compensated window sums, or every step in FP64."""
         flags = (PREC_FP64_TRAVELTIME if fp64_traveltime else 0) | \
-            (PREC_COMPENSATED if compensated else 0)
+            (PREC_COMPENSATED if compensated else 0) | (PREC_FP64 if fp64 else 0)
         self._check(self._lib.hpss_set_precision(self.h, flags))
 
     def set_grid_mode(self, mode: str):

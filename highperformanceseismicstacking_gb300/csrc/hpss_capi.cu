@@ -534,10 +534,11 @@ hpss_status hpss_set_traveltime(hpss_handle h, int model, uint32_t nParams,
 
 hpss_status hpss_set_precision(hpss_handle h, int flags) {
     if (!h) return HPSS_ERR_INVALID_ARGUMENT;
-    if (flags & ~(HPSS_PREC_FP64_TRAVELTIME | HPSS_PREC_COMPENSATED))
+    if (flags & ~(HPSS_PREC_FP64_TRAVELTIME | HPSS_PREC_COMPENSATED | HPSS_PREC_FP64))
         return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "unknown precision flags");
     h->precisionMode = (flags & HPSS_PREC_FP64_TRAVELTIME ? kPrecTt64 : 0) |
-                       (flags & HPSS_PREC_COMPENSATED ? kPrecCompensated : 0);
+                       (flags & HPSS_PREC_COMPENSATED ? kPrecCompensated : 0) |
+                       (flags & HPSS_PREC_FP64 ? kPrecF64 : 0);
     return HPSS_OK;
 }
 
@@ -761,7 +762,10 @@ hpss_status hpss_stretch_free(hpss_handle h, const float *m0s, uint32_t nM0,
     if (units > 0xffffffffull)
         return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "too many (midpoint, sample) units");
     const uint32_t grid = (uint32_t)std::min<uint64_t>((units + 7) / 8, (uint64_t)num_sms(h) * 8);
-    HPSS_CUDA_TRY(h, launch_sf(lp, h->model, grid, (uint32_t)units, h->stream));
+    // the precision mode with every step in FP64 applies to stretch-free too
+    HPSS_CUDA_TRY(h, (h->precisionMode & kPrecF64)
+                         ? launch_sf_f64(lp, h->model, (uint32_t)units, h->stream)
+                         : launch_sf(lp, h->model, grid, (uint32_t)units, h->stream));
     HPSS_CUDA_TRY(h, cudaEventRecord(h->ev2, h->stream));
     HPSS_CUDA_TRY(h, cudaMemcpyAsync(out, lp.out, outElems * sizeof(float),
                                      cudaMemcpyDeviceToHost, h->stream));

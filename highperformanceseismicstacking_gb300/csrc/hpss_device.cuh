@@ -55,6 +55,78 @@ __device__ __forceinline__ bool zocrs_time(float t0, float c, float a, float b,
     return false;
 }
 
+// ZO-CRS time with the squared time (t0 + A dm)^2 + B dm^2 + C h^2 formed in
+// FP64 from the FP32 inputs (h^2 as the FP32 product the reference's host
+// code forms) and the time rounded to FP32 once; false when the square is
+// negative (window skipped).  The precision mode HPSS_PREC_FP64_TRAVELTIME.
+__device__ __forceinline__ bool zocrs_time_tt64(float t0, float c, float a, float b, float dm,
+                                                float h_sq, float *t) {
+    const double x = (double)t0 + (double)a * (double)dm;
+    const double tmp = x * x + (double)b * (double)dm * (double)dm + (double)c * (double)h_sq;
+    *t = tmp >= 0 ? (float)sqrt(tmp) : 0.f;
+    return tmp >= 0;
+}
+
+// OCT displaced midpoint and time in FP64 (same formulas and operation
+// order as oct/common.cuh:7-94) from the FP32 inputs; returns as model_time
+// (-1 not used: displaced-midpoint error or |m - mh| > apm; 0 window skipped:
+// time error; 1 time valid).
+__device__ __forceinline__ int oct_time_d(double t0, double c, double slope, double m, double h,
+                                          double m0, double apm, double h0, double *t) {
+    const double theta = t0 * slope;
+    const double gamma = 2 * sqrt(h * h + h0 * h0);
+    const double tn0_sq = t0 * t0 - c * h0 * h0;
+    const double theta_sq = theta * theta, gamma_sq = gamma * gamma, tn0_quad = tn0_sq * tn0_sq;
+    double arg = tn0_quad * tn0_quad + tn0_quad * theta_sq * gamma_sq +
+                 16 * h * h * h0 * h0 * theta_sq * theta_sq;
+    if (arg < 0) return -1;
+    arg = theta_sq * gamma_sq + 2 * tn0_quad + 2 * sqrt(arg);
+    if (arg == 0) return -1;
+    const double mh = m0 + 2 * theta * (h * h - h0 * h0) / sqrt(arg);
+    if (fabs(m - mh) > apm) return -1;
+    const double w1 = (h + h0) * (h + h0) - (mh - m0) * (mh - m0);
+    const double w2 = (h - h0) * (h - h0) - (mh - m0) * (mh - m0);
+    if (w1 < 0 || w2 < 0) return 0;
+    const double u = sqrt(w1) + sqrt(w2);
+    double th = t0;
+    if (fabs(h) > fabs(h0)) {
+        if (!u) return 0;
+        const double sa = c * h * h + 4 * h * h / (u * u) * tn0_sq;
+        if (sa < 0) return 0;
+        th = sqrt(sa);
+    } else if (fabs(h) < fabs(h0)) {
+        if (!h0) return 0;
+        const double sa = c * h * h + u * u / (4 * h0 * h0) * tn0_sq;
+        if (sa < 0) return 0;
+        th = sqrt(sa);
+    }
+    const double tn_sq = th * th - c * h * h;
+    if (!th || !tn0_sq) return 0;
+    const double ah = (t0 * tn_sq) / (th * tn0_sq) * slope;
+    *t = th + ah * (m - mh);
+    return 1;
+}
+
+// The same with the time rounded to FP32 once (precision mode
+// HPSS_PREC_FP64_TRAVELTIME).
+__device__ __forceinline__ int oct_time_f64(float t0, float c, float slope, float m, float h,
+                                            float m0, float apm, float h0, float *t) {
+    double td = 0;
+    const int ok = oct_time_d(t0, c, slope, m, h, m0, apm, h0, &td);
+    if (ok > 0) *t = (float)td;
+    return ok;
+}
+
+// Knuth's two-sum: s + x as sum and rounding error, branch-free; the
+// error is kept in a compensation term (compensated summation of the window
+// sums, precision mode HPSS_PREC_COMPENSATED).
+__device__ __forceinline__ void two_sum_acc(float &s, float &comp, float x) {
+    const float t = __fadd_rn(s, x);
+    const float z = __fsub_rn(t, s);
+    comp = __fadd_rn(comp, __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(x, z)));
+    s = t;
+}
+
 // t0^2 - c h0^2 of the OCT formulas.
 __device__ __forceinline__ float oct_tn0_sq(float t0, float c, float h0) {
     return __fmaf_rn(t0, t0, -__fmul_rn(__fmul_rn(c, h0), h0));

@@ -33,6 +33,7 @@ constexpr int kGridInclusive = 1;
 // Precision modes of the linear search (HPSS_PREC_* of hpss.h).
 constexpr int kPrecTt64 = 1;
 constexpr int kPrecCompensated = 2;
+constexpr int kPrecF64 = 4;  // every step in FP64 (ls_f64.cu)
 
 // Near-tie tolerance (HPSS_NEAR_TIE_REL of hpss.h).
 constexpr float kNearTieRel = 1e-4f;
@@ -194,6 +195,10 @@ cudaError_t launch_chunk_bounds(const LsParams &p, float *bounds,
                                 cudaStream_t st);
 // precisionMode: kPrecTt64 | kPrecCompensated (0: the reference's FP32 arithmetic)
 cudaError_t launch_ls_plain(const LsParams &p, cudaStream_t st, int precisionMode = 0);
+// The linear search and the stretch-free stack with every step in FP64
+// (kPrecF64, ls_f64.cu); nUnits = nM0 * S.
+cudaError_t launch_ls_f64(const LsParams &p, cudaStream_t st);
+cudaError_t launch_sf_f64(const LsParams &p, int model, uint32_t nUnits, cudaStream_t st);
 // Tuned pair kernel (CMP / ZO-CRS) shapes, `variant`: 0 = 2 candidate pairs
 // per thread, 2 CTAs/SM; 1 = 1 pair, 3 CTAs/SM; 2 = 2 pairs, 3 CTAs/SM
 // (chunk = 8 warps x 2*pairs candidates).  exactStack selects the
@@ -214,8 +219,14 @@ cudaError_t launch_ls_tuned_zocrs_exact(const LsParams &p, uint32_t grid, uint32
 // `partial` holds oct_partial_bytes(nM0, S, parts) bytes.
 uint32_t oct_parts(const LsParams &p, uint32_t numSms);
 size_t oct_partial_bytes(uint32_t nM0, uint32_t S, uint32_t parts);
+// tt64: the displaced midpoint and time in FP64 (HPSS_PREC_FP64_TRAVELTIME).
 cudaError_t launch_ls_oct(const LsParams &p, uint32_t numSms, void *partial, uint32_t parts,
-                          cudaStream_t st);
+                          cudaStream_t st, bool tt64 = false);
+// Tuned pair kernel with a precision mode (prec: kPrecTt64 | kPrecCompensated,
+// not 0), shape 1 (one candidate pair per thread, 3 CTAs/SM; chunk of 16),
+// linear sum from the per-tap sums (ls_tuned_prec.cu).
+cudaError_t launch_ls_tuned_prec(const LsParams &p, int model, int prec, uint32_t grid,
+                                 uint32_t tiles, uint32_t nUnits, cudaStream_t st);
 // Per-trace factors of the OCT formulas for half-offset h0 (ls_oct.cu).
 cudaError_t launch_oct_trace_table(const float *mid, const float *hoff, uint32_t n, float h0,
                                    float4 *tab, cudaStream_t st);

@@ -208,11 +208,16 @@ hpss_status linear_search_impl(hpss_handle h, const float *d_m0s, uint32_t nM0,
     // kTunedVariants shapes (candidate pairs per thread x CTAs per SM), OCT the
     // branchy kernel (4 candidates per thread).  The chunk bounds depend on
     // the chunk size (8 warps x candidates per thread).
-    // precision modes run on the plain kernel
-    const bool pairKernel = tuned && h->precisionMode == 0 && h->model != HPSS_MODEL_OCT &&
-                            lp.w <= 15 && h->stride + 8 <= (uint32_t)tuned_stage_floats_min();
-    const bool octKernel =
-        tuned && h->precisionMode == 0 && h->model == HPSS_MODEL_OCT && lp.w <= 15;
+    // Precision modes: CMP / ZO-CRS run the pair kernel's precision
+    // instantiations (shape 1, not autotuned); OCT the OCT kernel with the
+    // FP64 traveltime; OCT with compensated sums runs the plain kernel.
+    // Every step in FP64 (kPrecF64) runs the FP64 kernel whatever is asked.
+    const int prec = h->precisionMode;
+    const bool f64 = (prec & kPrecF64) != 0;
+    const bool pairKernel = tuned && !f64 && h->model != HPSS_MODEL_OCT && lp.w <= 15 &&
+                            h->stride + 8 <= (uint32_t)tuned_stage_floats_min();
+    const bool octKernel = tuned && !f64 && h->model == HPSS_MODEL_OCT && lp.w <= 15 &&
+                           !(prec & kPrecCompensated);
     // chunk bounds (read by the pair kernel only), rebuilt when the chunk size
     // or the grid changed
     auto setChunks = [&](int perThread) -> cudaError_t {
@@ -306,7 +311,9 @@ hpss_status linear_search_impl(hpss_handle h, const float *d_m0s, uint32_t nM0,
             if (e0 != cudaSuccess) return e0;
         }
         cudaError_t e =
-            h->model == HPSS_MODEL_CMP
+            prec ? launch_ls_tuned_prec(q, h->model, prec, grid, tiles, (uint32_t)nUnits,
+                                        h->stream)
+            : h->model == HPSS_MODEL_CMP
                 ? launch_ls_tuned_cmp(q, grid, tiles, (uint32_t)nUnits, h->stream, variant,
                                       exactStack)
                 : launch_ls_tuned_zocrs(q, grid, tiles, (uint32_t)nUnits, h->stream, variant,
@@ -315,7 +322,10 @@ hpss_status linear_search_impl(hpss_handle h, const float *d_m0s, uint32_t nM0,
         return launch_merge_parts(q, q.parts, q.partial, h->stream);
     };
     int variant = 0;
-    if (pairKernel) {
+    if (pairKernel && prec) {
+        variant = 1;  // the precision instantiations' shape
+        HPSS_CUDA_TRY(h, setChunks(2 * kVariantPairs[variant]));
+    } else if (pairKernel) {
         // the autotuner's timing launches (a prefix of the units) count no
         // near-ties
         unsigned long long *ties = lp.nearTies;
@@ -339,9 +349,10 @@ hpss_status linear_search_impl(hpss_handle h, const float *d_m0s, uint32_t nM0,
         lp.unitCounter = unitCounter;
         HPSS_CUDA_TRY(h, cudaMemsetAsync(unitCounter, 0, sizeof(uint32_t), h->stream));
         HPSS_CUDA_TRY(h, launch_ls_oct(lp, (uint32_t)num_sms(h), h->partial.p, octParts,
-                                       h->stream));
+                                       h->stream, (prec & kPrecTt64) != 0));
     } else {
-        HPSS_CUDA_TRY(h, launch_ls_plain(lp, h->stream, h->precisionMode));
+        HPSS_CUDA_TRY(h, f64 ? launch_ls_f64(lp, h->stream)
+                             : launch_ls_plain(lp, h->stream, h->precisionMode));
     }
     h->lastVariant = pairKernel ? variant : -1;
     h->lastParts = pairKernel ? lastParts : octKernel ? octParts : 1;

@@ -57,7 +57,13 @@ constexpr int kOctMhBatch = 4;
 // slowest one is done.  Warp units are taken from the work queue one warp
 // at a time; without the queue CTA b's warps take the slots of units b,
 // b + grid, ... (the warps of a CTA read the same trace rows).
-template <int W>
+//
+// TT64 (precision mode HPSS_PREC_FP64_TRAVELTIME): every trace the box test
+// keeps gets the displaced midpoint and time in FP64 (oct_time_f64, the
+// plain kernel's form: same bits), one trace at a time; the box test's
+// margins cover the FP32 forms, and the FP64 values lie closer to the exact
+// ones.
+template <int W, bool TT64>
 __global__ void __launch_bounds__(kOctWarps * 32, 4)
 ls_oct_kernel(LsParams a, uint32_t tiles, uint32_t parts, uint32_t chunksPerPart,
               uint32_t nWarpUnits, PartBest *partial) {
@@ -109,6 +115,29 @@ ls_oct_kernel(LsParams a, uint32_t tiles, uint32_t parts, uint32_t chunksPerPart
             for (int j = 0; j < W; j++) num[j] = 0.f;
             float lin = 0.f, den = 0.f;
             unsigned used = 0, nu = 0;
+            // FP64 traveltime of one trace (TT64), then its window
+            auto evalTt64 = [&](uint32_t ti) {
+                float t;
+                const int ok = oct_time_f64(t0, cc, sl, a.mid[ti], a.hoff[ti], m0, a.apm, ol.h0, &t);
+                if (ok < 0) {
+                    nu++;
+                    return;
+                }
+                if (ok == 0) return;
+                const WinIdx wi = window_index(t, a.dt);
+                if (window_in_trace(wi.k, tau, S)) {
+                    float y[W + 1];
+                    load_window(a, ti, wi.k - tau, y);
+#pragma unroll
+                    for (int jj = 0; jj < W; jj++) {
+                        const float u = (y[jj + 1] - y[jj]) * wi.frac + y[jj];
+                        num[jj] += u;
+                        lin += u;
+                        den += u * u;
+                    }
+                    used++;
+                }
+            };
             if (boxOn) {
                 // blocks of 32 traces: lane j tests trace qb + j for the whole
                 // warp, then the warp evaluates the traces kept, in order
@@ -121,6 +150,12 @@ ls_oct_kernel(LsParams a, uint32_t tiles, uint32_t parts, uint32_t chunksPerPart
                     }
                     uint32_t mask = __ballot_sync(0xffffffffu, keep);
                     nu += n - (uint32_t)__popc(mask);
+                    if constexpr (TT64) {
+                        for (; mask; mask &= mask - 1) {
+                            const uint32_t bit = (uint32_t)__ffs(mask) - 1;
+                            evalTt64(a.selIdx ? a.selIdx[first + qb + bit] : first + qb + bit);
+                        }
+                    }
                     while (mask) {
                         uint32_t tb[kOctMhBatch];
                         bool live[kOctMhBatch];
@@ -140,6 +175,9 @@ ls_oct_kernel(LsParams a, uint32_t tiles, uint32_t parts, uint32_t chunksPerPart
                 // displaced-midpoint tests of kOctMhBatch traces side by side,
                 // then the passing traces in order; the rest one by one
                 uint32_t q = 0;
+                if constexpr (TT64) {
+                    for (; q < cnt; q++) evalTt64(a.selIdx ? a.selIdx[first + q] : first + q);
+                }
                 for (; q + kOctMhBatch <= cnt; q += kOctMhBatch) {
                     uint32_t tb[kOctMhBatch];
                     bool live[kOctMhBatch];
@@ -257,7 +295,7 @@ uint32_t oct_chunks(uint32_t P) {
     return (P + kOctWarps * R - 1) / (kOctWarps * R);
 }
 
-template <int W>
+template <int W, bool TT64>
 cudaError_t launch_oct_w(const LsParams &p, uint32_t numSms, void *partial, uint32_t parts,
                          cudaStream_t st) {
     const uint32_t tiles = (p.S + 31) / 32;
@@ -268,7 +306,7 @@ cudaError_t launch_oct_w(const LsParams &p, uint32_t numSms, void *partial, uint
     // warp-unit indices (and the queue counter past the last unit) stay below 2^31
     if (units * kOctWarps > 0x7fffffffull) return cudaErrorInvalidConfiguration;
     int perSm = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, ls_oct_kernel<W>,
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, ls_oct_kernel<W, TT64>,
                                                                   kOctWarps * 32, 0);
     if (e != cudaSuccess) return e;
     const uint32_t grid =
@@ -276,7 +314,7 @@ cudaError_t launch_oct_w(const LsParams &p, uint32_t numSms, void *partial, uint
     // one wave: every unit has its own CTA, the work queue only adds latency
     LsParams q = p;
     if (units <= grid) q.unitCounter = nullptr;
-    ls_oct_kernel<W><<<grid, kOctWarps * 32, 0, st>>>(
+    ls_oct_kernel<W, TT64><<<grid, kOctWarps * 32, 0, st>>>(
         q, tiles, parts, chunksPerPart, (uint32_t)(units * kOctWarps),
         static_cast<PartBest *>(partial));
     e = cudaGetLastError();
@@ -295,19 +333,26 @@ uint32_t oct_parts(const LsParams &p, uint32_t numSms) {
     return (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(parts, oct_chunks<R>(p.P)));
 }
 
-cudaError_t launch_ls_oct(const LsParams &p, uint32_t numSms, void *partial, uint32_t parts,
-                          cudaStream_t st) {
+template <bool TT64>
+cudaError_t launch_ls_oct_t(const LsParams &p, uint32_t numSms, void *partial, uint32_t parts,
+                            cudaStream_t st) {
     switch (p.w) {
-        case 1: return launch_oct_w<1>(p, numSms, partial, parts, st);
-        case 3: return launch_oct_w<3>(p, numSms, partial, parts, st);
-        case 5: return launch_oct_w<5>(p, numSms, partial, parts, st);
-        case 7: return launch_oct_w<7>(p, numSms, partial, parts, st);
-        case 9: return launch_oct_w<9>(p, numSms, partial, parts, st);
-        case 11: return launch_oct_w<11>(p, numSms, partial, parts, st);
-        case 13: return launch_oct_w<13>(p, numSms, partial, parts, st);
-        case 15: return launch_oct_w<15>(p, numSms, partial, parts, st);
+        case 1: return launch_oct_w<1, TT64>(p, numSms, partial, parts, st);
+        case 3: return launch_oct_w<3, TT64>(p, numSms, partial, parts, st);
+        case 5: return launch_oct_w<5, TT64>(p, numSms, partial, parts, st);
+        case 7: return launch_oct_w<7, TT64>(p, numSms, partial, parts, st);
+        case 9: return launch_oct_w<9, TT64>(p, numSms, partial, parts, st);
+        case 11: return launch_oct_w<11, TT64>(p, numSms, partial, parts, st);
+        case 13: return launch_oct_w<13, TT64>(p, numSms, partial, parts, st);
+        case 15: return launch_oct_w<15, TT64>(p, numSms, partial, parts, st);
         default: return cudaErrorNotSupported;
     }
+}
+
+cudaError_t launch_ls_oct(const LsParams &p, uint32_t numSms, void *partial, uint32_t parts,
+                          cudaStream_t st, bool tt64) {
+    return tt64 ? launch_ls_oct_t<true>(p, numSms, partial, parts, st)
+                : launch_ls_oct_t<false>(p, numSms, partial, parts, st);
 }
 
 }  // namespace hpss

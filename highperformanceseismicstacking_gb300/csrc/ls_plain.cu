@@ -26,55 +26,6 @@ namespace hpss {
 //   Kahan-Babuska sum): sum + compensation, the compensation added once at
 //   the end.
 
-// ZO-CRS time with an FP64 squared time; 0: window skipped (negative square).
-__device__ __forceinline__ int zocrs_time_f64(float t0, float c, float a, float b, float dm,
-                                              float h, float *t) {
-    const double x = (double)t0 + (double)a * (double)dm;
-    const double tmp = x * x + (double)b * (double)dm * (double)dm + (double)c * (double)h * (double)h;
-    if (tmp < 0) return 0;
-    *t = (float)sqrt(tmp);
-    return 1;
-}
-
-// OCT displaced midpoint and time in FP64 (same formulas as
-// oct/common.cuh:7-94); returns as model_time<kModelOct>.
-__device__ __forceinline__ int oct_time_f64(float t0f, float cf, float slopef, float mf, float hf,
-                                            float m0f, float apm, float h0f, float *t) {
-    const double t0 = t0f, c = cf, slope = slopef, m = mf, h = hf, m0 = m0f, h0 = h0f;
-    const double theta = t0 * slope;
-    const double gamma = 2 * sqrt(h * h + h0 * h0);
-    const double tn0_sq = t0 * t0 - c * h0 * h0;
-    const double theta_sq = theta * theta, gamma_sq = gamma * gamma, tn0_quad = tn0_sq * tn0_sq;
-    double arg = tn0_quad * tn0_quad + tn0_quad * theta_sq * gamma_sq +
-                 16 * h * h * h0 * h0 * theta_sq * theta_sq;
-    if (arg < 0) return -1;
-    arg = theta_sq * gamma_sq + 2 * tn0_quad + 2 * sqrt(arg);
-    if (arg == 0) return -1;
-    const double mh = m0 + 2 * theta * (h * h - h0 * h0) / sqrt(arg);
-    if (fabs(m - mh) > (double)apm) return -1;
-    const double w1 = (h + h0) * (h + h0) - (mh - m0) * (mh - m0);
-    const double w2 = (h - h0) * (h - h0) - (mh - m0) * (mh - m0);
-    if (w1 < 0 || w2 < 0) return 0;
-    const double u = sqrt(w1) + sqrt(w2);
-    double th = t0;
-    if (fabs(h) > fabs(h0)) {
-        if (!u) return 0;
-        const double sa = c * h * h + 4 * h * h / (u * u) * tn0_sq;
-        if (sa < 0) return 0;
-        th = sqrt(sa);
-    } else if (fabs(h) < fabs(h0)) {
-        if (!h0) return 0;
-        const double sa = c * h * h + u * u / (4 * h0 * h0) * tn0_sq;
-        if (sa < 0) return 0;
-        th = sqrt(sa);
-    }
-    const double tn_sq = th * th - c * h * h;
-    if (!th || !tn0_sq) return 0;
-    const double ah = (t0 * tn_sq) / (th * tn0_sq) * slope;
-    *t = (float)(th + ah * (m - mh));
-    return 1;
-}
-
 // Neumaier step: s + x with the rounding error of the add kept in comp.
 __device__ __forceinline__ void neumaier(float &s, float &comp, float x) {
     const float t = __fadd_rn(s, x);
@@ -130,7 +81,7 @@ ls_plain_kernel(LsParams a) {
             float t;
             int ok;
             if ((MODE & kPrecTt64) && MODEL == kModelZocrs)
-                ok = zocrs_time_f64(t0, c, p1, p2, a.mid[ti] - m0, a.hoff[ti], &t);
+                ok = zocrs_time_tt64(t0, c, p1, p2, a.mid[ti] - m0, a.hsq[ti], &t) ? 1 : 0;
             else if ((MODE & kPrecTt64) && MODEL == kModelOct)
                 ok = oct_time_f64(t0, c, p1, a.mid[ti], a.hoff[ti], m0, a.apm, h0, &t);
             else

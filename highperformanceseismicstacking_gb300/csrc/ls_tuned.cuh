@@ -200,9 +200,22 @@ __device__ __forceinline__ float half_bits_to_float(unsigned bits) {
 // as the sum of the W per-tap numerator sums at the end (the same quantity
 // summed in another order: one FADD2 per tap less, the stack within a few
 // ulp).  Semblance and the chosen candidate are identical either way.
-template <int MODEL, int W, int NP, int MINB, bool EXACT_STACK>
+//
+// PREC: precision modes (HPSS_PREC_*; 0 = the reference's FP32 arithmetic).
+//  * kPrecTt64 (ZO-CRS): the squared time in FP64, the time rounded to FP32
+//    once (zocrs_time_tt64, the plain kernel's form: same bits);
+//  * kPrecCompensated: when window x selected traces exceeds 4096 terms, the
+//    window sums are compensated across staging rounds: each round (the
+//    traces one stage holds, at most 256) is summed in FP32 as usual, and
+//    the round's sums are added into running totals with Knuth's two-sum,
+//    their rounding errors kept in compensation terms and added once at the
+//    end.  The error is then that of one round's plain sum instead of the
+//    whole aperture's.
+template <int MODEL, int W, int NP, int MINB, bool EXACT_STACK, int PREC = 0>
 __global__ void __launch_bounds__(kTunedThreads, MINB)
 ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
+    constexpr bool TT64 = (PREC & kPrecTt64) != 0 && MODEL == kModelZocrs;
+    constexpr bool COMP = (PREC & kPrecCompensated) != 0;
     constexpr int kStage = Stage2<MINB>::kFloats;
     constexpr int R = 2 * NP;
     extern __shared__ __align__(16) unsigned char smemRaw[];
@@ -298,6 +311,20 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
 #pragma unroll
                 for (int j = 0; j < W; j++) num[q][j] = f2(0.f, 0.f);
                 lin[q] = den[q] = f2(0.f, 0.f);
+            }
+            // compensated sums: running totals and compensations over the
+            // staging rounds (COMP, more than 4096 window x trace terms)
+            const bool comp = COMP && (uint64_t)W * cnt > 4096u;
+            float2 numT[COMP ? NP : 1][COMP ? W : 1], numC[COMP ? NP : 1][COMP ? W : 1];
+            float2 linT[COMP ? NP : 1], linC[COMP ? NP : 1], denT[COMP ? NP : 1],
+                denC[COMP ? NP : 1];
+            if constexpr (COMP) {
+#pragma unroll
+                for (int q = 0; q < NP; q++) {
+#pragma unroll
+                    for (int j = 0; j < W; j++) numT[q][j] = numC[q][j] = f2(0.f, 0.f);
+                    linT[q] = linC[q] = denT[q] = denC[q] = f2(0.f, 0.f);
+                }
             }
 #pragma unroll
             for (int r = 0; r < R; r++) used[r] = 0;
@@ -427,19 +454,29 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
                         const float2 cq = f2(cc[2 * qq], cc[2 * qq + 1]);
                         const float2 hsq2 = f2(md.hsq, md.hsq);
                         float2 t2;
-                        if (MODEL == kModelCmp) {
-                            t2 = __ffma2_rn(cq, hsq2, t0sq2);
-                        } else {
-                            const float2 dm2 = f2(md.dm, md.dm);
-                            const float2 x = __ffma2_rn(f2(c1[2 * qq], c1[2 * qq + 1]), dm2, t0p2);
-                            const float2 bd = __fmul2_rn(f2(c2[2 * qq], c2[2 * qq + 1]), dm2);
-                            t2 = __ffma2_rn(cq, hsq2, __ffma2_rn(bd, dm2, __fmul2_rn(x, x)));
-                        }
                         float2 t;
-                        if (MODEL == kModelCmp || FULL) {
-                            t = f2(sqrtf(t2.x), sqrtf(t2.y));
+                        if constexpr (TT64) {
+                            // FP64 squared time; t2 carries only its sign
+                            bool pa = zocrs_time_tt64(t0, cc[2 * qq], c1[2 * qq], c2[2 * qq],
+                                                      md.dm, md.hsq, &t.x);
+                            bool pb = zocrs_time_tt64(t0, cc[2 * qq + 1], c1[2 * qq + 1],
+                                                      c2[2 * qq + 1], md.dm, md.hsq, &t.y);
+                            t2 = f2(pa ? 1.f : -1.f, pb ? 1.f : -1.f);
                         } else {
-                            t = f2(sqrtf(fmaxf(t2.x, 0.f)), sqrtf(fmaxf(t2.y, 0.f)));
+                            if (MODEL == kModelCmp) {
+                                t2 = __ffma2_rn(cq, hsq2, t0sq2);
+                            } else {
+                                const float2 dm2 = f2(md.dm, md.dm);
+                                const float2 x =
+                                    __ffma2_rn(f2(c1[2 * qq], c1[2 * qq + 1]), dm2, t0p2);
+                                const float2 bd = __fmul2_rn(f2(c2[2 * qq], c2[2 * qq + 1]), dm2);
+                                t2 = __ffma2_rn(cq, hsq2, __ffma2_rn(bd, dm2, __fmul2_rn(x, x)));
+                            }
+                            if (MODEL == kModelCmp || FULL) {
+                                t = f2(sqrtf(t2.x), sqrtf(t2.y));
+                            } else {
+                                t = f2(sqrtf(fmaxf(t2.x, 0.f)), sqrtf(fmaxf(t2.y, 0.f)));
+                            }
                         }
                         // t / dt: the fast-math quotient equals t * (1/dt)
                         // bit for bit, so the reciprocal is taken once
@@ -510,13 +547,18 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
                 auto checkFull = [&](const TraceMeta2 &md, int j) {
                     if (md.len >= 0) return;
                     for (int r = 0; r < R; r++) {
-                        float t2;
+                        float t2, tt;
                         if (MODEL == kModelCmp) {
                             t2 = __fmaf_rn(cc[r], md.hsq, __fmul_rn(t0, t0));
+                            tt = sqrtf(t2);
+                        } else if (TT64) {
+                            t2 = zocrs_time_tt64(t0, cc[r], c1[r], c2[r], md.dm, md.hsq, &tt)
+                                     ? 1.f : -1.f;
                         } else {
                             t2 = zocrs_t2(t0, cc[r], c1[r], c2[r], md.dm, md.hsq);
+                            tt = sqrtf(fmaxf(t2, 0.f));
                         }
-                        const float ti = __fmul_rn(sqrtf(fmaxf(t2, 0.f)), rdt);
+                        const float ti = __fmul_rn(tt, rdt);
                         const int k = (int)ti;
                         const int b = md.base + k - tau;
                         if ((MODEL != kModelCmp && !(t2 > 0.f)) ||
@@ -563,6 +605,40 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
                     j++;
                 }
                 q0 += nfit;
+                if constexpr (COMP) {
+                    // fold this round's sums into the compensated totals
+                    if (comp) {
+#pragma unroll
+                        for (int qq = 0; qq < NP; qq++) {
+#pragma unroll
+                            for (int jj = 0; jj < W; jj++) {
+                                two_sum_acc(numT[qq][jj].x, numC[qq][jj].x, num[qq][jj].x);
+                                two_sum_acc(numT[qq][jj].y, numC[qq][jj].y, num[qq][jj].y);
+                                num[qq][jj] = f2(0.f, 0.f);
+                            }
+                            two_sum_acc(denT[qq].x, denC[qq].x, den[qq].x);
+                            two_sum_acc(denT[qq].y, denC[qq].y, den[qq].y);
+                            den[qq] = f2(0.f, 0.f);
+                            if (EXACT_STACK) {
+                                two_sum_acc(linT[qq].x, linC[qq].x, lin[qq].x);
+                                two_sum_acc(linT[qq].y, linC[qq].y, lin[qq].y);
+                                lin[qq] = f2(0.f, 0.f);
+                            }
+                        }
+                    }
+                }
+            }
+            if constexpr (COMP) {
+                if (comp) {
+#pragma unroll
+                    for (int qq = 0; qq < NP; qq++) {
+#pragma unroll
+                        for (int jj = 0; jj < W; jj++)
+                            num[qq][jj] = __fadd2_rn(numT[qq][jj], numC[qq][jj]);
+                        den[qq] = __fadd2_rn(denT[qq], denC[qq]);
+                        lin[qq] = __fadd2_rn(linT[qq], linC[qq]);
+                    }
+                }
             }
 
 #pragma unroll
@@ -637,14 +713,14 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
     }
 }
 
-template <int MODEL, int NP, int MINB, bool EXACT_STACK>
+template <int MODEL, int NP, int MINB, bool EXACT_STACK, int PREC = 0>
 cudaError_t launch_ls_tuned2_model(const LsParams &p, uint32_t grid,
                                    uint32_t tiles, uint32_t nUnits,
                                    cudaStream_t st) {
     const size_t smem = sizeof(Tuned2Smem<MINB>);
 #define HPSS_TUNED2_CASE(WV)                                                  \
     case WV: {                                                                \
-        auto k = ls_tuned2_kernel<MODEL, WV, NP, MINB, EXACT_STACK>;         \
+        auto k = ls_tuned2_kernel<MODEL, WV, NP, MINB, EXACT_STACK, PREC>;   \
         cudaError_t e = cudaFuncSetAttribute(                                 \
             k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);       \
         if (e != cudaSuccess) return e;                                       \

@@ -168,13 +168,22 @@ hpss_status hpss_set_grid_mode(hpss_handle h, int mode);
 /* Precision modes of the linear search (no reference counterpart; the
  * default 0 is the reference's FP32 arithmetic).  FP64_TRAVELTIME forms the
  * ZO-CRS / OCT traveltime in FP64 (square-root arguments, divisions, the
- * displaced midpoint) and rounds it to FP32 once; COMPENSATED accumulates
- * the window sums with Neumaier's compensated summation when window x
- * selected traces exceeds 4096 terms.  Either flag runs the plain kernel
- * family (the tuned kernels implement the reference's arithmetic only).
+ * displaced midpoint) and rounds it to FP32 once (CMP: no effect);
+ * COMPENSATED compensates the window sums when window x selected traces
+ * exceeds 4096 terms.  Both run in the tuned kernels: CMP / ZO-CRS in one
+ * fixed shape (no autotuning; FP64 traveltime bit-identical to the plain
+ * kernel's), summing each staging round (at most 256 traces) in FP32 and
+ * adding the rounds with Knuth's two-sum; OCT with the FP64 traveltime in
+ * the OCT kernel (bit-identical to the plain kernel's).  The plain kernel,
+ * and OCT with COMPENSATED, compensate every term (Neumaier).
  * Interpolation stays FP32. */
 #define HPSS_PREC_FP64_TRAVELTIME 1
 #define HPSS_PREC_COMPENSATED 2
+/* Every step in FP64 -- traveltime, window index and fraction,
+ * interpolation, sums, semblance, argmax -- rounded to FP32 once at the end:
+ * the FP64 reference the other modes are judged against (at a small
+ * fraction of the FP32 throughput; overrides the other flags). */
+#define HPSS_PREC_FP64 4
 hpss_status hpss_set_precision(hpss_handle h, int flags);
 
 /* OCT over several target half-offsets in one call (no reference
