@@ -25,7 +25,9 @@
 //    ties), raw parameters (velocity, not 4/v^2)        (selectBestIndividualsFor*)
 // The random stream differs: Philox-4x32-10 (Salmon et al., SC'11), keyed by
 // the seed and countered by (midpoint, sample, individual, draw), instead of
-// curand XORWOW seeded from time(NULL).
+// curand XORWOW seeded from time(NULL).  The midpoint enters as its FP32 bit
+// pattern, so a midpoint draws the same numbers whatever else its call holds
+// (other midpoints, other half-offsets, another process's shard).
 #include <algorithm>
 
 #include "hpss_device.cuh"
@@ -411,7 +413,7 @@ de_kernel(DeParams d, uint32_t spc, uint32_t groups, uint32_t nUnits) {
         const float m0 = a.m0s[mi];
         const uint32_t first = a.selFirst[mi], cnt = a.selCount[mi];
         const OctLine ol = oct_line(a, mi);          // OCT: the midpoint's h0 and table
-        const uint32_t mkey = m0_in_block(a, mi);    // random-stream key of the midpoint
+        const uint32_t mkey = __float_as_uint(m0);   // random-stream key of the midpoint
         const float t0 = static_cast<float>(active ? s : 0) * a.dt;
         const float s0f = static_cast<float>((unit % groups) * spc);  // the CTA's first sample
         float *xs = X + (size_t)(member ? ls : 0) * pop * NP;  // this sample's population
@@ -542,7 +544,7 @@ __global__ void de_select_oct_flags_kernel(DeParams d, const uint32_t *candFirst
     const uint32_t ti = candFirst[mi] + (uint32_t)(g - a.selFirst[mi]);
     const float m0 = a.m0s[mi];
     const float h0 = oct_line(a, mi).h0;
-    const uint32_t mkey = m0_in_block(a, mi);
+    const uint32_t mkey = __float_as_uint(m0);
     const float m = a.mid[ti], h = a.hoff[ti];
     bool used = false;
     for (uint32_t s = 0; s < a.S && !used; s++) {

@@ -31,8 +31,8 @@ hpss_status de_impl(hpss_handle h, const float *d_m0s, uint32_t nM0, uint32_t po
     d.ls.out = d_out;
     HPSS_CUDA_TRY(h, use_oct_table(h, d.ls));
     // OCT over several half-offsets: the midpoints in h0 blocks, one launch
-    // over all of them (the random stream is keyed by the midpoint's index
-    // in its block, so block b equals a one-h0 call at h0s[b])
+    // over all of them (the random stream is keyed by the midpoint's value,
+    // so block b equals a one-h0 call at h0s[b])
     HPSS_CUDA_TRY(h, expand_h0_blocks(h, d.ls));
     d_m0s = d.ls.m0s;
     nM0 = d.ls.nM0;

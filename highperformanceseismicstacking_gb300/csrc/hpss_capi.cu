@@ -290,6 +290,17 @@ int num_sms(hpss_handle h) {
     return v > 0 ? v : 1;
 }
 
+// 16-bit storage: the FP32 staging area of an upload, released once the
+// upload's copies and conversions have finished (stream synchronised), so
+// no FP32 rows stay resident.
+void release_upload_staging(hpss_handle h) {
+    if (h->storage == HPSS_STORAGE_FP32 || !h->dSamples) return;
+    cudaFree(h->dSamples);
+    h->deviceBytes -= h->capSamples;
+    h->dSamples = nullptr;
+    h->capSamples = 0;
+}
+
 // Rows of the FP32 staging area of a 16-bit upload (about 64 MB).
 size_t stage_rows(hpss_handle h) {
     constexpr size_t kStageBytes = size_t(64) << 20;
@@ -346,17 +357,32 @@ hpss_status prepare_line(hpss_handle h, const float *samples, const float *midpo
     h->hHsq.resize(nTraces);
     for (uint32_t i = 0; i < nTraces; i++) h->hHsq[i] = halfoffsets[i] * halfoffsets[i];
     const size_t n = nTraces, st = h->stride;
+    // the line is resident in one storage only: a buffer of the other one
+    // left by an earlier line is released (and the FP32 buffer shrunk to the
+    // staging area of a 16-bit upload)
+    auto release_line_buffer = [&](void **p, size_t &cap) {
+        if (*p) {
+            cudaFree(*p);
+            h->deviceBytes -= cap;
+        }
+        *p = nullptr;
+        cap = 0;
+    };
     if (storage == HPSS_STORAGE_FP32) {
+        release_line_buffer(reinterpret_cast<void **>(&h->dSamples16), h->capSamples16);
         HPSS_CUDA_TRY(h, grow_line_buffer(h, reinterpret_cast<void **>(&h->dSamples),
                                           h->capSamples, n * st * sizeof(float)));
     } else {
         // 16-bit storage: the line lives in 16-bit rows only; the FP32 rows
-        // pass through a staging area of at most kStageBytes on their way
+        // pass through a staging area of at most about 64 MB on their way,
+        // released when the upload is done (release_upload_staging)
+        const size_t stageBytes = std::min<size_t>(n, stage_rows(h)) * st * sizeof(float);
+        if (h->capSamples > std::max<size_t>(stageBytes, 16))
+            release_line_buffer(reinterpret_cast<void **>(&h->dSamples), h->capSamples);
         HPSS_CUDA_TRY(h, grow_line_buffer(h, reinterpret_cast<void **>(&h->dSamples16),
                                           h->capSamples16, n * st * sizeof(uint16_t)));
         HPSS_CUDA_TRY(h, grow_line_buffer(h, reinterpret_cast<void **>(&h->dSamples),
-                                          h->capSamples,
-                                          std::min<size_t>(n, stage_rows(h)) * st * sizeof(float)));
+                                          h->capSamples, stageBytes));
     }
     // mid, hoff, hsq and the 16-bit storage scale: four 256-byte aligned
     // slices of one buffer
@@ -499,6 +525,7 @@ hpss_status hpss_upload_gather(hpss_handle h, const float *samples,
                                          (size_t)nTraces * h->stride * sizeof(float), h->stream));
     HPSS_CUDA_TRY(h, copy_line_rows(h, samples, 0, nTraces, h->stream));
     HPSS_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    release_upload_staging(h);
     h->gatherReady = true;
     return HPSS_OK;
 }

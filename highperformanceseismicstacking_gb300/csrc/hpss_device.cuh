@@ -489,11 +489,6 @@ __device__ __forceinline__ OctLine oct_line(const LsParams &a, uint32_t mi) {
     }
     return l;
 }
-// The midpoint's index within its h0 block (keys of the DE random stream, so
-// that a block of a batched call draws what a one-h0 call would).
-__device__ __forceinline__ uint32_t m0_in_block(const LsParams &a, uint32_t mi) {
-    return a.m0PerH0 ? mi % a.m0PerH0 : mi;
-}
 
 // Window amplitudes y[0..n) of trace ti from sample k as FP32: the FP32 row,
 // or the 16-bit row widened (BF16: the high half of an FP32 word; FP16:

@@ -83,6 +83,8 @@ uint32_t h0_blocks(hpss_handle h);
 // changes.
 cudaError_t expand_h0_blocks(hpss_handle h, LsParams &lp);
 int num_sms(hpss_handle h);
+// 16-bit storage: free the FP32 staging area of a finished upload.
+void release_upload_staging(hpss_handle h);
 // Amplitudes of traces [a, b) of a line being uploaded, on stream st.
 cudaError_t copy_line_rows(hpss_handle h, const float *samples, uint32_t a, uint32_t b,
                            cudaStream_t st);

@@ -440,6 +440,7 @@ hpss_status stream_line_and_search(hpss_handle h, const float *samples, const fl
     if (nM0 == 0) {
         HPSS_CUDA_TRY(h, cudaStreamSynchronize(h->copyStream));
         HPSS_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+        release_upload_staging(h);
         if (stats) std::memset(stats, 0, sizeof(*stats));
         return HPSS_OK;
     }
@@ -507,6 +508,7 @@ hpss_status stream_line_and_search(hpss_handle h, const float *samples, const fl
     HPSS_CUDA_TRY(h, back(G - 1));
     HPSS_CUDA_TRY(h, cudaStreamSynchronize(h->copyStream));
     HPSS_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    release_upload_staging(h);
     const char *counters = static_cast<const char *>(h->notUsed.p);
     uint32_t err = 0;
     unsigned long long ties = 0;

@@ -254,7 +254,9 @@ hpss_status hpss_linear_search_device(hpss_handle h, const float *d_m0s,
  * runtime values (the reference compiles F = 0.85, CR = 0.5,
  * interface.h:5-6); `generations` counts the initial evaluation as the
  * reference does.  The random stream is a counter-based generator keyed by
- * `seed` (the reference's curand stream is seeded from time(NULL)).
+ * `seed` and by each midpoint's value (the reference's curand stream is
+ * seeded from time(NULL)): a midpoint's result does not depend on the other
+ * midpoints, half-offsets or shards of the call.
  * out (host): [nM0][2 + nParams][S] with RAW parameters (velocity, not 4/v^2),
  * as selectBestIndividualsFor* write them. */
 hpss_status hpss_differential_evolution(hpss_handle h, const float *m0s,

@@ -144,7 +144,8 @@ void oracle_select(int model, const float *mid, const float *hoff,
 /* ---- differential evolution helpers (engine's random stream) ----------
  * Philox-4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11), as the engine keys it:
  * key = seed (lo, hi words); counter = (gen << 8 | draw block, individual,
- * sample, midpoint index).  Uniforms in (0, 1]: ((v >> 8) + 1) * 2^-24. */
+ * sample, midpoint key: the midpoint's FP32 bit pattern).  Uniforms in (0, 1]:
+ * ((v >> 8) + 1) * 2^-24. */
 static void philox4x32_10(uint32_t c[4], uint32_t k0, uint32_t k1) {
     for (int r = 0; r < 10; r++) {
         uint64_t p0 = (uint64_t)0xD2511F53u * c[0];
@@ -161,7 +162,7 @@ static void philox4x32_10(uint32_t c[4], uint32_t k0, uint32_t k1) {
 
 static float u01(uint32_t v) { return (float)((v >> 8) + 1u) * (1.0f / 16777216.0f); }
 
-/* First n uniforms of the stream of (midpoint index, sample, individual,
+/* First n uniforms of the stream of (midpoint key, sample, individual,
  * generation). */
 void oracle_de_uniforms(uint64_t seed, uint32_t m0i, uint32_t s, uint32_t ind,
                         uint32_t gen, uint32_t n, float *out) {

@@ -281,6 +281,11 @@ def _de_sigs():
     return L
 
 
+def de_key(m0: float) -> int:
+    """The DE random stream's midpoint key: the midpoint's FP32 bit pattern."""
+    return int(np.asarray(m0, np.float32).view(np.uint32))
+
+
 def de_uniforms(seed: int, m0i: int, s: int, ind: int, gen: int, n: int) -> np.ndarray:
     out = np.zeros(n, np.float32)
     _de_sigs().oracle_de_uniforms(seed, m0i, s, ind, gen, n, _f(out))
@@ -288,7 +293,8 @@ def de_uniforms(seed: int, m0i: int, s: int, ind: int, gen: int, n: int) -> np.n
 
 
 def de_initial_population(seed: int, m0i: int, S: int, pop: int, lower, upper) -> np.ndarray:
-    """[S][pop][np] raw initial individuals of midpoint index m0i."""
+    """[S][pop][np] raw initial individuals of the midpoint whose stream key
+    is m0i (de_key(m0))."""
     lo = np.asarray(lower, np.float32)
     hi = np.asarray(upper, np.float32)
     out = np.zeros((S, pop, lo.size), np.float32)

@@ -65,7 +65,8 @@ def test_de_single_generation_is_best_initial_individual(engine):
     m0s = line.cdp_midpoints[:1]
     seed, pop = 77, 24
     de, _ = engine.differential_evolution(m0s, pop, 1, 0.85, 0.5, seed=seed)
-    init = oracle.de_initial_population(seed, 0, line.samples_per_trace, pop, lower, upper)
+    init = oracle.de_initial_population(seed, oracle.de_key(m0s[0]), line.samples_per_trace,
+                                        pop, lower, upper)
     sel = np.nonzero(line.midpoints == m0s[0])[0].astype(np.uint32)
     sem, _ = oracle.eval_raw("cmp", line.samples, line.midpoints, line.halfoffsets, sel,
                              m0s[0], float(line.dt), 2, init, precision="f32")
@@ -134,7 +135,7 @@ def test_de_oct_selection_from_initial_population(engine):
     for m0 in line.cdp_midpoints[2:8]:
         de, st = engine.differential_evolution([m0], pop, 3, 0.5, 0.9, seed=seed)
         assert np.all(np.isfinite(de))
-        init = oracle.de_initial_population(seed, 0, S, pop, lower, upper)
+        init = oracle.de_initial_population(seed, oracle.de_key(m0), S, pop, lower, upper)
         counts = []
         for f in (1.0, 1.0 - 5e-7, 1.0 + 5e-7):
             pert = init.copy()
@@ -155,7 +156,7 @@ def test_de_multi_wave_call_maps_units_to_midpoints(engine):
     takes them from the work queue, midpoints ordered by selected traces
     (uneven fold here); every unit must still work on its own midpoint: with
     one generation, every reported velocity is one of the initial individuals
-    the counter-based stream gives that midpoint's index."""
+    the counter-based stream gives that midpoint."""
     line = synthetic.structured_line(n_cmp=40, fold_range=(6, 20), h_max=1200, ns=400,
                                      dt_us=4000, n_reflectors=3, f=20.0, snr=8.0, seed=33)
     lower, upper = [1000.0], [5040.0]
@@ -167,7 +168,8 @@ def test_de_multi_wave_call_maps_units_to_midpoints(engine):
     assert st["device_error"] == 0
     S = line.samples_per_trace
     for i in (0, 7, 23, 39):
-        init = oracle.de_initial_population(seed, i, S, pop, lower, upper)
+        init = oracle.de_initial_population(seed, oracle.de_key(m0s[i]), S, pop, lower,
+                                            upper)
         member = np.array([np.any(init[s, :, 0] == de[i, 2, s]) for s in range(S)])
         assert member.all(), i
 

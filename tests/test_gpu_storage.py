@@ -1,11 +1,11 @@
 """16-bit amplitude storage (BF16; FP16 with a per-trace FP32 scale).
 
 The line is resident in 16-bit rows only (half the bytes); the tuned kernel
-widens the staged windows to FP32 in shared memory, the other kernels as they
-read them; interpolation and all sums stay FP32.  Rounding the amplitudes is a precision loss, so these modes are
-judged against the FP64 oracle: the fraction of samples whose chosen
-candidate differs (printed; bounded here) and the error of the chosen
-semblance.
+widens the staged windows to FP32 in shared memory, the other kernels as
+they read them; interpolation and all sums stay FP32.  Rounding the
+amplitudes is a precision loss, so these modes are judged against the FP64
+oracle: the fraction of samples whose chosen candidate differs (printed;
+bounded here) and the error of the chosen semblance.
 """
 import numpy as np
 import pytest
