@@ -16,7 +16,10 @@ Workload (default): CMP linear search at production size -- 2000 CMPs, fold
 
 `--impl reference` times the reference algorithm on the host CPU (the oracle's
 C restatement, all cores): the reference's only CPU path is its OpenCL build
-on a host OpenCL device, which this machine does not have.
+on a host OpenCL device, which this machine does not have.  Beside it, the
+same line carries `reference_cuda`: the reference's own CUDA kernels (built
+from its sources) timed on the same GPU over the midpoints of this arm's
+side measurements.
 """
 from __future__ import annotations
 
@@ -61,6 +64,19 @@ def parse():
                     help="midpoints of the ZO-CRS line measured beside the main workload "
                          "(0 = skip); 32 midpoints = 1504 (midpoint, tile) units, about five "
                          "waves of the persistent grid, so the last partial wave is small")
+    ap.add_argument("--oct-cmps", type=int, default=4,
+                    help="midpoints of the OCT linear-search side measurement (0: skip)")
+    ap.add_argument("--c5-cmps", type=int, default=2,
+                    help="midpoints of the OCT DE + stretch-free pipeline over three h0 "
+                         "(0: skip)")
+    ap.add_argument("--fp64-cmps", type=int, default=7,
+                    help="midpoints of the ZO-CRS line (1500 samples each) on which every "
+                         "FP32 mode is compared with the FP64 search (0: skip)")
+    ap.add_argument("--sf-cmps", type=int, default=20,
+                    help="midpoints of the CMP stretch-free side measurement (0: skip)")
+    ap.add_argument("--no-io-side", action="store_true", help="skip the SU input/output side")
+    ap.add_argument("--no-reference-cuda", action="store_true",
+                    help="reference arm: skip timing the reference's CUDA kernels")
     return ap.parse_args()
 
 
@@ -154,12 +170,20 @@ def profile_traffic(kernel_tag: str):
 
 # ----------------------------------------------------------------- workload
 
+_LINES = {}
+
+
 def make_workload(name: str, n_cmp=None):
+    """A workload's settings and its seeded synthetic line (generated once
+    per process and shared by the measurements that use it)."""
     from highperformanceseismicstacking_gb300 import synthetic
-    w = synthetic.WORKLOADS[name]
-    line = w.make_line(n_cmp=n_cmp)
-    lower, upper = synthetic.workload_bounds(w)
     from highperformanceseismicstacking_gb300.su import tau_index
+    w = synthetic.WORKLOADS[name]
+    key = (name, n_cmp)
+    if key not in _LINES:
+        _LINES[key] = w.make_line(n_cmp=n_cmp)
+    line = _LINES[key]
+    lower, upper = synthetic.workload_bounds(w)
     tau = tau_index(w.tau, line.dt)
     return w, line, lower, upper, tau
 
@@ -215,6 +239,8 @@ def zocrs_side_measure(n_cmp, local):
     peak = props.multi_processor_count * 128 * float(measured_peaks().get("sm_max_mhz", 2070.0)) * 1e6
     instr = 3 * (2 * tau + 1) + 5
     res["tuned"]["roofline_frac"] = res["tuned"]["value"] * instr / peak
+    res["tuned"]["roofline"] = fp32_roofline("zocrs", 2 * tau + 1, evals, 0.0,
+                                             res["tuned"]["ms"], local)
     return {"workload": "zocrs-ls", "cmps": int(len(m0s)), "evals": evals,
             "candidates": P, "mean_traces_per_midpoint": evals / P / line.samples_per_trace / len(m0s),
             "tuned": res["tuned"], "plain": res["plain"],
@@ -241,13 +267,129 @@ def de_side_measure(n_cmp, local):
             eng.differential_evolution(m0s, w.population, 2, w.de_f, w.de_cr, seed=1)
             res, st = eng.differential_evolution(m0s, w.population, w.generations, w.de_f,
                                                  w.de_cr, seed=7)
+        sel = st["selected_traces"]
         out[name] = {"cmps": int(len(m0s)), "samples": line.samples_per_trace,
                      "population": w.population, "generations": w.generations,
                      "evals": st["evals"], "not_used": st["not_used"],
-                     "kernel_ms": st["kernel_ms"],
+                     "kernel_ms": st["kernel_ms"], "selection_ms": st["selection_ms"],
                      "value": st["evals"] / (st["kernel_ms"] / 1e3),
-                     "mean_best_semblance": float(np.mean(res[:, 0]))}
+                     "mean_best_semblance": float(np.mean(res[:, 0])),
+                     "roofline": fp32_roofline(w.model, 2 * tau + 1, st["evals"], st["not_used"],
+                                               st["kernel_ms"], local,
+                                               alg_bytes=sel * line.samples_per_trace * 4 +
+                                               sel * 16)}
     return out
+
+
+def oct_ls_side(n_cmp, local):
+    """OCT linear search on midpoints of the OCT DE workload's line (11 x 5
+    candidates over the workload's bounds, window 9, h0 0): tuned vs plain,
+    device time from the engine's events (the first call tunes / loads)."""
+    from highperformanceseismicstacking_gb300 import capi
+    w, line, lower, upper, tau = make_workload("oct-de")
+    mid = len(line.cdp_midpoints) // 2
+    m0s = np.ascontiguousarray(line.cdp_midpoints[mid:mid + n_cmp])
+    gran = [11, 5]
+    S = line.samples_per_trace
+    out = {"cmps": int(len(m0s)), "candidates": 55, "window": 2 * tau + 1, "h0": 0.0}
+    with capi.Engine(local) as eng:
+        eng.upload_gather(line.samples, line.midpoints, line.halfoffsets, float(line.dt))
+        eng.set_traveltime("oct", lower, upper, w.apm, 0.0)
+        eng.set_window(tau)
+        res = {}
+        for kernel in ("tuned", "plain"):
+            eng.linear_search(m0s, gran, kernel)
+            got, st = eng.linear_search(m0s, gran, kernel)
+            res[kernel] = got
+            sel = st["selected_traces"]
+            out[kernel] = {"kernel_ms": st["kernel_ms"], "selection_ms": st["selection_ms"],
+                           "evals": st["evals"], "not_used": st["not_used"],
+                           "value": st["evals"] / (st["kernel_ms"] / 1e3),
+                           "roofline": fp32_roofline("oct", 2 * tau + 1, st["evals"],
+                                                     st["not_used"], st["kernel_ms"], local,
+                                                     alg_bytes=sel * S * 4 + sel * 16)}
+    out["speedup_tuned_vs_plain"] = out["plain"]["kernel_ms"] / out["tuned"]["kernel_ms"]
+    out["tuned_equals_plain"] = bool(np.array_equal(res["tuned"], res["plain"]))
+    return out
+
+
+def sf_side(n_cmp, local):
+    """CMP stretch-free stack (n in [-10, 10], window 7) on midpoints of the
+    CMP production line over the tuned search's velocities."""
+    from highperformanceseismicstacking_gb300 import capi
+    w, line, lower, upper, tau = make_workload("cmp-production")
+    m0s = np.ascontiguousarray(line.cdp_midpoints[:n_cmp])
+    S = line.samples_per_trace
+    with capi.Engine(local) as eng:
+        eng.upload_gather(line.samples, line.midpoints, line.halfoffsets, float(line.dt))
+        eng.set_traveltime("cmp", lower, upper)
+        eng.set_window(tau)
+        ls, _ = eng.linear_search(m0s, w.granularity, "tuned")
+        prior = np.ascontiguousarray(ls[:, 2:3])
+        eng.stretch_free(m0s, prior, 10)
+        sf, st = eng.stretch_free(m0s, prior, 10)
+    sel = st["selected_traces"]
+    return {"cmps": int(n_cmp), "n_values": 21, "window": 2 * tau + 1,
+            "kernel_ms": st["kernel_ms"], "evals": st["evals"],
+            "value": st["evals"] / (st["kernel_ms"] / 1e3),
+            "roofline": fp32_roofline("cmp", 2 * tau + 1, st["evals"], 0.0, st["kernel_ms"],
+                                      local, extra_per_eval=1,
+                                      alg_bytes=sel * S * 4 + sel * 8 + n_cmp * 4 * S * 4)}
+
+
+def su_io_side(line, d_out, n_m0, rows, S, n_cmp=200):
+    """SU input / output throughput on the host: the line's first n_cmp CMP
+    gathers written as one SU file and read back with the reference's gather
+    semantics (su.read_gather: filters, CDP map, sort), and the result files
+    of the whole line (rows SU files of one trace per CDP) written from the
+    device result slab by the batched writer (hpss_write_result_files)
+    against the reference's per-CDP loop of header and trace writes
+    (Dumper::dumpResult, common/src/output/Dumper.cpp:77-114), restated in
+    Python."""
+    import shutil
+    import tempfile
+    from highperformanceseismicstacking_gb300 import capi, su
+    tmp = Path(tempfile.mkdtemp(prefix="hpss_su_"))
+    try:
+        sel = np.isin(line.midpoints, line.cdp_midpoints[:n_cmp])
+        hdr, smp = line.headers[sel], line.samples[sel]
+        path = tmp / "line.su"
+        t0 = time.perf_counter()
+        su.write_su(str(path), hdr, smp)
+        t_w = time.perf_counter() - t0
+        nbytes = path.stat().st_size
+        t0 = time.perf_counter()
+        g = su.read_gather(str(path), aph=1e9, apm=0.0, tau=0.0, emulate_eof_cdp=False)
+        t_r = time.perf_counter() - t0
+        assert g.trace_count == smp.shape[0]
+        # result files of the whole line from the device slab
+        cdp_hdr = np.zeros(n_m0, su.SU_HEADER_DTYPE)
+        cdp_hdr["ns"] = S
+        cdp_hdr["cdp"] = np.arange(1, n_m0 + 1)
+        paths = [str(tmp / f"r{r}.su") for r in range(rows)]
+        slab_shape = np.empty((n_m0, rows, S), np.float32)  # shape only
+        t0 = time.perf_counter()
+        capi.write_result_files(slab_shape, cdp_hdr, paths, device_ptr=d_out.data_ptr())
+        t_b = time.perf_counter() - t0
+        res_bytes = sum(Path(p).stat().st_size for p in paths)
+        host = d_out.cpu().numpy()
+        t0 = time.perf_counter()
+        for r in range(rows):
+            with open(tmp / f"loop{r}.su", "wb") as f:
+                for i in range(n_m0):
+                    f.write(cdp_hdr[i].tobytes())
+                    f.write(host[i, r].tobytes())
+        t_l = time.perf_counter() - t0
+        same = all((tmp / f"loop{r}.su").read_bytes() == Path(paths[r]).read_bytes()
+                   for r in range(rows))
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+    return {"line_sample": f"{n_cmp} CMP gathers, {smp.shape[0]} traces, {nbytes / 1e6:.0f} MB",
+            "write_su_MBps": nbytes / t_w / 1e6, "read_gather_MBps": nbytes / t_r / 1e6,
+            "result_files": {"files": rows, "bytes": res_bytes,
+                             "batched_from_device_MBps": res_bytes / t_b / 1e6,
+                             "per_cdp_loop_MBps": res_bytes / t_l / 1e6,
+                             "identical_bytes": bool(same)}}
 
 
 # Algorithmic FP32-pipe instructions per evaluation (one (m0, t0, candidate,
@@ -525,6 +667,15 @@ def run_reference(args, world, rank):
            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
            "note": "reference CPU path is its OpenCL build on a host OpenCL device (absent); "
                    "timed here: the oracle's C restatement of the reference kernels"}
+    # the reference's CUDA build on the same GPU, beside: its own kernels,
+    # compiled from its sources (oracle/_ref), replayed per midpoint on the
+    # midpoints of the engine's side measurements (no engine code runs here)
+    if not args.no_reference_cuda:
+        try:
+            from oracle import ref_timing
+            out["reference_cuda"] = ref_timing.reference_cuda()
+        except Exception as e:  # no GPU, fatbins absent: reported, not fatal
+            out["reference_cuda"] = {"unavailable": f"{type(e).__name__}: {e}"}
     print(json.dumps(out))
 
 
@@ -745,13 +896,35 @@ def main():
     cpu = None
     if not args.no_cpu_baseline and world >= 1:
         cpu = cpu_baseline(w, line, lower, upper, tau, args.cpu_seconds)
+    su_io = None
+    if not args.no_io_side:
+        su_io = su_io_side(line, d_out, len(m0s), 2 + eng.np, S)
+    del pinned, host_samples
     zocrs = None
     if args.zocrs_cmps > 0 and args.workload != "zocrs-ls":
-        del pinned, host_samples
         zocrs = zocrs_side_measure(args.zocrs_cmps, local)
-    de = None
-    if args.de_cmps > 0:
-        de = de_side_measure(args.de_cmps, local)
+    de = de_side_measure(args.de_cmps, local) if args.de_cmps > 0 else None
+    oct_ls = oct_ls_side(args.oct_cmps, local) if args.oct_cmps > 0 else None
+    sf = sf_side(args.sf_cmps, local) if args.sf_cmps > 0 else None
+    c5 = c5_side_measure(args.c5_cmps, local) if args.c5_cmps > 0 else None
+    fp64 = fp64_agreement_side(args.fp64_cmps, local) if args.fp64_cmps > 0 else None
+    # every kernel against its roofline (FP32-pipe instructions; HBM view of
+    # the algorithmic bytes where the line is read)
+    rooflines = {f"ls_tuned ({w.name})": roof}
+    if zocrs:
+        rooflines["ls_tuned (zocrs-ls)"] = zocrs["tuned"].get("roofline")
+    if oct_ls:
+        rooflines["ls_oct (oct-de line, 55 candidates)"] = oct_ls["tuned"]["roofline"]
+    if de:
+        for k, v in de.items():
+            rooflines[f"de ({k})"] = v["roofline"]
+    if sf:
+        rooflines["sf (cmp-production)"] = sf["roofline"]
+    if c5:
+        for st_ in ("fp16", "fp32"):
+            if st_ in c5:
+                rooflines[f"de (oct-de, 3 h0, {st_})"] = c5[st_]["de"]["roofline"]
+                rooflines[f"sf (oct-de, 3 h0, {st_})"] = c5[st_]["stretch_free"]["roofline"]
 
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
            "steps": args.steps, "warmup": args.warmup,
@@ -782,7 +955,13 @@ def main():
            "roofline": roof,
            "cpu_baseline": cpu,
            "zocrs_linear_search": zocrs,
+           "oct_linear_search": oct_ls,
            "differential_evolution": de,
+           "stretch_free": sf,
+           "oct_de_stretch_free_pipeline": c5,
+           "fp64_agreement": fp64,
+           "su_io": su_io,
+           "rooflines": rooflines,
            "clocks": clk,
            "step_ms": step_ms}
     print(json.dumps(out))

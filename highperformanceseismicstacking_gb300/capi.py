@@ -37,6 +37,7 @@ EXPORTED = [
     "hpss_differential_evolution", "hpss_differential_evolution_device",
     "hpss_stretch_free", "hpss_select_traces", "hpss_stream", "hpss_device_bytes",
     "hpss_linear_search_noalloc", "hpss_noalloc_device_error", "hpss_linear_search_line",
+    "hpss_write_result_files",
 ]
 
 
@@ -91,6 +92,7 @@ def load_library(path: Optional[Path] = None) -> C.CDLL:
         "hpss_linear_search_noalloc": (i32, [i32, vp, u32, vp, vp, u32, u32, f32, i32, fp, fp,
                                              up, f32, vp, u32, vp, vp]),
         "hpss_noalloc_device_error": (i32, [vp, up]),
+        "hpss_write_result_files": (i32, [vp, i32, u32, u32, u32, vp, C.POINTER(C.c_char_p)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -284,3 +286,24 @@ class Engine:
         counts = np.zeros(m0s.size * self._blocks(), np.uint32)
         self._check(self._lib.hpss_select_traces(self.h, _fptr(m0s), m0s.size, _uptr(counts)))
         return counts
+
+
+def write_result_files(slab, headers: np.ndarray, paths: Sequence[Optional[str]],
+                       device_ptr: Optional[int] = None) -> None:
+    """SU result files from a result slab [nM0][rows][S] (numpy array, or a
+    device pointer with `slab` giving only the shape): file r holds, per
+    midpoint, headers[i] (240-byte SU header) and slab[i][r]
+    (hpss_write_result_files).  A None path skips its row."""
+    n, rows, S = slab.shape
+    hdr = np.ascontiguousarray(headers)
+    if hdr.nbytes != n * 240:
+        raise ValueError("headers must be nM0 SU trace headers (240 bytes each)")
+    arr = (C.c_char_p * rows)(*[p.encode() if p else None for p in paths])
+    if device_ptr is None:
+        host = np.ascontiguousarray(slab, dtype=np.float32)
+        rc = lib().hpss_write_result_files(host.ctypes.data, 0, n, rows, S, hdr.ctypes.data, arr)
+    else:
+        rc = lib().hpss_write_result_files(C.c_void_p(device_ptr), 1, n, rows, S,
+                                           hdr.ctypes.data, arr)
+    if rc != HPSS_OK:
+        raise HpssError(rc, lib().hpss_last_error(None).decode())

@@ -297,6 +297,19 @@ void *hpss_stream(hpss_handle h);
 /* Bytes of device memory currently held by the handle. */
 size_t hpss_device_bytes(hpss_handle h);
 
+/* Result files from a result slab [nM0][rows][S] (the layout of every
+ * search's output): one SU file per row r, paths[r] (NULL: row skipped),
+ * holding for every midpoint i in order the 240-byte trace header
+ * headers[i] (trace_info_t, the CDP's header) followed by slab[i][r][0..S).
+ * Replaces Dumper::dumpResult (common/src/output/Dumper.cpp:77-114), which
+ * writes one header and one trace per CDP from the ResultSet's per-CDP
+ * vectors: here each file image is assembled in one buffer -- from device
+ * memory (slabOnDevice != 0) by one strided copy per file -- and written at
+ * once.  Errors via hpss_last_error(NULL). */
+hpss_status hpss_write_result_files(const float *slab, int slabOnDevice, uint32_t nM0,
+                                    uint32_t rows, uint32_t S, const void *headers,
+                                    const char *const *paths);
+
 /* Linear search that allocates nothing -- no counterpart in the reference.
  * For callers that may not call cudaMalloc (a plug-in inside another
  * framework's memory pool, a process with a fixed device-memory budget): the

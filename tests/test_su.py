@@ -70,3 +70,32 @@ def test_scalco_negative_divides():
     hdr["gy"] = 3000
     m, h = su.midpoint_halfoffset(hdr, np.float32(0))
     assert m[0] == np.float32(200.0) and h[0] == np.float32(100.0)
+
+
+def _cdp_result_case(tmp_path):
+    line = synthetic.cmp_line(n_cmp=7, halfoffsets=[25, 75, 125], ns=40, dt_us=4000,
+                              n_reflectors=1, n_multiples=0, f=25.0, snr=10.0, seed=4)
+    p = tmp_path / "line.su"
+    su.write_su(str(p), line.headers, line.samples)
+    g = su.read_gather(str(p), aph=1000.0, apm=0.0, tau=0.008, emulate_eof_cdp=False)
+    cdps = list(g.cdps.values())
+    headers = np.stack([c.info for c in cdps]).astype(su.SU_HEADER_DTYPE)
+    slab = np.random.default_rng(0).standard_normal((len(cdps), 3, 40)).astype(np.float32)
+    return headers, slab
+
+
+def test_batched_result_writer_matches_per_cdp_writer(tmp_path):
+    """hpss_write_result_files (one image per file, one write) produces the
+    bytes of the reference's per-CDP Dumper::dumpResult loop: per CDP its
+    header, then the row's samples."""
+    from highperformanceseismicstacking_gb300 import capi
+    headers, slab = _cdp_result_case(tmp_path)
+    paths = [str(tmp_path / f"r{r}.su") for r in range(3)]
+    capi.write_result_files(slab, headers, paths)
+    for r in range(3):
+        ref = tmp_path / f"ref{r}.su"
+        su.write_su(str(ref), headers, slab[:, r, :])
+        assert (tmp_path / f"r{r}.su").read_bytes() == ref.read_bytes()
+    # a None path skips its row
+    capi.write_result_files(slab, headers, [None, str(tmp_path / "only1.su"), None])
+    assert (tmp_path / "only1.su").read_bytes() == (tmp_path / "ref1.su").read_bytes()
