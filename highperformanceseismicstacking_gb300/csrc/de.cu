@@ -29,6 +29,7 @@
 // pattern, so a midpoint draws the same numbers whatever else its call holds
 // (other midpoints, other half-offsets, another process's shard).
 #include <algorithm>
+#include <cstdlib>
 
 #include "hpss_device.cuh"
 #include "hpss_internal.h"
@@ -591,7 +592,13 @@ template <int MODEL>
 cudaError_t launch_de_model(const DeParams &d, uint32_t numSms, cudaStream_t st) {
     constexpr int NP = MODEL == kModelCmp ? 1 : (MODEL == kModelZocrs ? 3 : 2);
     const uint32_t pop = d.pop;
-    const uint32_t spc = pop >= (uint32_t)kDeThreads ? 1u : kDeThreads / pop;
+    uint32_t spc = pop >= (uint32_t)kDeThreads ? 1u : kDeThreads / pop;
+    // HPSS_DE_SAMPLES_PER_CTA: fewer samples (whole populations) per CTA
+    // (smaller CTAs, each generation barrier over fewer warps)
+    if (const char *env = std::getenv("HPSS_DE_SAMPLES_PER_CTA")) {
+        const int v = std::atoi(env);
+        if (v >= 1 && (uint32_t)v < spc) spc = (uint32_t)v;
+    }
     const uint32_t threads = ((spc * pop + 31) / 32) * 32;
     const uint32_t groups = (d.ls.S + spc - 1) / spc;
     const uint64_t units = (uint64_t)d.ls.nM0 * groups;

@@ -203,10 +203,19 @@ hpss_status run_selection(hpss_handle h, const float *d_m0s, uint32_t nM0,
     lp.selIdx = static_cast<uint32_t *>(h->selIdx.p);
     lp.m0s = d_m0s;
     lp.nM0 = nM0;
+    // slope and c ranges of the sampled candidates (the selection's box test)
+    float4 box = make_float4(INFINITY, -INFINITY, INFINITY, -INFINITY);
+    for (size_t i = 0; i + 1 < h->octCandsHost.size(); i += 2) {
+        box.z = std::min(box.z, h->octCandsHost[i]);
+        box.w = std::max(box.w, h->octCandsHost[i]);
+        box.x = std::min(box.x, h->octCandsHost[i + 1]);
+        box.y = std::max(box.y, h->octCandsHost[i + 1]);
+    }
+    HPSS_CUDA_TRY(h, use_oct_table(h, lp));
     HPSS_CUDA_TRY(h, launch_select_oct(lp, static_cast<const float *>(h->octCands.p),
                                        (uint32_t)(h->octCandsHost.size() / 2),
                                        static_cast<uint32_t *>(h->selIdx.p), count,
-                                       cf, cc, (uint64_t)total, h->stream));
+                                       cf, cc, (uint64_t)total, box, h->stream));
     return HPSS_OK;
 }
 

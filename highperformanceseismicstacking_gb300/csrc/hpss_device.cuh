@@ -467,6 +467,30 @@ __device__ __forceinline__ OctWarpBox oct_warp_box(bool enable, bool member, flo
     }
     return r;
 }
+// Box test of trace ti for one t0 and a set of candidates whose slopes lie in
+// [sLo, sHi] and whose c = 4/v^2 lie in [cLo, cHi] (trace selection: may any
+// of them reach the trace at this t0?).  The candidates' theta = t0 * slope
+// and T = t0^2 - c h0^2, rounded as their per-candidate tests round them, are
+// monotone in slope and c, so the box is taken from the extremes; false only
+// where the box test proves that no candidate passes.
+__device__ __forceinline__ bool oct_sample_may_pass(const float4 &tf, float h, float h0,
+                                                    float t0, float sLo, float sHi, float cLo,
+                                                    float cHi, float m0, float apm) {
+    if (h0 == 0.f) {
+        if (!(t0 >= kOctBoxMinT0)) return true;  // the per-candidate tests decide
+        return oct_box_may_pass(tf, sLo, sHi, t0, t0, m0, apm);
+    }
+    const float thLo = __fmul_rn(t0, sLo), thHi = __fmul_rn(t0, sHi);
+    float tLo = oct_tn0_sq(t0, cHi, h0), tHi = oct_tn0_sq(t0, cLo, h0);
+    if (tHi < 0.f) {  // T < 0 throughout: |T| in [-tHi, -tLo]
+        const float t = -tLo;
+        tLo = -tHi;
+        tHi = t;
+    }
+    if (!(tLo >= kOctBoxMinT) || !(tHi >= tLo) || !(thHi >= thLo)) return true;
+    return oct_box_may_pass_h0(tf, h, h0, thLo, thHi, tLo, tHi, m0, apm);
+}
+
 // Box test of trace ti (factor table entry and half-offset) for a warp.  The
 // box {aLo, aHi, bLo, bHi} is read from the warp's slot in shared memory
 // (volatile: reloaded at each test instead of held in registers through the

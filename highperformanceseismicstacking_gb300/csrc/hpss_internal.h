@@ -245,11 +245,14 @@ cudaError_t launch_merge_parts(const LsParams &p, uint32_t parts, const PartBest
 cudaError_t launch_select_compact(const LsParams &p, const uint32_t *candFirst,
                                   const uint32_t *candCount, uint32_t *selIdx,
                                   uint32_t *selCount, cudaStream_t st);
-// total: sum of candCount (the selIdx slots, p.selFirst their prefix).
+// total: sum of candCount (the selIdx slots, p.selFirst their prefix);
+// candBox: {min slope, max slope, min c, max c} of the sampled candidates;
+// p.octTab: the factor tables.
 cudaError_t launch_select_oct(const LsParams &p, const float *cands,
                               uint32_t nCand, uint32_t *selIdx,
                               uint32_t *selCount, const uint32_t *candFirst,
-                              const uint32_t *candCount, uint64_t total, cudaStream_t st);
+                              const uint32_t *candCount, uint64_t total, float4 candBox,
+                              cudaStream_t st);
 cudaError_t launch_convert_storage(const float *src, uint16_t *dst,
                                    float *scale, uint32_t nTraces, uint32_t S,
                                    uint32_t stride, int storage,

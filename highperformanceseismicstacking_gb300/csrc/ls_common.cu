@@ -111,9 +111,16 @@ cudaError_t launch_chunk_bounds(const LsParams &p, float *bounds,
 // slots are spread over all SMs rather than one CTA per midpoint), lanes
 // over the sampled candidates, early exit on the first hit; the 0 / 1 flag
 // goes to the slot in selIdx.
+//
+// Lanes first take 32 samples at a time through the box test of all sampled
+// candidates at that t0 (oct_sample_may_pass; candBox = their slope and c
+// ranges): only samples the box cannot rule out go through the
+// per-candidate tests, so a trace that is not selected costs one box test
+// per sample instead of one test per (sample, candidate).  The flags are
+// those of the per-candidate tests.
 __global__ void select_oct_flags_kernel(LsParams a, const float *cands, uint32_t nCand,
                                         const uint32_t *candFirst, uint64_t total,
-                                        uint32_t *selIdx) {
+                                        uint32_t *selIdx, float4 candBox) {
     const int lane = threadIdx.x & 31;
     const uint64_t g = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (g >= total) return;  // whole warps
@@ -128,21 +135,33 @@ __global__ void select_oct_flags_kernel(LsParams a, const float *cands, uint32_t
     const uint32_t mi = lo;
     const uint32_t ti = candFirst[mi] + (uint32_t)(g - a.selFirst[mi]);
     const float m0 = a.m0s[mi];
-    const float h0 = oct_line(a, mi).h0;
+    const OctLine ol = oct_line(a, mi);
+    const float h0 = ol.h0;
     const float m = a.mid[ti], h = a.hoff[ti];
+    const float4 tf = __ldg(ol.tab + ti);
     bool used = false;
-    for (uint32_t s = 0; s < a.S && !used; s++) {
-        const float t0 = static_cast<float>(s) * a.dt;
-        for (uint32_t p0 = 0; p0 < nCand && !used; p0 += 32) {
-            const uint32_t p = p0 + lane;
-            bool hit = false;
-            if (p < nCand) {
-                float mh;
-                const int e = oct_displaced_midpoint(h, h0, t0, m0, cands[2 * p],
-                                                     cands[2 * p + 1], &mh);
-                hit = (e == DE_OK && fabsf(m - mh) <= a.apm);
+    for (uint32_t s0 = 0; s0 < a.S && !used; s0 += 32) {
+        const uint32_t sl = s0 + lane;
+        // (HPSS_OCT_BOX_TEST=0 turns the box test off: every sample tested)
+        const bool may = sl < a.S &&
+                         (!a.octBox ||
+                          oct_sample_may_pass(tf, h, h0, static_cast<float>(sl) * a.dt,
+                                              candBox.x, candBox.y, candBox.z, candBox.w, m0,
+                                              a.apm));
+        for (uint32_t mask = __ballot_sync(0xffffffffu, may); mask && !used;
+             mask &= mask - 1) {
+            const float t0 = static_cast<float>(s0 + __ffs(mask) - 1) * a.dt;
+            for (uint32_t p0 = 0; p0 < nCand && !used; p0 += 32) {
+                const uint32_t p = p0 + lane;
+                bool hit = false;
+                if (p < nCand) {
+                    float mh;
+                    const int e = oct_displaced_midpoint(h, h0, t0, m0, cands[2 * p],
+                                                         cands[2 * p + 1], &mh);
+                    hit = (e == DE_OK && fabsf(m - mh) <= a.apm);
+                }
+                used = __any_sync(0xffffffffu, hit);
             }
-            used = __any_sync(0xffffffffu, hit);
         }
     }
     if (lane == 0) selIdx[g] = used ? 1u : 0u;
@@ -184,13 +203,14 @@ select_oct_compact_kernel(LsParams a, const uint32_t *candFirst, const uint32_t 
 cudaError_t launch_select_oct(const LsParams &p, const float *cands,
                               uint32_t nCand, uint32_t *selIdx,
                               uint32_t *selCount, const uint32_t *candFirst,
-                              const uint32_t *candCount, uint64_t total, cudaStream_t st) {
+                              const uint32_t *candCount, uint64_t total, float4 candBox,
+                              cudaStream_t st) {
     if (p.nM0 == 0) return cudaSuccess;
     if (total > 0) {
         const uint64_t blocks = (total * 32 + 255) / 256;
         if (blocks > 0x7fffffffull) return cudaErrorInvalidConfiguration;
         select_oct_flags_kernel<<<(uint32_t)blocks, 256, 0, st>>>(p, cands, nCand, candFirst,
-                                                                  total, selIdx);
+                                                                  total, selIdx, candBox);
         const cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }

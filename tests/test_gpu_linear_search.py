@@ -168,6 +168,28 @@ def test_oct_small_line(engine, h0):
 @pytest.mark.parametrize("slope,dt_us,h0", [(5e-3, 2000, 0.0), (2e-4, 1000, 0.0),
                                              (2e-2, 4000, 0.0), (5e-3, 2000, 500.0),
                                              (1e-3, 1000, 1000.0), (2e-2, 4000, 0.5)])
+def test_oct_selection_box_test_keeps_the_selection(engine, monkeypatch, slope, dt_us, h0):
+    """OCT trace selection: per sample, the box test over all sampled
+    candidates (their slope and c ranges) rules out samples at which no
+    candidate can reach the trace, before the per-candidate tests; the
+    selected traces equal those of the per-candidate tests alone
+    (HPSS_OCT_BOX_TEST=0), counts midpoint by midpoint."""
+    line = synthetic.structured_line(n_cmp=40, fold_range=(6, 12), h_max=2500, ns=300,
+                                     dt_us=dt_us, n_reflectors=3, f=20.0, snr=8.0, seed=19)
+    lower, upper = [1200.0, -slope], [5000.0, slope]
+    _setup(engine, line, "oct", lower, upper, 2, 150.0, h0)
+    m0s = line.cdp_midpoints[3::5]
+    on = engine.select_traces(m0s)
+    monkeypatch.setenv("HPSS_OCT_BOX_TEST", "0")
+    off = engine.select_traces(m0s)
+    monkeypatch.delenv("HPSS_OCT_BOX_TEST")
+    assert off.sum() > 0
+    assert np.array_equal(on, off)
+
+
+@pytest.mark.parametrize("slope,dt_us,h0", [(5e-3, 2000, 0.0), (2e-4, 1000, 0.0),
+                                             (2e-2, 4000, 0.0), (5e-3, 2000, 500.0),
+                                             (1e-3, 1000, 1000.0), (2e-2, 4000, 0.5)])
 def test_oct_tile_test_keeps_per_sample_results(engine, slope, dt_us, h0):
     """The OCT kernel drops, per 32-sample tile and candidate, the traces
     whose midpoint is farther than apm from every displaced midpoint the
