@@ -528,8 +528,36 @@ de_kernel(DeParams d, uint32_t spc, uint32_t groups, uint32_t nUnits) {
 // warp per (midpoint, candidate trace) slot over the whole GPU writes a 0 / 1
 // flag into the slot (d.ls.selFirst: the prefix of candCount); the flags are
 // then compacted in order (launch_select_compact).
+// Per (midpoint, sample): the slope and c = 4/v^2 ranges of the initial
+// population (the box the selection's per-sample box test takes).
+__global__ void de_select_boxes_kernel(DeParams d, float4 *boxes) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const LsParams &a = d.ls;
+    if (i >= (uint64_t)a.nM0 * a.S) return;
+    const uint32_t mi = (uint32_t)(i / a.S), s = (uint32_t)(i % a.S);
+    const uint32_t mkey = __float_as_uint(a.m0s[mi]);
+    const float inf = __int_as_float(0x7f800000);
+    float4 b = make_float4(inf, -inf, inf, -inf);
+    for (uint32_t ind = 0; ind < d.pop; ind++) {
+        Draws rng(d.seedLo, d.seedHi, mkey, s, ind, 0);
+        const float v = __fmaf_rn(rng.next(), __fsub_rn(d.hi[0], d.lo[0]), d.lo[0]);
+        const float sl = __fmaf_rn(rng.next(), __fsub_rn(d.hi[1], d.lo[1]), d.lo[1]);
+        const float c = 4.0f / (v * v);
+        b.x = fminf(b.x, sl);
+        b.y = fmaxf(b.y, sl);
+        b.z = fminf(b.z, c);
+        b.w = fmaxf(b.w, c);
+    }
+    boxes[i] = b;
+}
+
+// Lanes first take 32 samples at a time through the box test of their
+// sample's initial population (boxes; oct_sample_may_pass): only samples the
+// box cannot rule out go through the per-individual tests, whose results
+// are the flags.
 __global__ void de_select_oct_flags_kernel(DeParams d, const uint32_t *candFirst,
-                                           uint64_t total, uint32_t *selIdx) {
+                                           uint64_t total, uint32_t *selIdx,
+                                           const float4 *boxes) {
     const LsParams &a = d.ls;
     const int lane = threadIdx.x & 31;
     const uint64_t g = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -544,25 +572,41 @@ __global__ void de_select_oct_flags_kernel(DeParams d, const uint32_t *candFirst
     const uint32_t mi = lo;
     const uint32_t ti = candFirst[mi] + (uint32_t)(g - a.selFirst[mi]);
     const float m0 = a.m0s[mi];
-    const float h0 = oct_line(a, mi).h0;
+    const OctLine ol = oct_line(a, mi);
+    const float h0 = ol.h0;
     const uint32_t mkey = __float_as_uint(m0);
     const float m = a.mid[ti], h = a.hoff[ti];
+    const float4 tf = __ldg(ol.tab + ti);
+    const float4 *mbox = boxes + (size_t)mi * a.S;
     bool used = false;
-    for (uint32_t s = 0; s < a.S && !used; s++) {
-        const float t0 = static_cast<float>(s) * a.dt;
-        for (uint32_t i0 = 0; i0 < d.pop && !used; i0 += 32) {
-            const uint32_t ind = i0 + lane;
-            bool hit = false;
-            if (ind < d.pop) {
-                Draws rng(d.seedLo, d.seedHi, mkey, s, ind, 0);
-                const float v = __fmaf_rn(rng.next(), __fsub_rn(d.hi[0], d.lo[0]), d.lo[0]);
-                const float sl = __fmaf_rn(rng.next(), __fsub_rn(d.hi[1], d.lo[1]), d.lo[1]);
-                const float c = 4.0f / (v * v);
-                float mh;
-                const int e = oct_displaced_midpoint(h, h0, t0, m0, c, sl, &mh);
-                hit = (e == DE_OK && fabsf(m - mh) <= a.apm);
+    for (uint32_t s0 = 0; s0 < a.S && !used; s0 += 32) {
+        const uint32_t sl0 = s0 + lane;
+        bool may = false;
+        if (sl0 < a.S) {
+            const float4 b = mbox[sl0];
+            // (HPSS_OCT_BOX_TEST=0: every sample tested)
+            may = !a.octBox || oct_sample_may_pass(tf, h, h0, static_cast<float>(sl0) * a.dt,
+                                                   b.x, b.y, b.z, b.w, m0, a.apm);
+        }
+        for (uint32_t mask = __ballot_sync(0xffffffffu, may); mask && !used;
+             mask &= mask - 1) {
+            const uint32_t s = s0 + __ffs(mask) - 1;
+            const float t0 = static_cast<float>(s) * a.dt;
+            for (uint32_t i0 = 0; i0 < d.pop && !used; i0 += 32) {
+                const uint32_t ind = i0 + lane;
+                bool hit = false;
+                if (ind < d.pop) {
+                    Draws rng(d.seedLo, d.seedHi, mkey, s, ind, 0);
+                    const float v = __fmaf_rn(rng.next(), __fsub_rn(d.hi[0], d.lo[0]), d.lo[0]);
+                    const float sl =
+                        __fmaf_rn(rng.next(), __fsub_rn(d.hi[1], d.lo[1]), d.lo[1]);
+                    const float c = 4.0f / (v * v);
+                    float mh;
+                    const int e = oct_displaced_midpoint(h, h0, t0, m0, c, sl, &mh);
+                    hit = (e == DE_OK && fabsf(m - mh) <= a.apm);
+                }
+                used = __any_sync(0xffffffffu, hit);
             }
-            used = __any_sync(0xffffffffu, hit);
         }
     }
     if (lane == 0) selIdx[g] = used ? 1u : 0u;
@@ -627,14 +671,19 @@ cudaError_t launch_de(const DeParams &d, int model, uint32_t numSms, cudaStream_
 
 cudaError_t launch_de_select_oct(const DeParams &d, const uint32_t *candFirst,
                                  const uint32_t *candCount, uint32_t *selIdx,
-                                 uint32_t *selCount, uint64_t total, cudaStream_t st) {
+                                 uint32_t *selCount, uint64_t total, float4 *boxes,
+                                 cudaStream_t st) {
     if (d.ls.nM0 == 0) return cudaSuccess;
     if (total > 0) {
+        const uint64_t nb = (uint64_t)d.ls.nM0 * d.ls.S;
+        de_select_boxes_kernel<<<(uint32_t)((nb + 255) / 256), 256, 0, st>>>(d, boxes);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
         const uint64_t blocks = (total * 32 + 255) / 256;
         if (blocks > 0x7fffffffull) return cudaErrorInvalidConfiguration;
         de_select_oct_flags_kernel<<<(uint32_t)blocks, 256, 0, st>>>(d, candFirst, total,
-                                                                     selIdx);
-        const cudaError_t e = cudaGetLastError();
+                                                                     selIdx, boxes);
+        e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
     return launch_select_compact(d.ls, candFirst, candCount, selIdx, selCount, st);

@@ -76,9 +76,11 @@ hpss_status de_impl(hpss_handle h, const float *d_m0s, uint32_t nM0, uint32_t po
         const uint32_t *cf = static_cast<const uint32_t *>(h->candFirst.p);
         const uint32_t *cc = static_cast<const uint32_t *>(h->candCount.p);
         d.ls.selIdx = static_cast<uint32_t *>(h->selIdx.p);
+        HPSS_CUDA_TRY(h, ensure(h, h->deBoxes, (size_t)nM0 * h->S * sizeof(float4)));
         HPSS_CUDA_TRY(h, launch_de_select_oct(d, cf, cc, static_cast<uint32_t *>(h->selIdx.p),
                                               static_cast<uint32_t *>(h->selCount.p),
-                                              (uint64_t)total, h->stream));
+                                              (uint64_t)total,
+                                              static_cast<float4 *>(h->deBoxes.p), h->stream));
     }
     // work queue order: midpoints by descending selected traces
     if (ordered) {

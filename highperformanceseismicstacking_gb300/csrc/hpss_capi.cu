@@ -500,7 +500,7 @@ hpss_status hpss_destroy(hpss_handle h) {
     for (auto *b : {&h->params, &h->chunkBounds, &h->selFirst, &h->selCount, &h->selIdx,
                     &h->candFirst, &h->candCount, &h->notUsed, &h->errWord, &h->m0s,
                     &h->out, &h->octCands, &h->prior, &h->partial, &h->octTab, &h->order,
-                    &h->octH0sDev, &h->m0v})
+                    &h->octH0sDev, &h->m0v, &h->deBoxes})
         release(h, *b);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);

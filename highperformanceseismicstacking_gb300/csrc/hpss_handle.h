@@ -30,6 +30,7 @@ struct hpss_handle_s : public hpss::Handle {
     std::vector<float> octH0s;
     Buf octH0sDev;             // octH0s on the device
     Buf m0v;                   // midpoints of a call repeated per half-offset
+    Buf deBoxes;               // OCT DE selection: per-sample initial-population boxes
     std::string gridKey;       // grid held in `params` (empty: none)
     uint32_t boundsChunk = 0;  // chunk size of the bounds in `chunkBounds` (0: none)
     std::vector<float> octCandsHost;

@@ -263,8 +263,10 @@ cudaError_t launch_sf(const LsParams &p, int model, uint32_t grid, uint32_t nUni
 cudaError_t launch_sf_select_oct(const LsParams &p, const uint32_t *candFirst,
                                  const uint32_t *candCount, uint32_t *selIdx,
                                  uint32_t *selCount, uint64_t total, cudaStream_t st);
+// boxes: [nM0][S] float4 scratch (the initial populations' slope / c ranges).
 cudaError_t launch_de_select_oct(const DeParams &d, const uint32_t *candFirst,
                                  const uint32_t *candCount, uint32_t *selIdx,
-                                 uint32_t *selCount, uint64_t total, cudaStream_t st);
+                                 uint32_t *selCount, uint64_t total, float4 *boxes,
+                                 cudaStream_t st);
 
 }  // namespace hpss

@@ -36,7 +36,9 @@ __device__ __forceinline__ void neumaier(float &s, float &comp, float x) {
 
 constexpr int kCompensateAbove = 4096;  // window x traces terms
 
-template <int MODEL, int MODE>
+// S16: the line is stored in 16-bit rows (widened as read); a template
+// parameter so that the FP32 form carries no per-tap storage test.
+template <int MODEL, int MODE, bool S16>
 __global__ void __launch_bounds__(kPlainThreads)
 ls_plain_kernel(LsParams a) {
     const uint32_t mi = blockIdx.x / a.S;
@@ -95,10 +97,12 @@ ls_plain_kernel(LsParams a) {
             WinIdx wi = window_index(t, a.dt);
             if (window_in_trace(wi.k, a.tau, (int)a.S)) {
                 int k = wi.k - a.tau;
-                float y1 = amp_at(a, ti, k);
+                const float *tr = a.samples + (size_t)ti * a.stride;
+                const uint16_t *tr16 = a.samples16 + (size_t)ti * a.stride;
+                float y1 = S16 ? amp16(a, ti, tr16[k]) : tr[k];
                 for (int j = 0; j < a.w; j++, k++) {
                     float y0 = y1;
-                    y1 = amp_at(a, ti, k + 1);
+                    y1 = S16 ? amp16(a, ti, tr16[k + 1]) : tr[k + 1];
                     float u = (y1 - y0) * wi.frac + y0;
                     if (kMayComp && comp) {
                         neumaier(num[j], numc[j], u);
@@ -174,19 +178,27 @@ ls_plain_kernel(LsParams a) {
     }
 }
 
-template <int MODEL>
-void launch_plain_mode(const LsParams &p, unsigned blocks, int mode, cudaStream_t st) {
+template <int MODEL, bool S16>
+void launch_plain_mode_s(const LsParams &p, unsigned blocks, int mode, cudaStream_t st) {
     switch (mode & (kPrecTt64 | kPrecCompensated)) {
-        case 0: ls_plain_kernel<MODEL, 0><<<blocks, kPlainThreads, 0, st>>>(p); break;
-        case kPrecTt64: ls_plain_kernel<MODEL, kPrecTt64><<<blocks, kPlainThreads, 0, st>>>(p); break;
+        case 0: ls_plain_kernel<MODEL, 0, S16><<<blocks, kPlainThreads, 0, st>>>(p); break;
+        case kPrecTt64:
+            ls_plain_kernel<MODEL, kPrecTt64, S16><<<blocks, kPlainThreads, 0, st>>>(p);
+            break;
         case kPrecCompensated:
-            ls_plain_kernel<MODEL, kPrecCompensated><<<blocks, kPlainThreads, 0, st>>>(p);
+            ls_plain_kernel<MODEL, kPrecCompensated, S16><<<blocks, kPlainThreads, 0, st>>>(p);
             break;
         default:
-            ls_plain_kernel<MODEL, kPrecTt64 | kPrecCompensated>
+            ls_plain_kernel<MODEL, kPrecTt64 | kPrecCompensated, S16>
                 <<<blocks, kPlainThreads, 0, st>>>(p);
             break;
     }
+}
+
+template <int MODEL>
+void launch_plain_mode(const LsParams &p, unsigned blocks, int mode, cudaStream_t st) {
+    if (p.samples16) launch_plain_mode_s<MODEL, true>(p, blocks, mode, st);
+    else launch_plain_mode_s<MODEL, false>(p, blocks, mode, st);
 }
 
 cudaError_t launch_ls_plain(const LsParams &p, cudaStream_t st, int precisionMode) {

@@ -191,5 +191,7 @@ def test_de_oct_box_test_keeps_results(engine, monkeypatch, slope, h0):
     de0, st0 = engine.differential_evolution(m0s, 32, 12, 0.5, 0.9, seed=4)
     assert st["device_error"] == 0 and st0["device_error"] == 0
     assert st0["not_used"] > 0
+    # the selection's per-sample box test keeps the selected traces
+    assert st["selected_traces"] == st0["selected_traces"]
     assert st["not_used"] == st0["not_used"]
     assert np.array_equal(de, de0)
