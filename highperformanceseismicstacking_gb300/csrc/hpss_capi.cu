@@ -762,6 +762,7 @@ hpss_status hpss_stretch_free(hpss_handle h, const float *m0s, uint32_t nM0,
     lp.m0s = static_cast<float *>(h->m0s.p);
     lp.nM0 = nM0;
     // several OCT half-offsets: nH0 blocks of the midpoints, one launch
+    HPSS_CUDA_TRY(h, use_oct_table(h, lp));
     HPSS_CUDA_TRY(h, expand_h0_blocks(h, lp));
     const float *d_m0s = lp.m0s;
     nM0 = lp.nM0;

@@ -29,57 +29,98 @@ __global__ void __launch_bounds__(kSfWarps * 32) sf_kernel(LsParams a, uint32_t 
         const float m0 = a.m0s[mi];
         const uint32_t first = a.selFirst[mi], cnt = a.selCount[mi];
         const float *prior = a.prior + (size_t)mi * NP * a.S;
-        const float h0 = MODEL == kModelOct ? oct_line(a, mi).h0 : 0.f;
+        const OctLine ol = oct_line(a, mi);  // OCT: the midpoint's h0 and factor table
+        const float h0 = MODEL == kModelOct ? ol.h0 : 0.f;
         float best = -1.f, bestK = 0.f;
         uint32_t bestI = 0xffffffffu;
         unsigned nu = 0;
+        __shared__ float sfBox[kSfWarps][4];  // each warp's displaced-midpoint box (OCT)
         for (int ni0 = 0; ni0 < nn; ni0 += 32) {
             const int ni = ni0 + lane;
             const int n = ni - a.nmax;
             const int sn = s - n;
-            float sembl = 0.f, stack = 0.f;
-            if (ni < nn && sn >= 0 && sn < (int)a.S) {
-                const float t0n = static_cast<float>(sn) * a.dt;
-                const float v = prior[sn];
-                const float c = 4.0f / (v * v);
-                const float p1 = MODEL != kModelCmp ? prior[a.S + sn] : 0.f;
-                const float p2 = MODEL == kModelZocrs ? prior[2 * a.S + sn] : 0.f;
-                const float nf = static_cast<float>(n);
-                float num[kMaxWindow + 1];
-                for (int j = 0; j < a.w; j++) num[j] = 0.f;
-                float lin = 0.f, den = 0.f;
-                unsigned used = 0;
-                for (uint32_t q = 0; q < cnt; q++) {
-                    const uint32_t ti = a.selIdx ? a.selIdx[first + q] : first + q;
-                    float tn;
-                    int ok = model_time<MODEL>(t0n, c, p1, p2, a.mid[ti], a.hoff[ti], a.hsq[ti],
-                                               m0, a.apm, h0, &tn);
-                    if (ok < 0) {
-                        nu++;
-                        continue;
+            const bool member = ni < nn && sn >= 0 && sn < (int)a.S;
+            const int snc = member ? sn : s;  // lanes without an evaluation read sample s
+            const float t0n = static_cast<float>(snc) * a.dt;
+            const float v = prior[snc];
+            const float c = 4.0f / (v * v);
+            const float p1 = MODEL != kModelCmp ? prior[a.S + snc] : 0.f;
+            const float p2 = MODEL == kModelZocrs ? prior[2 * a.S + snc] : 0.f;
+            const float nf = static_cast<float>(n);
+            // OCT: the (t0, candidate) factors once, the trace factors from
+            // the line's table (the same roundings as model_time)
+            const OctCand kc = oct_cand(t0n, c, p1, h0);
+            float num[kMaxWindow + 1];
+            for (int j = 0; j < a.w; j++) num[j] = 0.f;
+            float lin = 0.f, den = 0.f;
+            unsigned used = 0;
+            auto evalTrace = [&](uint32_t ti) {
+                float tn;
+                int ok;
+                if (MODEL == kModelOct) {
+                    const float4 tf = __ldg(ol.tab + ti);  // {m, gamma^2, 16h^2h0^2, h^2-h0^2}
+                    ok = oct_model_time(kc, tf.y, tf.z, tf.w, t0n, c, p1, tf.x, a.hoff[ti], m0,
+                                        a.apm, h0, &tn);
+                } else {
+                    ok = model_time<MODEL>(t0n, c, p1, p2, a.mid[ti], a.hoff[ti], a.hsq[ti], m0,
+                                           a.apm, h0, &tn);
+                }
+                if (ok < 0) {
+                    nu++;
+                    return;
+                }
+                if (ok == 0) return;
+                // t_n + n dt as one fused multiply-add, as the reference
+                // compiles it (cmp/stretch_free.cu:55)
+                const float t = __fmaf_rn(nf, a.dt, tn);
+                WinIdx wi = window_index(t, a.dt);
+                if (window_in_trace(wi.k, a.tau, (int)a.S)) {
+                    const int k0 = wi.k - a.tau;
+                    float y1 = amp_at(a, ti, k0);
+                    for (int j = 0; j < a.w; j++) {
+                        float y0 = y1;
+                        y1 = amp_at(a, ti, k0 + j + 1);
+                        float u = (y1 - y0) * wi.frac + y0;
+                        num[j] += u;
+                        lin += u;
+                        den += u * u;
                     }
-                    if (ok == 0) continue;
-                    // t_n + n dt as one fused multiply-add, as the reference
-                    // compiles it (cmp/stretch_free.cu:55)
-                    const float t = __fmaf_rn(nf, a.dt, tn);
-                    WinIdx wi = window_index(t, a.dt);
-                    if (window_in_trace(wi.k, a.tau, (int)a.S)) {
-                        const int k0 = wi.k - a.tau;
-                        float y1 = amp_at(a, ti, k0);
-                        for (int j = 0; j < a.w; j++) {
-                            float y0 = y1;
-                            y1 = amp_at(a, ti, k0 + j + 1);
-                            float u = (y1 - y0) * wi.frac + y0;
-                            num[j] += u;
-                            lin += u;
-                            den += u * u;
+                    used++;
+                }
+            };
+            bool boxOn = false;
+            if (MODEL == kModelOct) {
+                // the warp's displaced-midpoint box over its lanes' (t0_n,
+                // parameters): per block of 32 traces, lane j tests trace j
+                // against it and the traces no lane can pass count as not
+                // used for every lane without their per-lane test
+                const OctWarpBox box = oct_warp_box(a.octBox, member, t0n, p1, kc, h0);
+                boxOn = box.on;
+                if (boxOn) {
+                    oct_box_store(sfBox[warp], box);
+                    for (uint32_t qb = 0; qb < cnt; qb += 32) {
+                        const uint32_t nb = min(32u, cnt - qb);
+                        bool keep = false;
+                        if ((uint32_t)lane < nb)
+                            keep = oct_box_keep(a, ol, a.selIdx ? a.selIdx[first + qb + lane]
+                                                                : first + qb + lane,
+                                                sfBox[warp], m0);
+                        uint32_t mask = __ballot_sync(0xffffffffu, keep);
+                        if (member) nu += nb - (uint32_t)__popc(mask);
+                        for (; mask; mask &= mask - 1) {
+                            const uint32_t bit = (uint32_t)__ffs(mask) - 1;
+                            if (member)
+                                evalTrace(a.selIdx ? a.selIdx[first + qb + bit] : first + qb + bit);
                         }
-                        used++;
                     }
                 }
-                reduce_semblance(num, lin, den, a.w, used, &sembl, &stack);
             }
-            if (ni < nn && sembl > best) {
+            if (!boxOn && member)
+                for (uint32_t q = 0; q < cnt; q++)
+                    evalTrace(a.selIdx ? a.selIdx[first + q] : first + q);
+            float sembl = 0.f, stack = 0.f;
+            if (member) reduce_semblance(num, lin, den, a.w, used, &sembl, &stack);
+            if (member && sembl > best) {
                 best = sembl;
                 bestK = stack;
                 bestI = (uint32_t)ni;

@@ -98,3 +98,29 @@ def test_stretch_free_argument_errors(engine):
     from highperformanceseismicstacking_gb300 import capi
     with pytest.raises(capi.HpssError):
         engine.stretch_free(z["m0s"][:1], z["results"][:1, 2:3], -1)
+
+
+@pytest.mark.parametrize("slope,h0", [(1e-3, 0.0), (5e-3, 0.0), (1e-3, 500.0), (5e-3, 1000.0)])
+def test_oct_stretch_free_box_test_keeps_results(engine, monkeypatch, slope, h0):
+    """OCT stretch-free: a warp (one sample, lanes over n) drops, per block of
+    32 traces, those no lane's displaced midpoint can reach (the box of the
+    lanes' t0 and parameters) before the per-lane tests; blocks and
+    not-used counts equal those with the box test off
+    (HPSS_OCT_BOX_TEST=0)."""
+    line = synthetic.structured_line(n_cmp=24, fold_range=(6, 12), h_max=2500, ns=400,
+                                     dt_us=2000, n_reflectors=4, f=20.0, snr=8.0, seed=14)
+    lower, upper = [1200.0, -slope], [5000.0, slope]
+    engine.upload_gather(line.samples, line.midpoints, line.halfoffsets, float(line.dt))
+    engine.set_traveltime("oct", lower, upper, 150.0, h0)
+    engine.set_window(4)
+    m0s = line.cdp_midpoints[2::5]
+    ls, _ = engine.linear_search(m0s, [9, 7], "tuned")
+    prior = np.ascontiguousarray(ls[:, 2:])
+    sf, st = engine.stretch_free(m0s, prior, 10)
+    monkeypatch.setenv("HPSS_OCT_BOX_TEST", "0")
+    sf0, st0 = engine.stretch_free(m0s, prior, 10)
+    monkeypatch.delenv("HPSS_OCT_BOX_TEST")
+    assert st0["not_used"] > 0
+    assert st["not_used"] == st0["not_used"]
+    assert st["selected_traces"] == st0["selected_traces"]
+    assert np.array_equal(sf, sf0)
