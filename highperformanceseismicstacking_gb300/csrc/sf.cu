@@ -118,9 +118,11 @@ __global__ void __launch_bounds__(kSfWarps * 32) sf_kernel(LsParams a, uint32_t 
             if (!boxOn && member)
                 for (uint32_t q = 0; q < cnt; q++)
                     evalTrace(a.selIdx ? a.selIdx[first + q] : first + q);
+            // an n whose sample s - n lies outside the trace keeps semblance
+            // 0 and still takes part in the argmax, as in the reference
             float sembl = 0.f, stack = 0.f;
             if (member) reduce_semblance(num, lin, den, a.w, used, &sembl, &stack);
-            if (member && sembl > best) {
+            if (ni < nn && sembl > best) {
                 best = sembl;
                 bestK = stack;
                 bestI = (uint32_t)ni;
