@@ -201,27 +201,22 @@ __device__ __forceinline__ void de_eval(const DeParams &d, const OctLine &ol, fl
                 const float2 d2 = __ffma2_rn(y0, kNeg1, de_f2(ya[j + 1], yb[j + 1]));
                 u2[j] = __ffma2_rn(d2, fq, y0);
             }
-            // the sums take trace ti0, then trace ti1
-            if (ina) {
+            // the sums take trace ti0, then trace ti1; a window outside its
+            // trace read zeros (u = 0: it adds nothing) and is not counted;
+            // the linear sum is taken from the per-tap sums at the end
 #pragma unroll
-                for (int j = 0; j < W; j++) {
-                    const float u = u2[j].x;
-                    num[j] += u;
-                    lin += u;
-                    den += u * u;
-                }
-                used++;
+            for (int j = 0; j < W; j++) {
+                const float u = u2[j].x;
+                num[j] += u;
+                den += u * u;
             }
-            if (inb) {
 #pragma unroll
-                for (int j = 0; j < W; j++) {
-                    const float u = u2[j].y;
-                    num[j] += u;
-                    lin += u;
-                    den += u * u;
-                }
-                used++;
+            for (int j = 0; j < W; j++) {
+                const float u = u2[j].y;
+                num[j] += u;
+                den += u * u;
             }
+            used += (ina ? 1u : 0u) + (inb ? 1u : 0u);
         }
     }
     // OCT: (t0, candidate) factors once, trace factors from the line's table
@@ -316,6 +311,13 @@ __device__ __forceinline__ void de_eval(const DeParams &d, const OctLine &ol, fl
             }
             used++;
         }
+    }
+    if (MODEL != kModelOct && W > 0) {
+        // CMP / ZO-CRS: the linear sum is the sum of the per-tap sums (the
+        // same values added in another order)
+        lin = 0.f;
+#pragma unroll
+        for (int j = 0; j < (W > 0 ? W : 1); j++) lin += num[j];
     }
     reduce_semblance(num, lin, den, w, used, sembl, stack);
     *notUsed += nu;

@@ -538,6 +538,44 @@ __device__ __forceinline__ void load_window(const LsParams &a, uint32_t ti, int 
         for (int j = 0; j < N; j++) y[j] = __ldg(r + j);
     }
 }
+// The W taps of the window of trace ti starting at sample k with fraction
+// frac, added to the sums (COMPUTE_SEMBLANCE, interface.h:26-44): each
+// amplitude loaded as its tap needs it (one live value, not W + 1).
+template <int W>
+__device__ __forceinline__ void accum_window(const LsParams &a, uint32_t ti, int k, float frac,
+                                             float (&num)[W], float &lin, float &den) {
+    if (a.samples16) {
+        const uint16_t *r = a.samples16 + (size_t)ti * a.stride + k;
+        const float sc = a.storage == 2 ? __ldg(a.scale + ti) : 1.f;
+        auto wid = [&](uint16_t b) {
+            return a.storage == 2 ? __half2float(__ushort_as_half(b)) * sc
+                                  : __uint_as_float((uint32_t)b << 16);
+        };
+        float y1 = wid(__ldg(r));
+#pragma unroll
+        for (int j = 0; j < W; j++) {
+            const float y0 = y1;
+            y1 = wid(__ldg(r + j + 1));
+            const float u = (y1 - y0) * frac + y0;
+            num[j] += u;
+            lin += u;
+            den += u * u;
+        }
+    } else {
+        const float *r = a.samples + (size_t)ti * a.stride + k;
+        float y1 = __ldg(r);
+#pragma unroll
+        for (int j = 0; j < W; j++) {
+            const float y0 = y1;
+            y1 = __ldg(r + j + 1);
+            const float u = (y1 - y0) * frac + y0;
+            num[j] += u;
+            lin += u;
+            den += u * u;
+        }
+    }
+}
+
 // One amplitude (runtime-sized windows).
 __device__ __forceinline__ float amp_at(const LsParams &a, uint32_t ti, int k) {
     return a.samples16 ? amp16(a, ti, __ldg(a.samples16 + (size_t)ti * a.stride + k))
@@ -595,16 +633,7 @@ __device__ __forceinline__ void oct_eval_batch(const LsParams &a, const OctLine 
             continue;
         const WinIdx wi = window_index(t, a.dt);
         if (window_in_trace(wi.k, a.tau, (int)a.S)) {
-            float y[W + 1];
-            load_window(a, tb[b], wi.k - a.tau, y);
-#pragma unroll
-            for (int jj = 0; jj < W; jj++) {
-                const float y0 = y[jj], y1 = y[jj + 1];
-                const float u = (y1 - y0) * wi.frac + y0;
-                num[jj] += u;
-                lin += u;
-                den += u * u;
-            }
+            accum_window<W>(a, tb[b], wi.k - a.tau, wi.frac, num, lin, den);
             used++;
         }
     }

@@ -126,15 +126,7 @@ ls_oct_kernel(LsParams a, uint32_t tiles, uint32_t parts, uint32_t chunksPerPart
                 if (ok == 0) return;
                 const WinIdx wi = window_index(t, a.dt);
                 if (window_in_trace(wi.k, tau, S)) {
-                    float y[W + 1];
-                    load_window(a, ti, wi.k - tau, y);
-#pragma unroll
-                    for (int jj = 0; jj < W; jj++) {
-                        const float u = (y[jj + 1] - y[jj]) * wi.frac + y[jj];
-                        num[jj] += u;
-                        lin += u;
-                        den += u * u;
-                    }
+                    accum_window<W>(a, ti, wi.k - tau, wi.frac, num, lin, den);
                     used++;
                 }
             };
