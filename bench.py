@@ -77,6 +77,10 @@ def parse():
     ap.add_argument("--no-io-side", action="store_true", help="skip the SU input/output side")
     ap.add_argument("--no-reference-cuda", action="store_true",
                     help="reference arm: skip timing the reference's CUDA kernels")
+    ap.add_argument("--profile-case", default=None, choices=sorted(PROFILE_CASES),
+                    help="run one small case of one kernel instead of the benchmark: a "
+                         "warm-up call, then the call an ncu capture takes "
+                         "(-k <kernel> -s 1 -c 1)")
     return ap.parse_args()
 
 
@@ -554,6 +558,78 @@ def fp64_agreement_side(n_mid, local):
     return res
 
 
+def _case_ls(workload, n_cmp, mid_count, gran=None, storage="fp32"):
+    from highperformanceseismicstacking_gb300 import capi
+    w, line, lower, upper, tau = make_workload(workload, n_cmp)
+    m0s = line.cdp_midpoints
+    if mid_count:
+        mid = len(m0s) // 2
+        m0s = m0s[mid:mid + mid_count]
+    with capi.Engine(0) as eng:
+        eng.upload_gather(line.samples, line.midpoints, line.halfoffsets, float(line.dt),
+                          storage=storage)
+        eng.set_traveltime(w.model, lower, upper, w.apm, 0.0)
+        eng.set_window(tau)
+        for _ in range(2):
+            _, st = eng.linear_search(m0s, gran or w.granularity, "tuned")
+    return st
+
+
+def _case_oct_pipeline(stage):
+    from highperformanceseismicstacking_gb300 import capi
+    w, line, lower, upper, tau = make_workload("oct-de")
+    mid = len(line.cdp_midpoints) // 2
+    m0s = line.cdp_midpoints[mid:mid + 1]
+    with capi.Engine(0) as eng:
+        eng.upload_gather(line.samples, line.midpoints, line.halfoffsets, float(line.dt),
+                          storage="fp16")
+        eng.set_traveltime("oct", lower, upper, w.apm, 0.0)
+        eng.set_window(tau)
+        eng.set_oct_half_offsets([0.0, 500.0, 1000.0])
+        gens = 20 if stage == "de" else 2
+        for _ in range(2):
+            de, st = eng.differential_evolution(m0s, w.population, gens, w.de_f, w.de_cr, seed=7)
+        if stage == "sf":
+            for _ in range(2):
+                _, st = eng.stretch_free(m0s, np.ascontiguousarray(de[:, 2:]), 10)
+    return st
+
+
+def _case_zocrs_de():
+    from highperformanceseismicstacking_gb300 import capi
+    w, line, lower, upper, tau = make_workload("zocrs-de")
+    mid = len(line.cdp_midpoints) // 2
+    m0s = line.cdp_midpoints[mid:mid + 16]
+    with capi.Engine(0) as eng:
+        eng.upload_gather(line.samples, line.midpoints, line.halfoffsets, float(line.dt))
+        eng.set_traveltime("zocrs", lower, upper, w.apm)
+        eng.set_window(tau)
+        for _ in range(2):
+            _, st = eng.differential_evolution(m0s, w.population, w.generations, w.de_f,
+                                               w.de_cr, seed=7)
+    return st
+
+
+# Small cases for ncu captures (the profiles' commands): each runs its kernel
+# once as a warm-up and once more; the tuned linear search with a fixed shape
+# (HPSS_LS_VARIANT) has one launch of its kernel per call.
+PROFILE_CASES = {
+    # ls_tuned2_kernel: 300 CMPs of the CMP production line (1.44e10 evals)
+    "cmp": lambda: _case_ls("cmp-production", 300, 0),
+    # ls_tuned2_kernel: 4 midpoints of the ZO-CRS line, 21 x 21 x 41 candidates
+    "zocrs": lambda: _case_ls("zocrs-ls", None, 4),
+    # ls_oct_kernel: 4 midpoints of the OCT DE line, 11 x 5 candidates
+    "octls": lambda: _case_ls("oct-de", None, 4, gran=[11, 5]),
+    # de_kernel: OCT DE over h0 0 / 500 / 1000 m, FP16 storage, 1 midpoint,
+    # population 48, 20 generations
+    "octde": lambda: _case_oct_pipeline("de"),
+    # sf_kernel: the OCT stretch-free stack after a 2-generation DE, 3 h0, FP16
+    "octsf": lambda: _case_oct_pipeline("sf"),
+    # de_kernel: ZO-CRS DE, 16 midpoints, population 32, 60 generations
+    "zocrsde": _case_zocrs_de,
+}
+
+
 def time_call(eng, stream, d_m0, n_m0, gran, d_out, kernel, reps=1):
     """One untimed call (autotuning, first-launch costs), then `reps` calls
     timed with CUDA events on the engine's stream; ms per call."""
@@ -706,6 +782,12 @@ def cpu_baseline(w, line, lower, upper, tau, seconds):
 def main():
     args = parse()
     world, rank, local = dist_env()
+    if args.profile_case:
+        st = PROFILE_CASES[args.profile_case]()
+        print(json.dumps({"profile_case": args.profile_case, "kernel_ms": st["kernel_ms"],
+                          "evals": st["evals"], "not_used": st["not_used"],
+                          "kernel_variant": st["kernel_variant"]}))
+        return
     if args.impl == "reference":
         run_reference(args, world, rank)
         return
