@@ -19,6 +19,7 @@ from __future__ import annotations
 
 import argparse
 import os
+from ctypes import c_int as C_int
 from typing import Callable, Dict, Optional, Sequence
 
 import numpy as np
@@ -115,8 +116,13 @@ def main(argv: Optional[Sequence[str]] = None) -> int:
             "h0s": a.h0 if len(a.h0) > 1 else None, "tau_index": g.tau_index,
             "population": a.population, "generations": a.generations, "F": a.de_f,
             "CR": a.de_cr, "seed": a.seed, "storage": a.storage}
+    # one GPU per process; more processes than GPUs share them round-robin
+    from . import capi
+    n_dev = C_int()
+    capi.lib().hpss_device_count(n_dev)
+    device = local % max(1, n_dev.value)
     part = run_shard(g.samples, g.midpoints, g.halfoffsets, float(g.dt), cdp, spec, world, rank,
-                     engine_compute(local))
+                     engine_compute(device))
     parts = [part]
     if world > 1:
         import torch.distributed as dist
