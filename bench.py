@@ -55,7 +55,10 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--de-cmps", type=int, default=2,
-                    help="midpoints of the DE side measurement (0: skip)")
+                    help="midpoints of the OCT DE side measurement (0: skip)")
+    ap.add_argument("--zocrs-de-cmps", type=int, default=8,
+                    help="midpoints of the ZO-CRS DE side measurement (8 midpoints x 1500 "
+                         "samples = 1500 CTAs of eight populations, about 2.5 waves)")
     ap.add_argument("--per-midpoint-calls", type=int, default=64,
                     help="one-midpoint calls timed beside the batched call (0: skip)")
     ap.add_argument("--no-storage-side", action="store_true",
@@ -72,8 +75,9 @@ def parse():
     ap.add_argument("--fp64-cmps", type=int, default=7,
                     help="midpoints of the ZO-CRS line (1500 samples each) on which every "
                          "FP32 mode is compared with the FP64 search (0: skip)")
-    ap.add_argument("--sf-cmps", type=int, default=20,
-                    help="midpoints of the CMP stretch-free side measurement (0: skip)")
+    ap.add_argument("--sf-cmps", type=int, default=2000,
+                    help="midpoints of the CMP stretch-free side measurement (0: skip); "
+                         "the default is the whole production line")
     ap.add_argument("--no-io-side", action="store_true", help="skip the SU input/output side")
     ap.add_argument("--no-reference-cuda", action="store_true",
                     help="reference arm: skip timing the reference's CUDA kernels")
@@ -253,7 +257,7 @@ def zocrs_side_measure(n_cmp, local):
             "storage": storage}
 
 
-def de_side_measure(n_cmp, local):
+def de_side_measure(n_cmp, local, n_cmp_zocrs=None):
     """Fused differential evolution on midpoints of the DE workloads: ZO-CRS
     (500-CMP line, 1500 samples, population 32, 60 generations, F 0.5, CR 0.9)
     and OCT (800-CMP line, 3000 samples, population 48, 80 generations,
@@ -263,7 +267,8 @@ def de_side_measure(n_cmp, local):
     for name in ("zocrs-de", "oct-de"):
         w, line, lower, upper, tau = make_workload(name)
         mid = len(line.cdp_midpoints) // 2
-        m0s = np.ascontiguousarray(line.cdp_midpoints[mid:mid + n_cmp])
+        k = n_cmp_zocrs if (name == "zocrs-de" and n_cmp_zocrs) else n_cmp
+        m0s = np.ascontiguousarray(line.cdp_midpoints[mid:mid + k])
         with capi.Engine(local) as eng:
             eng.upload_gather(line.samples, line.midpoints, line.halfoffsets, float(line.dt))
             eng.set_traveltime(w.model, lower, upper, w.apm, w.h0)
@@ -595,6 +600,21 @@ def _case_oct_pipeline(stage):
     return st
 
 
+def _case_cmp_sf():
+    from highperformanceseismicstacking_gb300 import capi
+    w, line, lower, upper, tau = make_workload("cmp-production", 300)
+    m0s = line.cdp_midpoints
+    with capi.Engine(0) as eng:
+        eng.upload_gather(line.samples, line.midpoints, line.halfoffsets, float(line.dt))
+        eng.set_traveltime("cmp", lower, upper)
+        eng.set_window(tau)
+        ls, _ = eng.linear_search(m0s, w.granularity, "tuned")
+        prior = np.ascontiguousarray(ls[:, 2:3])
+        for _ in range(2):
+            _, st = eng.stretch_free(m0s, prior, 10)
+    return st
+
+
 def _case_zocrs_de():
     from highperformanceseismicstacking_gb300 import capi
     w, line, lower, upper, tau = make_workload("zocrs-de")
@@ -623,8 +643,11 @@ PROFILE_CASES = {
     # de_kernel: OCT DE over h0 0 / 500 / 1000 m, FP16 storage, 1 midpoint,
     # population 48, 20 generations
     "octde": lambda: _case_oct_pipeline("de"),
-    # sf_kernel: the OCT stretch-free stack after a 2-generation DE, 3 h0, FP16
+    # sf_block_kernel: the OCT stretch-free stack after a 2-generation DE, 3 h0, FP16
     "octsf": lambda: _case_oct_pipeline("sf"),
+    # sf_block_kernel: CMP stretch-free (21 n, window 7) on 300 CMPs of the
+    # production line over the tuned search's velocities
+    "cmpsf": _case_cmp_sf,
     # de_kernel: ZO-CRS DE, 16 midpoints, population 32, 60 generations
     "zocrsde": _case_zocrs_de,
 }
@@ -985,7 +1008,8 @@ def main():
     zocrs = None
     if args.zocrs_cmps > 0 and args.workload != "zocrs-ls":
         zocrs = zocrs_side_measure(args.zocrs_cmps, local)
-    de = de_side_measure(args.de_cmps, local) if args.de_cmps > 0 else None
+    de = (de_side_measure(args.de_cmps, local, args.zocrs_de_cmps)
+          if args.de_cmps > 0 else None)
     oct_ls = oct_ls_side(args.oct_cmps, local) if args.oct_cmps > 0 else None
     sf = sf_side(args.sf_cmps, local) if args.sf_cmps > 0 else None
     c5 = c5_side_measure(args.c5_cmps, local) if args.c5_cmps > 0 else None

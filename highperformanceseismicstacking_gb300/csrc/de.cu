@@ -30,9 +30,11 @@
 // (other midpoints, other half-offsets, another process's shard).
 #include <algorithm>
 #include <cstdlib>
+#include <cstring>
 
 #include "hpss_device.cuh"
 #include "hpss_internal.h"
+#include "stage.cuh"
 
 namespace hpss {
 
@@ -323,6 +325,272 @@ __device__ __forceinline__ void de_eval(const DeParams &d, const OctLine &ol, fl
     *notUsed += nu;
 }
 
+// ---- CMP / ZO-CRS: the CTA's trials over spans staged in shared memory --
+//
+// The individuals of a sample sit at scattered parameters, so the windows a
+// warp reads from one trace are scattered, and a warp's load from L1 touches
+// many cache lines.  Instead the CTA stages, round by round, the sample spans
+// of consecutive selected traces that any window of its current trials can
+// touch (trace_span over the trials' parameter box and the CTA's t0 range;
+// the box is taken anew for every evaluation, so the spans shrink as the
+// populations converge) into shared memory -- bulk copies for FP32 rows,
+// widening loads for 16-bit rows -- and every thread reads its windows from
+// there.  Each trial's sums take the same values in the same trace order as
+// de_eval's, so the results are the same bit for bit.
+constexpr int kDeStageFloats = 10240;  // 40 KB of spans per CTA
+constexpr int kDeZeroPad = 16;         // zeros first: windows outside their trace read these
+
+struct DeStage {
+    float y[kDeStageFloats];
+    int base[kDeThreadsMax];  // per round slot: stage index of the trace's sample 0
+    int lo[kDeThreadsMax];
+    int len[kDeThreadsMax];
+    int warpSum[kDeThreadsMax / 32];
+    int warpLen[kDeThreadsMax / 32];
+    float boxW[kDeThreadsMax / 32][6];
+    unsigned long long bar;  // mbarrier of a round's bulk copies
+};
+
+// Stage index of a window's first sample, kept inside the stage (the spans
+// hold every window of the trials, so the clamp changes nothing; checked
+// builds report a window outside its span).
+__device__ __forceinline__ int de_stage_index(int b, int w) {
+    return (int)min((unsigned)b, (unsigned)(kDeStageFloats - w - 1));
+}
+
+// Called by every thread of the CTA (inactive threads stage and synchronise
+// only).  False when a round's copies did not complete in time (reported in
+// the error word); every thread then gets false.
+template <int MODEL, int W>
+__device__ bool de_eval_staged(const DeParams &d, DeStage &st, uint32_t &phase, float t0,
+                               float t0a, float t0b, float m0, uint32_t first, uint32_t cnt,
+                               bool active, const float *x, float *sembl, float *stack) {
+    const LsParams &a = d.ls;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nWarps = (int)(blockDim.x >> 5);
+    const float v = x[0];
+    const float c = 4.0f / (v * v);
+    const float p1 = MODEL != kModelCmp ? x[1] : 0.f;
+    const float p2 = MODEL == kModelZocrs ? x[2] : 0.f;
+    // the active trials' parameter box: (c, p1, p2), min and max
+    const float inf = __int_as_float(0x7f800000);
+    float bx[6] = {active ? c : inf,  active ? c : -inf,  active ? p1 : inf,
+                   active ? p1 : -inf, active ? p2 : inf, active ? p2 : -inf};
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+#pragma unroll
+        for (int j = 0; j < 6; j += 2) {
+            bx[j] = fminf(bx[j], __shfl_xor_sync(0xffffffffu, bx[j], o));
+            bx[j + 1] = fmaxf(bx[j + 1], __shfl_xor_sync(0xffffffffu, bx[j + 1], o));
+        }
+    }
+    __syncthreads();  // the previous evaluation's last round is read
+    if (lane == 0) {
+#pragma unroll
+        for (int j = 0; j < 6; j++) st.boxW[warp][j] = bx[j];
+    }
+    __syncthreads();
+    float cb[6];
+#pragma unroll
+    for (int j = 0; j < 6; j++) {
+        float r = st.boxW[0][j];
+        for (int wv = 1; wv < nWarps; wv++)
+            r = (j & 1) ? fmaxf(r, st.boxW[wv][j]) : fminf(r, st.boxW[wv][j]);
+        cb[j] = r;
+    }
+    const bool anyActive = cb[0] <= cb[1];
+
+    float num[W];
+#pragma unroll
+    for (int j = 0; j < W; j++) num[j] = 0.f;
+    float den = 0.f;
+    unsigned used = 0;
+    const float2 c2 = de_f2(c, c), a2 = de_f2(p1, p1), b2 = de_f2(p2, p2);
+    const float t0sq = __fmul_rn(t0, t0);
+    const float2 t02 = de_f2(t0, t0), t0sq2 = de_f2(t0sq, t0sq);
+    const float2 negM02 = de_f2(-m0, -m0);
+    const float rdt = 1.0f / a.dt;
+    const float2 rdt2 = de_f2(rdt, rdt);
+    const float2 kNeg1 = de_f2(-1.f, -1.f);
+    const float2 kMagic2 = de_f2(8388608.f, 8388608.f), kNegMagic2 = de_f2(-8388608.f, -8388608.f);
+    for (uint32_t q0 = 0; q0 < cnt;) {
+        // spans of the next traces, one per thread, packed in trace order
+        const uint32_t q = q0 + threadIdx.x;
+        int lo = 0, len = 0;
+        if (anyActive && q < cnt) {
+            const uint32_t ti = first + q;
+            trace_span<MODEL>(a, cb, m0, t0a, t0b, a.mid[ti], a.hsq[ti], &lo, &len);
+        }
+        int incl = len;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int vv = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += vv;
+        }
+        if (lane == 31) st.warpSum[warp] = incl;
+        __syncthreads();  // also: the previous round's windows are read
+        int off = kDeZeroPad + incl - len;
+        for (int wv = 0; wv < warp; wv++) off += st.warpSum[wv];
+        // the spans that fit form a prefix of the threads (offsets only grow)
+        const bool fits = q < cnt && off + len <= kDeStageFloats;
+        const int keptLen = __reduce_add_sync(0xffffffffu, fits ? len : 0);
+        if (lane == 0) st.warpLen[warp] = keptLen;
+        if (fits) {
+            st.base[threadIdx.x] = off - lo;
+            st.lo[threadIdx.x] = lo;
+            st.len[threadIdx.x] = len;
+        }
+        const uint32_t nfit = (uint32_t)__syncthreads_count(fits);
+        if (nfit == 0) {
+            // a span longer than the stage (the host stages only rows that fit)
+            if (threadIdx.x == 0) atomicOr(a.errorWord, kErrSpanOverflow);
+            break;
+        }
+        if (a.samples16 == nullptr) {
+            if (threadIdx.x == 0) {
+                uint32_t floats = 0;
+                for (int wv = 0; wv < nWarps; wv++) floats += (uint32_t)st.warpLen[wv];
+                stage_bar_expect(&st.bar, floats * 4u);
+            }
+            if (fits && len > 0) {
+                // the previous round's reads are ordered before the async-proxy writes
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                stage_bulk_copy(st.y + off, a.samples + (size_t)(first + q) * a.stride + lo,
+                                (uint32_t)len * 4u, &st.bar);
+            }
+            const bool ok = stage_bar_wait(&st.bar, phase, 1u << 22);
+            phase ^= 1u;
+            if (__syncthreads_or(!ok)) {
+                // report, wait (again bounded) for this CTA's copies in flight
+                if (threadIdx.x == 0) atomicOr(a.errorWord, kErrTimeout);
+                stage_bar_wait(&st.bar, phase ^ 1u, 1u << 22);
+                return false;
+            }
+        } else {
+            // 16-bit rows: a warp per trace, 4 samples per 8-byte load, widened
+            // to FP32 as load_window widens them
+            for (uint32_t j = (uint32_t)warp; j < nfit; j += (uint32_t)nWarps) {
+                const int lj = st.lo[j], nj = st.len[j];
+                const uint32_t ti = first + q0 + j;
+                float4 *dst = reinterpret_cast<float4 *>(st.y + st.base[j] + lj);
+                const uint2 *src =
+                    reinterpret_cast<const uint2 *>(a.samples16 + (size_t)ti * a.stride + lj);
+                const float sc = a.storage == 2 ? __ldg(a.scale + ti) : 1.f;
+                for (int vv = lane; vv < (nj >> 2); vv += 32) {
+                    const uint2 w4 = __ldg(src + vv);
+                    dst[vv] = a.storage == 2
+                                  ? make_float4(half_bits_to_float(w4.x & 0xffffu) * sc,
+                                                half_bits_to_float(w4.x >> 16) * sc,
+                                                half_bits_to_float(w4.y & 0xffffu) * sc,
+                                                half_bits_to_float(w4.y >> 16) * sc)
+                                  : make_float4(__uint_as_float(w4.x << 16),
+                                                __uint_as_float(w4.x & 0xffff0000u),
+                                                __uint_as_float(w4.y << 16),
+                                                __uint_as_float(w4.y & 0xffff0000u));
+                }
+            }
+            __syncthreads();
+        }
+        if (active) {
+            uint32_t j = 0;
+            // two traces per step, as de_eval: both traveltimes and floors in
+            // packed f32x2 ops, both windows read before the sums, which take
+            // the traces in order
+            for (; j + 1 < nfit; j += 2) {
+                const uint32_t ti0 = first + q0 + j, ti1 = ti0 + 1;
+                const float2 hsq2 = de_f2(a.hsq[ti0], a.hsq[ti1]);
+                float2 tt2;
+                if (MODEL == kModelCmp) {
+                    tt2 = __ffma2_rn(c2, hsq2, t0sq2);
+                } else {
+                    const float2 dm2 = __fadd2_rn(de_f2(a.mid[ti0], a.mid[ti1]), negM02);
+                    const float2 x2 = __ffma2_rn(a2, dm2, t02);
+                    const float2 bd2 = __fmul2_rn(b2, dm2);
+                    tt2 = __ffma2_rn(c2, hsq2, __ffma2_rn(bd2, dm2, __fmul2_rn(x2, x2)));
+                }
+                const bool oka = MODEL == kModelCmp || tt2.x >= 0.f;
+                const bool okb = MODEL == kModelCmp || tt2.y >= 0.f;
+                const float2 t2 = MODEL == kModelCmp
+                                      ? de_f2(sqrtf(tt2.x), sqrtf(tt2.y))
+                                      : de_f2(sqrtf(fmaxf(tt2.x, 0.f)), sqrtf(fmaxf(tt2.y, 0.f)));
+                const float2 ti2 = __fmul2_rn(t2, rdt2);
+                const float2 rk = __fadd2_rz(ti2, kMagic2);
+                const float2 fq = __ffma2_rn(__fadd2_rn(rk, kNegMagic2), kNeg1, ti2);  // frac
+                const int ka = __float_as_int(rk.x) - 0x4B000000;
+                const int kb = __float_as_int(rk.y) - 0x4B000000;
+                const bool ina = oka && window_in_trace(ka, a.tau, (int)a.S);
+                const bool inb = okb && window_in_trace(kb, a.tau, (int)a.S);
+#ifdef HPSS_CHECKED
+                if ((ina && (ka - a.tau < st.lo[j] || ka - a.tau + W >= st.lo[j] + st.len[j])) ||
+                    (inb && (kb - a.tau < st.lo[j + 1] ||
+                             kb - a.tau + W >= st.lo[j + 1] + st.len[j + 1])))
+                    atomicOr(a.errorWord, kErrSmemBounds);
+#endif
+                // a window outside its trace reads the zero pad (u = 0); the
+                // clamp keeps every read inside the stage whatever the span
+                const float *ya = st.y + de_stage_index(ina ? st.base[j] + ka - a.tau : 0, W);
+                const float *yb = st.y + de_stage_index(inb ? st.base[j + 1] + kb - a.tau : 0, W);
+                float2 u2[W];
+                float y0a = ya[0], y0b = yb[0];
+#pragma unroll
+                for (int jj = 0; jj < W; jj++) {
+                    const float y1a = ya[jj + 1], y1b = yb[jj + 1];
+                    const float2 y0 = de_f2(y0a, y0b);
+                    const float2 dd = __ffma2_rn(y0, kNeg1, de_f2(y1a, y1b));
+                    u2[jj] = __ffma2_rn(dd, fq, y0);
+                    y0a = y1a;
+                    y0b = y1b;
+                }
+#pragma unroll
+                for (int jj = 0; jj < W; jj++) {
+                    num[jj] += u2[jj].x;
+                    den += u2[jj].x * u2[jj].x;
+                }
+#pragma unroll
+                for (int jj = 0; jj < W; jj++) {
+                    num[jj] += u2[jj].y;
+                    den += u2[jj].y * u2[jj].y;
+                }
+                used += (ina ? 1u : 0u) + (inb ? 1u : 0u);
+            }
+            if (j < nfit) {
+                // an odd trace at the end of the round: de_eval's one-trace step
+                const uint32_t ti = first + q0 + j;
+                float t;
+                const int ok = model_time<MODEL>(t0, c, p1, p2, a.mid[ti], a.hoff[ti], a.hsq[ti],
+                                                 m0, a.apm, a.h0, &t);
+                if (ok > 0) {
+                    const WinIdx wi = window_index(t, a.dt);
+                    if (window_in_trace(wi.k, a.tau, (int)a.S)) {
+#ifdef HPSS_CHECKED
+                        if (wi.k - a.tau < st.lo[j] || wi.k - a.tau + W >= st.lo[j] + st.len[j])
+                            atomicOr(a.errorWord, kErrSmemBounds);
+#endif
+                        const float *yr = st.y + de_stage_index(st.base[j] + wi.k - a.tau, W);
+                        float y1 = yr[0];
+#pragma unroll
+                        for (int jj = 0; jj < W; jj++) {
+                            const float y0 = y1;
+                            y1 = yr[jj + 1];
+                            const float u = (y1 - y0) * wi.frac + y0;
+                            num[jj] += u;
+                            den += u * u;
+                        }
+                        used++;
+                    }
+                }
+            }
+        }
+        q0 += nfit;
+    }
+    // the linear sum is the sum of the per-tap sums, as in de_eval
+    float lin = 0.f;
+#pragma unroll
+    for (int j = 0; j < W; j++) lin += num[j];
+    reduce_semblance(num, lin, den, W, used, sembl, stack);
+    return true;
+}
+
 // One thread per individual.  A CTA holds `spc` whole populations of
 // consecutive samples of one midpoint (thread = sample-in-CTA * pop +
 // individual, the reference's thread layout), so every lane works for any
@@ -354,6 +622,17 @@ de_kernel(DeParams d, uint32_t spc, uint32_t groups, uint32_t nUnits) {
     float *RES = KEY + blockDim.x;                      // [threads][2] fitness, stack
     uint32_t *PERM = reinterpret_cast<uint32_t *>(RES + 2 * (size_t)blockDim.x);
     __shared__ unsigned long long nuCta;
+    // CMP / ZO-CRS with staged spans: the stage follows the populations
+    constexpr bool kStaged = MODEL != kModelOct && W > 0;
+    const bool staged = kStaged && d.staged;
+    DeStage *stg = reinterpret_cast<DeStage *>(
+        deSmem + (((size_t)spc * pop * (NP + 2) + 3) & ~(size_t)3));
+    uint32_t stagePhase = 0;
+    if (staged) {
+        if (threadIdx.x < kDeZeroPad) stg->y[threadIdx.x] = 0.f;
+        if (threadIdx.x == 0) stage_bar_init(&stg->bar);
+        __syncthreads();
+    }
     const uint32_t ls = threadIdx.x / pop;       // sample within the CTA
     const uint32_t ind = threadIdx.x % pop;      // individual
     const bool member = ls < spc;                // threads past spc * pop only sync
@@ -419,6 +698,9 @@ de_kernel(DeParams d, uint32_t spc, uint32_t groups, uint32_t nUnits) {
         const uint32_t mkey = __float_as_uint(m0);   // random-stream key of the midpoint
         const float t0 = static_cast<float>(active ? s : 0) * a.dt;
         const float s0f = static_cast<float>((unit % groups) * spc);  // the CTA's first sample
+        // the t0 range of the CTA's samples (staged spans)
+        const float t0a = s0f * a.dt;
+        const float t0b = static_cast<float>(min((unit % groups) * spc + spc - 1, a.S - 1)) * a.dt;
         float *xs = X + (size_t)(member ? ls : 0) * pop * NP;  // this sample's population
         float x[NP];
         float fx = -1.f, fxk = 0.f;
@@ -434,11 +716,23 @@ de_kernel(DeParams d, uint32_t spc, uint32_t groups, uint32_t nUnits) {
                 x[j] = __fmaf_rn(rng.next(), __fsub_rn(d.hi[j], d.lo[j]), d.lo[j]);
                 xs[ind * NP + j] = x[j];
             }
-            if (MODEL != kModelOct)
+            if (MODEL != kModelOct && !staged)
                 de_eval<MODEL, W>(d, ol, t0, m0, first, cnt, x, &fx, &fxk, &notUsed);
         } else {
 #pragma unroll
             for (int j = 0; j < NP; j++) x[j] = d.lo[j];
+        }
+        if constexpr (kStaged) {
+            if (staged) {
+                float f0, k0;
+                if (!de_eval_staged<MODEL, W>(d, *stg, stagePhase, t0, t0a, t0b, m0, first, cnt,
+                                              active, x, &f0, &k0))
+                    return;  // copies timed out (error word); every thread leaves
+                if (active) {
+                    fx = f0;
+                    fxk = k0;
+                }
+            }
         }
         if (MODEL == kModelOct) {
             evalSorted(x, active, s0f, m0, ol, first, cnt, &fx, &fxk, &notUsed);
@@ -476,8 +770,13 @@ de_kernel(DeParams d, uint32_t spc, uint32_t groups, uint32_t nUnits) {
             float fu = -1.f, fuk = 0.f;
             if (MODEL == kModelOct)
                 evalSorted(u, active, s0f, m0, ol, first, cnt, &fu, &fuk, &notUsed);
+            if constexpr (kStaged) {
+                if (staged && !de_eval_staged<MODEL, W>(d, *stg, stagePhase, t0, t0a, t0b, m0,
+                                                        first, cnt, active, u, &fu, &fuk))
+                    return;  // copies timed out (error word); every thread leaves
+            }
             if (active) {
-                if (MODEL != kModelOct)
+                if (MODEL != kModelOct && !staged)
                     de_eval<MODEL, W>(d, ol, t0, m0, first, cnt, u, &fu, &fuk, &notUsed);
                 if (fu > fx) {
 #pragma unroll
@@ -622,8 +921,11 @@ template <int MODEL, int W>
 cudaError_t launch_de_w(const DeParams &d, uint32_t numSms, uint32_t spc, uint32_t threads,
                         uint32_t groups, uint64_t units, size_t smem, cudaStream_t st) {
     int perSm = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, de_kernel<MODEL, W>,
-                                                                  (int)threads, smem);
+    cudaError_t e = cudaFuncSetAttribute(de_kernel<MODEL, W>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, de_kernel<MODEL, W>, (int)threads,
+                                                      smem);
     if (e != cudaSuccess) return e;
     const uint32_t grid =
         (uint32_t)std::min<uint64_t>(units, (uint64_t)numSms * (uint64_t)std::max(perSm, 1));
@@ -652,16 +954,25 @@ cudaError_t launch_de_model(const DeParams &d, uint32_t numSms, cudaStream_t st)
     if (units > 0x7fffffffull) return cudaErrorInvalidConfiguration;
     // OCT adds the slope-sorted evaluation's regions: trial vectors, keys,
     // fitness / stack pairs and the permutation, one each per thread
-    const size_t smem = de_smem_bytes(spc, pop, NP) +
-                        (MODEL == kModelOct ? (size_t)threads * (NP + 4) * sizeof(float) : 0);
+    // CMP / ZO-CRS: windows from spans staged in shared memory when a whole
+    // row fits the stage (HPSS_DE_STAGED=0: read through L1 instead; the
+    // results are the same bit for bit)
+    DeParams q = d;
+    const char *stagedEnv = std::getenv("HPSS_DE_STAGED");
+    q.staged = MODEL != kModelOct && d.ls.w >= 1 && d.ls.w <= 11 && !d.ls.selIdx &&
+               d.ls.stride + kDeZeroPad <= (uint32_t)kDeStageFloats &&
+               !(stagedEnv && std::strcmp(stagedEnv, "0") == 0);
+    size_t smem = de_smem_bytes(spc, pop, NP) +
+                  (MODEL == kModelOct ? (size_t)threads * (NP + 4) * sizeof(float) : 0);
+    if (q.staged) smem = ((smem + 15) & ~(size_t)15) + sizeof(DeStage);
     switch (d.ls.w) {
-        case 1: return launch_de_w<MODEL, 1>(d, numSms, spc, threads, groups, units, smem, st);
-        case 3: return launch_de_w<MODEL, 3>(d, numSms, spc, threads, groups, units, smem, st);
-        case 5: return launch_de_w<MODEL, 5>(d, numSms, spc, threads, groups, units, smem, st);
-        case 7: return launch_de_w<MODEL, 7>(d, numSms, spc, threads, groups, units, smem, st);
-        case 9: return launch_de_w<MODEL, 9>(d, numSms, spc, threads, groups, units, smem, st);
-        case 11: return launch_de_w<MODEL, 11>(d, numSms, spc, threads, groups, units, smem, st);
-        default: return launch_de_w<MODEL, 0>(d, numSms, spc, threads, groups, units, smem, st);
+        case 1: return launch_de_w<MODEL, 1>(q, numSms, spc, threads, groups, units, smem, st);
+        case 3: return launch_de_w<MODEL, 3>(q, numSms, spc, threads, groups, units, smem, st);
+        case 5: return launch_de_w<MODEL, 5>(q, numSms, spc, threads, groups, units, smem, st);
+        case 7: return launch_de_w<MODEL, 7>(q, numSms, spc, threads, groups, units, smem, st);
+        case 9: return launch_de_w<MODEL, 9>(q, numSms, spc, threads, groups, units, smem, st);
+        case 11: return launch_de_w<MODEL, 11>(q, numSms, spc, threads, groups, units, smem, st);
+        default: return launch_de_w<MODEL, 0>(q, numSms, spc, threads, groups, units, smem, st);
     }
 }
 

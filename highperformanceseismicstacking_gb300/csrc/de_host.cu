@@ -6,6 +6,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <string>
 #include <vector>
 
 #include "hpss_handle.h"
@@ -97,6 +98,9 @@ hpss_status de_impl(hpss_handle h, const float *d_m0s, uint32_t nM0, uint32_t po
     HPSS_CUDA_TRY(h, cudaEventRecord(h->ev2, h->stream));
     if (stats || sync) {
         HPSS_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+        uint32_t err = 0;
+        HPSS_CUDA_TRY(h, cudaMemcpy(&err, d.ls.errorWord, sizeof(uint32_t),
+                                    cudaMemcpyDeviceToHost));
         if (stats) {
             std::memset(stats, 0, sizeof(*stats));
             std::vector<uint32_t> cnt(nM0);
@@ -119,7 +123,12 @@ hpss_status de_impl(hpss_handle h, const float *d_m0s, uint32_t nM0, uint32_t po
             cudaEventElapsedTime(&ms, h->ev0, h->ev1);
             stats->selection_ms = ms;
             stats->kernel_variant = -1;
+            stats->device_error = err;
         }
+        if (err & kErrTimeout)
+            return set_error(h, HPSS_ERR_TIMEOUT,
+                             "staging copies did not complete in time, error word " +
+                                 std::to_string(err));
     }
     return HPSS_OK;
 }

@@ -798,11 +798,10 @@ hpss_status hpss_stretch_free(hpss_handle h, const float *m0s, uint32_t nM0,
     const uint64_t units = (uint64_t)nM0 * h->S;
     if (units > 0xffffffffull)
         return set_error(h, HPSS_ERR_INVALID_ARGUMENT, "too many (midpoint, sample) units");
-    const uint32_t grid = (uint32_t)std::min<uint64_t>((units + 7) / 8, (uint64_t)num_sms(h) * 8);
     // the precision mode with every step in FP64 applies to stretch-free too
     HPSS_CUDA_TRY(h, (h->precisionMode & kPrecF64)
                          ? launch_sf_f64(lp, h->model, (uint32_t)units, h->stream)
-                         : launch_sf(lp, h->model, grid, (uint32_t)units, h->stream));
+                         : launch_sf(lp, h->model, num_sms(h), h->stream));
     HPSS_CUDA_TRY(h, cudaEventRecord(h->ev2, h->stream));
     HPSS_CUDA_TRY(h, cudaMemcpyAsync(out, lp.out, outElems * sizeof(float),
                                      cudaMemcpyDeviceToHost, h->stream));

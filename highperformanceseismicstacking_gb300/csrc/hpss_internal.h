@@ -142,6 +142,7 @@ struct DeParams {
     float F, CR;
     uint32_t seedLo, seedHi;
     float lo[3], hi[3];
+    uint32_t staged;      // CMP / ZO-CRS: windows read from spans staged in shared memory
 };
 constexpr uint32_t kDeMaxPopulation = 128;
 // Target half-offsets of one OCT call (hpss_set_oct_half_offsets).
@@ -258,8 +259,8 @@ cudaError_t launch_convert_storage(const float *src, uint16_t *dst,
                                    uint32_t stride, int storage,
                                    cudaStream_t st);
 cudaError_t launch_de(const DeParams &d, int model, uint32_t numSms, cudaStream_t st);
-cudaError_t launch_sf(const LsParams &p, int model, uint32_t grid, uint32_t nUnits,
-                      cudaStream_t st);
+// stretch-free over p.nM0 midpoints x p.S samples (grid from the SM count)
+cudaError_t launch_sf(const LsParams &p, int model, int numSms, cudaStream_t st);
 cudaError_t launch_sf_select_oct(const LsParams &p, const uint32_t *candFirst,
                                  const uint32_t *candCount, uint32_t *selIdx,
                                  uint32_t *selCount, uint64_t total, cudaStream_t st);

@@ -6,10 +6,22 @@
 // previous search chose at sample s - n are applied at t0 = (s - n) dt and the
 // traveltime is shifted by n dt; the window semblance and stack follow, and
 // the n with the highest semblance is kept (strict '>' over n ascending, so
-// the most negative n wins ties).  A warp owns one sample, its lanes the n
-// values.  The reference runs only CMP on CUDA (its OCT case falls through
-// into `throw`, CudaStretchFreeAlgorithm.cu:86-110); all three models run
-// here, with the same per-model traveltime arithmetic as the searches.
+// the most negative n wins ties).  The reference runs only CMP on CUDA (its
+// OCT case falls through into `throw`, CudaStretchFreeAlgorithm.cu:86-110);
+// all three models run here, with the same per-model traveltime arithmetic
+// as the searches.
+//
+// Two kernels.  sf_block_kernel (windows 3..11, up to 32 n values): a CTA
+// takes 32 consecutive samples of one midpoint, one warp per n value and one
+// lane per sample, so a warp's lanes read consecutive prior parameters and
+// windows lying side by side in each trace (coalesced loads, all lanes busy);
+// the (n, sample) semblances and stacks go to shared memory and one warp then
+// scans n upwards for each sample.  sf_kernel (any window or n count): a warp
+// owns one sample, its lanes the n values.
+#include <algorithm>
+#include <cstdlib>
+#include <cstring>
+
 #include "hpss_device.cuh"
 #include "hpss_internal.h"
 
@@ -193,15 +205,176 @@ __global__ void sf_select_oct_flags_kernel(LsParams a, const uint32_t *candFirst
     if (lane == 0) selIdx[g] = used ? 1u : 0u;
 }
 
-cudaError_t launch_sf(const LsParams &p, int model, uint32_t grid, uint32_t nUnits,
-                      cudaStream_t st) {
-    if (model == kModelCmp)
-        sf_kernel<kModelCmp><<<grid, kSfWarps * 32, 0, st>>>(p, nUnits);
-    else if (model == kModelZocrs)
-        sf_kernel<kModelZocrs><<<grid, kSfWarps * 32, 0, st>>>(p, nUnits);
-    else
-        sf_kernel<kModelOct><<<grid, kSfWarps * 32, 0, st>>>(p, nUnits);
+// ---------------------------------------------------------------------------
+// Block kernel: 32 samples per CTA, warp = n value, lane = sample.
+constexpr int kSfBlockMaxN = 32;  // n values (warps) per CTA
+
+template <int MODEL, int W>
+__global__ void __maxnreg__(40)
+sf_block_kernel(LsParams a, uint32_t blocksPerM0, uint32_t nUnits) {
+    __shared__ float pairS[kSfBlockMaxN][32], pairK[kSfBlockMaxN][32];  // [n][sample]
+    __shared__ float sfBox[kSfBlockMaxN][4];  // each warp's displaced-midpoint box (OCT)
+    constexpr int NP = MODEL == kModelCmp ? 1 : (MODEL == kModelZocrs ? 3 : 2);
+    const int lane = threadIdx.x & 31;
+    const int ni = threadIdx.x >> 5;  // this warp's n value: n = ni - nmax
+    const int S = (int)a.S;
+    const int nn = 2 * a.nmax + 1;    // = warps of the CTA
+    for (uint32_t unit = blockIdx.x; unit < nUnits; unit += gridDim.x) {
+        const uint32_t mi = unit / blocksPerM0;
+        const int s = (int)(unit % blocksPerM0) * 32 + lane;
+        const float m0 = a.m0s[mi];
+        const uint32_t first = a.selFirst[mi], cnt = a.selCount[mi];
+        const float *prior = a.prior + (size_t)mi * NP * a.S;
+        const OctLine ol = oct_line(a, mi);  // OCT: the midpoint's h0 and factor table
+        const float h0 = MODEL == kModelOct ? ol.h0 : 0.f;
+        unsigned nu = 0;
+        const int n = ni - a.nmax;
+        const int sn = s - n;
+        const bool member = s < S && sn >= 0 && sn < S;
+        const int snc = member ? sn : min(s, S - 1);  // a valid sample for the others
+        const float t0n = static_cast<float>(snc) * a.dt;
+        const float v = prior[snc];
+        const float c = 4.0f / (v * v);
+        const float p1 = MODEL != kModelCmp ? prior[a.S + snc] : 0.f;
+        const float p2 = MODEL == kModelZocrs ? prior[2 * a.S + snc] : 0.f;
+        const float nf = static_cast<float>(n);
+        const OctCand kc = oct_cand(t0n, c, p1, h0);
+        float num[W];
+#pragma unroll
+        for (int j = 0; j < W; j++) num[j] = 0.f;
+        float lin = 0.f, den = 0.f;
+        unsigned used = 0;
+        auto evalTrace = [&](uint32_t ti) {
+            float tn;
+            int ok;
+            if (MODEL == kModelOct) {
+                const float4 tf = __ldg(ol.tab + ti);  // {m, gamma^2, 16h^2h0^2, h^2-h0^2}
+                ok = oct_model_time(kc, tf.y, tf.z, tf.w, t0n, c, p1, tf.x, a.hoff[ti], m0,
+                                    a.apm, h0, &tn);
+            } else {
+                ok = model_time<MODEL>(t0n, c, p1, p2, a.mid[ti], a.hoff[ti], a.hsq[ti], m0,
+                                       a.apm, h0, &tn);
+            }
+            if (ok < 0) {
+                nu++;
+                return;
+            }
+            if (ok == 0) return;
+            // t_n + n dt as one fused multiply-add (cmp/stretch_free.cu:55)
+            const float t = __fmaf_rn(nf, a.dt, tn);
+            const WinIdx wi = window_index(t, a.dt);
+            if (window_in_trace(wi.k, a.tau, S)) {
+                accum_window<W>(a, ti, wi.k - a.tau, wi.frac, num, lin, den);
+                used++;
+            }
+        };
+        bool boxOn = false;
+        if (MODEL == kModelOct) {
+            // the warp's displaced-midpoint box over its lanes' (t0_n,
+            // parameters); traces no lane can pass count as not used for
+            // every member lane without their per-lane test
+            const OctWarpBox box = oct_warp_box(a.octBox, member, t0n, p1, kc, h0);
+            boxOn = box.on;
+            if (boxOn) {
+                oct_box_store(sfBox[ni], box);
+                for (uint32_t qb = 0; qb < cnt; qb += 32) {
+                    const uint32_t nb = min(32u, cnt - qb);
+                    bool keep = false;
+                    if ((uint32_t)lane < nb)
+                        keep = oct_box_keep(a, ol, a.selIdx ? a.selIdx[first + qb + lane]
+                                                            : first + qb + lane,
+                                            sfBox[ni], m0);
+                    uint32_t mask = __ballot_sync(0xffffffffu, keep);
+                    if (member) nu += nb - (uint32_t)__popc(mask);
+                    for (; mask; mask &= mask - 1) {
+                        const uint32_t bit = (uint32_t)__ffs(mask) - 1;
+                        if (member)
+                            evalTrace(a.selIdx ? a.selIdx[first + qb + bit] : first + qb + bit);
+                    }
+                }
+            }
+        }
+        if (!boxOn && member)
+            for (uint32_t q = 0; q < cnt; q++) evalTrace(a.selIdx ? a.selIdx[first + q] : first + q);
+        // an n whose sample s - n lies outside the trace keeps semblance 0 and
+        // still takes part in the argmax, as in the reference
+        float sembl = 0.f, stack = 0.f;
+        if (member) reduce_semblance(num, lin, den, W, used, &sembl, &stack);
+        pairS[ni][lane] = sembl;
+        pairK[ni][lane] = stack;
+        if (MODEL == kModelOct && a.notUsed) {
+#pragma unroll
+            for (int o = 16; o; o >>= 1) nu += __shfl_xor_sync(0xffffffffu, nu, o);
+            if (lane == 0 && nu) atomicAdd(a.notUsed + mi, (unsigned long long)nu);
+        }
+        __syncthreads();
+        // per sample: strict '>' over n ascending (the most negative n wins ties)
+        if (ni == 0 && s < S) {
+            float best = -1.f, bestK = 0.f;
+            int bestI = -1;
+            for (int k = 0; k < nn; k++) {
+                const float sv = pairS[k][lane];
+                if (sv > best) {
+                    best = sv;
+                    bestK = pairK[k][lane];
+                    bestI = k;
+                }
+            }
+            float *out = a.out + (size_t)mi * 3 * a.S;
+            out[s] = best;
+            out[a.S + s] = bestK;
+            out[2 * a.S + s] = bestI >= 0 ? (float)(bestI - a.nmax) : 0.f;
+        }
+        __syncthreads();  // the pair arrays are read before the next unit writes them
+    }
+}
+
+template <int MODEL, int W>
+static cudaError_t launch_sf_block(const LsParams &p, int numSms, cudaStream_t st) {
+    const uint32_t blocksPerM0 = (p.S + 31) / 32;
+    const uint64_t units = (uint64_t)p.nM0 * blocksPerM0;
+    if (units > 0xffffffffull) return cudaErrorInvalidConfiguration;
+    const int threads = (2 * p.nmax + 1) * 32;
+    int perSm = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &perSm, sf_block_kernel<MODEL, W>, threads, 0);
+    if (e != cudaSuccess) return e;
+    const uint32_t grid =
+        (uint32_t)std::min<uint64_t>(units, (uint64_t)numSms * (uint64_t)std::max(perSm, 1));
+    sf_block_kernel<MODEL, W><<<grid, threads, 0, st>>>(p, blocksPerM0, (uint32_t)units);
     return cudaGetLastError();
+}
+
+template <int MODEL>
+static cudaError_t launch_sf_model(const LsParams &p, int numSms, cudaStream_t st) {
+    const int nn = 2 * p.nmax + 1;
+    // HPSS_SF_KERNEL=warp: the warp-per-sample kernel for every call (the
+    // two kernels give the same results bit for bit)
+    const char *pick = std::getenv("HPSS_SF_KERNEL");
+    const bool warpKernel = pick && std::strcmp(pick, "warp") == 0;
+    if (nn <= kSfBlockMaxN && !warpKernel) {
+        switch (p.w) {
+            case 3: return launch_sf_block<MODEL, 3>(p, numSms, st);
+            case 5: return launch_sf_block<MODEL, 5>(p, numSms, st);
+            case 7: return launch_sf_block<MODEL, 7>(p, numSms, st);
+            case 9: return launch_sf_block<MODEL, 9>(p, numSms, st);
+            case 11: return launch_sf_block<MODEL, 11>(p, numSms, st);
+            default: break;
+        }
+    }
+    const uint64_t units = (uint64_t)p.nM0 * p.S;
+    if (units > 0xffffffffull) return cudaErrorInvalidConfiguration;
+    const uint32_t grid = (uint32_t)std::min<uint64_t>((units + kSfWarps - 1) / kSfWarps,
+                                                       (uint64_t)numSms * 8);
+    sf_kernel<MODEL><<<grid, kSfWarps * 32, 0, st>>>(p, (uint32_t)units);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sf(const LsParams &p, int model, int numSms, cudaStream_t st) {
+    if (p.nM0 == 0 || p.S == 0) return cudaSuccess;
+    if (model == kModelCmp) return launch_sf_model<kModelCmp>(p, numSms, st);
+    if (model == kModelZocrs) return launch_sf_model<kModelZocrs>(p, numSms, st);
+    return launch_sf_model<kModelOct>(p, numSms, st);
 }
 
 cudaError_t launch_sf_select_oct(const LsParams &p, const uint32_t *candFirst,

@@ -77,6 +77,31 @@ def test_checked_build_reports_no_error_and_same_results(checked_lib, case, kern
     assert np.array_equal(got, want)
 
 
+@pytest.mark.parametrize("model", ["cmp", "zocrs"])
+def test_checked_build_staged_de_windows_stay_in_their_spans(checked_lib, model):
+    """Differential evolution with staged spans in the checked build: every
+    window read from shared memory lies inside its trace's staged span (no
+    HPSS_DEVERR_SMEM_BOUNDS), and the results equal the default build's."""
+    zl = synthetic.structured_line(n_cmp=16, fold_range=(6, 12), h_max=1000, ns=300,
+                                   dt_us=4000, n_reflectors=4, f=20.0, snr=5.0, seed=305)
+    if model == "cmp":
+        lower, upper, apm = [1000.0], [5040.0], 0.0
+    else:
+        a, b = synthetic.zocrs_bounds(1414.2136, 2000.0, 90.0, 0.05)
+        lower, upper, apm = [1414.2136, -a, -b], [6324.5553, a, b], 125.0
+    outs = []
+    for lib in (checked_lib, capi.lib()):
+        with capi.Engine(0, library=lib) as eng:
+            eng.upload_gather(zl.samples, zl.midpoints, zl.halfoffsets, float(zl.dt))
+            eng.set_traveltime(model, lower, upper, apm)
+            eng.set_window(3)
+            got, st = eng.differential_evolution(zl.cdp_midpoints[4:12], 32, 20, 0.5, 0.9,
+                                                 seed=3)
+            assert st["device_error"] == 0
+            outs.append(got)
+    assert np.array_equal(outs[0], outs[1])
+
+
 def test_staging_timeout_is_reported_and_context_survives(checked_lib, monkeypatch):
     line, model, lower, upper, gran, tau, apm = _cases()["cmp-small"]
     want, _ = _search(checked_lib, line, model, lower, upper, gran, tau, apm, "tuned")

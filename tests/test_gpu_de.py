@@ -195,3 +195,34 @@ def test_de_oct_box_test_keeps_results(engine, monkeypatch, slope, h0):
     assert st["selected_traces"] == st0["selected_traces"]
     assert st["not_used"] == st0["not_used"]
     assert np.array_equal(de, de0)
+
+
+@pytest.mark.parametrize("model", ["cmp", "zocrs"])
+@pytest.mark.parametrize("storage", ["fp32", "fp16", "bf16"])
+@pytest.mark.parametrize("tau", [0, 2, 5])
+def test_de_staged_spans_equal_unstaged(engine, monkeypatch, model, storage, tau):
+    """CMP / ZO-CRS DE reads its windows from trace spans staged in shared
+    memory (the spans any window of the CTA's trials can touch); the results
+    equal the evaluation through L1 (HPSS_DE_STAGED=0) bit for bit, with
+    uneven fold (rounds of different trace counts), odd trace counts per
+    round, windows at the trace ends and several sample groups per
+    midpoint, and no device error."""
+    line = synthetic.structured_line(n_cmp=14, fold_range=(5, 13), h_max=1100, ns=260,
+                                     dt_us=4000, n_reflectors=4, f=20.0, snr=5.0, seed=71)
+    if model == "cmp":
+        lower, upper, apm = [1000.0], [5040.0], 0.0
+    else:
+        a, b = synthetic.zocrs_bounds(1414.2136, 2000.0, 90.0, 0.05)
+        lower, upper, apm = [1414.2136, -a, -b], [6324.5553, a, b], 150.0
+    engine.upload_gather(line.samples, line.midpoints, line.halfoffsets, float(line.dt),
+                         storage=storage)
+    engine.set_traveltime(model, lower, upper, apm)
+    engine.set_window(tau)
+    m0s = line.cdp_midpoints[3:11]
+    monkeypatch.delenv("HPSS_DE_STAGED", raising=False)
+    got, st = engine.differential_evolution(m0s, 32, 12, 0.5, 0.9, seed=5)
+    monkeypatch.setenv("HPSS_DE_STAGED", "0")
+    want, st0 = engine.differential_evolution(m0s, 32, 12, 0.5, 0.9, seed=5)
+    monkeypatch.delenv("HPSS_DE_STAGED", raising=False)
+    assert st["device_error"] == 0 and st0["device_error"] == 0
+    assert np.array_equal(got, want)

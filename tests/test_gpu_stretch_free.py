@@ -90,6 +90,45 @@ def test_stretch_free_other_models_vs_oracle(engine, model):
         _check_sf(out[i], sem, stk, 10)
 
 
+@pytest.mark.parametrize("model", ["cmp", "zocrs", "oct"])
+@pytest.mark.parametrize("storage", ["fp32", "fp16"])
+def test_block_kernel_equals_warp_kernel(engine, monkeypatch, model, storage):
+    """The stretch-free block kernel (warp = n value, lane = sample) and the
+    warp-per-sample kernel (lanes = n values) give the same block bit for
+    bit, not-used counts included; a window or n count outside the block
+    kernel's instantiations (window 13, 33 n values) runs the warp kernel."""
+    line = synthetic.structured_line(n_cmp=10, fold_range=(5, 9), h_max=900, ns=300,
+                                     dt_us=4000, n_reflectors=3, f=20.0, snr=6.0, seed=67)
+    if model == "cmp":
+        lower, upper, gran, apm, h0 = [1200.0], [5000.0], [41], 0.0, 0.0
+    elif model == "zocrs":
+        a, b = synthetic.zocrs_bounds(1414.2136, 2000.0, 90.0, 0.05)
+        lower, upper, gran, apm, h0 = [1414.2136, -a, -b], [6324.5553, a, b], [6, 5, 5], 100.0, 0.0
+    else:
+        lower, upper, gran, apm, h0 = [1200.0, -1e-3], [5000.0, 1e-3], [8, 5], 60.0, 300.0
+    engine.upload_gather(line.samples, line.midpoints, line.halfoffsets, float(line.dt),
+                         storage=storage)
+    engine.set_traveltime(model, lower, upper, apm, h0)
+    engine.set_window(3)
+    m0s = line.cdp_midpoints[2:8]
+    ls, _ = engine.linear_search(m0s, gran, "plain")
+    prior = np.ascontiguousarray(ls[:, 2:])
+    for nmax in (0, 7, 15):
+        monkeypatch.delenv("HPSS_SF_KERNEL", raising=False)
+        blk, st_b = engine.stretch_free(m0s, prior, nmax)
+        monkeypatch.setenv("HPSS_SF_KERNEL", "warp")
+        wrp, st_w = engine.stretch_free(m0s, prior, nmax)
+        assert np.array_equal(blk, wrp), (model, storage, nmax)
+        assert st_b["not_used"] == st_w["not_used"]
+    monkeypatch.delenv("HPSS_SF_KERNEL", raising=False)
+    # warp kernel by shape: 33 n values, and window 13
+    big, _ = engine.stretch_free(m0s, prior, 16)
+    assert np.all(np.isfinite(big)) and np.all(np.abs(big[:, 2]) <= 16)
+    engine.set_window(6)
+    w13, _ = engine.stretch_free(m0s, prior, 10)
+    assert np.all(np.isfinite(w13)) and np.all(np.abs(w13[:, 2]) <= 10)
+
+
 def test_stretch_free_argument_errors(engine):
     z = np.load(GOLDEN / "ref_cmp.npz")
     engine.upload_gather(z["samples"], z["midpoints"], z["halfoffsets"], float(z["dt"]))
