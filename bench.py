@@ -79,6 +79,9 @@ def parse():
                     help="midpoints of the CMP stretch-free side measurement (0: skip); "
                          "the default is the whole production line")
     ap.add_argument("--no-io-side", action="store_true", help="skip the SU input/output side")
+    ap.add_argument("--no-whole-lines", action="store_true",
+                    help="skip the whole-line ZO-CRS DE (500 midpoints) and ZO-CRS linear "
+                         "search (1000 midpoints, about a minute) calls")
     ap.add_argument("--no-reference-cuda", action="store_true",
                     help="reference arm: skip timing the reference's CUDA kernels")
     ap.add_argument("--profile-case", default=None, choices=sorted(PROFILE_CASES),
@@ -255,6 +258,54 @@ def zocrs_side_measure(n_cmp, local):
             "speedup_tuned_vs_plain": res["tuned"]["value"] / res["plain"]["value"],
             "tuned_vs_plain": compare_outputs(outs["tuned"], outs["plain"]),
             "storage": storage}
+
+
+def whole_workloads_side(local):
+    """Two workloads end to end in one call each: C4, the ZO-CRS DE over all
+    500 midpoints of the ZO-CRS DE line (population 32, 60 generations), and
+    C3, the tuned ZO-CRS linear search over all 1000 midpoints of the ZO-CRS
+    line (21 x 21 x 41 candidates).  Each after a short warm-up call on the
+    same engine (module load, autotuning); device time from the engine's
+    events, wall time of the call on the host."""
+    from highperformanceseismicstacking_gb300 import capi
+    out = {}
+    w, line, lower, upper, tau = make_workload("zocrs-de")
+    m0s = np.ascontiguousarray(line.cdp_midpoints)
+    with capi.Engine(local) as eng:
+        eng.upload_gather(line.samples, line.midpoints, line.halfoffsets, float(line.dt))
+        eng.set_traveltime(w.model, lower, upper, w.apm, w.h0)
+        eng.set_window(tau)
+        eng.differential_evolution(m0s[:8], w.population, 2, w.de_f, w.de_cr, seed=1)
+        t0 = time.perf_counter()
+        res, st = eng.differential_evolution(m0s, w.population, w.generations, w.de_f, w.de_cr,
+                                             seed=7)
+        wall = time.perf_counter() - t0
+    sel = st["selected_traces"]
+    out["zocrs_de_whole_line"] = {
+        "cmps": int(len(m0s)), "population": w.population, "generations": w.generations,
+        "evals": st["evals"], "kernel_ms": st["kernel_ms"], "selection_ms": st["selection_ms"],
+        "call_wall_s": wall, "value": st["evals"] / (st["kernel_ms"] / 1e3),
+        "mean_best_semblance": float(np.mean(res[:, 0])),
+        "roofline": fp32_roofline(w.model, 2 * tau + 1, st["evals"], 0.0, st["kernel_ms"], local,
+                                  alg_bytes=sel * line.samples_per_trace * 4 + sel * 16)}
+    w, line, lower, upper, tau = make_workload("zocrs-ls")
+    m0s = np.ascontiguousarray(line.cdp_midpoints)
+    with capi.Engine(local) as eng:
+        eng.upload_gather(line.samples, line.midpoints, line.halfoffsets, float(line.dt))
+        eng.set_traveltime(w.model, lower, upper, w.apm, w.h0)
+        eng.set_window(tau)
+        mid = len(m0s) // 2
+        eng.linear_search(m0s[mid:mid + 4], w.granularity, "tuned")
+        t0 = time.perf_counter()
+        _, st = eng.linear_search(m0s, w.granularity, "tuned")
+        wall = time.perf_counter() - t0
+    out["zocrs_ls_whole_line"] = {
+        "cmps": int(len(m0s)), "candidates": int(np.prod(w.granularity)), "evals": st["evals"],
+        "kernel_ms": st["kernel_ms"], "selection_ms": st["selection_ms"], "call_wall_s": wall,
+        "kernel_variant": st["kernel_variant"], "value": st["evals"] / (st["kernel_ms"] / 1e3),
+        "roofline": fp32_roofline("zocrs", 2 * tau + 1, st["evals"], 0.0, st["kernel_ms"],
+                                  local)}
+    return out
 
 
 def de_side_measure(n_cmp, local, n_cmp_zocrs=None):
@@ -826,7 +877,10 @@ def main():
     # Weak scaling: the job is a line of `world` segments of the workload's
     # size; rank r owns segment r (its CMPs shifted past the previous
     # segments), so the work per GPU stays fixed as ranks are added and no
-    # data crosses ranks (midpoints are independent units).
+    # data crosses ranks (midpoints are independent units).  This is the
+    # shard plan of that line (sharding.shard_plan): a CMP gather selects
+    # only its own traces (selection radius 0), so rank r's shard is exactly
+    # segment r, with no halo traces.
     if world > 1 and rank > 0:
         shift = np.float32(rank * (float(line.cdp_midpoints[-1] - line.cdp_midpoints[0]) + 1000.0))
         line.midpoints = (line.midpoints + shift).astype(np.float32)
@@ -1014,6 +1068,7 @@ def main():
     sf = sf_side(args.sf_cmps, local) if args.sf_cmps > 0 else None
     c5 = c5_side_measure(args.c5_cmps, local) if args.c5_cmps > 0 else None
     fp64 = fp64_agreement_side(args.fp64_cmps, local) if args.fp64_cmps > 0 else None
+    whole = None if args.no_whole_lines else whole_workloads_side(local)
     # every kernel against its roofline (FP32-pipe instructions; HBM view of
     # the algorithmic bytes where the line is read)
     rooflines = {f"ls_tuned ({w.name})": roof}
@@ -1031,6 +1086,9 @@ def main():
             if st_ in c5:
                 rooflines[f"de (oct-de, 3 h0, {st_})"] = c5[st_]["de"]["roofline"]
                 rooflines[f"sf (oct-de, 3 h0, {st_})"] = c5[st_]["stretch_free"]["roofline"]
+    if whole:
+        rooflines["de (zocrs-de, whole line)"] = whole["zocrs_de_whole_line"]["roofline"]
+        rooflines["ls_tuned (zocrs-ls, whole line)"] = whole["zocrs_ls_whole_line"]["roofline"]
 
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
            "steps": args.steps, "warmup": args.warmup,
@@ -1066,6 +1124,7 @@ def main():
            "stretch_free": sf,
            "oct_de_stretch_free_pipeline": c5,
            "fp64_agreement": fp64,
+           "whole_workloads": whole,
            "su_io": su_io,
            "rooflines": rooflines,
            "clocks": clk,
