@@ -689,6 +689,8 @@ PROFILE_CASES = {
     "cmp": lambda: _case_ls("cmp-production", 300, 0),
     # ls_tuned2_kernel: 4 midpoints of the ZO-CRS line, 21 x 21 x 41 candidates
     "zocrs": lambda: _case_ls("zocrs-ls", None, 4),
+    # ls_tuned2_kernel (16-bit rows): the same with BF16 amplitude storage
+    "zocrsbf16": lambda: _case_ls("zocrs-ls", None, 4, storage="bf16"),
     # ls_oct_kernel: 4 midpoints of the OCT DE line, 11 x 5 candidates
     "octls": lambda: _case_ls("oct-de", None, 4, gran=[11, 5]),
     # de_kernel: OCT DE over h0 0 / 500 / 1000 m, FP16 storage, 1 midpoint,

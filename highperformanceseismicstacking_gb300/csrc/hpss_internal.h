@@ -211,6 +211,11 @@ cudaError_t launch_ls_tuned_cmp(const LsParams &p, uint32_t grid, uint32_t tiles
 cudaError_t launch_ls_tuned_zocrs(const LsParams &p, uint32_t grid, uint32_t tiles,
                                   uint32_t nUnits, cudaStream_t st, int variant,
                                   bool exactStack);
+// 16-bit rows staged by bulk copies (S16 instantiations)
+cudaError_t launch_ls_tuned_cmp16(const LsParams &p, uint32_t grid, uint32_t tiles,
+                                  uint32_t nUnits, cudaStream_t st, int variant);
+cudaError_t launch_ls_tuned_zocrs16(const LsParams &p, uint32_t grid, uint32_t tiles,
+                                    uint32_t nUnits, cudaStream_t st, int variant);
 cudaError_t launch_ls_tuned_cmp_exact(const LsParams &p, uint32_t grid, uint32_t tiles,
                                       uint32_t nUnits, cudaStream_t st, int variant);
 cudaError_t launch_ls_tuned_zocrs_exact(const LsParams &p, uint32_t grid, uint32_t tiles,

@@ -83,10 +83,13 @@ hpss_status choose_variant(hpss_handle h, const LsParams &lp, uint32_t units, bo
             return HPSS_OK;
         }
     }
-    // trial prefix: three waves of the 2-CTA shape, two of the 3-CTA shapes
-    // (a ZO-CRS unit of 18081 candidates takes ~0.3 s, so the prefix bounds
-    // the first call's tuning time)
-    const uint32_t sub = std::min<uint32_t>(units, (uint32_t)num_sms(h) * 6);
+    // trial prefix: at least three waves of the 2-CTA shape and two of the
+    // 3-CTA shapes, grown (doubling, up to the whole call) until the first
+    // shape's trial takes kTrialMs, so that the launches' timing noise stays
+    // small against the shapes' differences; a ZO-CRS unit of 18081
+    // candidates takes ~0.3 s, so there the first prefix is long enough
+    constexpr float kTrialMs = 4.f;
+    uint32_t sub = std::min<uint32_t>(units, (uint32_t)num_sms(h) * 6);
     struct Events {
         cudaEvent_t a = nullptr, b = nullptr;
         ~Events() {
@@ -97,22 +100,46 @@ hpss_status choose_variant(hpss_handle h, const LsParams &lp, uint32_t units, bo
     HPSS_CUDA_TRY(h, cudaEventCreate(&ev.a));
     HPSS_CUDA_TRY(h, cudaEventCreate(&ev.b));
     cudaEvent_t a = ev.a, b = ev.b;
-    float best = 3.4e38f;
-    int bestV = 0;
-    for (int v = 0; v < kTunedVariants; v++) {
+    auto trial = [&](int v, uint32_t n, float *ms) -> hpss_status {
         HPSS_CUDA_TRY(h, setChunks(2 * kVariantPairs[v]));
-        HPSS_CUDA_TRY(h, launch(v, std::min<uint32_t>(sub, 64)));  // first-launch costs
         HPSS_CUDA_TRY(h, cudaEventRecord(a, h->stream));
-        HPSS_CUDA_TRY(h, launch(v, sub));
+        HPSS_CUDA_TRY(h, launch(v, n));
         HPSS_CUDA_TRY(h, cudaEventRecord(b, h->stream));
         HPSS_CUDA_TRY(h, cudaEventSynchronize(b));
-        float ms = 0;
-        HPSS_CUDA_TRY(h, cudaEventElapsedTime(&ms, a, b));
-        if (ms < best) {
-            best = ms;
-            bestV = v;
+        HPSS_CUDA_TRY(h, cudaEventElapsedTime(ms, a, b));
+        return HPSS_OK;
+    };
+    for (int v = 0; v < kTunedVariants; v++) {  // first-launch costs
+        HPSS_CUDA_TRY(h, setChunks(2 * kVariantPairs[v]));
+        HPSS_CUDA_TRY(h, launch(v, std::min<uint32_t>(sub, 64)));
+    }
+    float t0ms = 0;
+    hpss_status trc = trial(0, sub, &t0ms);
+    if (trc != HPSS_OK) return trc;
+    while (t0ms < kTrialMs && sub < units) {
+        sub = (uint32_t)std::min<uint64_t>((uint64_t)sub * 2, units);
+        trc = trial(0, sub, &t0ms);
+        if (trc != HPSS_OK) return trc;
+    }
+    // every shape timed on the same prefix, twice in alternating order when
+    // a trial is short (the faster of the two counts); shape 0 stays unless
+    // another is faster by more than the noise margin
+    float tms[kTunedVariants];
+    tms[0] = t0ms;
+    const int rounds = t0ms < 50.f ? 2 : 1;
+    for (int r = 0; r < rounds; r++) {
+        for (int i = 0; i < kTunedVariants; i++) {
+            const int v = r % 2 ? kTunedVariants - 1 - i : i;
+            if (r == 0 && v == 0) continue;  // timed above
+            float ms = 0;
+            trc = trial(v, sub, &ms);
+            if (trc != HPSS_OK) return trc;
+            tms[v] = r == 0 ? ms : std::min(tms[v], ms);
         }
     }
+    int bestV = 0;
+    for (int v = 1; v < kTunedVariants; v++)
+        if (tms[v] < tms[bestV] * 0.985f) bestV = v;
     h->variantCache[key] = bestV;
     {
         std::lock_guard<std::mutex> lock(g_variantMutex);

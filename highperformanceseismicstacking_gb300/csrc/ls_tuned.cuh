@@ -101,7 +101,16 @@ __device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b
 //    their rounding errors kept in compensation terms and added once at the
 //    end.  The error is then that of one round's plain sum instead of the
 //    whole aperture's.
-template <int MODEL, int W, int NP, int MINB, bool EXACT_STACK, int PREC = 0>
+//
+// S16: 16-bit rows staged by the TMA engine.  Spans are rounded to 8 samples
+// (16 bytes of 16-bit data); each kept trace's raw span is bulk-copied into
+// the upper half of its FP32 area of the stage and widened in place, a warp
+// per trace, in chunks of 256 samples taken in increasing order: a chunk's
+// lanes read all their raw words before any writes, and the FP32 words of
+// element i only overwrite raw elements below i, which earlier chunks have
+// read.  The widened values are those of the S16 = false kernel's LSU
+// widening (which also serves the precision modes and the exact stack).
+template <int MODEL, int W, int NP, int MINB, bool EXACT_STACK, int PREC = 0, bool S16 = false>
 __global__ void __launch_bounds__(kTunedThreads, MINB)
 ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
     constexpr bool TT64 = (PREC & kPrecTt64) != 0 && MODEL == kModelZocrs;
@@ -229,7 +238,8 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
                     const uint32_t ti = a.selIdx ? a.selIdx[first + q] : first + q;
                     tm = a.mid[ti];
                     thsq = a.hsq[ti];
-                    trace_span<MODEL>(a, cbl, m0, t0a, t0b, tm, thsq, &lo, &len, &full);
+                    trace_span<MODEL, S16 ? 8 : 4>(a, cbl, m0, t0a, t0b, tm, thsq, &lo, &len,
+                                                   &full);
                 }
                 int incl = len;
 #pragma unroll
@@ -276,6 +286,66 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
                     break;
                 }
                 __syncthreads();
+                if constexpr (S16) {
+                    // 16-bit rows: one bulk copy of the raw span into the
+                    // upper half of the trace's FP32 area, then widened in place
+                    if (threadIdx.x == 0) {
+                        uint32_t floats = 0;
+#pragma unroll
+                        for (int wv = 0; wv < kTunedWarps; wv++) floats += (uint32_t)sm.warpLen[wv];
+                        stage_bar_expect(&sm.stageBar, floats * 2u + drillBytes);
+                    }
+                    if (keep) {
+                        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                        const uint32_t ti = a.selIdx ? a.selIdx[first + q] : first + q;
+                        stage_bulk_copy(reinterpret_cast<uint16_t *>(sm.y + off) + len,
+                                        a.samples16 + (size_t)ti * a.stride + lo, (uint32_t)len * 2u,
+                                        &sm.stageBar);
+                    }
+                    const bool ok = stage_bar_wait(&sm.stageBar, stagePhase, waitLimit);
+                    stagePhase ^= 1u;
+                    if (__syncthreads_or(!ok)) {
+                        if (threadIdx.x == 0) atomicOr(a.errorWord, kErrTimeout);
+                        stage_bar_wait(&sm.stageBar, stagePhase ^ 1u, waitLimit);
+                        return;
+                    }
+                    for (int j = warp; j < nkeep; j += kTunedWarps) {
+                        const TraceMeta2 md = sm.meta[j];
+                        const int lo_j = sm.lo[j];
+                        const int n16 = md.len & kLenMask;
+                        float *dst = sm.y + md.base + lo_j;
+                        const uint16_t *raw = reinterpret_cast<const uint16_t *>(dst) + n16;
+                        const float sc = a.storage == 2 ? a.scale[sm.ti[j]] : 1.f;
+                        for (int c0 = 0; c0 < n16; c0 += 256) {
+                            const int i = c0 + 8 * lane;
+                            uint4 r8 = make_uint4(0u, 0u, 0u, 0u);
+                            if (i < n16) r8 = *reinterpret_cast<const uint4 *>(raw + i);
+                            __syncwarp();  // every raw word of the chunk read before any write
+                            if (i < n16) {
+                                float4 *d4 = reinterpret_cast<float4 *>(dst + i);
+                                if (a.storage == 2) {
+                                    d4[0] = make_float4(half_bits_to_float(r8.x & 0xffffu) * sc,
+                                                        half_bits_to_float(r8.x >> 16) * sc,
+                                                        half_bits_to_float(r8.y & 0xffffu) * sc,
+                                                        half_bits_to_float(r8.y >> 16) * sc);
+                                    d4[1] = make_float4(half_bits_to_float(r8.z & 0xffffu) * sc,
+                                                        half_bits_to_float(r8.z >> 16) * sc,
+                                                        half_bits_to_float(r8.w & 0xffffu) * sc,
+                                                        half_bits_to_float(r8.w >> 16) * sc);
+                                } else {
+                                    d4[0] = make_float4(__uint_as_float(r8.x << 16),
+                                                        __uint_as_float(r8.x & 0xffff0000u),
+                                                        __uint_as_float(r8.y << 16),
+                                                        __uint_as_float(r8.y & 0xffff0000u));
+                                    d4[1] = make_float4(__uint_as_float(r8.z << 16),
+                                                        __uint_as_float(r8.z & 0xffff0000u),
+                                                        __uint_as_float(r8.w << 16),
+                                                        __uint_as_float(r8.w & 0xffff0000u));
+                                }
+                            }
+                        }
+                    }
+                } else {
                 if (a.samples16 == nullptr) {
                     // FP32: one bulk copy per span on the TMA engine, the
                     // round's bytes counted off the staging barrier
@@ -326,6 +396,7 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
                         }
                     }
                 }
+                }  // S16
                 __syncthreads();
                 // One trace for all candidates of the thread.  FULL: every
                 // window lies inside the trace (trace_span's conservative
@@ -603,14 +674,14 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
     }
 }
 
-template <int MODEL, int NP, int MINB, bool EXACT_STACK, int PREC = 0>
+template <int MODEL, int NP, int MINB, bool EXACT_STACK, int PREC = 0, bool S16 = false>
 cudaError_t launch_ls_tuned2_model(const LsParams &p, uint32_t grid,
                                    uint32_t tiles, uint32_t nUnits,
                                    cudaStream_t st) {
     const size_t smem = sizeof(Tuned2Smem<MINB>);
 #define HPSS_TUNED2_CASE(WV)                                                  \
     case WV: {                                                                \
-        auto k = ls_tuned2_kernel<MODEL, WV, NP, MINB, EXACT_STACK, PREC>;   \
+        auto k = ls_tuned2_kernel<MODEL, WV, NP, MINB, EXACT_STACK, PREC, S16>; \
         cudaError_t e = cudaFuncSetAttribute(                                 \
             k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);       \
         if (e != cudaSuccess) return e;                                       \

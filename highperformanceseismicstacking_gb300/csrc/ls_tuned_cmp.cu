@@ -9,6 +9,7 @@ cudaError_t launch_ls_tuned_cmp(const LsParams &p, uint32_t grid, uint32_t tiles
                                 uint32_t nUnits, cudaStream_t st, int variant,
                                 bool exactStack) {
     if (exactStack) return launch_ls_tuned_cmp_exact(p, grid, tiles, nUnits, st, variant);
+    if (p.samples16) return launch_ls_tuned_cmp16(p, grid, tiles, nUnits, st, variant);
     if (variant == 1) return launch_ls_tuned2_model<kModelCmp, 1, 3, false>(p, grid, tiles, nUnits, st);
     if (variant == 2) return launch_ls_tuned2_model<kModelCmp, 2, 3, false>(p, grid, tiles, nUnits, st);
     return launch_ls_tuned2_model<kModelCmp, 2, 2, false>(p, grid, tiles, nUnits, st);

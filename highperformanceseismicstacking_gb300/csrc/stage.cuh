@@ -14,12 +14,13 @@ namespace hpss {
 
 // Sample span [lo, lo+len) of trace (m, h, hsq) touched by any in-trace
 // window of the tile [t0a, t0b] and the chunk parameter box.  Conservative by
-// one sample each side; rounded to multiples of 4 samples (16 B) for vector
-// copies.  len = 0 if no window of the tile/chunk can lie inside the trace.
+// one sample each side; rounded to multiples of ALIGN samples (4: 16 bytes
+// of FP32; 8: 16 bytes of 16-bit rows, whose stride is a multiple of 8) for
+// bulk copies.  len = 0 if no window of the tile/chunk can lie inside the trace.
 // *full (optional): every window of the tile and chunk box lies inside the
 // trace (for ZO-CRS also: every squared time is positive), judged on the same
 // conservative bounds, so the evaluation may skip the per-candidate checks.
-template <int MODEL>
+template <int MODEL, int ALIGN = 4>
 __device__ __forceinline__ void trace_span(const LsParams &a, const float *cb,
                                            float m0, float t0a, float t0b,
                                            float m, float hsq, int *lo,
@@ -69,9 +70,9 @@ __device__ __forceinline__ void trace_span(const LsParams &a, const float *cb,
         if (full) *full = false;
         return;
     }
-    int l = (kmin - tau) & ~3;
-    int h = kmax + tau + 1;                  // last sample read
-    int e = min((h + 4) & ~3, (int)a.stride); // exclusive, multiple of 4
+    int l = (kmin - tau) & ~(ALIGN - 1);
+    int h = kmax + tau + 1;                                      // last sample read
+    int e = min((h + ALIGN) & ~(ALIGN - 1), (int)a.stride);      // exclusive, multiple of ALIGN
     *lo = l;
     *len = e - l;
 }

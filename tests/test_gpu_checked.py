@@ -77,6 +77,27 @@ def test_checked_build_reports_no_error_and_same_results(checked_lib, case, kern
     assert np.array_equal(got, want)
 
 
+@pytest.mark.parametrize("storage", ["bf16", "fp16"])
+@pytest.mark.parametrize("case", ["cmp-production-slice-w7", "zocrs", "window-edge-w15"])
+def test_checked_build_16bit_bulk_staging(checked_lib, case, storage):
+    """16-bit rows staged by bulk copies and widened in shared memory, in the
+    checked build: every window inside its staged span, no error, and the
+    default build's results bit for bit."""
+    line, model, lower, upper, gran, tau, apm = _cases()[case]
+    outs = []
+    for lib in (checked_lib, capi.lib()):
+        with capi.Engine(0, library=lib) as eng:
+            eng.upload_gather(line.samples, line.midpoints, line.halfoffsets, float(line.dt),
+                              storage=storage)
+            eng.set_traveltime(model, lower, upper, apm)
+            eng.set_window(tau)
+            got, st = eng.linear_search(line.cdp_midpoints, gran, "tuned")
+            assert st["device_error"] == 0
+            assert st["kernel_variant"] >= 0
+            outs.append(got)
+    assert np.array_equal(outs[0], outs[1])
+
+
 @pytest.mark.parametrize("model", ["cmp", "zocrs"])
 def test_checked_build_staged_de_windows_stay_in_their_spans(checked_lib, model):
     """Differential evolution with staged spans in the checked build: every
