@@ -687,6 +687,8 @@ def _case_zocrs_de():
 PROFILE_CASES = {
     # ls_tuned2_kernel: 300 CMPs of the CMP production line (1.44e10 evals)
     "cmp": lambda: _case_ls("cmp-production", 300, 0),
+    # ls_tuned2_kernel (16-bit rows): the same with BF16 amplitude storage
+    "cmpbf16": lambda: _case_ls("cmp-production", 300, 0, storage="bf16"),
     # ls_tuned2_kernel: 4 midpoints of the ZO-CRS line, 21 x 21 x 41 candidates
     "zocrs": lambda: _case_ls("zocrs-ls", None, 4),
     # ls_tuned2_kernel (16-bit rows): the same with BF16 amplitude storage
