@@ -105,7 +105,7 @@ __device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b
 // S16: 16-bit rows staged by the TMA engine.  Spans are rounded to 8 samples
 // (16 bytes of 16-bit data); each kept trace's raw span is bulk-copied into
 // the upper half of its FP32 area of the stage and widened in place, a warp
-// per trace, in chunks of 256 samples taken in increasing order: a chunk's
+// per trace, in chunks of 128 samples taken in increasing order: a chunk's
 // lanes read all their raw words before any writes, and the FP32 words of
 // element i only overwrite raw elements below i, which earlier chunks have
 // read.  The widened values are those of the S16 = false kernel's LSU
@@ -316,32 +316,22 @@ ls_tuned2_kernel(LsParams a, uint32_t tiles, uint32_t nUnits) {
                         float *dst = sm.y + md.base + lo_j;
                         const uint16_t *raw = reinterpret_cast<const uint16_t *>(dst) + n16;
                         const float sc = a.storage == 2 ? a.scale[sm.ti[j]] : 1.f;
-                        for (int c0 = 0; c0 < n16; c0 += 256) {
-                            const int i = c0 + 8 * lane;
-                            uint4 r8 = make_uint4(0u, 0u, 0u, 0u);
-                            if (i < n16) r8 = *reinterpret_cast<const uint4 *>(raw + i);
+                        for (int c0 = 0; c0 < n16; c0 += 128) {
+                            const int i = c0 + 4 * lane;
+                            uint2 r4 = make_uint2(0u, 0u);
+                            if (i < n16) r4 = *reinterpret_cast<const uint2 *>(raw + i);
                             __syncwarp();  // every raw word of the chunk read before any write
                             if (i < n16) {
-                                float4 *d4 = reinterpret_cast<float4 *>(dst + i);
-                                if (a.storage == 2) {
-                                    d4[0] = make_float4(half_bits_to_float(r8.x & 0xffffu) * sc,
-                                                        half_bits_to_float(r8.x >> 16) * sc,
-                                                        half_bits_to_float(r8.y & 0xffffu) * sc,
-                                                        half_bits_to_float(r8.y >> 16) * sc);
-                                    d4[1] = make_float4(half_bits_to_float(r8.z & 0xffffu) * sc,
-                                                        half_bits_to_float(r8.z >> 16) * sc,
-                                                        half_bits_to_float(r8.w & 0xffffu) * sc,
-                                                        half_bits_to_float(r8.w >> 16) * sc);
-                                } else {
-                                    d4[0] = make_float4(__uint_as_float(r8.x << 16),
-                                                        __uint_as_float(r8.x & 0xffff0000u),
-                                                        __uint_as_float(r8.y << 16),
-                                                        __uint_as_float(r8.y & 0xffff0000u));
-                                    d4[1] = make_float4(__uint_as_float(r8.z << 16),
-                                                        __uint_as_float(r8.z & 0xffff0000u),
-                                                        __uint_as_float(r8.w << 16),
-                                                        __uint_as_float(r8.w & 0xffff0000u));
-                                }
+                                *reinterpret_cast<float4 *>(dst + i) =
+                                    a.storage == 2
+                                        ? make_float4(half_bits_to_float(r4.x & 0xffffu) * sc,
+                                                      half_bits_to_float(r4.x >> 16) * sc,
+                                                      half_bits_to_float(r4.y & 0xffffu) * sc,
+                                                      half_bits_to_float(r4.y >> 16) * sc)
+                                        : make_float4(__uint_as_float(r4.x << 16),
+                                                      __uint_as_float(r4.x & 0xffff0000u),
+                                                      __uint_as_float(r4.y << 16),
+                                                      __uint_as_float(r4.y & 0xffff0000u));
                             }
                         }
                     }
