@@ -31,6 +31,7 @@
 #include <algorithm>
 #include <cstdlib>
 #include <cstring>
+#include <type_traits>
 
 #include "hpss_device.cuh"
 #include "hpss_internal.h"
@@ -345,6 +346,7 @@ struct DeStage {
     int base[kDeThreadsMax];  // per round slot: stage index of the trace's sample 0
     int lo[kDeThreadsMax];
     int len[kDeThreadsMax];
+    int full[kDeThreadsMax];  // every window of the trials lies inside the trace
     int warpSum[kDeThreadsMax / 32];
     int warpLen[kDeThreadsMax / 32];
     float boxW[kDeThreadsMax / 32][6];
@@ -417,9 +419,10 @@ __device__ bool de_eval_staged(const DeParams &d, DeStage &st, uint32_t &phase, 
         // spans of the next traces, one per thread, packed in trace order
         const uint32_t q = q0 + threadIdx.x;
         int lo = 0, len = 0;
+        bool full = false;
         if (anyActive && q < cnt) {
             const uint32_t ti = first + q;
-            trace_span<MODEL>(a, cb, m0, t0a, t0b, a.mid[ti], a.hsq[ti], &lo, &len);
+            trace_span<MODEL>(a, cb, m0, t0a, t0b, a.mid[ti], a.hsq[ti], &lo, &len, &full);
         }
         int incl = len;
 #pragma unroll
@@ -439,6 +442,7 @@ __device__ bool de_eval_staged(const DeParams &d, DeStage &st, uint32_t &phase, 
             st.base[threadIdx.x] = off - lo;
             st.lo[threadIdx.x] = lo;
             st.len[threadIdx.x] = len;
+            st.full[threadIdx.x] = full ? 1 : 0;
         }
         const uint32_t nfit = (uint32_t)__syncthreads_count(fits);
         if (nfit == 0) {
@@ -492,11 +496,15 @@ __device__ bool de_eval_staged(const DeParams &d, DeStage &st, uint32_t &phase, 
             __syncthreads();
         }
         if (active) {
-            uint32_t j = 0;
             // two traces per step, as de_eval: both traveltimes and floors in
             // packed f32x2 ops, both windows read before the sums, which take
-            // the traces in order
-            for (; j + 1 < nfit; j += 2) {
+            // the traces in order.  FULL: every window of the CTA's trials
+            // lies inside both traces (trace_span's conservative bounds, for
+            // ZO-CRS with every squared time positive), so the range tests,
+            // the zero-pad redirect and the per-trace count are skipped (the
+            // same sums: those tests pass for every window)
+            auto pairStep = [&](uint32_t j, auto fullTag) {
+                constexpr bool FULL = decltype(fullTag)::value;
                 const uint32_t ti0 = first + q0 + j, ti1 = ti0 + 1;
                 const float2 hsq2 = de_f2(a.hsq[ti0], a.hsq[ti1]);
                 float2 tt2;
@@ -510,7 +518,7 @@ __device__ bool de_eval_staged(const DeParams &d, DeStage &st, uint32_t &phase, 
                 }
                 const bool oka = MODEL == kModelCmp || tt2.x >= 0.f;
                 const bool okb = MODEL == kModelCmp || tt2.y >= 0.f;
-                const float2 t2 = MODEL == kModelCmp
+                const float2 t2 = (MODEL == kModelCmp || FULL)
                                       ? de_f2(sqrtf(tt2.x), sqrtf(tt2.y))
                                       : de_f2(sqrtf(fmaxf(tt2.x, 0.f)), sqrtf(fmaxf(tt2.y, 0.f)));
                 const float2 ti2 = __fmul2_rn(t2, rdt2);
@@ -518,12 +526,15 @@ __device__ bool de_eval_staged(const DeParams &d, DeStage &st, uint32_t &phase, 
                 const float2 fq = __ffma2_rn(__fadd2_rn(rk, kNegMagic2), kNeg1, ti2);  // frac
                 const int ka = __float_as_int(rk.x) - 0x4B000000;
                 const int kb = __float_as_int(rk.y) - 0x4B000000;
-                const bool ina = oka && window_in_trace(ka, a.tau, (int)a.S);
-                const bool inb = okb && window_in_trace(kb, a.tau, (int)a.S);
+                const bool ina = FULL || (oka && window_in_trace(ka, a.tau, (int)a.S));
+                const bool inb = FULL || (okb && window_in_trace(kb, a.tau, (int)a.S));
 #ifdef HPSS_CHECKED
                 if ((ina && (ka - a.tau < st.lo[j] || ka - a.tau + W >= st.lo[j] + st.len[j])) ||
                     (inb && (kb - a.tau < st.lo[j + 1] ||
                              kb - a.tau + W >= st.lo[j + 1] + st.len[j + 1])))
+                    atomicOr(a.errorWord, kErrSmemBounds);
+                if (FULL && !(oka && okb && window_in_trace(ka, a.tau, (int)a.S) &&
+                              window_in_trace(kb, a.tau, (int)a.S)))
                     atomicOr(a.errorWord, kErrSmemBounds);
 #endif
                 // a window outside its trace reads the zero pad (u = 0); the
@@ -551,7 +562,15 @@ __device__ bool de_eval_staged(const DeParams &d, DeStage &st, uint32_t &phase, 
                     num[jj] += u2[jj].y;
                     den += u2[jj].y * u2[jj].y;
                 }
-                used += (ina ? 1u : 0u) + (inb ? 1u : 0u);
+                used += FULL ? 2u : (ina ? 1u : 0u) + (inb ? 1u : 0u);
+            };
+            uint32_t j = 0;
+            for (; j + 1 < nfit; j += 2) {
+                // the same for every thread of the CTA: no divergence
+                if (st.full[j] & st.full[j + 1])
+                    pairStep(j, std::true_type{});
+                else
+                    pairStep(j, std::false_type{});
             }
             if (j < nfit) {
                 // an odd trace at the end of the round: de_eval's one-trace step
