@@ -98,11 +98,14 @@ def test_checked_build_16bit_bulk_staging(checked_lib, case, storage):
     assert np.array_equal(outs[0], outs[1])
 
 
+@pytest.mark.parametrize("storage", ["fp32", "fp16"])
 @pytest.mark.parametrize("model", ["cmp", "zocrs"])
-def test_checked_build_staged_de_windows_stay_in_their_spans(checked_lib, model):
-    """Differential evolution with staged spans in the checked build: every
-    window read from shared memory lies inside its trace's staged span (no
-    HPSS_DEVERR_SMEM_BOUNDS), and the results equal the default build's."""
+def test_checked_build_staged_de_windows_stay_in_their_spans(checked_lib, model, storage):
+    """Differential evolution with staged spans in the checked build, FP32
+    and 16-bit rows: every window read from shared memory lies inside its
+    trace's staged span, and every pair of traces taken on the path without
+    range tests has all its windows inside the trace (no
+    HPSS_DEVERR_SMEM_BOUNDS); the results equal the default build's."""
     zl = synthetic.structured_line(n_cmp=16, fold_range=(6, 12), h_max=1000, ns=300,
                                    dt_us=4000, n_reflectors=4, f=20.0, snr=5.0, seed=305)
     if model == "cmp":
@@ -113,7 +116,8 @@ def test_checked_build_staged_de_windows_stay_in_their_spans(checked_lib, model)
     outs = []
     for lib in (checked_lib, capi.lib()):
         with capi.Engine(0, library=lib) as eng:
-            eng.upload_gather(zl.samples, zl.midpoints, zl.halfoffsets, float(zl.dt))
+            eng.upload_gather(zl.samples, zl.midpoints, zl.halfoffsets, float(zl.dt),
+                              storage=storage)
             eng.set_traveltime(model, lower, upper, apm)
             eng.set_window(3)
             got, st = eng.differential_evolution(zl.cdp_midpoints[4:12], 32, 20, 0.5, 0.9,
