@@ -326,6 +326,47 @@ __device__ __forceinline__ void de_eval(const DeParams &d, const OctLine &ol, fl
     *notUsed += nu;
 }
 
+// ---- DE/rand/1/bin operators of one individual ---------------------------
+// Initial individual: x_j = min_j + U (max_j - min_j) as one fused
+// multiply-add, as the reference's startPopulations compiles.
+template <int NP>
+__device__ __forceinline__ void de_init_individual(const DeParams &d, uint32_t mkey, uint32_t s,
+                                                   uint32_t ind, float (&x)[NP]) {
+    Draws rng(d.seedLo, d.seedHi, mkey, s, ind, 0);
+#pragma unroll
+    for (int j = 0; j < NP; j++) x[j] = __fmaf_rn(rng.next(), __fsub_rn(d.hi[j], d.lo[j]), d.lo[j]);
+}
+
+// Trial vector of individual `ind` in generation `gen`: mutation from three
+// donors of the sample's population xs (trunc(U (pop - 1)), not necessarily
+// distinct), clamped with fminf(max) then fmaxf(min); binomial crossover
+// with the parameter l = trunc(U (nParams - 1)) always from the mutant.
+template <int NP>
+__device__ __forceinline__ void de_trial_vector(const DeParams &d, uint32_t mkey, uint32_t s,
+                                                uint32_t ind, uint32_t gen, const float *xs,
+                                                const float (&x)[NP], float (&u)[NP]) {
+    const uint32_t pop = d.pop;
+    Draws rng(d.seedLo, d.seedHi, mkey, s, ind, gen);
+    float v[NP];
+#pragma unroll
+    for (int j = 0; j < NP; j++) {
+        const float q1 = rng.next(), q2 = rng.next(), q3 = rng.next();
+        const uint32_t r1 = (uint32_t)(q1 * (float)(pop - 1));
+        const uint32_t r2 = (uint32_t)(q2 * (float)(pop - 1));
+        const uint32_t r3 = (uint32_t)(q3 * (float)(pop - 1));
+        float nv = __fmaf_rn(d.F, __fsub_rn(xs[r2 * NP + j], xs[r3 * NP + j]), xs[r1 * NP + j]);
+        nv = fminf(nv, d.hi[j]);
+        nv = fmaxf(nv, d.lo[j]);
+        v[j] = nv;
+    }
+    const uint32_t l = (uint32_t)(rng.next() * (float)(NP - 1));
+#pragma unroll
+    for (int j = 0; j < NP; j++) {
+        const float r = rng.next();
+        u[j] = (r > d.CR && l != (uint32_t)j) ? x[j] : v[j];
+    }
+}
+
 // ---- CMP / ZO-CRS: the CTA's trials over spans staged in shared memory --
 //
 // The individuals of a sample sit at scattered parameters, so the windows a
@@ -360,24 +401,12 @@ __device__ __forceinline__ int de_stage_index(int b, int w) {
     return (int)min((unsigned)b, (unsigned)(kDeStageFloats - w - 1));
 }
 
-// Called by every thread of the CTA (inactive threads stage and synchronise
-// only).  False when a round's copies did not complete in time (reported in
-// the error word); every thread then gets false.
-template <int MODEL, int W>
-__device__ bool de_eval_staged(const DeParams &d, DeStage &st, uint32_t &phase, float t0,
-                               float t0a, float t0b, float m0, uint32_t first, uint32_t cnt,
-                               bool active, const float *x, float *sembl, float *stack) {
-    const LsParams &a = d.ls;
+// The CTA-wide (min, max) of every parameter over the trials of its active
+// threads: bx holds a thread's own (min, max) pairs of (c, p1, p2) (+inf /
+// -inf where it has no trial).  Called by every thread of the CTA.
+__device__ __forceinline__ void de_cta_box(DeStage &st, float (&bx)[6], float (&cb)[6]) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int nWarps = (int)(blockDim.x >> 5);
-    const float v = x[0];
-    const float c = 4.0f / (v * v);
-    const float p1 = MODEL != kModelCmp ? x[1] : 0.f;
-    const float p2 = MODEL == kModelZocrs ? x[2] : 0.f;
-    // the active trials' parameter box: (c, p1, p2), min and max
-    const float inf = __int_as_float(0x7f800000);
-    float bx[6] = {active ? c : inf,  active ? c : -inf,  active ? p1 : inf,
-                   active ? p1 : -inf, active ? p2 : inf, active ? p2 : -inf};
 #pragma unroll
     for (int o = 16; o; o >>= 1) {
 #pragma unroll
@@ -392,7 +421,6 @@ __device__ bool de_eval_staged(const DeParams &d, DeStage &st, uint32_t &phase, 
         for (int j = 0; j < 6; j++) st.boxW[warp][j] = bx[j];
     }
     __syncthreads();
-    float cb[6];
 #pragma unroll
     for (int j = 0; j < 6; j++) {
         float r = st.boxW[0][j];
@@ -400,22 +428,23 @@ __device__ bool de_eval_staged(const DeParams &d, DeStage &st, uint32_t &phase, 
             r = (j & 1) ? fmaxf(r, st.boxW[wv][j]) : fminf(r, st.boxW[wv][j]);
         cb[j] = r;
     }
-    const bool anyActive = cb[0] <= cb[1];
+}
 
-    float num[W];
-#pragma unroll
-    for (int j = 0; j < W; j++) num[j] = 0.f;
-    float den = 0.f;
-    unsigned used = 0;
-    const float2 c2 = de_f2(c, c), a2 = de_f2(p1, p1), b2 = de_f2(p2, p2);
-    const float t0sq = __fmul_rn(t0, t0);
-    const float2 t02 = de_f2(t0, t0), t0sq2 = de_f2(t0sq, t0sq);
-    const float2 negM02 = de_f2(-m0, -m0);
-    const float rdt = 1.0f / a.dt;
-    const float2 rdt2 = de_f2(rdt, rdt);
-    const float2 kNeg1 = de_f2(-1.f, -1.f);
-    const float2 kMagic2 = de_f2(8388608.f, 8388608.f), kNegMagic2 = de_f2(-8388608.f, -8388608.f);
-    for (uint32_t q0 = 0; q0 < cnt;) {
+// One staging round, called by every thread of the CTA: the spans of the
+// selected traces q0, q0 + 1, ... (one per thread) that any window of the
+// box cb and the t0 range [t0a, t0b] can touch are packed into the stage in
+// trace order, as many as fit, and copied (bulk copies for FP32 rows,
+// widening loads for 16-bit rows); slot j of the stage holds trace q0 + j.
+// Returns the traces staged; 0 when a span is longer than the stage (the
+// host stages only rows that fit; reported in the error word), -1 when the
+// copies did not complete in time (reported; every thread gets -1).
+template <int MODEL>
+__device__ int de_stage_round(const DeParams &d, DeStage &st, uint32_t &phase,
+                              const float (&cb)[6], bool anyActive, float t0a, float t0b,
+                              float m0, uint32_t first, uint32_t cnt, uint32_t q0) {
+    const LsParams &a = d.ls;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nWarps = (int)(blockDim.x >> 5);
         // spans of the next traces, one per thread, packed in trace order
         const uint32_t q = q0 + threadIdx.x;
         int lo = 0, len = 0;
@@ -448,7 +477,7 @@ __device__ bool de_eval_staged(const DeParams &d, DeStage &st, uint32_t &phase, 
         if (nfit == 0) {
             // a span longer than the stage (the host stages only rows that fit)
             if (threadIdx.x == 0) atomicOr(a.errorWord, kErrSpanOverflow);
-            break;
+            return 0;
         }
         if (a.samples16 == nullptr) {
             if (threadIdx.x == 0) {
@@ -468,7 +497,7 @@ __device__ bool de_eval_staged(const DeParams &d, DeStage &st, uint32_t &phase, 
                 // report, wait (again bounded) for this CTA's copies in flight
                 if (threadIdx.x == 0) atomicOr(a.errorWord, kErrTimeout);
                 stage_bar_wait(&st.bar, phase ^ 1u, 1u << 22);
-                return false;
+                return -1;
             }
         } else {
             // 16-bit rows: a warp per trace, 4 samples per 8-byte load, widened
@@ -495,6 +524,48 @@ __device__ bool de_eval_staged(const DeParams &d, DeStage &st, uint32_t &phase, 
             }
             __syncthreads();
         }
+    return (int)nfit;
+}
+
+// Called by every thread of the CTA (inactive threads stage and synchronise
+// only).  False when a round's copies did not complete in time (reported in
+// the error word); every thread then gets false.
+template <int MODEL, int W>
+__device__ bool de_eval_staged(const DeParams &d, DeStage &st, uint32_t &phase, float t0,
+                               float t0a, float t0b, float m0, uint32_t first, uint32_t cnt,
+                               bool active, const float *x, float *sembl, float *stack) {
+    const LsParams &a = d.ls;
+    const float v = x[0];
+    const float c = 4.0f / (v * v);
+    const float p1 = MODEL != kModelCmp ? x[1] : 0.f;
+    const float p2 = MODEL == kModelZocrs ? x[2] : 0.f;
+    // the active trials' parameter box: (c, p1, p2), min and max
+    const float inf = __int_as_float(0x7f800000);
+    float bx[6] = {active ? c : inf,  active ? c : -inf,  active ? p1 : inf,
+                   active ? p1 : -inf, active ? p2 : inf, active ? p2 : -inf};
+    float cb[6];
+    de_cta_box(st, bx, cb);
+    const bool anyActive = cb[0] <= cb[1];
+
+    float num[W];
+#pragma unroll
+    for (int j = 0; j < W; j++) num[j] = 0.f;
+    float den = 0.f;
+    unsigned used = 0;
+    const float2 c2 = de_f2(c, c), a2 = de_f2(p1, p1), b2 = de_f2(p2, p2);
+    const float t0sq = __fmul_rn(t0, t0);
+    const float2 t02 = de_f2(t0, t0), t0sq2 = de_f2(t0sq, t0sq);
+    const float2 negM02 = de_f2(-m0, -m0);
+    const float rdt = 1.0f / a.dt;
+    const float2 rdt2 = de_f2(rdt, rdt);
+    const float2 kNeg1 = de_f2(-1.f, -1.f);
+    const float2 kMagic2 = de_f2(8388608.f, 8388608.f), kNegMagic2 = de_f2(-8388608.f, -8388608.f);
+    for (uint32_t q0 = 0; q0 < cnt;) {
+        const int staged = de_stage_round<MODEL>(d, st, phase, cb, anyActive, t0a, t0b, m0,
+                                                  first, cnt, q0);
+        if (staged < 0) return false;
+        if (staged == 0) break;
+        const uint32_t nfit = (uint32_t)staged;
         if (active) {
             // two traces per step, as de_eval: both traveltimes and floors in
             // packed f32x2 ops, both windows read before the sums, which take
@@ -608,6 +679,266 @@ __device__ bool de_eval_staged(const DeParams &d, DeStage &st, uint32_t &phase, 
     for (int j = 0; j < W; j++) lin += num[j];
     reduce_semblance(num, lin, den, W, used, sembl, stack);
     return true;
+}
+
+// Two trials per thread (individuals 2i and 2i + 1 of a sample) over the
+// staged spans: per trace, both trials' traveltimes, floors, window terms
+// and sums run in packed f32x2 ops, each half carrying one trial with the
+// same IEEE operations, in the same trace order, as de_eval_staged gives it
+// alone -- the same sums bit for bit, with one instruction for both trials
+// where de_eval_staged issues one per trial for the sums.  Called by every
+// thread of the CTA; act[k] false: no trial k (staging and synchronisation
+// only).  False when a round's copies did not complete in time.
+template <int MODEL, int W>
+__device__ bool de_eval_staged2(const DeParams &d, DeStage &st, uint32_t &phase, float t0,
+                                float t0a, float t0b, float m0, uint32_t first, uint32_t cnt,
+                                const bool (&act)[2], const float (&x0)[MODEL == kModelCmp ? 1 : 3],
+                                const float (&x1)[MODEL == kModelCmp ? 1 : 3], float (&sembl)[2],
+                                float (&stack)[2]) {
+    const LsParams &a = d.ls;
+    const float cA = 4.0f / (x0[0] * x0[0]), cB = 4.0f / (x1[0] * x1[0]);
+    const float pA = MODEL != kModelCmp ? x0[MODEL != kModelCmp ? 1 : 0] : 0.f;
+    const float pB = MODEL != kModelCmp ? x1[MODEL != kModelCmp ? 1 : 0] : 0.f;
+    const float qA = MODEL == kModelZocrs ? x0[MODEL == kModelZocrs ? 2 : 0] : 0.f;
+    const float qB = MODEL == kModelZocrs ? x1[MODEL == kModelZocrs ? 2 : 0] : 0.f;
+    const float inf = __int_as_float(0x7f800000);
+    auto lo2 = [&](float u, float v) { return fminf(act[0] ? u : inf, act[1] ? v : inf); };
+    auto hi2 = [&](float u, float v) { return fmaxf(act[0] ? u : -inf, act[1] ? v : -inf); };
+    float bx[6] = {lo2(cA, cB), hi2(cA, cB), lo2(pA, pB), hi2(pA, pB), lo2(qA, qB), hi2(qA, qB)};
+    float cb[6];
+    de_cta_box(st, bx, cb);
+    const bool anyActive = cb[0] <= cb[1];
+
+    float2 num[W];
+#pragma unroll
+    for (int j = 0; j < W; j++) num[j] = de_f2(0.f, 0.f);
+    float2 den = de_f2(0.f, 0.f);
+    unsigned usedA = 0, usedB = 0;
+    const float2 c2 = de_f2(cA, cB), a2 = de_f2(pA, pB), b2 = de_f2(qA, qB);
+    const float t0sq = __fmul_rn(t0, t0);
+    const float2 t02 = de_f2(t0, t0), t0sq2 = de_f2(t0sq, t0sq);
+    const float rdt = 1.0f / a.dt;
+    const float2 rdt2 = de_f2(rdt, rdt);
+    const float2 kNeg1 = de_f2(-1.f, -1.f);
+    const float2 kMagic2 = de_f2(8388608.f, 8388608.f), kNegMagic2 = de_f2(-8388608.f, -8388608.f);
+    const bool anyOwn = act[0] || act[1];
+    for (uint32_t q0 = 0; q0 < cnt;) {
+        const int staged = de_stage_round<MODEL>(d, st, phase, cb, anyActive, t0a, t0b, m0,
+                                                  first, cnt, q0);
+        if (staged < 0) return false;
+        if (staged == 0) break;
+        const uint32_t nfit = (uint32_t)staged;
+        if (anyOwn) {
+            // FULL: every window of the CTA's trials lies inside the trace
+            // (the range tests, zero-pad redirect and count are skipped)
+            auto traceStep = [&](uint32_t j, auto fullTag) {
+                constexpr bool FULL = decltype(fullTag)::value;
+                const uint32_t ti = first + q0 + j;
+                const float hsq = a.hsq[ti];
+                const float2 hsq2 = de_f2(hsq, hsq);
+                float2 tt2;
+                if (MODEL == kModelCmp) {
+                    tt2 = __ffma2_rn(c2, hsq2, t0sq2);
+                } else {
+                    // m - m0 as m + (-m0): de_eval_staged's rounding
+                    const float dm = __fadd_rn(a.mid[ti], -m0);
+                    const float2 dm2 = de_f2(dm, dm);
+                    const float2 xx = __ffma2_rn(a2, dm2, t02);
+                    const float2 bd2 = __fmul2_rn(b2, dm2);
+                    tt2 = __ffma2_rn(c2, hsq2, __ffma2_rn(bd2, dm2, __fmul2_rn(xx, xx)));
+                }
+                const bool oka = MODEL == kModelCmp || tt2.x >= 0.f;
+                const bool okb = MODEL == kModelCmp || tt2.y >= 0.f;
+                const float2 t2 = (MODEL == kModelCmp || FULL)
+                                      ? de_f2(sqrtf(tt2.x), sqrtf(tt2.y))
+                                      : de_f2(sqrtf(fmaxf(tt2.x, 0.f)), sqrtf(fmaxf(tt2.y, 0.f)));
+                const float2 ti2 = __fmul2_rn(t2, rdt2);
+                const float2 rk = __fadd2_rz(ti2, kMagic2);
+                const float2 fq = __ffma2_rn(__fadd2_rn(rk, kNegMagic2), kNeg1, ti2);  // frac
+                const int ka = __float_as_int(rk.x) - 0x4B000000;
+                const int kb = __float_as_int(rk.y) - 0x4B000000;
+                const bool ina = FULL || (oka && window_in_trace(ka, a.tau, (int)a.S));
+                const bool inb = FULL || (okb && window_in_trace(kb, a.tau, (int)a.S));
+                const int base = st.base[j];
+#ifdef HPSS_CHECKED
+                if ((act[0] && ina && (ka - a.tau < st.lo[j] || ka - a.tau + W >= st.lo[j] + st.len[j])) ||
+                    (act[1] && inb && (kb - a.tau < st.lo[j] || kb - a.tau + W >= st.lo[j] + st.len[j])))
+                    atomicOr(a.errorWord, kErrSmemBounds);
+                if (FULL && ((act[0] && !(oka && window_in_trace(ka, a.tau, (int)a.S))) ||
+                             (act[1] && !(okb && window_in_trace(kb, a.tau, (int)a.S)))))
+                    atomicOr(a.errorWord, kErrSmemBounds);
+#endif
+                // a window outside its trace reads the zero pad (u = 0); the
+                // clamp keeps every read inside the stage whatever the span
+                const float *ya = st.y + de_stage_index(ina ? base + ka - a.tau : 0, W);
+                const float *yb = st.y + de_stage_index(inb ? base + kb - a.tau : 0, W);
+                float y0a = ya[0], y0b = yb[0];
+#pragma unroll
+                for (int jj = 0; jj < W; jj++) {
+                    const float y1a = ya[jj + 1], y1b = yb[jj + 1];
+                    const float2 y0 = de_f2(y0a, y0b);
+                    const float2 dd = __ffma2_rn(y0, kNeg1, de_f2(y1a, y1b));
+                    const float2 u = __ffma2_rn(dd, fq, y0);
+                    num[jj] = __fadd2_rn(num[jj], u);
+                    den = __ffma2_rn(u, u, den);
+                    y0a = y1a;
+                    y0b = y1b;
+                }
+                usedA += FULL || ina ? 1u : 0u;
+                usedB += FULL || inb ? 1u : 0u;
+            };
+            for (uint32_t j = 0; j < nfit; j++) {
+                if (st.full[j])  // the same for every thread of the CTA
+                    traceStep(j, std::true_type{});
+                else
+                    traceStep(j, std::false_type{});
+            }
+        }
+        q0 += nfit;
+    }
+    // per trial: the linear sum is the sum of the per-tap sums, as in de_eval
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+        float nm[W];
+        float lin = 0.f;
+#pragma unroll
+        for (int j = 0; j < W; j++) {
+            nm[j] = k ? num[j].y : num[j].x;
+            lin += nm[j];
+        }
+        reduce_semblance(nm, lin, k ? den.y : den.x, W, k ? usedB : usedA, &sembl[k], &stack[k]);
+    }
+    return true;
+}
+
+// CMP / ZO-CRS with staged spans and an even population: two individuals
+// per thread (2i and 2i + 1 of one sample; a CTA holds `spc` whole
+// populations of consecutive samples, 2 x threads individuals), evaluated
+// together by de_eval_staged2.  Every individual draws its own counter-based
+// stream and runs the same operators as in de_kernel, so the results are
+// de_kernel's bit for bit.
+template <int MODEL, int W>
+__global__ void __launch_bounds__(kDeThreadsMax, 4)
+de_pair_kernel(DeParams d, uint32_t spc, uint32_t groups, uint32_t nUnits) {
+    constexpr int NP = MODEL == kModelCmp ? 1 : 3;
+    const LsParams &a = d.ls;
+    extern __shared__ __align__(16) float deSmem[];
+    const uint32_t pop = d.pop, half = pop / 2;
+    float *X = deSmem;                           // [spc][pop][NP]
+    float *FX = deSmem + (size_t)spc * pop * NP; // [spc][pop] (final argmax)
+    float *FK = FX + (size_t)spc * pop;          // [spc][pop]
+    DeStage *stg = reinterpret_cast<DeStage *>(
+        deSmem + (((size_t)spc * pop * (NP + 2) + 3) & ~(size_t)3));
+    uint32_t stagePhase = 0;
+    if (threadIdx.x < kDeZeroPad) stg->y[threadIdx.x] = 0.f;
+    if (threadIdx.x == 0) stage_bar_init(&stg->bar);
+    __syncthreads();
+    const uint32_t ls = threadIdx.x / half;      // sample within the CTA
+    const uint32_t pi = threadIdx.x % half;      // individuals 2 pi, 2 pi + 1
+    const bool member = ls < spc;                // threads past spc * half only sync
+    const uint32_t ind[2] = {2 * pi, 2 * pi + 1};
+    __shared__ uint32_t nextUnit;
+    for (uint32_t unit = blockIdx.x;; unit += gridDim.x) {
+        if (a.unitCounter) {
+            __syncthreads();  // every thread has read the previous unit
+            if (threadIdx.x == 0) nextUnit = atomicAdd(a.unitCounter, 1u);
+            __syncthreads();
+            unit = nextUnit;
+        }
+        if (unit >= nUnits) break;
+        const uint32_t mi = a.order ? a.order[unit / groups] : unit / groups;
+        const uint32_t s = (unit % groups) * spc + ls;
+        const bool active = member && s < a.S;
+        const bool act[2] = {active, active};
+        const float m0 = a.m0s[mi];
+        const uint32_t first = a.selFirst[mi], cnt = a.selCount[mi];
+        const uint32_t mkey = __float_as_uint(m0);
+        const float t0 = static_cast<float>(active ? s : 0) * a.dt;
+        const float t0a = static_cast<float>((unit % groups) * spc) * a.dt;
+        const float t0b = static_cast<float>(min((unit % groups) * spc + spc - 1, a.S - 1)) * a.dt;
+        float *xs = X + (size_t)(member ? ls : 0) * pop * NP;  // this sample's population
+        // the population (xs) and its fitness and stack (FX, FK) live in
+        // shared memory; a thread holds only its two trial vectors
+        float *fx = FX + (size_t)(member ? ls : 0) * pop;
+        float *fk = FK + (size_t)(member ? ls : 0) * pop;
+        // ---- initial population and its fitness (generation 1)
+        {
+            float x[2][NP];
+#pragma unroll
+            for (int k = 0; k < 2; k++) {
+                if (active) {
+                    de_init_individual<NP>(d, mkey, s, ind[k], x[k]);
+#pragma unroll
+                    for (int j = 0; j < NP; j++) xs[ind[k] * NP + j] = x[k][j];
+                } else {
+#pragma unroll
+                    for (int j = 0; j < NP; j++) x[k][j] = d.lo[j];
+                }
+            }
+            float f[2], fs[2];
+            if (!de_eval_staged2<MODEL, W>(d, *stg, stagePhase, t0, t0a, t0b, m0, first, cnt, act,
+                                           x[0], x[1], f, fs))
+                return;  // copies timed out (error word); every thread leaves
+            if (member) {
+#pragma unroll
+                for (int k = 0; k < 2; k++) {
+                    fx[ind[k]] = active ? f[k] : -1.f;
+                    fk[ind[k]] = active ? fs[k] : 0.f;
+                }
+            }
+        }
+        // ---- generations 2 .. G
+        for (uint32_t gen = 1; gen < d.gens; gen++) {
+            __syncthreads();  // population of the previous generation complete
+            float u[2][NP];
+#pragma unroll
+            for (int k = 0; k < 2; k++) {
+                float x[NP];
+#pragma unroll
+                for (int j = 0; j < NP; j++) x[j] = active ? xs[ind[k] * NP + j] : d.lo[j];
+#pragma unroll
+                for (int j = 0; j < NP; j++) u[k][j] = x[j];
+                if (active) de_trial_vector<NP>(d, mkey, s, ind[k], gen, xs, x, u[k]);
+            }
+            __syncthreads();  // every donor read before any replacement
+            float fu[2], fuk[2];
+            if (!de_eval_staged2<MODEL, W>(d, *stg, stagePhase, t0, t0a, t0b, m0, first, cnt, act,
+                                           u[0], u[1], fu, fuk))
+                return;
+            if (active) {
+#pragma unroll
+                for (int k = 0; k < 2; k++) {
+                    if (fu[k] > fx[ind[k]]) {
+#pragma unroll
+                        for (int j = 0; j < NP; j++) xs[ind[k] * NP + j] = u[k][j];
+                        fx[ind[k]] = fu[k];
+                        fk[ind[k]] = fuk[k];
+                    }
+                }
+            }
+        }
+        // ---- best individual per sample: strict '>' from -1 in index order
+        __syncthreads();
+        if (active && pi == 0) {
+            float best = -1.f, bestK = 0.f;
+            uint32_t bi = 0xffffffffu;
+            for (uint32_t i = 0; i < pop; i++) {
+                const float f = FX[ls * pop + i];
+                if (f > best) {
+                    best = f;
+                    bestK = FK[ls * pop + i];
+                    bi = i;
+                }
+            }
+            float *out = a.out + (size_t)mi * (2 + NP) * a.S;
+            out[s] = best;
+            out[a.S + s] = bestK;
+#pragma unroll
+            for (int j = 0; j < NP; j++)
+                out[(size_t)(2 + j) * a.S + s] = bi != 0xffffffffu ? xs[bi * NP + j] : 0.f;
+        }
+        __syncthreads();  // shared memory reused by the next unit
+    }
 }
 
 // One thread per individual.  A CTA holds `spc` whole populations of
@@ -727,14 +1058,9 @@ de_kernel(DeParams d, uint32_t spc, uint32_t groups, uint32_t nUnits) {
         if (threadIdx.x == 0) nuCta = 0;
         // ---- initial population and its fitness (generation 1)
         if (active) {
-            Draws rng(d.seedLo, d.seedHi, mkey, s, ind, 0);
+            de_init_individual<NP>(d, mkey, s, ind, x);
 #pragma unroll
-            for (int j = 0; j < NP; j++) {
-                // min + ratio * (max - min) as one fused multiply-add, as the
-                // reference's startPopulations compiles
-                x[j] = __fmaf_rn(rng.next(), __fsub_rn(d.hi[j], d.lo[j]), d.lo[j]);
-                xs[ind * NP + j] = x[j];
-            }
+            for (int j = 0; j < NP; j++) xs[ind * NP + j] = x[j];
             if (MODEL != kModelOct && !staged)
                 de_eval<MODEL, W>(d, ol, t0, m0, first, cnt, x, &fx, &fxk, &notUsed);
         } else {
@@ -763,28 +1089,7 @@ de_kernel(DeParams d, uint32_t spc, uint32_t groups, uint32_t nUnits) {
             float u[NP];
 #pragma unroll
             for (int j = 0; j < NP; j++) u[j] = x[j];
-            if (active) {
-                Draws rng(d.seedLo, d.seedHi, mkey, s, ind, gen);
-                float v[NP];
-#pragma unroll
-                for (int j = 0; j < NP; j++) {
-                    const float q1 = rng.next(), q2 = rng.next(), q3 = rng.next();
-                    const uint32_t r1 = (uint32_t)(q1 * (float)(pop - 1));
-                    const uint32_t r2 = (uint32_t)(q2 * (float)(pop - 1));
-                    const uint32_t r3 = (uint32_t)(q3 * (float)(pop - 1));
-                    float nv = __fmaf_rn(d.F, __fsub_rn(xs[r2 * NP + j], xs[r3 * NP + j]),
-                                         xs[r1 * NP + j]);
-                    nv = fminf(nv, d.hi[j]);
-                    nv = fmaxf(nv, d.lo[j]);
-                    v[j] = nv;
-                }
-                const uint32_t l = (uint32_t)(rng.next() * (float)(NP - 1));
-#pragma unroll
-                for (int j = 0; j < NP; j++) {
-                    const float r = rng.next();
-                    u[j] = (r > d.CR && l != (uint32_t)j) ? x[j] : v[j];
-                }
-            }
+            if (active) de_trial_vector<NP>(d, mkey, s, ind, gen, xs, x, u);
             __syncthreads();  // every donor read before any replacement
             float fu = -1.f, fuk = 0.f;
             if (MODEL == kModelOct)
@@ -955,6 +1260,48 @@ cudaError_t launch_de_w(const DeParams &d, uint32_t numSms, uint32_t spc, uint32
     return cudaGetLastError();
 }
 
+template <int MODEL, int W>
+cudaError_t launch_de_pair_w(const DeParams &d, uint32_t numSms, uint32_t spc, uint32_t threads,
+                             uint32_t groups, uint64_t units, size_t smem, cudaStream_t st) {
+    int perSm = 0;
+    cudaError_t e = cudaFuncSetAttribute(de_pair_kernel<MODEL, W>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, de_pair_kernel<MODEL, W>,
+                                                      (int)threads, smem);
+    if (e != cudaSuccess) return e;
+    const uint32_t grid =
+        (uint32_t)std::min<uint64_t>(units, (uint64_t)numSms * (uint64_t)std::max(perSm, 1));
+    DeParams q = d;
+    if (units <= grid) q.ls.unitCounter = nullptr;
+    de_pair_kernel<MODEL, W><<<grid, threads, smem, st>>>(q, spc, groups, (uint32_t)units);
+    return cudaGetLastError();
+}
+
+// CMP / ZO-CRS with staged spans and an even population: two individuals per
+// thread (HPSS_DE_PAIRS=0: one, de_kernel; the same results)
+template <int MODEL>
+cudaError_t launch_de_pairs(const DeParams &d, uint32_t numSms, cudaStream_t st) {
+    constexpr int NP = MODEL == kModelCmp ? 1 : 3;
+    const uint32_t pop = d.pop;
+    const uint32_t spc = std::max<uint32_t>(1u, 2u * kDeThreads / pop);
+    const uint32_t threads = ((spc * pop / 2 + 31) / 32) * 32;
+    const uint32_t groups = (d.ls.S + spc - 1) / spc;
+    const uint64_t units = (uint64_t)d.ls.nM0 * groups;
+    if (units == 0) return cudaSuccess;
+    if (units > 0x7fffffffull) return cudaErrorInvalidConfiguration;
+    const size_t smem = ((de_smem_bytes(spc, pop, NP) + 15) & ~(size_t)15) + sizeof(DeStage);
+    switch (d.ls.w) {
+        case 1: return launch_de_pair_w<MODEL, 1>(d, numSms, spc, threads, groups, units, smem, st);
+        case 3: return launch_de_pair_w<MODEL, 3>(d, numSms, spc, threads, groups, units, smem, st);
+        case 5: return launch_de_pair_w<MODEL, 5>(d, numSms, spc, threads, groups, units, smem, st);
+        case 7: return launch_de_pair_w<MODEL, 7>(d, numSms, spc, threads, groups, units, smem, st);
+        case 9: return launch_de_pair_w<MODEL, 9>(d, numSms, spc, threads, groups, units, smem, st);
+        case 11: return launch_de_pair_w<MODEL, 11>(d, numSms, spc, threads, groups, units, smem, st);
+        default: return cudaErrorNotSupported;
+    }
+}
+
 template <int MODEL>
 cudaError_t launch_de_model(const DeParams &d, uint32_t numSms, cudaStream_t st) {
     constexpr int NP = MODEL == kModelCmp ? 1 : (MODEL == kModelZocrs ? 3 : 2);
@@ -984,6 +1331,11 @@ cudaError_t launch_de_model(const DeParams &d, uint32_t numSms, cudaStream_t st)
     size_t smem = de_smem_bytes(spc, pop, NP) +
                   (MODEL == kModelOct ? (size_t)threads * (NP + 4) * sizeof(float) : 0);
     if (q.staged) smem = ((smem + 15) & ~(size_t)15) + sizeof(DeStage);
+    if constexpr (MODEL != kModelOct) {
+        const char *pairEnv = std::getenv("HPSS_DE_PAIRS");
+        if (q.staged && pop % 2 == 0 && !(pairEnv && std::strcmp(pairEnv, "0") == 0))
+            return launch_de_pairs<MODEL>(q, numSms, st);
+    }
     switch (d.ls.w) {
         case 1: return launch_de_w<MODEL, 1>(q, numSms, spc, threads, groups, units, smem, st);
         case 3: return launch_de_w<MODEL, 3>(q, numSms, spc, threads, groups, units, smem, st);

@@ -202,11 +202,13 @@ def test_de_oct_box_test_keeps_results(engine, monkeypatch, slope, h0):
 @pytest.mark.parametrize("tau", [0, 2, 5])
 def test_de_staged_spans_equal_unstaged(engine, monkeypatch, model, storage, tau):
     """CMP / ZO-CRS DE reads its windows from trace spans staged in shared
-    memory (the spans any window of the CTA's trials can touch); the results
-    equal the evaluation through L1 (HPSS_DE_STAGED=0) bit for bit, with
-    uneven fold (rounds of different trace counts), odd trace counts per
-    round, windows at the trace ends and several sample groups per
-    midpoint, and no device error."""
+    memory (the spans any window of the CTA's trials can touch), two
+    individuals per thread when the population is even; the results equal
+    one individual per thread (HPSS_DE_PAIRS=0) and the evaluation through
+    L1 (HPSS_DE_STAGED=0) bit for bit, with uneven fold (rounds of different
+    trace counts), odd trace counts per round, windows at the trace ends,
+    several sample groups per midpoint and populations 32, 48 and 7, and no
+    device error."""
     line = synthetic.structured_line(n_cmp=14, fold_range=(5, 13), h_max=1100, ns=260,
                                      dt_us=4000, n_reflectors=4, f=20.0, snr=5.0, seed=71)
     if model == "cmp":
@@ -219,10 +221,21 @@ def test_de_staged_spans_equal_unstaged(engine, monkeypatch, model, storage, tau
     engine.set_traveltime(model, lower, upper, apm)
     engine.set_window(tau)
     m0s = line.cdp_midpoints[3:11]
-    monkeypatch.delenv("HPSS_DE_STAGED", raising=False)
-    got, st = engine.differential_evolution(m0s, 32, 12, 0.5, 0.9, seed=5)
-    monkeypatch.setenv("HPSS_DE_STAGED", "0")
-    want, st0 = engine.differential_evolution(m0s, 32, 12, 0.5, 0.9, seed=5)
-    monkeypatch.delenv("HPSS_DE_STAGED", raising=False)
-    assert st["device_error"] == 0 and st0["device_error"] == 0
-    assert np.array_equal(got, want)
+    for pop in (32, 48, 7):
+        runs = {}
+        # default: staged spans, two individuals per thread for an even
+        # population; then one per thread; then through L1
+        for name, env in (("pairs", {}), ("single", {"HPSS_DE_PAIRS": "0"}),
+                          ("l1", {"HPSS_DE_STAGED": "0"})):
+            for k in ("HPSS_DE_PAIRS", "HPSS_DE_STAGED"):
+                monkeypatch.delenv(k, raising=False)
+            for k, v in env.items():
+                monkeypatch.setenv(k, v)
+            runs[name] = engine.differential_evolution(m0s, pop, 12, 0.5, 0.9, seed=5)
+        for k in ("HPSS_DE_PAIRS", "HPSS_DE_STAGED"):
+            monkeypatch.delenv(k, raising=False)
+        want, st0 = runs["l1"]
+        for name in ("pairs", "single"):
+            got, st = runs[name]
+            assert st["device_error"] == 0, (name, pop)
+            assert np.array_equal(got, want), (name, pop)
