@@ -56,9 +56,9 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--de-cmps", type=int, default=2,
                     help="midpoints of the OCT DE side measurement (0: skip)")
-    ap.add_argument("--zocrs-de-cmps", type=int, default=8,
-                    help="midpoints of the ZO-CRS DE side measurement (8 midpoints x 1500 "
-                         "samples = 1500 CTAs of eight populations, about 2.5 waves)")
+    ap.add_argument("--zocrs-de-cmps", type=int, default=16,
+                    help="midpoints of the ZO-CRS DE side measurement (16 midpoints x 1500 "
+                         "samples = 1500 CTAs of sixteen populations, about 2.5 waves)")
     ap.add_argument("--per-midpoint-calls", type=int, default=64,
                     help="one-midpoint calls timed beside the batched call (0: skip)")
     ap.add_argument("--no-storage-side", action="store_true",
