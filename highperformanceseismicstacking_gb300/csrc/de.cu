@@ -1279,7 +1279,8 @@ cudaError_t launch_de_pair_w(const DeParams &d, uint32_t numSms, uint32_t spc, u
 }
 
 // CMP / ZO-CRS with staged spans and an even population: two individuals per
-// thread (HPSS_DE_PAIRS=0: one, de_kernel; the same results)
+// thread (HPSS_DE_PAIRS=0: one, de_kernel; =1: two even for calls too small
+// to fill a wave; the same results either way)
 template <int MODEL>
 cudaError_t launch_de_pairs(const DeParams &d, uint32_t numSms, cudaStream_t st) {
     constexpr int NP = MODEL == kModelCmp ? 1 : 3;
@@ -1332,8 +1333,15 @@ cudaError_t launch_de_model(const DeParams &d, uint32_t numSms, cudaStream_t st)
                   (MODEL == kModelOct ? (size_t)threads * (NP + 4) * sizeof(float) : 0);
     if (q.staged) smem = ((smem + 15) & ~(size_t)15) + sizeof(DeStage);
     if constexpr (MODEL != kModelOct) {
+        // two individuals per thread halve the CTAs of a call (twice the
+        // samples per CTA): taken when the call still fills a wave of four
+        // CTAs per SM, so that small calls keep every SM busy
         const char *pairEnv = std::getenv("HPSS_DE_PAIRS");
-        if (q.staged && pop % 2 == 0 && !(pairEnv && std::strcmp(pairEnv, "0") == 0))
+        const uint32_t pairSpc = std::max<uint32_t>(1u, 2u * kDeThreads / pop);
+        const uint64_t pairUnits = (uint64_t)d.ls.nM0 * ((d.ls.S + pairSpc - 1) / pairSpc);
+        const bool forced = pairEnv && std::strcmp(pairEnv, "1") == 0;
+        if (q.staged && pop % 2 == 0 && !(pairEnv && std::strcmp(pairEnv, "0") == 0) &&
+            (forced || pairUnits >= (uint64_t)numSms * 4))
             return launch_de_pairs<MODEL>(q, numSms, st);
     }
     switch (d.ls.w) {

@@ -203,8 +203,9 @@ def test_de_oct_box_test_keeps_results(engine, monkeypatch, slope, h0):
 def test_de_staged_spans_equal_unstaged(engine, monkeypatch, model, storage, tau):
     """CMP / ZO-CRS DE reads its windows from trace spans staged in shared
     memory (the spans any window of the CTA's trials can touch), two
-    individuals per thread when the population is even; the results equal
-    one individual per thread (HPSS_DE_PAIRS=0) and the evaluation through
+    individuals per thread when the population is even (HPSS_DE_PAIRS=1);
+    the results equal one individual per thread (HPSS_DE_PAIRS=0) and the
+    evaluation through
     L1 (HPSS_DE_STAGED=0) bit for bit, with uneven fold (rounds of different
     trace counts), odd trace counts per round, windows at the trace ends,
     several sample groups per midpoint and populations 32, 48 and 7, and no
@@ -225,7 +226,7 @@ def test_de_staged_spans_equal_unstaged(engine, monkeypatch, model, storage, tau
         runs = {}
         # default: staged spans, two individuals per thread for an even
         # population; then one per thread; then through L1
-        for name, env in (("pairs", {}), ("single", {"HPSS_DE_PAIRS": "0"}),
+        for name, env in (("pairs", {"HPSS_DE_PAIRS": "1"}), ("single", {"HPSS_DE_PAIRS": "0"}),
                           ("l1", {"HPSS_DE_STAGED": "0"})):
             for k in ("HPSS_DE_PAIRS", "HPSS_DE_STAGED"):
                 monkeypatch.delenv(k, raising=False)
