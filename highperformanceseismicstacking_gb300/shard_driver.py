@@ -19,6 +19,7 @@ from __future__ import annotations
 
 import argparse
 import os
+import re
 from ctypes import c_int as C_int
 from typing import Callable, Dict, Optional, Sequence
 
@@ -84,8 +85,11 @@ def assemble(parts: Sequence[Dict], n_blocks: int = 1) -> np.ndarray:
     return whole.reshape((-1,) + whole.shape[2:])
 
 
-def main(argv: Optional[Sequence[str]] = None) -> int:
+def parse_args(argv: Optional[Sequence[str]] = None) -> argparse.Namespace:
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
+    # parameter bounds such as -1e-3 are values, not options (argparse alone
+    # takes only plain negative numbers, -1 or -0.5, for values)
+    ap._negative_number_matcher = re.compile(r"^-(\d+\.?\d*|\.\d+)([eE][-+]?\d+)?$")
     ap.add_argument("--input", required=True, help="SU file of the line")
     ap.add_argument("--model", required=True, choices=["cmp", "zocrs", "oct"])
     ap.add_argument("--algorithm", default="linear-search", choices=["linear-search", "de"])
@@ -103,8 +107,11 @@ def main(argv: Optional[Sequence[str]] = None) -> int:
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--storage", default="fp32", choices=["fp32", "bf16", "fp16"])
     ap.add_argument("--output", required=True, help=".npy of the gathered result blocks")
-    a = ap.parse_args(argv)
+    return ap.parse_args(argv)
 
+
+def main(argv: Optional[Sequence[str]] = None) -> int:
+    a = parse_args(argv)
     from . import su
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

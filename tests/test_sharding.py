@@ -148,3 +148,16 @@ def test_shard_plan_splits_at_interior_cmps():
     # the halos overlap: rank 0 reads past its last midpoint, rank 1 before its first
     assert tb0 > np.searchsorted(line.midpoints, line.cdp_midpoints[b0 - 1], side="right")
     assert ta1 < np.searchsorted(line.midpoints, line.cdp_midpoints[a1], side="left")
+
+
+def test_driver_arguments_take_negative_exponents():
+    """Parameter bounds like -1e-3 are values of --lower / --upper, as the
+    module's usage line writes them."""
+    from highperformanceseismicstacking_gb300 import shard_driver
+    a = shard_driver.parse_args(["--input", "l.su", "--model", "zocrs", "--lower", "1414.2136",
+                                 "-1e-3", "-1e-7", "--upper", "6324.5553", "1e-3", "1e-7",
+                                 "--granularity", "41", "21", "21", "--apm", "375",
+                                 "--tau", "0.010", "--output", "r.npy"])
+    assert a.lower == [1414.2136, -1e-3, -1e-7]
+    assert a.upper == [6324.5553, 1e-3, 1e-7]
+    assert a.granularity == [41, 21, 21]
