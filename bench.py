@@ -1056,23 +1056,26 @@ def main():
     if traffic_note:
         roof["traffic_note"] = traffic_note
 
+    # the CPU baseline and the single-GPU side measurements run with one GPU
+    # only: with N ranks the other GPUs would wait for rank 0 meanwhile
+    one = world == 1
     cpu = None
-    if not args.no_cpu_baseline and world >= 1:
+    if not args.no_cpu_baseline and one:
         cpu = cpu_baseline(w, line, lower, upper, tau, args.cpu_seconds)
     su_io = None
-    if not args.no_io_side:
+    if not args.no_io_side and one:
         su_io = su_io_side(line, d_out, len(m0s), 2 + eng.np, S)
     del pinned, host_samples
     zocrs = None
-    if args.zocrs_cmps > 0 and args.workload != "zocrs-ls":
+    if args.zocrs_cmps > 0 and args.workload != "zocrs-ls" and one:
         zocrs = zocrs_side_measure(args.zocrs_cmps, local)
     de = (de_side_measure(args.de_cmps, local, args.zocrs_de_cmps)
-          if args.de_cmps > 0 else None)
-    oct_ls = oct_ls_side(args.oct_cmps, local) if args.oct_cmps > 0 else None
-    sf = sf_side(args.sf_cmps, local) if args.sf_cmps > 0 else None
-    c5 = c5_side_measure(args.c5_cmps, local) if args.c5_cmps > 0 else None
-    fp64 = fp64_agreement_side(args.fp64_cmps, local) if args.fp64_cmps > 0 else None
-    whole = None if args.no_whole_lines else whole_workloads_side(local)
+          if args.de_cmps > 0 and one else None)
+    oct_ls = oct_ls_side(args.oct_cmps, local) if args.oct_cmps > 0 and one else None
+    sf = sf_side(args.sf_cmps, local) if args.sf_cmps > 0 and one else None
+    c5 = c5_side_measure(args.c5_cmps, local) if args.c5_cmps > 0 and one else None
+    fp64 = fp64_agreement_side(args.fp64_cmps, local) if args.fp64_cmps > 0 and one else None
+    whole = None if (args.no_whole_lines or not one) else whole_workloads_side(local)
     # every kernel against its roofline (FP32-pipe instructions; HBM view of
     # the algorithmic bytes where the line is read)
     rooflines = {f"ls_tuned ({w.name})": roof}
