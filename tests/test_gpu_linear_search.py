@@ -463,9 +463,10 @@ def test_linear_search_line_equals_upload_then_search(storage):
                 assert np.array_equal(plain, want_plain), (model, storage, "plain")
 
 
+@pytest.mark.parametrize("storage", ["fp32", "bf16"])
 @pytest.mark.parametrize("ns, tau, tuned_runs", [(16376, 3, True), (16377, 3, False),
                                                  (2000, 15, False)])
-def test_size_limits_of_the_tuned_kernel(engine, ns, tau, tuned_runs):
+def test_size_limits_of_the_tuned_kernel(engine, ns, tau, tuned_runs, storage):
     """Sizes at the tuned kernel's limits: a trace row must fit its shared-
     memory stage (stride + 8 <= 16384 floats) and the window must be at most
     15 samples; beyond either the tuned call runs the plain kernel
@@ -475,6 +476,8 @@ def test_size_limits_of_the_tuned_kernel(engine, ns, tau, tuned_runs):
     line = synthetic.cmp_line(n_cmp=2, halfoffsets=list(range(25, 1176, 50)), ns=ns, dt_us=250,
                               n_reflectors=6, n_multiples=0, f=25.0, snr=10.0, seed=51)
     _setup(engine, line, "cmp", w.lower, w.upper, tau)
+    engine.upload_gather(line.samples, line.midpoints, line.halfoffsets, float(line.dt),
+                         storage=storage)  # 16-bit rows: the bulk-copied staging at its limit
     m0s = line.cdp_midpoints
     tuned, st = engine.linear_search(m0s, [61], "tuned")
     plain, st_p = engine.linear_search(m0s, [61], "plain")
