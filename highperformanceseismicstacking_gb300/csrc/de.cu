@@ -104,11 +104,12 @@ struct Draws {
 
 __device__ __forceinline__ float2 de_f2(float a, float b) { return make_float2(a, b); }
 
-// OCT: displaced-midpoint tests run side by side per thread (four at five
-// CTAs per SM: OCT DE 2 midpoints 876 -> 783 ms, 8 midpoints 2919 -> 2704 ms;
-// two at six CTAs 876 / 2768 ms, four at six 905 / 2824 ms, four at four
-// 814 / 3037 ms)
-constexpr int kDeOctBatch = 4;
+// OCT: displaced-midpoint tests run side by side per thread, five CTAs per
+// SM (before the warp box test, four side by side: OCT DE 2 midpoints 876 ->
+// 783 ms; with it, three beat four and two: 3-h0 FP16 DE, 20 generations,
+// 2 midpoints 450.2 -> 429.2 ms, two 438.7 ms; four or three CTAs per SM
+// 465.8 / 510.7 ms)
+constexpr int kDeOctBatch = 3;
 
 // threads of a DE CTA (kDeThreads below), for the per-warp box slots
 constexpr int kDeThreadsMax = 256;

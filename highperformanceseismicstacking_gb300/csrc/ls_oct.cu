@@ -42,10 +42,12 @@ constexpr int kOctWarps = 8;
 // (against two candidates per thread, OCT DE line geometry, 11 x 5
 // candidates: 4.07 -> 3.10 ms on one midpoint, 12.1 -> 10.0 ms on four).
 // The displaced-midpoint tests of kOctMhBatch traces run side by side
-// (independent chains) before the passing traces are taken in order: four
-// CTAs per SM (63 registers, no spills), 3.10 -> 2.77 ms on one midpoint,
-// 9.88 -> 9.05 ms on four, 37.9 -> 34.8 ms on sixteen.
-constexpr int kOctMhBatch = 4;
+// (independent chains) before the passing traces are taken in order, four
+// CTAs per SM (before the warp box test, four side by side: 3.10 -> 2.77 ms
+// on one midpoint; with it, two beat four and three: 3.24 / 9.60 / 38.7 ms
+// -> 3.17 / 9.48 / 38.0 ms on 1 / 4 / 16 midpoints, three 3.27 / 9.73 /
+// 39.2 ms).
+constexpr int kOctMhBatch = 2;
 
 // Warp units: a (midpoint, 32-sample tile, candidate part) unit is split
 // into kOctWarps warp units, warp slot k taking candidates chunk * kOctWarps + k
