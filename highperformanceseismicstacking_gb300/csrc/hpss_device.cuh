@@ -247,13 +247,6 @@ __device__ __forceinline__ int oct_time_k(float h, float h0, float t0, float tn0
     return DE_OK;
 }
 
-// OCT traveltime at the displaced midpoint (oct/common.cuh:37-94).
-__device__ __forceinline__ int oct_time(float h, float h0, float t0, float m0,
-                                        float m, float mh, float c,
-                                        float slope, float *out) {
-    return oct_time_k(h, h0, t0, oct_tn0_sq(t0, c, h0), m0, m, mh, c, slope, out);
-}
-
 // OCT traveltime of one trace for the candidate factors k (candidate c,
 // slope), trace factors f and midpoint m, half-offset h; returns as
 // model_time below.
