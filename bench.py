@@ -614,7 +614,8 @@ def fp64_agreement_side(n_mid, local):
     return res
 
 
-def _case_ls(workload, n_cmp, mid_count, gran=None, storage="fp32"):
+def _case_ls(workload, n_cmp, mid_count, gran=None, storage="fp32", kernel="tuned",
+             fp64=False):
     from highperformanceseismicstacking_gb300 import capi
     w, line, lower, upper, tau = make_workload(workload, n_cmp)
     m0s = line.cdp_midpoints
@@ -626,8 +627,10 @@ def _case_ls(workload, n_cmp, mid_count, gran=None, storage="fp32"):
                           storage=storage)
         eng.set_traveltime(w.model, lower, upper, w.apm, 0.0)
         eng.set_window(tau)
+        if fp64:
+            eng.set_precision(fp64=True)
         for _ in range(2):
-            _, st = eng.linear_search(m0s, gran or w.granularity, "tuned")
+            _, st = eng.linear_search(m0s, gran or w.granularity, kernel)
     return st
 
 
@@ -689,6 +692,11 @@ PROFILE_CASES = {
     "cmp": lambda: _case_ls("cmp-production", 300, 0),
     # ls_tuned2_kernel (16-bit rows): the same with BF16 amplitude storage
     "cmpbf16": lambda: _case_ls("cmp-production", 300, 0, storage="bf16"),
+    # ls_plain_kernel: the plain baseline on the same 300 CMPs
+    "cmpplain": lambda: _case_ls("cmp-production", 300, 0, kernel="plain"),
+    # ls_f64_kernel: every step in FP64, one ZO-CRS midpoint, 5 x 5 x 5 candidates
+    "zocrsf64": lambda: _case_ls("zocrs-ls", None, 1, gran=[5, 5, 5], kernel="plain",
+                                 fp64=True),
     # ls_tuned2_kernel: 4 midpoints of the ZO-CRS line, 21 x 21 x 41 candidates
     "zocrs": lambda: _case_ls("zocrs-ls", None, 4),
     # ls_tuned2_kernel (16-bit rows): the same with BF16 amplitude storage
