@@ -429,12 +429,20 @@ hpss_status linear_search_impl(hpss_handle h, const float *d_m0s, uint32_t nM0,
 }
 
 // Body of hpss_linear_search_line, after prepare_line: the amplitudes go
-// to the device in kStreamChunks trace ranges on the copy stream, the
-// midpoints are searched in kStreamGroups contiguous groups on the handle's
+// to the device in trace ranges on the copy stream, the midpoints are
+// searched in contiguous groups on the handle's
 // stream, each group waiting only for the chunk that holds the last trace
 // its midpoints can select, and each group's results go back on the copy
-// stream while the next group runs.
-constexpr uint32_t kStreamChunks = 8, kStreamGroups = 8;
+// stream while the next group runs.  HPSS_STREAM_CHUNKS / HPSS_STREAM_GROUPS
+// (1 .. 64) set the numbers of trace ranges and midpoint groups.
+constexpr uint32_t kStreamChunks = 8, kStreamGroups = 8, kStreamMax = 64;
+
+static uint32_t stream_count(const char *name, uint32_t dflt) {
+    const char *env = std::getenv(name);
+    if (!env) return dflt;
+    const int v = std::atoi(env);
+    return v >= 1 && v <= (int)kStreamMax ? (uint32_t)v : dflt;
+}
 
 
 hpss_status stream_line_and_search(hpss_handle h, const float *samples, const float *m0s,
@@ -442,7 +450,9 @@ hpss_status stream_line_and_search(hpss_handle h, const float *samples, const fl
                                    float *out, hpss_stats *stats) {
     if (!h->copyStream)
         HPSS_CUDA_TRY(h, cudaStreamCreateWithFlags(&h->copyStream, cudaStreamNonBlocking));
-    while (h->streamEvents.size() < kStreamChunks + kStreamGroups) {
+    const uint32_t nChunks = stream_count("HPSS_STREAM_CHUNKS", kStreamChunks);
+    const uint32_t nGroups = stream_count("HPSS_STREAM_GROUPS", kStreamGroups);
+    while (h->streamEvents.size() < nChunks + nGroups) {
         cudaEvent_t e;
         HPSS_CUDA_TRY(h, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         h->streamEvents.push_back(e);
@@ -450,15 +460,15 @@ hpss_status stream_line_and_search(hpss_handle h, const float *samples, const fl
     if (!h->streamT0) HPSS_CUDA_TRY(h, cudaEventCreate(&h->streamT0));
     if (!h->streamT1) HPSS_CUDA_TRY(h, cudaEventCreate(&h->streamT1));
     cudaEvent_t *chunkDone = h->streamEvents.data();
-    cudaEvent_t *groupDone = chunkDone + kStreamChunks;
+    cudaEvent_t *groupDone = chunkDone + nChunks;
     const uint32_t n = h->nTraces;
-    uint32_t bound[kStreamChunks + 1];
-    for (uint32_t k = 0; k <= kStreamChunks; k++)
-        bound[k] = (uint32_t)((uint64_t)n * k / kStreamChunks);
+    uint32_t bound[kStreamMax + 1];
+    for (uint32_t k = 0; k <= nChunks; k++)
+        bound[k] = (uint32_t)((uint64_t)n * k / nChunks);
     if (n && h->stride != h->S && h->storage == HPSS_STORAGE_FP32)
         HPSS_CUDA_TRY(h, cudaMemsetAsync(h->dSamples, 0, (size_t)n * h->stride * sizeof(float),
                                          h->copyStream));
-    for (uint32_t k = 0; k < kStreamChunks; k++) {
+    for (uint32_t k = 0; k < nChunks; k++) {
         HPSS_CUDA_TRY(h, copy_line_rows(h, samples, bound[k], bound[k + 1], h->copyStream));
         HPSS_CUDA_TRY(h, cudaEventRecord(chunkDone[k], h->copyStream));
     }
@@ -488,11 +498,11 @@ hpss_status stream_line_and_search(hpss_handle h, const float *samples, const fl
                          : h->model == HPSS_MODEL_ZOCRS
                              ? h->apm
                              : h->apm + std::sqrt(hmax * hmax + h->h0 * h->h0);
-    // groups of ceil(nM0 / kStreamGroups) midpoints, the last one smaller: the
+    // groups of ceil(nM0 / nGroups) midpoints, the last one smaller: the
     // first group is the largest, so the per-call buffers the search grows
     // (selection, candidate parts) are sized by it and never reallocated
     // under a later group's launches
-    const uint32_t per = (nM0 + kStreamGroups - 1) / kStreamGroups;
+    const uint32_t per = (nM0 + nGroups - 1) / nGroups;
     const uint32_t G = (nM0 + per - 1) / per;
     auto first = [&](uint32_t g) { return std::min(g * per, nM0); };
     auto back = [&](uint32_t g) -> cudaError_t {

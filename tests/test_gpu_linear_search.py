@@ -430,14 +430,19 @@ def _line_cases():
             ("oct", ol, [1200.0, -1e-3], [5000.0, 1e-3], [6, 5], 60.0, 300.0)]
 
 
-@pytest.mark.parametrize("storage", ["fp32", "bf16"])
-def test_linear_search_line_equals_upload_then_search(storage):
+@pytest.mark.parametrize("storage, chunks, groups", [("fp32", None, None), ("bf16", None, None),
+                                                     ("fp32", "5", "3"), ("fp32", "1", "64")])
+def test_linear_search_line_equals_upload_then_search(storage, chunks, groups, monkeypatch):
     """hpss_linear_search_line (upload streamed in trace ranges, midpoints
     searched in groups as their traces arrive) gives the blocks and
     statistics of hpss_upload_gather followed by hpss_linear_search, for all
     three models, rows with padding (301 samples), calls with more and fewer
-    midpoints than groups and a midpoint outside the line; the line stays
-    resident afterwards."""
+    midpoints than groups and a midpoint outside the line, with the default
+    numbers of trace ranges and groups and with others (HPSS_STREAM_CHUNKS,
+    HPSS_STREAM_GROUPS); the line stays resident afterwards."""
+    if chunks:
+        monkeypatch.setenv("HPSS_STREAM_CHUNKS", chunks)
+        monkeypatch.setenv("HPSS_STREAM_GROUPS", groups)
     tau = 2
     for model, line, lower, upper, gran, apm, h0 in _line_cases():
         for m0s in (line.cdp_midpoints,

@@ -90,15 +90,20 @@ def test_stretch_free_other_models_vs_oracle(engine, model):
         _check_sf(out[i], sem, stk, 10)
 
 
-@pytest.mark.parametrize("model", ["cmp", "zocrs", "oct"])
+@pytest.mark.parametrize("model, wide", [("cmp", False), ("zocrs", False), ("zocrs", True),
+                                         ("oct", False), ("oct", True)])
 @pytest.mark.parametrize("storage", ["fp32", "fp16"])
-def test_block_kernel_equals_warp_kernel(engine, monkeypatch, model, storage):
-    """The stretch-free block kernel (warp = n value, lane = sample) and the
-    warp-per-sample kernel (lanes = n values) give the same block bit for
-    bit, not-used counts included; a window or n count outside the block
-    kernel's instantiations (window 13, 33 n values) runs the warp kernel."""
-    line = synthetic.structured_line(n_cmp=10, fold_range=(5, 9), h_max=900, ns=300,
-                                     dt_us=4000, n_reflectors=3, f=20.0, snr=6.0, seed=67)
+def test_block_kernels_equal_warp_kernel(engine, monkeypatch, model, wide, storage):
+    """The stretch-free block kernels (warp = n value, lane = sample): the
+    per-pair one (CMP; HPSS_SF_KERNEL=block for any model) and the one that
+    shares each (s - n, trace) traveltime among the pairs (ZO-CRS, OCT, in
+    batches of 64 traces: `wide` apertures hold more than one batch) give
+    the warp-per-sample kernel's block (lanes = n values) bit for bit,
+    not-used counts included; a window or n count outside the block
+    kernels' instantiations (window 13, 33 n values) runs the warp kernel."""
+    line = synthetic.structured_line(n_cmp=16 if wide else 10, fold_range=(5, 9), h_max=900,
+                                     ns=300, dt_us=4000, n_reflectors=3, f=20.0, snr=6.0,
+                                     seed=67)
     if model == "cmp":
         lower, upper, gran, apm, h0 = [1200.0], [5000.0], [41], 0.0, 0.0
     elif model == "zocrs":
@@ -106,6 +111,8 @@ def test_block_kernel_equals_warp_kernel(engine, monkeypatch, model, storage):
         lower, upper, gran, apm, h0 = [1414.2136, -a, -b], [6324.5553, a, b], [6, 5, 5], 100.0, 0.0
     else:
         lower, upper, gran, apm, h0 = [1200.0, -1e-3], [5000.0, 1e-3], [8, 5], 60.0, 300.0
+    if wide:
+        apm *= 8.0
     engine.upload_gather(line.samples, line.midpoints, line.halfoffsets, float(line.dt),
                          storage=storage)
     engine.set_traveltime(model, lower, upper, apm, h0)
@@ -115,11 +122,16 @@ def test_block_kernel_equals_warp_kernel(engine, monkeypatch, model, storage):
     prior = np.ascontiguousarray(ls[:, 2:])
     for nmax in (0, 7, 15):
         monkeypatch.delenv("HPSS_SF_KERNEL", raising=False)
+        dflt, st_d = engine.stretch_free(m0s, prior, nmax)
+        monkeypatch.setenv("HPSS_SF_KERNEL", "block")
         blk, st_b = engine.stretch_free(m0s, prior, nmax)
         monkeypatch.setenv("HPSS_SF_KERNEL", "warp")
         wrp, st_w = engine.stretch_free(m0s, prior, nmax)
-        assert np.array_equal(blk, wrp), (model, storage, nmax)
-        assert st_b["not_used"] == st_w["not_used"]
+        assert np.array_equal(dflt, wrp), (model, storage, nmax, "default")
+        assert np.array_equal(blk, wrp), (model, storage, nmax, "block")
+        assert st_d["not_used"] == st_w["not_used"] == st_b["not_used"]
+        if wide:  # more than one batch of traces per midpoint
+            assert st_d["selected_traces"] > 64 * len(m0s), st_d["selected_traces"]
     monkeypatch.delenv("HPSS_SF_KERNEL", raising=False)
     # warp kernel by shape: 33 n values, and window 13
     big, _ = engine.stretch_free(m0s, prior, 16)
