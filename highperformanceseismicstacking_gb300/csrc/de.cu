@@ -380,12 +380,13 @@ __device__ __forceinline__ void de_trial_vector(const DeParams &d, uint32_t mkey
 // widening loads for 16-bit rows -- and every thread reads its windows from
 // there.  Each trial's sums take the same values in the same trace order as
 // de_eval's, so the results are the same bit for bit.
-constexpr int kDeStageFloats = 10240;  // 40 KB of spans per CTA
+constexpr int kDeStageFloats = 9728;   // 38 KB of spans per CTA
 constexpr int kDeZeroPad = 16;         // zeros first: windows outside their trace read these
 
 struct DeStage {
     float y[kDeStageFloats];
-    int base[kDeThreadsMax];  // per round slot: stage index of the trace's sample 0
+    float2 hm[kDeThreadsMax];  // per round slot: the trace's h^2 and m - m0 (as m + (-m0))
+    int base[kDeThreadsMax];   // per round slot: stage index of the trace's sample 0
     int lo[kDeThreadsMax];
     int len[kDeThreadsMax];
     int full[kDeThreadsMax];  // every window of the trials lies inside the trace
@@ -450,9 +451,11 @@ __device__ int de_stage_round(const DeParams &d, DeStage &st, uint32_t &phase,
         const uint32_t q = q0 + threadIdx.x;
         int lo = 0, len = 0;
         bool full = false;
-        if (anyActive && q < cnt) {
-            const uint32_t ti = first + q;
-            trace_span<MODEL>(a, cb, m0, t0a, t0b, a.mid[ti], a.hsq[ti], &lo, &len, &full);
+        float tm = 0.f, thsq = 0.f;
+        if (q < cnt) {
+            tm = a.mid[first + q];
+            thsq = a.hsq[first + q];
+            if (anyActive) trace_span<MODEL>(a, cb, m0, t0a, t0b, tm, thsq, &lo, &len, &full);
         }
         int incl = len;
 #pragma unroll
@@ -473,6 +476,9 @@ __device__ int de_stage_round(const DeParams &d, DeStage &st, uint32_t &phase,
             st.lo[threadIdx.x] = lo;
             st.len[threadIdx.x] = len;
             st.full[threadIdx.x] = full ? 1 : 0;
+            // the evaluation's per-trace inputs, read from here instead of
+            // from global memory by every thread (m - m0 rounded as there)
+            st.hm[threadIdx.x] = make_float2(thsq, __fadd_rn(tm, -m0));
         }
         const uint32_t nfit = (uint32_t)__syncthreads_count(fits);
         if (nfit == 0) {
@@ -556,8 +562,9 @@ __device__ bool de_eval_staged(const DeParams &d, DeStage &st, uint32_t &phase, 
     const float2 c2 = de_f2(c, c), a2 = de_f2(p1, p1), b2 = de_f2(p2, p2);
     const float t0sq = __fmul_rn(t0, t0);
     const float2 t02 = de_f2(t0, t0), t0sq2 = de_f2(t0sq, t0sq);
-    const float2 negM02 = de_f2(-m0, -m0);
     const float rdt = 1.0f / a.dt;
+    // windows whose start k - tau keeps the whole window inside the trace
+    const unsigned winSpan = (int)a.S > 2 * a.tau + 1 ? (unsigned)((int)a.S - 2 * a.tau - 1) : 0u;
     const float2 rdt2 = de_f2(rdt, rdt);
     const float2 kNeg1 = de_f2(-1.f, -1.f);
     const float2 kMagic2 = de_f2(8388608.f, 8388608.f), kNegMagic2 = de_f2(-8388608.f, -8388608.f);
@@ -577,13 +584,13 @@ __device__ bool de_eval_staged(const DeParams &d, DeStage &st, uint32_t &phase, 
             // same sums: those tests pass for every window)
             auto pairStep = [&](uint32_t j, auto fullTag) {
                 constexpr bool FULL = decltype(fullTag)::value;
-                const uint32_t ti0 = first + q0 + j, ti1 = ti0 + 1;
-                const float2 hsq2 = de_f2(a.hsq[ti0], a.hsq[ti1]);
+                const float2 hmA = st.hm[j], hmB = st.hm[j + 1];
+                const float2 hsq2 = de_f2(hmA.x, hmB.x);
                 float2 tt2;
                 if (MODEL == kModelCmp) {
                     tt2 = __ffma2_rn(c2, hsq2, t0sq2);
                 } else {
-                    const float2 dm2 = __fadd2_rn(de_f2(a.mid[ti0], a.mid[ti1]), negM02);
+                    const float2 dm2 = de_f2(hmA.y, hmB.y);  // m + (-m0), both traces
                     const float2 x2 = __ffma2_rn(a2, dm2, t02);
                     const float2 bd2 = __fmul2_rn(b2, dm2);
                     tt2 = __ffma2_rn(c2, hsq2, __ffma2_rn(bd2, dm2, __fmul2_rn(x2, x2)));
@@ -598,8 +605,9 @@ __device__ bool de_eval_staged(const DeParams &d, DeStage &st, uint32_t &phase, 
                 const float2 fq = __ffma2_rn(__fadd2_rn(rk, kNegMagic2), kNeg1, ti2);  // frac
                 const int ka = __float_as_int(rk.x) - 0x4B000000;
                 const int kb = __float_as_int(rk.y) - 0x4B000000;
-                const bool ina = FULL || (oka && window_in_trace(ka, a.tau, (int)a.S));
-                const bool inb = FULL || (okb && window_in_trace(kb, a.tau, (int)a.S));
+                // k - tau >= 0 && k + tau + 1 < S as one unsigned compare
+                const bool ina = FULL || (oka && (unsigned)(ka - a.tau) < winSpan);
+                const bool inb = FULL || (okb && (unsigned)(kb - a.tau) < winSpan);
 #ifdef HPSS_CHECKED
                 if ((ina && (ka - a.tau < st.lo[j] || ka - a.tau + W >= st.lo[j] + st.len[j])) ||
                     (inb && (kb - a.tau < st.lo[j + 1] ||
@@ -719,6 +727,8 @@ __device__ bool de_eval_staged2(const DeParams &d, DeStage &st, uint32_t &phase,
     const float t0sq = __fmul_rn(t0, t0);
     const float2 t02 = de_f2(t0, t0), t0sq2 = de_f2(t0sq, t0sq);
     const float rdt = 1.0f / a.dt;
+    // windows whose start k - tau keeps the whole window inside the trace
+    const unsigned winSpan = (int)a.S > 2 * a.tau + 1 ? (unsigned)((int)a.S - 2 * a.tau - 1) : 0u;
     const float2 rdt2 = de_f2(rdt, rdt);
     const float2 kNeg1 = de_f2(-1.f, -1.f);
     const float2 kMagic2 = de_f2(8388608.f, 8388608.f), kNegMagic2 = de_f2(-8388608.f, -8388608.f);
@@ -734,16 +744,13 @@ __device__ bool de_eval_staged2(const DeParams &d, DeStage &st, uint32_t &phase,
             // (the range tests, zero-pad redirect and count are skipped)
             auto traceStep = [&](uint32_t j, auto fullTag) {
                 constexpr bool FULL = decltype(fullTag)::value;
-                const uint32_t ti = first + q0 + j;
-                const float hsq = a.hsq[ti];
-                const float2 hsq2 = de_f2(hsq, hsq);
+                const float2 hm = st.hm[j];  // h^2, m + (-m0): de_eval_staged's rounding
+                const float2 hsq2 = de_f2(hm.x, hm.x);
                 float2 tt2;
                 if (MODEL == kModelCmp) {
                     tt2 = __ffma2_rn(c2, hsq2, t0sq2);
                 } else {
-                    // m - m0 as m + (-m0): de_eval_staged's rounding
-                    const float dm = __fadd_rn(a.mid[ti], -m0);
-                    const float2 dm2 = de_f2(dm, dm);
+                    const float2 dm2 = de_f2(hm.y, hm.y);
                     const float2 xx = __ffma2_rn(a2, dm2, t02);
                     const float2 bd2 = __fmul2_rn(b2, dm2);
                     tt2 = __ffma2_rn(c2, hsq2, __ffma2_rn(bd2, dm2, __fmul2_rn(xx, xx)));
@@ -758,8 +765,9 @@ __device__ bool de_eval_staged2(const DeParams &d, DeStage &st, uint32_t &phase,
                 const float2 fq = __ffma2_rn(__fadd2_rn(rk, kNegMagic2), kNeg1, ti2);  // frac
                 const int ka = __float_as_int(rk.x) - 0x4B000000;
                 const int kb = __float_as_int(rk.y) - 0x4B000000;
-                const bool ina = FULL || (oka && window_in_trace(ka, a.tau, (int)a.S));
-                const bool inb = FULL || (okb && window_in_trace(kb, a.tau, (int)a.S));
+                // k - tau >= 0 && k + tau + 1 < S as one unsigned compare
+                const bool ina = FULL || (oka && (unsigned)(ka - a.tau) < winSpan);
+                const bool inb = FULL || (okb && (unsigned)(kb - a.tau) < winSpan);
                 const int base = st.base[j];
 #ifdef HPSS_CHECKED
                 if ((act[0] && ina && (ka - a.tau < st.lo[j] || ka - a.tau + W >= st.lo[j] + st.len[j])) ||
