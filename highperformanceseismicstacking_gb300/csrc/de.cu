@@ -378,8 +378,10 @@ __device__ __forceinline__ void de_trial_vector(const DeParams &d, uint32_t mkey
 // the box is taken anew for every evaluation, so the spans shrink as the
 // populations converge) into shared memory -- bulk copies for FP32 rows,
 // widening loads for 16-bit rows -- and every thread reads its windows from
-// there.  Each trial's sums take the same values in the same trace order as
-// de_eval's, so the results are the same bit for bit.
+// there, and each trace's h^2 and m - m0 from the round's slot (one shared
+// word per trace instead of two global loads per thread and trace).  Each
+// trial's sums take the same values in the same trace order as de_eval's,
+// so the results are the same bit for bit.
 constexpr int kDeStageFloats = 9728;   // 38 KB of spans per CTA
 constexpr int kDeZeroPad = 16;         // zeros first: windows outside their trace read these
 
