@@ -55,7 +55,7 @@ def test_two_ranks_on_the_gpu_equal_one_call(tmp_path, model):
     argv = ["--input", str(path), "--output", str(out)] + ARGS[model]
     mp.start_processes(_rank, args=(2, _free_port(), argv), nprocs=2, start_method="spawn")
     got = np.load(out)
-    # one call over the whole line, on the gather the driver reads
+    # one call over the whole line, on the gather shard_driver.py reads
     a = dict(zip(argv[::2], argv[1::2]))
     apm = float(a.get("--apm", 0.0))
     g = su.read_gather(str(path), aph=1e30, apm=apm, tau=float(a["--tau"]),
