@@ -82,7 +82,7 @@ def build_engine(force: bool = False, extra_flags=(), flavour: str = "") -> Path
 
 
 def build_oracle(force: bool = False) -> Path:
-    """Compile the oracle's C restatement (checker only) to oracle/liboracle.so."""
+    """Compile the oracle's C restatement (test infrastructure) to oracle/liboracle.so."""
     src = ORACLE_DIR / "hpss_oracle.c"
     deps = [src, ORACLE_DIR / "hpss_oracle_impl.inc", ORACLE_DIR / "hpss_oracle.h"]
     out = ORACLE_DIR / ORACLE_LIB

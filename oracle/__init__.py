@@ -1,5 +1,5 @@
 """The oracle: a CPU restatement of the reference's semblance hot path.
 
 Test infrastructure only -- imported by tests/, __graft_entry__.smoke() and the
-CPU-baseline leg of bench.py as the checker, never by the product path.
+CPU-baseline leg of bench.py to check against, never by the product path.
 """

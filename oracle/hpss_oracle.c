@@ -1,7 +1,7 @@
 /*
  * hpss_oracle.c -- CPU restatement of the reference's semblance hot path.
  * TEST INFRASTRUCTURE ONLY: loaded by tests/, __graft_entry__.smoke() and the
- * CPU-baseline leg of bench.py as the checker; never by the product path.
+ * CPU-baseline leg of bench.py to check against; never by the product path.
  *
  * Built with -O2 -ffp-contract=off so that x86-64 and aarch64 hosts produce
  * identical float results (no fused multiply-add contraction).
