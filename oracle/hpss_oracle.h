@@ -1,6 +1,6 @@
 /*
  * hpss_oracle.h -- CPU restatement of the semblance hot path of
- * HighPerformanceSeismicStacking, used ONLY as the checker (tests, smoke(),
+ * HighPerformanceSeismicStacking, used ONLY to check against (tests, smoke(),
  * and the CPU-baseline leg of bench.py).  It is test infrastructure: no
  * product code path links, loads or calls it.
  *
