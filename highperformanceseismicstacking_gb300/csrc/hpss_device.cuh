@@ -582,6 +582,14 @@ __device__ __forceinline__ void oct_box_store(volatile float *slot, const OctWar
     slot[3] = r.bHi;
     __syncwarp();
 }
+// The warp box test of one trace, with its table entry and half-offset given.
+__device__ __forceinline__ bool oct_box_keep_tf(const LsParams &a, const OctLine &ol, float4 tf,
+                                                float hoff, const volatile float *slot,
+                                                float m0) {
+    const float aLo = slot[0], aHi = slot[1], bLo = slot[2], bHi = slot[3];
+    return ol.h0 == 0.f ? oct_box_may_pass(tf, bLo, bHi, aLo, aHi, m0, a.apm)
+                        : oct_box_may_pass_h0(tf, hoff, ol.h0, aLo, aHi, bLo, bHi, m0, a.apm);
+}
 __device__ __forceinline__ bool oct_box_keep(const LsParams &a, const OctLine &ol, uint32_t ti,
                                              const volatile float *slot, float m0) {
     const float4 tf = __ldg(ol.tab + ti);
@@ -591,23 +599,46 @@ __device__ __forceinline__ bool oct_box_keep(const LsParams &a, const OctLine &o
                                               m0, a.apm);
 }
 
+// Where oct_eval_traces takes trace b's table entry, half-offset and index
+// from: the line in global memory (trace indices tb) ...
+template <int B>
+struct OctGlobalTraces {
+    const float4 *tab;
+    const float *hoffs;
+    uint32_t tb[B];
+    __device__ __forceinline__ float4 entry(int b) const { return __ldg(tab + tb[b]); }
+    __device__ __forceinline__ float hoff(int b) const { return hoffs[tb[b]]; }
+    __device__ __forceinline__ uint32_t index(int b) const { return tb[b]; }
+};
+// ... or a warp's block of 32 traces copied to shared memory by its box test
+// (slots bit[b] of the block)
+template <int B>
+struct OctBlockTraces {
+    const float4 *tab;
+    const float *hoffs;
+    const uint32_t *ti;
+    uint32_t bit[B];
+    __device__ __forceinline__ float4 entry(int b) const { return tab[bit[b]]; }
+    __device__ __forceinline__ float hoff(int b) const { return hoffs[bit[b]]; }
+    __device__ __forceinline__ uint32_t index(int b) const { return ti[bit[b]]; }
+};
+
 // B traces of one thread's OCT candidate (factors kc, c = 4/v^2, slope):
 // the displaced-midpoint tests side by side (independent chains), then time
 // and window of the passing traces in order, as COMPUTE_SEMBLANCE
 // (interface.h:26-44).  live[b] false: padding, neither evaluated nor
 // counted.
-template <int W, int B>
-__device__ __forceinline__ void oct_eval_batch(const LsParams &a, const OctLine &ol,
-                                               const uint32_t (&tb)[B],
-                                               const bool (&live)[B], const OctCand &kc,
-                                               float c, float slope, float t0, float m0,
-                                               float (&num)[W], float &lin, float &den,
-                                               unsigned &used, unsigned &nu) {
+template <int W, int B, typename Traces>
+__device__ __forceinline__ void oct_eval_traces(const LsParams &a, const OctLine &ol,
+                                                const Traces &tr, const bool (&live)[B],
+                                                const OctCand &kc, float c, float slope,
+                                                float t0, float m0, float (&num)[W], float &lin,
+                                                float &den, unsigned &used, unsigned &nu) {
     float4 fb[B];  // {m, gamma^2, 16h^2h0^2, h^2-h0^2}
     float mhb[B];
     bool pass[B];
 #pragma unroll
-    for (int b = 0; b < B; b++) fb[b] = __ldg(ol.tab + tb[b]);
+    for (int b = 0; b < B; b++) fb[b] = tr.entry(b);
 #pragma unroll
     for (int b = 0; b < B; b++) {
         const int e = oct_mh_all(kc, fb[b].y, fb[b].z, fb[b].w, m0, &mhb[b]);
@@ -621,15 +652,31 @@ __device__ __forceinline__ void oct_eval_batch(const LsParams &a, const OctLine 
             continue;
         }
         float t;
-        if (oct_time_k(a.hoff[tb[b]], ol.h0, t0, kc.tn0_sq, m0, fb[b].x, mhb[b], c, slope, &t) !=
+        if (oct_time_k(tr.hoff(b), ol.h0, t0, kc.tn0_sq, m0, fb[b].x, mhb[b], c, slope, &t) !=
             DE_OK)
             continue;
         const WinIdx wi = window_index(t, a.dt);
         if (window_in_trace(wi.k, a.tau, (int)a.S)) {
-            accum_window<W>(a, tb[b], wi.k - a.tau, wi.frac, num, lin, den);
+            accum_window<W>(a, tr.index(b), wi.k - a.tau, wi.frac, num, lin, den);
             used++;
         }
     }
+}
+
+// oct_eval_traces over traces tb of the line in global memory.
+template <int W, int B>
+__device__ __forceinline__ void oct_eval_batch(const LsParams &a, const OctLine &ol,
+                                               const uint32_t (&tb)[B],
+                                               const bool (&live)[B], const OctCand &kc,
+                                               float c, float slope, float t0, float m0,
+                                               float (&num)[W], float &lin, float &den,
+                                               unsigned &used, unsigned &nu) {
+    OctGlobalTraces<B> tr;
+    tr.tab = ol.tab;
+    tr.hoffs = a.hoff;
+#pragma unroll
+    for (int b = 0; b < B; b++) tr.tb[b] = tb[b];
+    oct_eval_traces<W, B>(a, ol, tr, live, kc, c, slope, t0, m0, num, lin, den, used, nu);
 }
 
 }  // namespace hpss

@@ -73,6 +73,11 @@ ls_oct_kernel(LsParams a, uint32_t tiles, uint32_t parts, uint32_t chunksPerPart
     const int S = (int)a.S, tau = a.tau;
     const uint32_t nChunks = (a.P + kOctWarps - 1) / kOctWarps;
     __shared__ float shBox[kOctWarps][4];  // each warp's displaced-midpoint box
+    // each warp's block of 32 traces as its box test read them: table entry,
+    // half-offset, trace index (the evaluation takes them from here)
+    __shared__ float4 blkTab[kOctWarps][32];
+    __shared__ float blkHoff[kOctWarps][32];
+    __shared__ uint32_t blkTi[kOctWarps][32];
     for (uint32_t k = 0;; k++) {
         uint32_t wu;
         if (a.unitCounter) {
@@ -140,9 +145,15 @@ ls_oct_kernel(LsParams a, uint32_t tiles, uint32_t parts, uint32_t chunksPerPart
                     bool keep = false;
                     if ((uint32_t)lane < n) {
                         const uint32_t ti = a.selIdx ? a.selIdx[first + qb + lane] : first + qb + lane;
-                        keep = oct_box_keep(a, ol, ti, shBox[warp], m0);
+                        const float4 tf = __ldg(ol.tab + ti);
+                        const float hf = __ldg(a.hoff + ti);
+                        keep = oct_box_keep_tf(a, ol, tf, hf, shBox[warp], m0);
+                        blkTab[warp][lane] = tf;
+                        blkHoff[warp][lane] = hf;
+                        blkTi[warp][lane] = ti;
                     }
                     uint32_t mask = __ballot_sync(0xffffffffu, keep);
+                    __syncwarp();  // the block's slots written before they are read
                     nu += n - (uint32_t)__popc(mask);
                     if constexpr (TT64) {
                         for (; mask; mask &= mask - 1) {
@@ -151,19 +162,22 @@ ls_oct_kernel(LsParams a, uint32_t tiles, uint32_t parts, uint32_t chunksPerPart
                         }
                     }
                     while (mask) {
-                        uint32_t tb[kOctMhBatch];
+                        OctBlockTraces<kOctMhBatch> tr;
+                        tr.tab = blkTab[warp];
+                        tr.hoffs = blkHoff[warp];
+                        tr.ti = blkTi[warp];
                         bool live[kOctMhBatch];
                         const uint32_t firstBit = (uint32_t)__ffs(mask) - 1;
 #pragma unroll
                         for (int bb = 0; bb < kOctMhBatch; bb++) {
                             live[bb] = mask != 0;
-                            const uint32_t bit = live[bb] ? (uint32_t)__ffs(mask) - 1 : firstBit;
+                            tr.bit[bb] = live[bb] ? (uint32_t)__ffs(mask) - 1 : firstBit;
                             if (live[bb]) mask &= mask - 1;
-                            tb[bb] = a.selIdx ? a.selIdx[first + qb + bit] : first + qb + bit;
                         }
-                        oct_eval_batch<W, kOctMhBatch>(a, ol, tb, live, kc, cc, sl, t0, m0, num, lin,
-                                                       den, used, nu);
+                        oct_eval_traces<W, kOctMhBatch>(a, ol, tr, live, kc, cc, sl, t0, m0, num,
+                                                        lin, den, used, nu);
                     }
+                    __syncwarp();  // the block's slots read before the next block writes them
                 }
             } else {
                 // displaced-midpoint tests of kOctMhBatch traces side by side,
