@@ -42,6 +42,6 @@ def test_profile_cases_are_listed():
     r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--help"], capture_output=True,
                        text=True, timeout=120, cwd=ROOT)
     assert r.returncode == 0
-    for case in ("cmp", "cmpbf16", "cmpsf", "octde", "octls", "octsf", "zocrs", "zocrsbf16",
-                 "zocrsde"):
+    for case in ("cmp", "cmpbf16", "cmpplain", "cmpsf", "octde", "octls", "octsf", "zocrs",
+                 "zocrsbf16", "zocrsde", "zocrsf64"):
         assert case in r.stdout, case
